@@ -1,0 +1,288 @@
+#!/usr/bin/env python3
+"""Benchmark: closure edges/s and time-to-fixpoint of the GB300 engine.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl {grg,reference}]
+
+Workload (one step = one pass of the hot path over one graph): the
+block-structured dataflow graph -- 2,000 procedure blocks x 1,000 vertices,
+6,000,000 'e' edges plus their 'N' seed copies, grammar N ::= N e | e,
+filter_flag 1 -- closed to its fixpoint (1,316,964,027 edges). A step builds
+the element tables from the edge arrays already resident in HBM and runs the
+semi-naive rounds until no delta remains. L2 is flushed (a 512 MiB write)
+before every timed step.
+
+`e2e` runs the same step through the public API from pinned host arrays
+(host->device copy of the edges and device->host read of the per-label counts
+inside the timed region).
+
+`--impl reference` times the CPU implementation of the path (the oracle port
+in oracle/, all host threads) on a bounded sample of the same workload: every
+8th procedure block's source rows (rows are independent under filter 1).
+
+Multi-GPU: the closure of one graph does not shard without an exchange step,
+so N GPUs run N independent replicas (one per rank, weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [ROOT, os.path.join(ROOT, "graspan-g_gb300")]
+
+import numpy as np  # noqa: E402
+
+METRIC = "closure_edges_per_sec"
+UNIT = "edges/s"
+WORKLOAD = ("dataflow_blocks: 2000 blocks x 1000 vertices, 6M 'e' edges + 6M 'N' seeds, "
+            "grammar N ::= N e | e, filter_flag 1")
+SAMPLE_EVERY = 8
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_baseline(w, nthreads=None):
+    """Oracle port on every SAMPLE_EVERY-th block's source rows, all host threads."""
+    from oracle import oracle as O
+    O.build()
+    nthreads = nthreads or os.cpu_count() or 1
+    block = w.meta.get("block", 1000)
+    mask = ((np.arange(w.num_vars) // block) % SAMPLE_EVERY == 0).astype(np.uint8)
+    t = time.perf_counter()
+    r = O.closure(w.num_vars, w.rule_ids(), w.num_labels, w.filter_flag, w.src, w.dst, w.lab,
+                  row_mask=mask, nthreads=nthreads)
+    dt = time.perf_counter() - t
+    total = r.total
+    del r
+    return {"value": total / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"closure of every {SAMPLE_EVERY}th block's source rows ({int(mask.sum())} rows, "
+                      f"{total} edges, {dt:.2f} s)", "seconds": dt, "edges": total}
+
+
+def run_reference(args, w, world, rank):
+    if rank != 0:
+        return
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(w)
+        if i >= args.warmup:
+            vals.append(cb)
+    v = statistics.mean(c["value"] for c in vals)
+    secs = statistics.mean(c["seconds"] for c in vals)
+    last = vals[-1]
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": secs * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "u32", "data": "synthetic (seeded generator)", "impl": "reference",
+           "config": {"workload": WORKLOAD, "num_vars": w.num_vars, "input_edges": w.num_edges,
+                      "sample": last["sample"]},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": last["cores"], "kind": "port", "sample": last["sample"]},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="grg", choices=["grg", "reference"])
+    ap.add_argument("--blocks", type=int, default=2000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup(args)
+
+    import grg_gen as G
+    edges = 6_000_000 * args.blocks // 2000
+    w = G.dataflow_blocks(num_blocks=args.blocks, num_edges=edges)
+    if args.impl == "reference":
+        run_reference(args, w, world, rank)
+        return
+
+    import torch
+    import grg
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    stream = torch.cuda.current_stream()
+    ctx = grg.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.transfer_rules(w.rule_ids(), w.num_labels)
+    ctx.allocate_pool(0)
+    d_src = torch.from_numpy(w.src.view(np.int32)).cuda()
+    d_dst = torch.from_numpy(w.dst.view(np.int32)).cuda()
+    d_lab = torch.from_numpy(w.lab).cuda()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    def step(timing):
+        ctx.set_kernel_timing(timing)
+        ctx.load_edges_device(w.num_vars, w.num_edges, d_src.data_ptr(), d_dst.data_ptr(), d_lab.data_ptr())
+        return ctx.closure(w.filter_flag)
+
+    for _ in range(args.warmup):
+        step(False)
+    # timed device-resident steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stats = []
+    barrier()
+    with ClockSampler(local) as clk:
+        t_wall = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            stats.append(step(True))
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+    barrier()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms = statistics.mean(step_ms)
+    total = stats[-1]["total_edges"]
+    # e2e through the public API from pinned host memory
+    h_src = torch.from_numpy(w.src.view(np.int32)).pin_memory()
+    h_dst = torch.from_numpy(w.dst.view(np.int32)).pin_memory()
+    h_lab = torch.from_numpy(w.lab).pin_memory()
+    lib = grg.load_library()
+    import ctypes
+    counts = np.zeros(w.num_labels, np.uint64)
+    e2e_ms = []
+    for i in range(args.steps + 1):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        st = lib.grg_load_edges(ctx._h, w.num_vars, w.num_edges, ctypes.c_void_p(h_src.data_ptr()),
+                                ctypes.c_void_p(h_dst.data_ptr()), ctypes.c_void_p(h_lab.data_ptr()), 0)
+        assert st == 0, st
+        ctx.closure(w.filter_flag)
+        counts[:] = ctx.label_counts()
+        dt = time.perf_counter() - t
+        if i > 0:
+            e2e_ms.append(dt * 1e3)
+    assert int(counts.sum()) == total
+    # max over ranks
+    vals = torch.tensor([ms, statistics.mean(e2e_ms)], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(vals, op=dist.ReduceOp.MAX)
+    ms_max, e2e_max = vals.tolist()
+    if rank == 0:
+        hbm, peak_kind = peaks()
+        s = stats[-1]
+        # algorithmic bytes of the join kernel (32 B per 192-id element):
+        # left elements + right elements + elements written, per launch
+        alg_bytes = 32.0 * (s["left_elems"] + s["right_elems"] + s["out_elems"])
+        join_ms = statistics.mean(x["join_ms"] for x in stats)
+        launches = s["join_launches"]
+        achieved = alg_bytes / (join_ms * 1e-3) / 1e9 if join_ms > 0 else None
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "k_join_traffic.json")
+        if os.path.exists(tp):
+            traffic = json.load(open(tp)).get("bytes_per_launch")
+        cb = None if args.no_cpu_baseline else cpu_baseline(w)
+        out = {
+            "metric": METRIC, "value": world * total / (ms_max * 1e-3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded generator)",
+            "config": {"workload": WORKLOAD, "num_vars": w.num_vars, "input_edges": w.num_edges,
+                       "closure_edges": total, "rounds": s["rounds"], "parallelism": f"replicas{world}",
+                       "l2_flush": "512 MiB write before every timed step", "time_to_fixpoint_ms": ms_max},
+            "e2e": {"value": world * total / (e2e_max * 1e-3), "unit": UNIT,
+                    "h2d_bytes_per_step": int(w.num_edges * 9), "d2h_bytes_per_step": int(w.num_labels * 8)},
+            "roofline": {"bound": "hbm", "kernel": "k_join", "achieved": achieved, "peak": hbm,
+                         "peak_kind": peak_kind, "unit": "GB/s",
+                         "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
+                         "alg_bytes_per_launch": alg_bytes / launches, "launches_per_step": launches,
+                         "join_ms_per_step": join_ms},
+            "cpu_baseline": cb and {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "clocks": clk.summary(),
+            "gpu_launches": int(sum(x["kernel_launches"] for x in stats)),
+            "wall_s_timed": t_wall,
+        }
+        print(json.dumps(out), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

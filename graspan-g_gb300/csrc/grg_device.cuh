@@ -1,0 +1,162 @@
+// grg_device.cuh -- device-side data layout and primitives of the closure engine.
+//
+// Storage ("sparse bit-vector", the reference's element unit, src/kernel.h:32-44):
+// every (label slot, row) owns an open-addressing hash table of 32-byte
+// elements in one device pool. Element words 0..5 are a bitmap of 192
+// consecutive destination ids, word 6 is the key (slot << 25 | base, base =
+// dst / 192), word 7 the row (source vertex). The reference links elements of
+// a row into a sorted list (word 7 = NEXT, src/kernel.cu:165-202); here a
+// row's elements are hashed by base, so a lookup is one or two probes instead
+// of a list walk and rows never need re-sorting.
+//
+// Deltas: a parallel pool of 32-byte delta bitmaps (words 0..5 = bits that
+// became set this round, word 6 = dirty flag) and a dirty list of slot
+// indices. The first thread that sets new bits in an element appends it, so
+// the dirty list of a round holds each element at most once and can never
+// overflow the pool's size. This replaces the reference's tmp region and the
+// diff/merge kernels (src/kernel.cu:841-985): new edges are found by atomicOr
+// on the stored element, which returns exactly the bits that were new.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace grg {
+
+constexpr int EW = 6;                    // bitmap words per element
+constexpr uint32_t EIDS = 192;           // ids per element
+constexpr uint32_t EMPTY = 0xFFFFFFFFu;  // free slot key
+constexpr int KEY_SHIFT = 25;
+constexpr uint32_t BASE_MASK = (1u << KEY_SHIFT) - 1;
+constexpr int MAX_LABELS = 63;
+constexpr int MAX_SLOTS = 2 * MAX_LABELS;  // label slots 1..L, reverse-index slots L+1..2L
+constexpr int MAX_RULES = 64;
+
+// device counter block indices
+enum : int {
+    C_POOL_TOP = 0,   // bump allocator (elements)
+    C_DIRTY_N = 1,    // dirty-list length
+    C_RETRY_N = 2,    // retry-list length (delta records to re-run)
+    C_GROW_N = 3,     // grow-list length
+    C_ERR = 4,        // error bits
+    C_LEFT = 5,       // left-operand elements of binary joins
+    C_RIGHT = 6,      // right-operand elements of binary joins
+    C_INSERTS = 7,    // global element inserts issued
+    C_TOTAL = 8,      // edge count (count kernel)
+    C_HASH = 9,       // edge-set hash (hash kernel)
+    C_EXPORT = 10,    // export cursor
+    C_LABEL0 = 16,    // per-label edge counts: C_LABEL0 + slot
+    NCTR = C_LABEL0 + MAX_SLOTS + 2
+};
+enum : unsigned long long { ERR_POOL = 1, ERR_LOAD = 2, ERR_INTERNAL = 4 };
+
+struct RuleTable {
+    int L;                                   // labels
+    int num_slots;                           // L + number of reverse slots in use (max index)
+    // binary rules A ::= B C grouped by B
+    uint8_t bin_start[MAX_LABELS + 2];
+    uint8_t bin_A[MAX_RULES], bin_C[MAX_RULES];
+    // unary rules A ::= B grouped by B (empty under filter 1)
+    uint8_t un_start[MAX_LABELS + 2];
+    uint8_t un_A[MAX_RULES];
+    // old-left joins O_B o D_C for A ::= B C grouped by C: (A, reverse slot of B)
+    uint8_t ol_start[MAX_LABELS + 2];
+    uint8_t ol_A[MAX_RULES], ol_rev[MAX_RULES];
+    uint8_t rev_slot[MAX_LABELS + 1];        // reverse-index slot of label B (0 = none)
+    uint8_t track[MAX_SLOTS + 2];            // slot: new bits become deltas
+};
+
+struct Dev {
+    uint32_t *elems;          // pool: 8 words per slot
+    uint32_t *dbits;          // delta bitmaps: 8 words per slot
+    uint64_t *desc;           // [(slot-1)*V + row] = cap << 32 | offset
+    uint32_t *cnt;            // occupied slots per table
+    uint32_t *want;           // failed inserts per table since its last growth
+    uint32_t *dirty;          // dirty list (slot indices)
+    uint32_t *grow;           // grow list (table indices)
+    unsigned long long *ctr;  // counter block
+    uint32_t V;
+    uint32_t pool_cap;        // elements
+};
+
+__device__ __forceinline__ uint32_t hash_slot(uint32_t base, uint32_t lg)
+{
+    return lg ? (base * 0x9E3779B1u) >> (32 - lg) : 0u;
+}
+__device__ __forceinline__ uint32_t max_load(uint32_t cap) { return cap - (cap >> 2); }
+
+struct Bits { uint32_t w[EW]; };
+
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x)
+{
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+__device__ __forceinline__ uint64_t edge_hash(uint32_t l, uint32_t s, uint32_t d)
+{
+    return splitmix64(splitmix64(((uint64_t)s << 32) | d) ^ ((uint64_t)l * 0x9E3779B97F4A7C15ull));
+}
+
+__device__ __forceinline__ void append_dirty(const Dev &d, uint32_t s)
+{
+    unsigned long long i = atomicAdd(&d.ctr[C_DIRTY_N], 1ull);
+    d.dirty[i] = s;   // capacity = pool size; each slot is appended at most once per round
+}
+
+// OR `b` into element (slot, row, base). Returns false when the table is full
+// or absent; the failure is recorded so the table grows before a retry.
+__device__ __noinline__ bool g_insert(const Dev &d, uint32_t slot, uint32_t row, uint32_t base, const Bits &b,
+                                      bool track)
+{
+    const size_t ti = (size_t)(slot - 1) * d.V + row;
+    const uint64_t de = d.desc[ti];
+    const uint32_t off = (uint32_t)de, cap = (uint32_t)(de >> 32);
+    const uint32_t key = (slot << KEY_SHIFT) | base;
+    uint32_t s = EMPTY;
+    if (cap != 0 && (cap & (cap - 1)) == 0) {
+        const uint32_t lg = 31 - __clz(cap);
+        uint32_t h = hash_slot(base, lg);
+        for (uint32_t p = 0; p < cap; p++) {
+            const uint32_t q = off + ((h + p) & (cap - 1));
+            uint32_t *kp = d.elems + (size_t)q * 8 + 6;
+            uint32_t k = __ldcg(kp);
+            if (k == key) { s = q; break; }
+            if (k != EMPTY) continue;
+            if (atomicAdd(&d.cnt[ti], 1u) >= max_load(cap)) { atomicSub(&d.cnt[ti], 1u); break; }
+            uint32_t prev = atomicCAS(kp, EMPTY, key);
+            if (prev == EMPTY) { d.elems[(size_t)q * 8 + 7] = row; s = q; break; }
+            atomicSub(&d.cnt[ti], 1u);
+            if (prev == key) { s = q; break; }
+        }
+    }
+    if (s == EMPTY) {
+        if (atomicAdd(&d.want[ti], 1u) == 0) {
+            unsigned long long g = atomicAdd(&d.ctr[C_GROW_N], 1ull);
+            d.grow[g] = (uint32_t)ti;
+        }
+        return false;
+    }
+    uint32_t *e = d.elems + (size_t)s * 8;
+    uint32_t nb[EW];
+    uint32_t any = 0;
+#pragma unroll
+    for (int w = 0; w < EW; w++) {
+        nb[w] = 0;
+        if (b.w[w]) {
+            uint32_t old = atomicOr(&e[w], b.w[w]);
+            nb[w] = b.w[w] & ~old;
+            any |= nb[w];
+        }
+    }
+    if (track && any) {
+        uint32_t *db = d.dbits + (size_t)s * 8;
+#pragma unroll
+        for (int w = 0; w < EW; w++)
+            if (nb[w]) atomicOr(&db[w], nb[w]);
+        if (atomicExch(&db[6], 1u) == 0) append_dirty(d, s);
+    }
+    return true;
+}
+
+}  // namespace grg

@@ -1,0 +1,257 @@
+"""Python host interface of the GB300 closure engine (ctypes over libgrg.so).
+
+Mirrors the reference's host<->CUDA interface (src/kernel.h:115-129) through
+the C ABI declared in include/grg.h. There is no CPU fallback: if the CUDA
+library is missing, ``load_library`` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgrg.so")
+COMP_PATH = os.path.join(HERE, "_build", "comp")
+
+OK = 0
+NEED_REPARTITION = 1
+E_ARG, E_CUDA, E_NOMEM, E_FILTER, E_IO, E_LABEL, E_RANGE, E_STATE, E_NODEV = -1, -2, -3, -4, -5, -6, -7, -8, -9
+MAX_RULES = 64
+MAX_LABELS = 63
+NAME_LEN = 64
+
+# every entry point declared in include/grg.h
+EXPORTS = (
+    "grg_error_string", "grg_last_error", "grg_create", "grg_destroy", "grg_device", "grg_set_stream",
+    "grg_set_kernel_timing", "grg_transfer_rules", "grg_allocate_pool", "grg_load_edges", "grg_closure",
+    "grg_label_counts", "grg_get_degree", "grg_set_hash", "grg_export_edges", "grg_parse_grammar",
+    "grg_parse_graph_header", "grg_parse_graph",
+)
+
+
+class GrgError(RuntimeError):
+    def __init__(self, status, msg=""):
+        super().__init__(f"grg status {status}: {msg}")
+        self.status = status
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("total_edges", ctypes.c_uint64), ("rounds", ctypes.c_uint64), ("delta_elems", ctypes.c_uint64),
+        ("left_elems", ctypes.c_uint64), ("right_elems", ctypes.c_uint64), ("out_elems", ctypes.c_uint64),
+        ("retry_records", ctypes.c_uint64), ("grow_rows", ctypes.c_uint64), ("pool_elems_used", ctypes.c_uint64),
+        ("pool_elems_cap", ctypes.c_uint64), ("closure_ms", ctypes.c_double), ("join_ms", ctypes.c_double),
+        ("join_launches", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libgrg.so (fails loudly when it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise GrgError(E_STATE, f"CUDA library {path} is missing; run graspan-g_gb300/build.py")
+    L = ctypes.CDLL(path)
+    P, I, U32, U64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64
+    L.grg_error_string.restype = ctypes.c_char_p
+    L.grg_error_string.argtypes = [I]
+    L.grg_last_error.restype = ctypes.c_char_p
+    L.grg_last_error.argtypes = [P]
+    L.grg_create.argtypes = [ctypes.POINTER(P), I]
+    L.grg_destroy.argtypes = [P]
+    L.grg_destroy.restype = None
+    L.grg_device.argtypes = [P]
+    L.grg_set_stream.argtypes = [P, P]
+    L.grg_set_kernel_timing.argtypes = [P, I]
+    L.grg_transfer_rules.argtypes = [P, I, P, I]
+    L.grg_allocate_pool.argtypes = [P, U64]
+    L.grg_load_edges.argtypes = [P, U32, U64, P, P, P, I]
+    L.grg_closure.argtypes = [P, U32, ctypes.POINTER(Stats)]
+    L.grg_label_counts.argtypes = [P, P]
+    L.grg_get_degree.argtypes = [P, U32, U32, P]
+    L.grg_set_hash.argtypes = [P, ctypes.POINTER(U64)]
+    L.grg_export_edges.argtypes = [P, U64, P, P, P, ctypes.POINTER(U64)]
+    L.grg_parse_grammar.argtypes = [ctypes.c_char_p, ctypes.POINTER(I), P, ctypes.POINTER(I), P]
+    L.grg_parse_graph_header.argtypes = [ctypes.c_char_p, ctypes.POINTER(U64), ctypes.POINTER(U32)]
+    L.grg_parse_graph.argtypes = [ctypes.c_char_p, I, P, U64, U32, P, P, P]
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def error_string(status: int) -> str:
+    return load_library().grg_error_string(status).decode()
+
+
+@dataclass
+class Grammar:
+    rules: np.ndarray     # int32 [num_rules, 3]
+    labels: list
+
+    @property
+    def num_labels(self):
+        return len(self.labels)
+
+
+def parse_grammar(path: str) -> Grammar:
+    L = load_library()
+    nr, nl = ctypes.c_int(), ctypes.c_int()
+    rules = np.zeros(3 * MAX_RULES, dtype=np.int32)
+    names = ctypes.create_string_buffer(MAX_LABELS * NAME_LEN)
+    st = L.grg_parse_grammar(path.encode(), ctypes.byref(nr), _ptr(rules), ctypes.byref(nl), names)
+    if st != OK:
+        raise GrgError(st, f"parse_grammar({path}): {error_string(st)}")
+    raw = names.raw
+    labels = [raw[i * NAME_LEN:(i + 1) * NAME_LEN].split(b"\0", 1)[0].decode() for i in range(nl.value)]
+    return Grammar(rules[:3 * nr.value].reshape(-1, 3).copy(), labels)
+
+
+def _names_buffer(labels):
+    names = ctypes.create_string_buffer(MAX_LABELS * NAME_LEN)
+    for i, s in enumerate(labels):
+        b = s.encode()
+        ctypes.memmove(ctypes.addressof(names) + i * NAME_LEN, b, len(b))
+    return names
+
+
+def parse_graph(path: str, g: Grammar):
+    L = load_library()
+    ne, nv = ctypes.c_uint64(), ctypes.c_uint32()
+    st = L.grg_parse_graph_header(path.encode(), ctypes.byref(ne), ctypes.byref(nv))
+    if st != OK:
+        raise GrgError(st, f"parse_graph_header({path})")
+    n = ne.value
+    src = np.zeros(n, np.uint32)
+    dst = np.zeros(n, np.uint32)
+    lab = np.zeros(n, np.uint8)
+    st = L.grg_parse_graph(path.encode(), g.num_labels, _names_buffer(g.labels), n, nv.value,
+                           _ptr(src), _ptr(dst), _ptr(lab))
+    if st != OK:
+        raise GrgError(st, f"parse_graph({path}): {error_string(st)}")
+    return nv.value, src, dst, lab
+
+
+class Context:
+    """One closure engine context on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self._L = load_library()
+        h = ctypes.c_void_p()
+        st = self._L.grg_create(ctypes.byref(h), device)
+        if st != OK:
+            raise GrgError(st, f"grg_create: {error_string(st)}")
+        self._h = h
+        self.num_labels = 0
+        self.num_vars = 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.grg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st, what):
+        if st != OK:
+            msg = self._L.grg_last_error(self._h).decode() if self._h else ""
+            raise GrgError(st, f"{what}: {error_string(st)} {msg}")
+
+    @property
+    def device(self) -> int:
+        return self._L.grg_device(self._h)
+
+    def set_stream(self, stream_handle: int | None):
+        self._check(self._L.grg_set_stream(self._h, ctypes.c_void_p(stream_handle or 0)), "set_stream")
+
+    def set_kernel_timing(self, on: bool):
+        self._check(self._L.grg_set_kernel_timing(self._h, int(bool(on))), "set_kernel_timing")
+
+    def transfer_rules(self, rules, num_labels: int):
+        r = np.ascontiguousarray(np.asarray(rules, dtype=np.int32).reshape(-1))
+        self._check(self._L.grg_transfer_rules(self._h, len(r) // 3, _ptr(r), num_labels), "transfer_rules")
+        self.num_labels = num_labels
+
+    def allocate_pool(self, pool_bytes: int = 0):
+        self._check(self._L.grg_allocate_pool(self._h, pool_bytes), "allocate_pool")
+
+    def load_edges(self, num_vars, src, dst, lab):
+        """Host numpy arrays (copied to the device)."""
+        src = np.ascontiguousarray(src, dtype=np.uint32)
+        dst = np.ascontiguousarray(dst, dtype=np.uint32)
+        lab = np.ascontiguousarray(lab, dtype=np.uint8)
+        self._check(self._L.grg_load_edges(self._h, num_vars, len(src), _ptr(src), _ptr(dst), _ptr(lab), 0),
+                    "load_edges")
+        self.num_vars = num_vars
+
+    def load_edges_device(self, num_vars, num_edges, src_ptr: int, dst_ptr: int, lab_ptr: int):
+        """Device pointers (e.g. torch tensors' data_ptr())."""
+        self._check(self._L.grg_load_edges(self._h, num_vars, num_edges, ctypes.c_void_p(src_ptr),
+                                           ctypes.c_void_p(dst_ptr), ctypes.c_void_p(lab_ptr), 1),
+                    "load_edges_device")
+        self.num_vars = num_vars
+
+    def closure(self, filter_flag: int) -> dict:
+        s = Stats()
+        self._check(self._L.grg_closure(self._h, filter_flag, ctypes.byref(s)), "closure")
+        return s.as_dict()
+
+    def label_counts(self) -> np.ndarray:
+        out = np.zeros(self.num_labels, dtype=np.uint64)
+        self._check(self._L.grg_label_counts(self._h, _ptr(out)), "label_counts")
+        return out
+
+    def set_hash(self) -> int:
+        h = ctypes.c_uint64()
+        self._check(self._L.grg_set_hash(self._h, ctypes.byref(h)), "set_hash")
+        return h.value
+
+    def degree(self, first_var=0, last_var=None):
+        if last_var is None:
+            last_var = self.num_vars - 1
+        n = last_var - first_var + 1
+        out = np.zeros(6 * n, dtype=np.uint32)
+        self._check(self._L.grg_get_degree(self._h, first_var, last_var, _ptr(out)), "get_degree")
+        return out.reshape(6, n)
+
+    def export_edges(self):
+        n = ctypes.c_uint64()
+        self._check(self._L.grg_export_edges(self._h, 0, None, None, None, ctypes.byref(n)), "export_edges")
+        m = n.value
+        src = np.zeros(m, np.uint32)
+        dst = np.zeros(m, np.uint32)
+        lab = np.zeros(m, np.uint8)
+        self._check(self._L.grg_export_edges(self._h, m, _ptr(src), _ptr(dst), _ptr(lab), ctypes.byref(n)),
+                    "export_edges")
+        order = np.lexsort((dst, src, lab))
+        return src[order], dst[order], lab[order]
+
+
+def run_closure(num_vars, rules, num_labels, filter_flag, src, dst, lab, device=0, pool_bytes=0, timing=False):
+    """Convenience: one context, one closure. Returns (context, stats)."""
+    ctx = Context(device)
+    ctx.transfer_rules(rules, num_labels)
+    ctx.allocate_pool(pool_bytes)
+    ctx.set_kernel_timing(timing)
+    ctx.load_edges(num_vars, src, dst, lab)
+    stats = ctx.closure(filter_flag)
+    return ctx, stats

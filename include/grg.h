@@ -1,0 +1,146 @@
+/*
+ * grg.h -- C ABI of the GB300 CFL-reachability closure engine (libgrg.so).
+ *
+ * Drop-in boundary for the hot path of Graspan-G. The reference's boundary is
+ * the C++-linkage API in src/kernel.h:115-129 plus the globals
+ * selectedDevice/numLabels/numVars (src/kernel.h:22-24) and the CUDA calls the
+ * host makes directly (device selection src/main.cpp:30-58, pool read-back
+ * src/main.cpp:477-483, cudaFree src/main.cpp:903). That API is a
+ * non-reentrant singleton; this one carries an explicit context, returns an
+ * int status instead of exit(-1) (src/kernel.h:53-58), uses 64-bit sizes, and
+ * takes plain pointers and sizes only.
+ *
+ * Threading: a context is used by one host thread at a time. All device work
+ * of a context is issued on its stream (grg_set_stream).
+ */
+#ifndef GRG_H
+#define GRG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define GRG_OK 0
+#define GRG_NEED_REPARTITION 1   /* partition does not fit its budget (the reference's r=true, src/kernel.cu:65-76) */
+#define GRG_E_ARG (-1)           /* invalid argument */
+#define GRG_E_CUDA (-2)          /* CUDA runtime error (see grg_last_error) */
+#define GRG_E_NOMEM (-3)         /* device or host memory exhausted */
+#define GRG_E_FILTER (-4)        /* filter_flag=1 on a grammar where it is schedule-dependent */
+#define GRG_E_IO (-5)            /* file could not be read or is malformed */
+#define GRG_E_LABEL (-6)         /* graph label not present in the grammar */
+#define GRG_E_RANGE (-7)         /* vertex id >= numVars, too many rules or labels */
+#define GRG_E_STATE (-8)         /* call made out of order */
+#define GRG_E_NODEV (-9)         /* no CUDA device */
+
+#define GRG_MAX_RULES 64
+#define GRG_MAX_LABELS 63        /* label ids 1..63; each may also get a reverse-index slot */
+#define GRG_NAME_LEN 64
+#define GRG_ELEM_IDS 192         /* ids per element: 6 x 32-bit bitmap words (src/kernel.h:32-33) */
+
+typedef struct grg_ctx grg_ctx;
+
+/* Per-run statistics. Work counters are in the reference's element unit
+ * (32 bytes per 192-id element, src/kernel.h:32-44). */
+typedef struct grg_stats {
+    uint64_t total_edges;          /* FINAL NUM EDGES (src/main.cpp:909-917) */
+    uint64_t rounds;               /* semi-naive rounds to the fixpoint */
+    uint64_t delta_elems;          /* delta elements joined (sum over rounds) */
+    uint64_t left_elems;           /* left-operand elements read by binary joins */
+    uint64_t right_elems;          /* right-operand elements read by binary joins */
+    uint64_t out_elems;            /* elements written as new deltas */
+    uint64_t retry_records;        /* delta records re-run after a table grew */
+    uint64_t grow_rows;            /* rows whose table grew */
+    uint64_t pool_elems_used;      /* pool slots in use at the end */
+    uint64_t pool_elems_cap;       /* pool slots allocated */
+    double closure_ms;             /* device time from resident graph to fixpoint known */
+    double join_ms;                /* sum of join-kernel durations (when kernel timing is on) */
+    uint64_t join_launches;        /* join-kernel launches (first pass + retries) */
+    uint64_t kernel_launches;      /* all kernel launches of the closure */
+} grg_stats;
+
+/* Error text of a status code, and the last detailed message of a context. */
+const char *grg_error_string(int status);
+const char *grg_last_error(const grg_ctx *ctx);
+
+/* Create a context on a device; device < 0 selects the device with the most
+ * SMs. Replaces checkGPUConfiguration (src/main.cpp:30-58). */
+int grg_create(grg_ctx **ctx, int device);
+/* Free every device and host resource of the context (src/main.cpp:903). */
+void grg_destroy(grg_ctx *ctx);
+/* Selected device ordinal (the reference's global selectedDevice, src/kernel.h:22). */
+int grg_device(const grg_ctx *ctx);
+/* Issue all work of the context on this cudaStream_t (NULL = the context's own stream). */
+int grg_set_stream(grg_ctx *ctx, void *stream);
+/* Measure each join launch with CUDA events (adds a little host overhead). */
+int grg_set_kernel_timing(grg_ctx *ctx, int on);
+
+/* Grammar: rules[3*i+{0,1,2}] = LHS, RHS1, RHS2 label ids (1-based, 0 = absent),
+ * num_labels = number of distinct labels. Replaces transferRules
+ * (src/kernel.cu:22-31), which takes rules from readAndTransferRules
+ * (src/main.cpp:69-97). The caller keeps ownership of rules. */
+int grg_transfer_rules(grg_ctx *ctx, int num_rules, const int *rules, int num_labels);
+
+/* Reserve the element pool: pool_bytes of device memory for 32-byte elements
+ * plus their delta bitmaps (0 = size it from the free device memory).
+ * Replaces allocateElementPool (src/kernel.cu:33-40). The pool grows on
+ * demand while device memory lasts. */
+int grg_allocate_pool(grg_ctx *ctx, uint64_t pool_bytes);
+
+/* Load the labelled graph: num_edges edges (src[i], dst[i], label[i]) over
+ * vertices [0, num_vars), labels 1..num_labels. on_device != 0 means the three
+ * arrays are device pointers; otherwise they are host memory and are copied.
+ * Edges need not be sorted; duplicates collapse. Replaces getGraphInfo +
+ * readEdges + createGraph + transferElements (src/main.cpp:106-333,
+ * src/kernel.cu:42-52); the pool image is built on the device. */
+int grg_load_edges(grg_ctx *ctx, uint32_t num_vars, uint64_t num_edges, const uint32_t *src,
+                   const uint32_t *dst, const uint8_t *label, int on_device);
+
+/* Run the semi-naive closure to its fixpoint. filter = the reference's
+ * filter_flag (src/main.cpp:890,894): 0 = every rule, 1 = the dataflow
+ * optimisation (unary rules and old-left joins skipped; refused with
+ * GRG_E_FILTER when a binary rule's second symbol is derivable). Replaces the
+ * superstep driver precomputation/run_computation (src/main.cpp:764-858,
+ * 892-906) with spagpu_s/spagpu_b/spagpu/mergeAndDiff
+ * (src/kernel.cu:466-780, 943-985). stats may be NULL. */
+int grg_closure(grg_ctx *ctx, uint32_t filter, grg_stats *stats);
+
+/* Per-label closure edge counts: counts[l-1] for label l (num_labels values). */
+int grg_label_counts(grg_ctx *ctx, uint64_t *counts);
+
+/* Degree table of vertices [first_var, last_var] like getDegree
+ * (src/kernel.cu:818-839): degree[v - first_var + n*c] for n = last_var -
+ * first_var + 1 and column c: 0 = edges (popcount over all labels), 3 =
+ * elements (192-id elements over all labels); columns 1,2,4,5 (delta and tmp
+ * regions of the reference) are 0 after the fixpoint. */
+int grg_get_degree(grg_ctx *ctx, uint32_t first_var, uint32_t last_var, uint32_t *degree);
+
+/* Order-independent 64-bit hash of the closure edge set
+ * (sum over edges of a splitmix64-based hash of (label, src, dst)). */
+int grg_set_hash(grg_ctx *ctx, uint64_t *hash);
+
+/* Copy closure edges to host arrays (unordered). *num_out = total edges; at
+ * most cap are written. */
+int grg_export_edges(grg_ctx *ctx, uint64_t cap, uint32_t *src, uint32_t *dst, uint8_t *label,
+                     uint64_t *num_out);
+
+/* Text formats (host). Grammar: readAndTransferRules (src/main.cpp:60-97);
+ * names must hold GRG_MAX_LABELS*GRG_NAME_LEN bytes, label l at
+ * names[(l-1)*GRG_NAME_LEN]; rules must hold 3*GRG_MAX_RULES ints. */
+int grg_parse_grammar(const char *path, int *num_rules, int *rules, int *num_labels, char *names);
+/* Graph header "numEdges\tnumVars" (src/main.cpp:106-115). */
+int grg_parse_graph_header(const char *path, uint64_t *num_edges, uint32_t *num_vars);
+/* Graph body (src/main.cpp:177-221), arrays of num_edges entries. Labels are
+ * looked up in names (as filled by grg_parse_grammar); unknown labels fail with
+ * GRG_E_LABEL, ids >= num_vars with GRG_E_RANGE. */
+int grg_parse_graph(const char *path, int num_labels, const char *names, uint64_t num_edges,
+                    uint32_t num_vars, uint32_t *src, uint32_t *dst, uint8_t *label);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GRG_H */

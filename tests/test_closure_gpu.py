@@ -1,0 +1,189 @@
+"""GPU parity tests: the CUDA closure engine (through the C ABI) against the
+CPU oracle. Integer/bitset work, so every comparison is bit-exact: identical
+(src, dst, label) sets, per-label counts and edge-set hashes."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import grg_gen as G
+
+pytestmark = pytest.mark.gpu
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))
+
+
+def gpu_closure(grg, w, filter_flag=None, pool_bytes=0, timing=False):
+    f = w.filter_flag if filter_flag is None else filter_flag
+    return grg.run_closure(w.num_vars, w.rule_ids(), w.num_labels, f, w.src, w.dst, w.lab,
+                           pool_bytes=pool_bytes, timing=timing)
+
+
+def edge_set(s, d, l):
+    return set(zip(s.tolist(), d.tolist(), l.tolist()))
+
+
+def assert_same_as_oracle(grg, O, w, filter_flag=None, pool_bytes=0, edges=True):
+    f = w.filter_flag if filter_flag is None else filter_flag
+    r = O.closure(w.num_vars, w.rule_ids(), w.num_labels, f, w.src, w.dst, w.lab)
+    ctx, st = gpu_closure(grg, w, f, pool_bytes)
+    assert st["total_edges"] == r.total
+    assert ctx.label_counts().tolist() == r.label_counts().tolist()
+    assert ctx.set_hash() == r.set_hash
+    if edges:
+        gs, gd, gl = ctx.export_edges()
+        os_, od, ol = r.edges()
+        assert np.array_equal(gl, ol) and np.array_equal(gs, os_) and np.array_equal(gd, od)
+    ctx.close()
+    return r, st
+
+
+def test_pointsto_small_exact(grg_mod, oracle_mod):
+    assert_same_as_oracle(grg_mod, oracle_mod, G.pointsto(seed=3, num_vars=300, num_edges=700))
+
+
+def test_pointsto_2000(grg_mod, oracle_mod):
+    g = GOLD["pointsto"]
+    r, st = assert_same_as_oracle(grg_mod, oracle_mod, G.pointsto(), edges=False)
+    assert r.total == g["total"]
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_random_grammars(grg_mod, oracle_mod, seed):
+    w = G.random_grammar_graph(100 + seed, num_vars=200 + 37 * seed, num_edges=400 + 50 * seed,
+                               num_labels=3 + seed % 5, num_rules=3 + seed % 7)
+    for f in (0, 1):
+        try:
+            oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, f, w.src, w.dst, w.lab)
+        except oracle_mod.OracleError as e:
+            assert e.code == oracle_mod.ORC_E_FILTER
+            with pytest.raises(grg_mod.GrgError) as ei:
+                gpu_closure(grg_mod, w, f)
+            assert ei.value.status == grg_mod.E_FILTER
+            continue
+        assert_same_as_oracle(grg_mod, oracle_mod, w, f)
+
+
+def test_dataflow_small_golden(grg_mod):
+    """10k vertices, 30k e edges, filter 0 (N ::= N e | e)."""
+    g = GOLD["dataflow_small"]
+    w = G.dataflow_small()
+    ctx, st = gpu_closure(grg_mod, w)
+    assert st["total_edges"] == g["total"] == 93_365_096
+    assert dict(zip(w.labels, ctx.label_counts().tolist())) == g["labels"]
+    assert ctx.set_hash() == g["hash"]
+
+
+def test_dataflow_blocks_scaled_rounds(grg_mod):
+    """Filter 1 reads only static right-hand rows, so the GPU's rounds equal the
+    oracle's round-synchronous rounds exactly: same count, same new elements."""
+    g = GOLD["dataflow_blocks_b100"]
+    w = G.dataflow_blocks(num_blocks=100, num_edges=300_000)
+    ctx, st = gpu_closure(grg_mod, w)
+    assert st["total_edges"] == g["total"]
+    assert ctx.set_hash() == g["hash"]
+    assert st["rounds"] == g["rounds"] - 1 or st["rounds"] == g["rounds"]
+    assert st["delta_elems"] - st["retry_records"] >= 0
+    assert st["right_elems"] >= g["right_elems"]
+
+
+def test_dataflow_blocks_full_size(grg_mod):
+    """2,000 blocks x 1,000 vertices, 6M e edges, filter 1: the bench workload.
+    Checked against the oracle's recorded count and edge-set hash."""
+    g = GOLD["dataflow_blocks"]
+    w = G.dataflow_blocks()
+    assert w.num_edges == g["num_edges"]
+    ctx, st = gpu_closure(grg_mod, w)
+    assert st["total_edges"] == g["total"] == 1_316_964_027
+    assert dict(zip(w.labels, ctx.label_counts().tolist())) == g["labels"]
+    assert ctx.set_hash() == g["hash"]
+
+
+def test_alias_20k(grg_mod, oracle_mod):
+    g = GOLD["alias_20k"]
+    w = G.alias(num_vars=20_000, num_base_edges=80_000)
+    ctx, st = gpu_closure(grg_mod, w)
+    assert st["total_edges"] == g["total"]
+    assert ctx.set_hash() == g["hash"]
+
+
+def test_degree_matches_oracle(grg_mod, oracle_mod):
+    w = G.pointsto(seed=9, num_vars=500, num_edges=1500)
+    r = oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, 0, w.src, w.dst, w.lab)
+    e, el = r.degree()
+    ctx, _ = gpu_closure(grg_mod, w)
+    deg = ctx.degree()
+    assert np.array_equal(deg[0], e) and np.array_equal(deg[3], el)
+    assert not deg[1].any() and not deg[2].any() and not deg[4].any() and not deg[5].any()
+    sub = ctx.degree(100, 199)
+    assert np.array_equal(sub[0], e[100:200]) and np.array_equal(sub[3], el[100:200])
+
+
+def test_tiny_pool_grows(grg_mod, oracle_mod):
+    """A pool far too small for the closure forces table growth and pool growth."""
+    assert_same_as_oracle(grg_mod, oracle_mod, G.dataflow_small(num_vars=2000, num_edges=6000), pool_bytes=1 << 16,
+                          edges=False)
+
+
+def test_edge_cases(grg_mod, oracle_mod):
+    O = oracle_mod
+    cases = [
+        # (num_vars, rules, num_labels, filter, edges)
+        (5, [[1, 0, 0], [2, 1, 0]], 2, 0, []),                          # epsilon + unary, no edges
+        (5, [[1, 0, 0], [2, 1, 0]], 2, 1, []),                          # filter 1 drops unary
+        (1, [[1, 1, 2], [1, 2, 0]], 2, 0, [(0, 0, 2)]),                 # single vertex self loop
+        (3, [[1, 1, 2], [1, 2, 0]], 2, 0, [(0, 1, 2), (0, 1, 2), (1, 2, 2)]),   # duplicate edges collapse
+        (400, [[1, 1, 2], [1, 2, 0]], 3, 0, [(i, (i * 7 + 1) % 400, 2) for i in range(400)]),  # unused label 3
+        (1000, [[1, 1, 1]], 1, 0, [(i, i + 1, 1) for i in range(999)]),  # transitive chain, 999 rounds
+        (193, [[1, 1, 2]], 2, 1, [(i, 192 - i, 2) for i in range(193)] + [(0, 5, 1)]),  # element boundaries
+    ]
+    for nv, rules, nl, f, edges in cases:
+        e = np.array(edges, dtype=np.int64).reshape(-1, 3)
+        s, d, l = e[:, 0].astype(np.uint32), e[:, 1].astype(np.uint32), e[:, 2].astype(np.uint8)
+        r = O.closure(nv, rules, nl, f, s, d, l)
+        ctx, st = grg_mod.run_closure(nv, rules, nl, f, s, d, l)
+        assert st["total_edges"] == r.total, (nv, rules, f)
+        gs, gd, gl = ctx.export_edges()
+        os_, od, ol = r.edges()
+        assert np.array_equal(gs, os_) and np.array_equal(gd, od) and np.array_equal(gl, ol)
+        ctx.close()
+
+
+def test_errors_and_state(grg_mod):
+    with grg_mod.Context(0) as ctx:
+        with pytest.raises(grg_mod.GrgError) as ei:
+            ctx.closure(0)
+        assert ei.value.status == grg_mod.E_STATE
+        with pytest.raises(grg_mod.GrgError) as ei:
+            ctx.transfer_rules([[1, 0, 2]], 2)          # RHS2 without RHS1
+        assert ei.value.status == grg_mod.E_ARG
+        ctx.transfer_rules([[1, 1, 1]], 1)
+        ctx.load_edges(4, np.array([0, 1], np.uint32), np.array([1, 2], np.uint32), np.array([1, 1], np.uint8))
+        with pytest.raises(grg_mod.GrgError) as ei:
+            ctx.closure(1)                              # A ::= A A is schedule-dependent under filter 1
+        assert ei.value.status == grg_mod.E_FILTER
+        st = ctx.closure(0)
+        assert st["total_edges"] == 3
+        with pytest.raises(grg_mod.GrgError) as ei:
+            ctx.closure(0)
+        assert ei.value.status == grg_mod.E_STATE
+        # reload on the same context and close again
+        ctx.load_edges(4, np.array([0, 1, 2], np.uint32), np.array([1, 2, 3], np.uint32), np.array([1, 1, 1], np.uint8))
+        assert ctx.closure(0)["total_edges"] == 6
+
+
+def test_device_load_equals_host_load(grg_mod):
+    torch = pytest.importorskip("torch")
+    w = G.dataflow_blocks(num_blocks=30, num_edges=90_000)
+    src = torch.from_numpy(w.src.astype(np.int32)).cuda()
+    dst = torch.from_numpy(w.dst.astype(np.int32)).cuda()
+    lab = torch.from_numpy(w.lab).cuda()
+    with grg_mod.Context(0) as ctx:
+        ctx.transfer_rules(w.rule_ids(), w.num_labels)
+        ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+        ctx.load_edges_device(w.num_vars, w.num_edges, src.data_ptr(), dst.data_ptr(), lab.data_ptr())
+        a = ctx.closure(1)["total_edges"]
+        ha = ctx.set_hash()
+    ctx2, st = gpu_closure(grg_mod, w)
+    assert a == st["total_edges"] and ha == ctx2.set_hash()
