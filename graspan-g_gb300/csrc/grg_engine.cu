@@ -1187,3 +1187,257 @@ int grg_export_edges(grg_ctx *c, uint64_t cap, uint32_t *src, uint32_t *dst, uin
 }
 
 }  // extern "C"
+
+// ====================================================================== allocation-free closure
+//
+// grg_closure_noalloc runs the same kernels as grg_load_edges + grg_closure,
+// but every scratch buffer they need (element pool, delta bitmaps, dirty and
+// retry lists, delta records, table descriptors, counters) lives in one
+// file-scope device array of fixed size instead of cudaMalloc'd memory. It is
+// for callers that cannot allocate device memory while they run: a serving
+// loop whose device memory is owned by another allocator or budget, or a
+// process that must not let cudaMalloc/cudaFree synchronize the device while
+// other jobs are in flight. Every GPU that loads this library reserves the
+// array until the process exits.
+
+namespace grg {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = 64ull << 20;   // GRG_NOALLOC_SCRATCH_BYTES in grg.h
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+// Device address of g_noalloc_scratch per device ordinal, looked up once per
+// device with that device current (the host-side symbol is not a device address).
+static void *g_noalloc_addr[256];
+
+static inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Rule table for the allocation-free path (same rules as build_rules, without a context).
+static int noalloc_rules(const int *rules, int R, int L, uint32_t filter, RuleTable &rt, bool *derivable)
+{
+    memset(&rt, 0, sizeof rt);
+    rt.L = L;
+    for (int l = 0; l <= MAX_LABELS; l++) derivable[l] = false;
+    for (int q = 0; q < R; q++) {
+        const int *r = &rules[3 * q];
+        const bool unary = r[1] && !r[2];
+        if (!(filter && unary)) derivable[r[0]] = true;
+    }
+    bool need_ol[GRG_MAX_RULES] = {false};
+    for (int q = 0; q < R; q++) {
+        const int *r = &rules[3 * q];
+        if (r[1] && r[2] && derivable[r[2]]) {
+            if (filter) return GRG_E_FILTER;
+            need_ol[q] = true;
+        }
+    }
+    int next_rev = L + 1;
+    for (int q = 0; q < R; q++)
+        if (need_ol[q] && !rt.rev_slot[rules[3 * q + 1]]) rt.rev_slot[rules[3 * q + 1]] = (uint8_t)next_rev++;
+    rt.num_slots = next_rev - 1;
+    int k = 0;
+    for (int B = 1; B <= L + 1; B++) {
+        rt.bin_start[B] = (uint8_t)k;
+        if (B > L) break;
+        for (int q = 0; q < R; q++)
+            if (rules[3 * q + 1] == B && rules[3 * q + 2]) {
+                rt.bin_A[k] = (uint8_t)rules[3 * q];
+                rt.bin_C[k] = (uint8_t)rules[3 * q + 2];
+                k++;
+            }
+    }
+    k = 0;
+    for (int B = 1; B <= L + 1; B++) {
+        rt.un_start[B] = (uint8_t)k;
+        if (B > L || filter) continue;
+        for (int q = 0; q < R; q++)
+            if (rules[3 * q + 1] == B && !rules[3 * q + 2]) rt.un_A[k++] = (uint8_t)rules[3 * q];
+    }
+    k = 0;
+    for (int C = 1; C <= L + 1; C++) {
+        rt.ol_start[C] = (uint8_t)k;
+        if (C > L) break;
+        for (int q = 0; q < R; q++)
+            if (need_ol[q] && rules[3 * q + 2] == C) {
+                rt.ol_A[k] = (uint8_t)rules[3 * q];
+                rt.ol_rev[k] = rt.rev_slot[rules[3 * q + 1]];
+                k++;
+            }
+    }
+    for (int q = 0; q < R; q++) {
+        const int *r = &rules[3 * q];
+        const bool unary = r[1] && !r[2];
+        if (r[1] && !(filter && unary)) rt.track[r[1]] = 1;
+        if (need_ol[q]) rt.track[r[2]] = 1;
+    }
+    return GRG_OK;
+}
+
+}  // namespace grg
+
+#define NA_CUDA(call)                                   \
+    do {                                                \
+        if ((call) != cudaSuccess) return GRG_E_CUDA;   \
+    } while (0)
+
+static int na_read(unsigned long long *h, const unsigned long long *ctr, cudaStream_t s)
+{
+    // pageable destination: no pinned buffer is needed (or allocated) by this path
+    NA_CUDA(cudaMemcpyAsync(h, ctr, sizeof(unsigned long long) * NCTR, cudaMemcpyDeviceToHost, s));
+    NA_CUDA(cudaStreamSynchronize(s));
+    return GRG_OK;
+}
+
+namespace {
+// restores the caller's current device on every return path
+struct DeviceGuard {
+    int prev = -1;
+    ~DeviceGuard()
+    {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+}  // namespace
+
+extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, const int *rules, int num_labels,
+                                   uint32_t filter, uint32_t num_vars, uint64_t num_edges, const uint32_t *d_src,
+                                   const uint32_t *d_dst, const uint8_t *d_label, uint64_t *d_label_counts,
+                                   uint64_t *d_set_hash, uint64_t *rounds_out)
+{
+    if (device < 0 || device >= 256 || num_rules < 0 || num_rules > GRG_MAX_RULES || (num_rules && !rules) ||
+        num_labels < 1 || num_labels > GRG_MAX_LABELS || filter > 1 || !d_label_counts ||
+        (num_edges && (!d_src || !d_dst || !d_label)))
+        return GRG_E_ARG;
+    for (int q = 0; q < num_rules; q++) {
+        const int *r = &rules[3 * q];
+        if (r[0] < 1 || r[0] > num_labels || r[1] < 0 || r[1] > num_labels || r[2] < 0 || r[2] > num_labels ||
+            (r[1] == 0 && r[2] != 0))
+            return GRG_E_ARG;
+    }
+    // scratch layout: counters | descriptors | cnt | want | grow | pool arrays (108 B per element)
+    const uint64_t ntab = (uint64_t)(2 * num_labels) * num_vars;
+    size_t off = 0;
+    const size_t o_ctr = off; off = align256(off + sizeof(unsigned long long) * NCTR);
+    const size_t o_desc = off; off = align256(off + ntab * 8);
+    const size_t o_cnt = off; off = align256(off + ntab * 4);
+    const size_t o_want = off; off = align256(off + ntab * 4);
+    const size_t o_grow = off; off = align256(off + ntab * 4);
+    if (off >= NOALLOC_SCRATCH_BYTES) return GRG_E_RANGE;            // tables alone exceed the scratch
+    uint64_t pool = (NOALLOC_SCRATCH_BYTES - off - 6 * 256) / 108;
+    if (pool < 4096 || num_edges > pool / 2) return GRG_E_RANGE;    // graph too large for the scratch
+    const size_t o_elems = off; off = align256(off + pool * 32);
+    const size_t o_dbits = off; off = align256(off + pool * 32);
+    const size_t o_dirty = off; off = align256(off + pool * 4);
+    const size_t o_delta = off; off = align256(off + pool * 32);
+    const size_t o_retry0 = off; off = align256(off + pool * 4);
+    const size_t o_retry1 = off; off = align256(off + pool * 4);
+    if (off > NOALLOC_SCRATCH_BYTES) return GRG_E_RANGE;
+
+    RuleTable rt;
+    bool derivable[MAX_LABELS + 1];
+    int st = noalloc_rules(rules, num_rules, num_labels, filter, rt, derivable);
+    if (st) return st;
+
+    DeviceGuard guard;
+    NA_CUDA(cudaGetDevice(&guard.prev));
+    NA_CUDA(cudaSetDevice(device));
+    if (!g_noalloc_addr[device]) {                 // set-up, once per device, with the device current
+        void *p = nullptr;
+        NA_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_addr[device] = p;
+    }
+    unsigned char *base = (unsigned char *)g_noalloc_addr[device];
+    cudaStream_t s = (cudaStream_t)stream;
+    int sms = 0;
+    NA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    auto grid = [&](uint64_t n, int block, int per_sm) {
+        uint64_t g = (n + block - 1) / block, cap = (uint64_t)sms * per_sm;
+        return (int)std::max<uint64_t>(std::min(g, cap), 1);
+    };
+
+    Dev d;
+    d.ctr = (unsigned long long *)(base + o_ctr);
+    d.desc = (uint64_t *)(base + o_desc);
+    d.cnt = (uint32_t *)(base + o_cnt);
+    d.want = (uint32_t *)(base + o_want);
+    d.grow = (uint32_t *)(base + o_grow);
+    d.elems = (uint32_t *)(base + o_elems);
+    d.dbits = (uint32_t *)(base + o_dbits);
+    d.dirty = (uint32_t *)(base + o_dirty);
+    d.V = num_vars;
+    d.pool_cap = (uint32_t)pool;
+    uint4 *delta = (uint4 *)(base + o_delta);
+    uint32_t *retry[2] = {(uint32_t *)(base + o_retry0), (uint32_t *)(base + o_retry1)};
+    unsigned long long h[NCTR];
+
+    // the array keeps the previous call's contents: clear everything that must start at zero
+    NA_CUDA(cudaMemsetAsync(d.ctr, 0, sizeof(unsigned long long) * NCTR, s));
+    NA_CUDA(cudaMemsetAsync(d.desc, 0, ntab * 8, s));
+    NA_CUDA(cudaMemsetAsync(d.cnt, 0, ntab * 4, s));
+    NA_CUDA(cudaMemsetAsync(d.want, 0, ntab * 4, s));
+    NA_CUDA(cudaMemcpyToSymbolAsync(c_rt, &rt, sizeof rt, 0, cudaMemcpyHostToDevice, s));
+
+    // load (grg_load_edges)
+    const uint64_t nlab = (uint64_t)num_labels * num_vars;
+    if (num_edges) k_load_hist<<<grid(num_edges, 256, 8), 256, 0, s>>>(d, d_src, d_label, num_edges);
+    for (int q = 0; q < num_rules; q++)
+        if (rules[3 * q + 1] == 0) k_eps_hist<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)rules[3 * q]);
+    k_load_alloc<<<grid(nlab, 256, 8), 256, 0, s>>>(d, nlab);
+    if ((st = na_read(h, d.ctr, s))) return st;
+    if (h[C_ERR] & ERR_POOL) return GRG_E_NOMEM;
+    const uint64_t top0 = h[C_POOL_TOP];
+    if (top0) k_init_region<<<grid(top0, 256, 8), 256, 0, s>>>(d.elems, d.dbits, 0, top0);
+    if (num_edges) k_load_insert<<<grid(num_edges, 256, 8), 256, 0, s>>>(d, d_src, d_dst, d_label, num_edges);
+    for (int q = 0; q < num_rules; q++)
+        if (rules[3 * q + 1] == 0) k_eps_insert<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)rules[3 * q]);
+    for (int l = 1; l <= num_labels; l++)
+        if (!derivable[l]) k_compact_static<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)l);
+    if (top0) k_mark_all<<<grid(top0, 256, 8), 256, 0, s>>>(d, top0);
+    NA_CUDA(cudaGetLastError());
+    if ((st = na_read(h, d.ctr, s))) return st;
+    if (h[C_ERR]) return GRG_E_CUDA;
+
+    // semi-naive rounds (grg_closure); the pool cannot grow here
+    uint64_t rounds = 0;
+    for (;;) {
+        if ((st = na_read(h, d.ctr, s))) return st;
+        const uint64_t nd = h[C_DIRTY_N];
+        if (nd == 0) break;
+        rounds++;
+        k_gather<<<grid(nd, 256, 8), 256, 0, s>>>(d, nd, delta);
+        NA_CUDA(cudaMemsetAsync(d.ctr + C_DIRTY_N, 0, 8, s));
+        NA_CUDA(cudaMemsetAsync(d.ctr + C_RETRY_N, 0, 16, s));
+        const uint32_t *idx = nullptr;
+        uint64_t n = nd;
+        int rb = 0;
+        for (int pass = 0;; pass++) {
+            k_join<<<grid(n, JOIN_WARPS, 16), JOIN_WARPS * 32, 0, s>>>(d, delta, n, idx, retry[rb]);
+            NA_CUDA(cudaGetLastError());
+            if ((st = na_read(h, d.ctr, s))) return st;
+            const uint64_t nr = h[C_RETRY_N];
+            if (nr == 0) break;
+            NA_CUDA(cudaMemsetAsync(d.ctr + C_ERR, 0, 8, s));
+            k_grow<<<grid(h[C_GROW_N] * 32, 256, 8), 256, 0, s>>>(d, h[C_GROW_N]);
+            if ((st = na_read(h, d.ctr, s))) return st;
+            if (h[C_ERR] & ERR_POOL) return GRG_E_NOMEM;          // closure outgrew the scratch
+            if (pass > 64) return GRG_E_CUDA;
+            idx = retry[rb];
+            n = nr;
+            rb ^= 1;
+            NA_CUDA(cudaMemsetAsync(d.ctr + C_RETRY_N, 0, 16, s));
+        }
+    }
+
+    // per-label counts and edge-set hash into the caller's device buffers
+    NA_CUDA(cudaMemsetAsync(d.ctr + C_LABEL0, 0, sizeof(unsigned long long) * (MAX_SLOTS + 2), s));
+    NA_CUDA(cudaMemsetAsync(d.ctr + C_HASH, 0, 8, s));
+    for (int l = 1; l <= num_labels; l++)
+        k_count<<<grid((uint64_t)num_vars * 32, 256, 8), 256, 0, s>>>(d, (uint32_t)l, nullptr, nullptr, 0, 0,
+                                                                     d_set_hash ? 1 : 0);
+    NA_CUDA(cudaMemcpyAsync(d_label_counts, d.ctr + C_LABEL0 + 1, sizeof(uint64_t) * num_labels,
+                            cudaMemcpyDeviceToDevice, s));
+    if (d_set_hash) NA_CUDA(cudaMemcpyAsync(d_set_hash, d.ctr + C_HASH, 8, cudaMemcpyDeviceToDevice, s));
+    NA_CUDA(cudaGetLastError());
+    NA_CUDA(cudaStreamSynchronize(s));
+    if (rounds_out) *rounds_out = rounds;
+    return GRG_OK;
+}

@@ -28,7 +28,7 @@ EXPORTS = (
     "grg_error_string", "grg_last_error", "grg_create", "grg_destroy", "grg_device", "grg_set_stream",
     "grg_set_kernel_timing", "grg_transfer_rules", "grg_allocate_pool", "grg_load_edges", "grg_closure",
     "grg_label_counts", "grg_get_degree", "grg_set_hash", "grg_export_edges", "grg_parse_grammar",
-    "grg_parse_graph_header", "grg_parse_graph",
+    "grg_parse_graph_header", "grg_parse_graph", "grg_closure_noalloc",
 )
 
 
@@ -84,6 +84,7 @@ def load_library(path: str = LIB_PATH):
     L.grg_parse_grammar.argtypes = [ctypes.c_char_p, ctypes.POINTER(I), P, ctypes.POINTER(I), P]
     L.grg_parse_graph_header.argtypes = [ctypes.c_char_p, ctypes.POINTER(U64), ctypes.POINTER(U32)]
     L.grg_parse_graph.argtypes = [ctypes.c_char_p, I, P, U64, U32, P, P, P]
+    L.grg_closure_noalloc.argtypes = [I, P, I, P, I, U32, U32, U64, P, P, P, P, P, ctypes.POINTER(U64)]
     _lib = L
     return L
 

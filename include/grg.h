@@ -139,6 +139,41 @@ int grg_parse_graph_header(const char *path, uint64_t *num_edges, uint32_t *num_
 int grg_parse_graph(const char *path, int num_labels, const char *names, uint64_t num_edges,
                     uint32_t num_vars, uint32_t *src, uint32_t *dst, uint8_t *label);
 
+/* Allocation-free closure. No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory while they run: a serving
+ * loop whose device memory belongs to another allocator or budget, or a
+ * process that must not let cudaMalloc/cudaFree synchronize the device while
+ * other work is in flight. It runs the same load and closure kernels as
+ * grg_load_edges + grg_closure, but all their scratch memory lives in one
+ * static device array of GRG_NOALLOC_SCRATCH_BYTES (64 MiB), which every GPU
+ * that loads this library holds until the process exits. No cudaMalloc,
+ * cudaFree or other allocating routine is called, and no context is needed.
+ *
+ * Inputs: the grammar as for grg_transfer_rules, and num_edges edges as
+ * DEVICE arrays d_src/d_dst/d_label over vertices [0, num_vars). Outputs:
+ * d_label_counts (DEVICE, num_labels uint64 values), d_set_hash (DEVICE, one
+ * uint64, may be NULL) and *rounds_out (host, may be NULL). stream may be NULL
+ * (the legacy default stream); the call returns after the stream is idle.
+ *
+ * Limits: the tables take 40 bytes per (label, vertex) and the rest of the
+ * array holds 108 bytes per element slot; graphs whose tables leave fewer
+ * than 4096 slots, or with more edges than half the slots, are rejected with
+ * GRG_E_RANGE before any launch; a closure that outgrows the array returns
+ * GRG_E_NOMEM.
+ *
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture. Every call reuses the same array and clears it
+ * itself, so calls that overlap on the GPU race, with each other and with a
+ * grg_closure running on the same device (they share the rule table in
+ * constant memory). */
+#define GRG_NOALLOC_SCRATCH_BYTES (64ull << 20)
+int grg_closure_noalloc(int device, void *stream, int num_rules, const int *rules, int num_labels,
+                        uint32_t filter, uint32_t num_vars, uint64_t num_edges, const uint32_t *d_src,
+                        const uint32_t *d_dst, const uint8_t *d_label, uint64_t *d_label_counts,
+                        uint64_t *d_set_hash, uint64_t *rounds_out);
+
 #ifdef __cplusplus
 }
 #endif
