@@ -162,6 +162,7 @@ def main():
     ap.add_argument("--impl", default="grg", choices=["grg", "reference"])
     ap.add_argument("--blocks", type=int, default=2000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--pool-gb", type=float, default=0.0, help="initial element pool (0 = 1/8 of free memory)")
     args = ap.parse_args()
     world, rank, local = dist_setup(args)
 
@@ -189,7 +190,7 @@ def main():
     ctx = grg.Context(local)
     ctx.set_stream(stream.cuda_stream)
     ctx.transfer_rules(w.rule_ids(), w.num_labels)
-    ctx.allocate_pool(0)
+    ctx.allocate_pool(int(args.pool_gb * (1 << 30)))
     d_src = torch.from_numpy(w.src.view(np.int32)).cuda()
     d_dst = torch.from_numpy(w.dst.view(np.int32)).cuda()
     d_lab = torch.from_numpy(w.lab).cuda()
