@@ -266,7 +266,10 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded generator)",
             "config": {"workload": WORKLOAD, "num_vars": w.num_vars, "input_edges": w.num_edges,
                        "closure_edges": total, "rounds": s["rounds"], "parallelism": f"replicas{world}",
-                       "l2_flush": "512 MiB write before every timed step", "time_to_fixpoint_ms": ms_max},
+                       "l2_flush": "512 MiB write before every timed step", "time_to_fixpoint_ms": ms_max,
+                       "join_launches": s["join_launches"], "retry_records": s["retry_records"],
+                       "grow_rows": s["grow_rows"], "delta_elems": s["delta_elems"],
+                       "pool_elems_used": s["pool_elems_used"]},
             "e2e": {"value": world * total / (e2e_max * 1e-3), "unit": UNIT,
                     "h2d_bytes_per_step": int(w.num_edges * 9), "d2h_bytes_per_step": int(w.num_labels * 8)},
             "roofline": {"bound": "hbm", "kernel": "k_join", "achieved": achieved, "peak": hbm,

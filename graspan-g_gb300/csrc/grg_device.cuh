@@ -9,10 +9,11 @@
 // row's elements are hashed by base, so a lookup is one or two probes instead
 // of a list walk and rows never need re-sorting.
 //
-// Deltas: a parallel pool of 32-byte delta bitmaps (words 0..5 = bits that
-// became set this round, word 6 = dirty flag) and a dirty list of slot
-// indices. The first thread that sets new bits in an element appends it, so
-// the dirty list of a round holds each element at most once and can never
+// Deltas: two parallel pools of 32-byte delta bitmaps (words 0..5 = bits that
+// became set, word 6 = dirty flag) and two dirty lists of slot indices, used
+// alternately: round t reads the bitmaps and list written in round t-1 and
+// writes the next ones. The first thread that sets new bits in an element
+// appends it, so a dirty list holds each element at most once and can never
 // overflow the pool's size. This replaces the reference's tmp region and the
 // diff/merge kernels (src/kernel.cu:841-985): new edges are found by atomicOr
 // on the stored element, which returns exactly the bits that were new.
@@ -63,11 +64,17 @@ struct RuleTable {
     uint8_t ol_A[MAX_RULES], ol_rev[MAX_RULES];
     uint8_t rev_slot[MAX_LABELS + 1];        // reverse-index slot of label B (0 = none)
     uint8_t track[MAX_SLOTS + 2];            // slot: new bits become deltas
+    // labels never inserted into after the load that are a rule's second
+    // symbol also get a CSR copy (row pointers + destination ids): joins read
+    // 4 bytes per edge instead of a 32-byte element per 192-id block
+    const uint2 *csr_row[MAX_LABELS + 1];    // {first edge, degree | min(elements,255) << 24}
+    const uint32_t *csr_col[MAX_LABELS + 1];
 };
 
 struct Dev {
     uint32_t *elems;          // pool: 8 words per slot
-    uint32_t *dbits;          // delta bitmaps: 8 words per slot
+    uint32_t *dbits;          // delta bitmaps written this round: 8 words per slot
+    uint32_t *dcur;           // delta bitmaps read (and cleared) this round
     uint64_t *desc;           // [(slot-1)*V + row] = cap << 32 | offset
     uint32_t *cnt;            // occupied slots per table
     uint32_t *want;           // failed inserts per table since its last growth
@@ -105,10 +112,14 @@ __device__ __forceinline__ void append_dirty(const Dev &d, uint32_t s)
 }
 
 // OR `b` into element (slot, row, base). Returns false when the table is full
-// or absent; the failure is recorded so the table grows before a retry.
-__device__ __noinline__ bool g_insert(const Dev &d, uint32_t slot, uint32_t row, uint32_t base, const Bits &b,
-                                      bool track)
+// or absent; the failure is recorded so the table grows before a retry. With
+// `track`, the bits that were new go to the element's delta bitmap, and if they
+// are the element's first new bits of the round `dirty_slot` receives the slot
+// (the caller appends it to the dirty list); otherwise dirty_slot = EMPTY.
+__device__ __forceinline__ bool g_insert(const Dev &d, uint32_t slot, uint32_t row, uint32_t base, const Bits b,
+                                         bool track, uint32_t &dirty_slot)
 {
+    dirty_slot = EMPTY;
     const size_t ti = (size_t)(slot - 1) * d.V + row;
     const uint64_t de = d.desc[ti];
     const uint32_t off = (uint32_t)de, cap = (uint32_t)(de >> 32);
@@ -116,15 +127,15 @@ __device__ __noinline__ bool g_insert(const Dev &d, uint32_t slot, uint32_t row,
     uint32_t s = EMPTY;
     if (cap != 0 && (cap & (cap - 1)) == 0) {
         const uint32_t lg = 31 - __clz(cap);
-        uint32_t h = hash_slot(base, lg);
+        const uint32_t h = hash_slot(base, lg);
         for (uint32_t p = 0; p < cap; p++) {
             const uint32_t q = off + ((h + p) & (cap - 1));
             uint32_t *kp = d.elems + (size_t)q * 8 + 6;
-            uint32_t k = __ldcg(kp);
+            const uint32_t k = __ldcg(kp);
             if (k == key) { s = q; break; }
             if (k != EMPTY) continue;
             if (atomicAdd(&d.cnt[ti], 1u) >= max_load(cap)) { atomicSub(&d.cnt[ti], 1u); break; }
-            uint32_t prev = atomicCAS(kp, EMPTY, key);
+            const uint32_t prev = atomicCAS(kp, EMPTY, key);
             if (prev == EMPTY) { d.elems[(size_t)q * 8 + 7] = row; s = q; break; }
             atomicSub(&d.cnt[ti], 1u);
             if (prev == key) { s = q; break; }
@@ -132,31 +143,44 @@ __device__ __noinline__ bool g_insert(const Dev &d, uint32_t slot, uint32_t row,
     }
     if (s == EMPTY) {
         if (atomicAdd(&d.want[ti], 1u) == 0) {
-            unsigned long long g = atomicAdd(&d.ctr[C_GROW_N], 1ull);
+            const unsigned long long g = atomicAdd(&d.ctr[C_GROW_N], 1ull);
             d.grow[g] = (uint32_t)ti;
         }
         return false;
     }
     uint32_t *e = d.elems + (size_t)s * 8;
-    uint32_t nb[EW];
+    Bits nb;
     uint32_t any = 0;
 #pragma unroll
     for (int w = 0; w < EW; w++) {
-        nb[w] = 0;
+        nb.w[w] = 0;
         if (b.w[w]) {
-            uint32_t old = atomicOr(&e[w], b.w[w]);
-            nb[w] = b.w[w] & ~old;
-            any |= nb[w];
+            const uint32_t old = atomicOr(&e[w], b.w[w]);
+            nb.w[w] = b.w[w] & ~old;
+            any |= nb.w[w];
         }
     }
     if (track && any) {
         uint32_t *db = d.dbits + (size_t)s * 8;
 #pragma unroll
         for (int w = 0; w < EW; w++)
-            if (nb[w]) atomicOr(&db[w], nb[w]);
-        if (atomicExch(&db[6], 1u) == 0) append_dirty(d, s);
+            if (nb.w[w]) atomicOr(&db[w], nb.w[w]);
+        if (atomicExch(&db[6], 1u) == 0) dirty_slot = s;
     }
     return true;
+}
+
+// Warp-aggregated append of the lanes' dirty slots (EMPTY = none). All 32 lanes call it.
+__device__ __forceinline__ void warp_append_dirty(const Dev &d, uint32_t ds)
+{
+    const unsigned m = __ballot_sync(0xffffffffu, ds != EMPTY);
+    if (!m) return;
+    const uint32_t lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    unsigned long long b = 0;
+    if ((int)lane == leader) b = atomicAdd(&d.ctr[C_DIRTY_N], (unsigned long long)__popc(m));
+    b = __shfl_sync(0xffffffffu, b, leader);
+    if (ds != EMPTY) d.dirty[b + __popc(m & ((1u << lane) - 1u))] = ds;
 }
 
 }  // namespace grg

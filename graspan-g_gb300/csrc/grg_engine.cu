@@ -6,7 +6,7 @@
 //             unary rules A ::= B, and dedup of every candidate against the
 //             stored rows. Replaces compute11/compute10 (src/kernel.cu:403-442)
 //             and diff/merge (src/kernel.cu:841-985).
-//   k_gather  turns the dirty list of the last round into delta records
+//             Its delta records come straight from the last round's dirty list
 //             (the reference's Delta region, mergeAndDiff src/kernel.cu:943-985).
 //   k_grow    re-hashes tables that overflowed; their delta records are re-run
 //             (the reference instead repartitions on overflow, src/main.cpp:633-762).
@@ -29,22 +29,29 @@ namespace grg {
 
 __constant__ RuleTable c_rt;
 
-constexpr int JOIN_WARPS = 8;     // warps per join block
-constexpr int ACC = 64;           // per-warp accumulator entries
+constexpr int JOIN_WARPS = 4;     // warps per join block
+constexpr int RB = 32;            // delta records per warp batch (one per lane)
+constexpr int WIN = 8;            // dense accumulator window: elements base-WIN_LO .. base+WIN-1-WIN_LO
+constexpr int WIN_LO = 3;
+constexpr int ACC_LG = 6;
+constexpr int ACC = 1 << ACC_LG;  // per-warp hash accumulator entries (candidates outside the window)
 constexpr int ACC_MAX = ACC * 3 / 4;
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
 
 // ---------------------------------------------------------------- loader
 
-__global__ void k_init_region(uint32_t *elems, uint32_t *dbits, uint64_t begin, uint64_t end)
+__global__ void k_init_region(uint32_t *elems, uint32_t *dbits0, uint32_t *dbits1, uint64_t begin, uint64_t end)
 {
     for (uint64_t s = begin + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < end;
          s += (uint64_t)gridDim.x * blockDim.x) {
         uint4 *e = reinterpret_cast<uint4 *>(elems + s * 8);
         e[0] = make_uint4(0, 0, 0, 0);
         e[1] = make_uint4(0, 0, EMPTY, 0);
-        uint4 *b = reinterpret_cast<uint4 *>(dbits + s * 8);
+        uint4 *b = reinterpret_cast<uint4 *>(dbits0 + s * 8);
+        b[0] = make_uint4(0, 0, 0, 0);
+        b[1] = make_uint4(0, 0, 0, 0);
+        b = reinterpret_cast<uint4 *>(dbits1 + s * 8);
         b[0] = make_uint4(0, 0, 0, 0);
         b[1] = make_uint4(0, 0, 0, 0);
     }
@@ -101,11 +108,11 @@ __global__ void k_load_insert(Dev d, const uint32_t *src, const uint32_t *dst, c
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t v = dst[i];
         Bits b;
+        const uint32_t o = v % EIDS;
 #pragma unroll
-        for (int w = 0; w < EW; w++) b.w[w] = 0;
-        uint32_t o = v % EIDS;
-        b.w[o >> 5] = 1u << (o & 31);
-        if (!g_insert(d, lab[i], src[i], v / EIDS, b, false)) atomicOr(&d.ctr[C_ERR], (unsigned long long)ERR_LOAD);
+        for (int w = 0; w < EW; w++) b.w[w] = (uint32_t)w == (o >> 5) ? 1u << (o & 31) : 0u;
+        uint32_t ds;
+        if (!g_insert(d, lab[i], src[i], v / EIDS, b, false, ds)) atomicOr(&d.ctr[C_ERR], (unsigned long long)ERR_LOAD);
     }
 }
 
@@ -114,11 +121,11 @@ __global__ void k_eps_insert(Dev d, uint32_t slot)
 {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < d.V; v += gridDim.x * blockDim.x) {
         Bits b;
+        const uint32_t o = v % EIDS;
 #pragma unroll
-        for (int w = 0; w < EW; w++) b.w[w] = 0;
-        uint32_t o = v % EIDS;
-        b.w[o >> 5] = 1u << (o & 31);
-        if (!g_insert(d, slot, v, v / EIDS, b, false)) atomicOr(&d.ctr[C_ERR], (unsigned long long)ERR_LOAD);
+        for (int w = 0; w < EW; w++) b.w[w] = (uint32_t)w == (o >> 5) ? 1u << (o & 31) : 0u;
+        uint32_t ds;
+        if (!g_insert(d, slot, v, v / EIDS, b, false, ds)) atomicOr(&d.ctr[C_ERR], (unsigned long long)ERR_LOAD);
     }
 }
 
@@ -167,38 +174,109 @@ __global__ void k_mark_all(Dev d, uint64_t end)
 
 // ---------------------------------------------------------------- rounds
 
-// Dirty slots -> delta records (32 B: bits[6], key, row); clears the delta bitmap.
-__global__ void k_gather(Dev d, uint64_t n, uint4 *delta)
+// Dirty slots of the last round -> delta records (32 B: bits[6], key, row);
+// clears the slots' delta bitmaps of that parity.
+__global__ void k_gather(Dev d, const uint32_t *__restrict__ list, uint64_t n, uint4 *out)
 {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t s = d.dirty[i];
-        uint4 *b = reinterpret_cast<uint4 *>(d.dbits + (size_t)s * 8);
+        const uint32_t s = list[i];
+        uint4 *b = reinterpret_cast<uint4 *>(d.dcur + (size_t)s * 8);
         const uint4 b0 = b[0], b1 = b[1];
         const uint4 e1 = reinterpret_cast<const uint4 *>(d.elems + (size_t)s * 8)[1];
         b[0] = make_uint4(0, 0, 0, 0);
         b[1] = make_uint4(0, 0, 0, 0);
-        delta[2 * i] = b0;
-        delta[2 * i + 1] = make_uint4(b1.x, b1.y, e1.z, e1.w);
+        out[2 * i] = b0;
+        out[2 * i + 1] = make_uint4(b1.x, b1.y, e1.z, e1.w);
     }
 }
 
 struct __align__(16) WarpSmem {
-    uint32_t acc_bits[ACC][EW];
-    uint32_t acc_key[ACC];
-    uint32_t klist[EIDS];
-    uint32_t koff[EIDS];
-    uint32_t kpre[EIDS + 1];
+    uint32_t win[RB][WIN][EW];    // dense window accumulator per record
+    uint32_t acc_bits[ACC][EW];   // hash accumulator: OR of candidate bitmaps
+    uint32_t acc_key[ACC];        // key = record << 25 | base (EMPTY = free)
+    uint32_t rbits[RB][EW];       // the batch's delta records
+    uint32_t rrow[RB];
+    uint32_t rbase[RB];
+    uint32_t rA[RB];              // per record: output label of the current rule pass
+    uint32_t rC[RB];              // per record: right operand label / reverse slot
+    uint32_t rOff[RB];            // per record: row offset (old-left pass)
+    uint32_t kpre[RB + 1];        // exclusive prefix of per-record task counts
     uint32_t acc_n;
+    uint32_t fail;                // records with a failed insert (retry after growth)
 };
 
-__device__ __forceinline__ bool acc_insert(WarpSmem &w, uint32_t base, const Bits &b)
+__device__ __forceinline__ uint32_t popc6(const Bits &b)
+{
+    uint32_t c = 0;
+#pragma unroll
+    for (int x = 0; x < EW; x++) c += __popc(b.w[x]);
+    return c;
+}
+
+// Position of the n-th (0-based) set bit of a 32-bit word (broadword select, no loop).
+__device__ __forceinline__ uint32_t select32(uint32_t w, uint32_t n)
+{
+    uint32_t pos = 0, c;
+    c = __popc(w & 0xFFFFu); if (n >= c) { n -= c; pos += 16; w >>= 16; }
+    c = __popc(w & 0xFFu);   if (n >= c) { n -= c; pos += 8;  w >>= 8; }
+    c = __popc(w & 0xFu);    if (n >= c) { n -= c; pos += 4;  w >>= 4; }
+    c = __popc(w & 0x3u);    if (n >= c) { n -= c; pos += 2;  w >>= 2; }
+    c = w & 1u;              if (n >= c) { pos += 1; }
+    return pos;
+}
+
+// Position (0..191) of the idx-th set bit of a record's bitmap in shared memory.
+__device__ __forceinline__ uint32_t select_bit(const uint32_t *bits, uint32_t idx)
+{
+    uint32_t pos = 0, wsel = 0, found = 0;
+#pragma unroll
+    for (int x = 0; x < EW; x++) {
+        const uint32_t bw = bits[x];
+        const uint32_t c = __popc(bw);
+        const bool here = !found && idx < c;
+        if (here) { wsel = bw; pos = x * 32; found = 1; }
+        else if (!found) idx -= c;
+    }
+    return pos + select32(wsel, idx);
+}
+
+// Exclusive warp prefix of per-lane task counts into kpre[0..RB]; returns the total.
+__device__ __forceinline__ uint32_t warp_tasks(WarpSmem &w, uint32_t cnt)
+{
+    const uint32_t lane = lane_id();
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    w.kpre[lane] = incl - cnt;
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    if (lane == 31) w.kpre[RB] = total;
+    __syncwarp();
+    return total;
+}
+
+// Record owning flattened task t: largest r with kpre[r] <= t.
+__device__ __forceinline__ uint32_t task_record(const WarpSmem &w, uint32_t t)
+{
+    uint32_t lo = 0, hi = RB - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (w.kpre[mid] <= t) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// OR (key, b) into the warp's hash accumulator; false when it is full.
+__device__ __forceinline__ bool acc_insert(WarpSmem &w, uint32_t key, const Bits b)
 {
     volatile uint32_t *keys = w.acc_key;
-    uint32_t h = (base * 0x9E3779B1u) >> (32 - 6);
+    const uint32_t h = (key * 0x9E3779B1u) >> (32 - ACC_LG);
     for (int p = 0; p < ACC; p++) {
-        uint32_t q = (h + p) & (ACC - 1);
-        uint32_t k = keys[q];
-        if (k == base) {
+        const uint32_t q = (h + p) & (ACC - 1);
+        const uint32_t k = keys[q];
+        if (k == key) {
 #pragma unroll
             for (int x = 0; x < EW; x++)
                 if (b.w[x]) atomicOr(&w.acc_bits[q][x], b.w[x]);
@@ -209,9 +287,9 @@ __device__ __forceinline__ bool acc_insert(WarpSmem &w, uint32_t base, const Bit
             atomicSub(&w.acc_n, 1u);
             return false;
         }
-        uint32_t prev = atomicCAS(&w.acc_key[q], EMPTY, base);
+        const uint32_t prev = atomicCAS(&w.acc_key[q], EMPTY, key);
         if (prev != EMPTY) atomicSub(&w.acc_n, 1u);
-        if (prev == EMPTY || prev == base) {
+        if (prev == EMPTY || prev == key) {
 #pragma unroll
             for (int x = 0; x < EW; x++)
                 if (b.w[x]) atomicOr(&w.acc_bits[q][x], b.w[x]);
@@ -221,31 +299,63 @@ __device__ __forceinline__ bool acc_insert(WarpSmem &w, uint32_t base, const Bit
     return false;
 }
 
-// Flush the warp's accumulator into row (A, row). Returns false if any insert failed.
-__device__ __forceinline__ bool acc_flush(const Dev &d, WarpSmem &w, uint32_t A, uint32_t row, bool track,
-                                          uint32_t &inserts)
+// Flush the hash accumulator: entry (r, base) goes to row (rA[r], rrow[r]). Warp-uniform.
+__device__ __forceinline__ void acc_flush(const Dev &d, WarpSmem &w, uint32_t &inserts)
 {
     __syncwarp();
-    bool ok = true;
-    for (int j = lane_id(); j < ACC; j += 32) {
-        uint32_t k = w.acc_key[j];
-        if (k == EMPTY) continue;
-        Bits b;
+#pragma unroll 1
+    for (int it = 0; it < ACC / 32; it++) {
+        const int j = it * 32 + (int)lane_id();
+        const uint32_t k = w.acc_key[j];
+        uint32_t ds = EMPTY;
+        if (k != EMPTY) {
+            Bits b;
 #pragma unroll
-        for (int x = 0; x < EW; x++) { b.w[x] = w.acc_bits[j][x]; w.acc_bits[j][x] = 0; }
-        w.acc_key[j] = EMPTY;
-        ok &= g_insert(d, A, row, k, b, track);
-        inserts++;
+            for (int x = 0; x < EW; x++) { b.w[x] = w.acc_bits[j][x]; w.acc_bits[j][x] = 0; }
+            w.acc_key[j] = EMPTY;
+            const uint32_t r = k >> KEY_SHIFT, A = w.rA[r];
+            if (!g_insert(d, A, w.rrow[r], k & BASE_MASK, b, c_rt.track[A], ds)) atomicOr(&w.fail, 1u << r);
+            inserts++;
+        }
+        warp_append_dirty(d, ds);
     }
     __syncwarp();
     if (lane_id() == 0) w.acc_n = 0;
     __syncwarp();
-    return ok;
 }
 
-// One warp per delta record (label B, row i, base, bits).
-__global__ void __launch_bounds__(JOIN_WARPS * 32) k_join(Dev d, const uint4 *__restrict__ delta, uint64_t n,
-                                                          const uint32_t *__restrict__ idx, uint32_t *retry_out)
+// Flush every record's window into row (rA[r], rrow[r]) and clear it. Warp-uniform.
+__device__ __forceinline__ void win_flush(const Dev &d, WarpSmem &w, uint32_t &inserts)
+{
+    __syncwarp();
+#pragma unroll 1
+    for (int it = 0; it < RB * WIN / 32; it++) {
+        const uint32_t p = it * 32 + lane_id();
+        const uint32_t r = p / WIN, dd = p % WIN;
+        Bits b;
+        uint32_t any = 0;
+#pragma unroll
+        for (int x = 0; x < EW; x++) { b.w[x] = w.win[r][dd][x]; any |= b.w[x]; }
+        uint32_t ds = EMPTY;
+        if (any) {
+#pragma unroll
+            for (int x = 0; x < EW; x++) w.win[r][dd][x] = 0;
+            const uint32_t A = w.rA[r];
+            if (!g_insert(d, A, w.rrow[r], w.rbase[r] + dd - WIN_LO, b, c_rt.track[A], ds)) atomicOr(&w.fail, 1u << r);
+            inserts++;
+        }
+        warp_append_dirty(d, ds);
+    }
+    __syncwarp();
+}
+
+// One warp per batch of RB delta records (label B, row i, base, bits); lane r
+// owns record r for per-record work, and (record, k) tasks and their right-hand
+// items are flattened over the lanes so every phase keeps 32 independent memory
+// operations in flight.
+__global__ void __launch_bounds__(JOIN_WARPS * 32, 6) k_join(Dev d, const uint32_t *__restrict__ list,
+                                                             const uint4 *__restrict__ recs, uint64_t n,
+                                                             uint4 *retry_out)
 {
     __shared__ WarpSmem smem[JOIN_WARPS];
     WarpSmem &w = smem[threadIdx.x >> 5];
@@ -255,139 +365,370 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32) k_join(Dev d, const uint4 *__
 #pragma unroll
         for (int x = 0; x < EW; x++) w.acc_bits[j][x] = 0;
     }
-    if (lane == 0) { w.acc_n = 0; w.kpre[0] = 0; }
+    for (int j = lane; j < RB * WIN * EW; j += 32) (&w.win[0][0][0])[j] = 0;
+    if (lane == 0) w.acc_n = 0;
     __syncwarp();
     unsigned long long n_left = 0, n_right = 0;
     uint32_t inserts = 0;
     const uint64_t nwarps = (uint64_t)gridDim.x * JOIN_WARPS;
-    for (uint64_t r = blockIdx.x * (uint64_t)JOIN_WARPS + (threadIdx.x >> 5); r < n; r += nwarps) {
-        const uint64_t ri = idx ? idx[r] : r;
-        const uint32_t *rec = reinterpret_cast<const uint32_t *>(delta + 2 * ri);
-        uint32_t word = lane < 8 ? rec[lane] : 0u;
+    const uint64_t nbatch = (n + RB - 1) / RB;
+    for (uint64_t bt = blockIdx.x * (uint64_t)JOIN_WARPS + (threadIdx.x >> 5); bt < nbatch; bt += nwarps) {
+        const uint64_t ri = bt * RB + lane;
+        const bool have = ri < n;
         Bits rb;
+        uint32_t key = EMPTY, row = 0;
+        if (have) {
+            uint4 a, b;
+            if (list) {
+                // first pass: the record is the dirty slot's delta bitmap (cleared here) + its key and row
+                const uint32_t s = list[ri];
+                uint4 *db = reinterpret_cast<uint4 *>(d.dcur + (size_t)s * 8);
+                a = db[0];
+                const uint4 b1 = db[1];
+                const uint4 e1 = reinterpret_cast<const uint4 *>(d.elems + (size_t)s * 8)[1];
+                db[0] = make_uint4(0, 0, 0, 0);
+                db[1] = make_uint4(0, 0, 0, 0);
+                b = make_uint4(b1.x, b1.y, e1.z, e1.w);
+            } else {
+                a = recs[2 * ri];
+                b = recs[2 * ri + 1];
+            }
+            rb.w[0] = a.x; rb.w[1] = a.y; rb.w[2] = a.z; rb.w[3] = a.w; rb.w[4] = b.x; rb.w[5] = b.y;
+            key = b.z;
+            row = b.w;
+        } else {
 #pragma unroll
-        for (int x = 0; x < EW; x++) rb.w[x] = __shfl_sync(0xffffffffu, word, x);
-        const uint32_t key = __shfl_sync(0xffffffffu, word, 6);
-        const uint32_t row = __shfl_sync(0xffffffffu, word, 7);
-        const uint32_t B = key >> KEY_SHIFT, base = key & BASE_MASK;
+            for (int x = 0; x < EW; x++) rb.w[x] = 0;
+        }
+        const uint32_t B = have ? key >> KEY_SHIFT : 0, base = key & BASE_MASK;
+#pragma unroll
+        for (int x = 0; x < EW; x++) w.rbits[lane][x] = rb.w[x];
+        w.rrow[lane] = row;
+        w.rbase[lane] = base;
+        if (lane == 0) w.fail = 0;
+        __syncwarp();
         bool ok = true;
+        const uint32_t nbits = popc6(rb);
 
         // unary rules A ::= B (compute10): the delta itself joins row (A, row)
-        for (int q = c_rt.un_start[B]; q < c_rt.un_start[B + 1]; q++)
-            if (lane == 0) { ok &= g_insert(d, c_rt.un_A[q], row, base, rb, c_rt.track[c_rt.un_A[q]]); inserts++; }
-
-        // decode the intermediate vertices k of this record
-        uint32_t nk = 0;
-#pragma unroll
-        for (int x = 0; x < EW; x++) {
-            const uint32_t bw = rb.w[x];
-            if ((bw >> lane) & 1u) w.klist[nk + __popc(bw & ((1u << lane) - 1u))] = base * EIDS + x * 32 + lane;
-            nk += __popc(bw);
+        const uint32_t nu = have ? c_rt.un_start[B + 1] - c_rt.un_start[B] : 0;
+        const uint32_t maxu = __reduce_max_sync(0xffffffffu, nu);
+        for (uint32_t u = 0; u < maxu; u++) {
+            uint32_t ds = EMPTY;
+            if (u < nu) {
+                const uint32_t A = c_rt.un_A[c_rt.un_start[B] + u];
+                ok &= g_insert(d, A, row, base, rb, c_rt.track[A], ds);
+                inserts++;
+            }
+            warp_append_dirty(d, ds);
         }
-        __syncwarp();
 
         // reverse index of B (needed by old-left joins): rev_B[k] gets row
-        const uint32_t rs = c_rt.rev_slot[B];
-        if (rs) {
-            Bits ib;
+        {
+            const uint32_t rs = have ? c_rt.rev_slot[B] : 0;
+            w.rC[lane] = rs;
+            const uint32_t total = warp_tasks(w, rs ? nbits : 0);
+            for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+                const uint32_t t = t0 + lane;
+                if (t < total) {
+                    const uint32_t r = task_record(w, t);
+                    const uint32_t k = w.rbase[r] * EIDS + select_bit(w.rbits[r], t - w.kpre[r]);
+                    const uint32_t rr = w.rrow[r], o = rr % EIDS;
+                    Bits ib;
 #pragma unroll
-            for (int x = 0; x < EW; x++) ib.w[x] = 0;
-            const uint32_t o = row % EIDS;
-            ib.w[o >> 5] = 1u << (o & 31);
-            for (uint32_t j = lane; j < nk; j += 32) { ok &= g_insert(d, rs, w.klist[j], row / EIDS, ib, false); inserts++; }
+                    for (int x = 0; x < EW; x++) ib.w[x] = (uint32_t)x == (o >> 5) ? 1u << (o & 31) : 0u;
+                    uint32_t ds;
+                    if (!g_insert(d, w.rC[r], k, rr / EIDS, ib, false, ds)) atomicOr(&w.fail, 1u << r);
+                    inserts++;
+                }
+            }
         }
 
         // binary rules A ::= B C, delta-left: union of rows C[k] into row (A, row)
-        for (int q = c_rt.bin_start[B]; q < c_rt.bin_start[B + 1]; q++) {
-            const uint32_t A = c_rt.bin_A[q], C = c_rt.bin_C[q];
-            const bool trk = c_rt.track[A];
-            uint32_t total = 0;
-            for (uint32_t j0 = 0; j0 < nk; j0 += 32) {
-                const uint32_t j = j0 + lane;
-                uint32_t cap = 0, off = 0;
-                if (j < nk) {
-                    const uint64_t de = d.desc[(size_t)(C - 1) * d.V + w.klist[j]];
-                    off = (uint32_t)de;
-                    cap = (uint32_t)(de >> 32);
+        const uint32_t nbr = have ? c_rt.bin_start[B + 1] - c_rt.bin_start[B] : 0;
+        const uint32_t maxb = __reduce_max_sync(0xffffffffu, nbr);
+        for (uint32_t rho = 0; rho < maxb; rho++) {
+            const bool hr = rho < nbr;
+            const uint32_t q = c_rt.bin_start[B] + rho;
+            w.rA[lane] = hr ? c_rt.bin_A[q] : 0;
+            w.rC[lane] = hr ? c_rt.bin_C[q] : 0;
+            n_left += hr;
+            const uint32_t total = warp_tasks(w, hr ? nbits : 0);
+            for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+                // task (record r, intermediate k) -> items of row C[k]
+                const uint32_t t = t0 + lane;
+                uint32_t r = 0, C = 0, beg = 0, cnt = 0, csr = 0;
+                if (t < total) {
+                    r = task_record(w, t);
+                    C = w.rC[r];
+                    const uint32_t k = w.rbase[r] * EIDS + select_bit(w.rbits[r], t - w.kpre[r]);
+                    const uint2 *cr = c_rt.csr_row[C];
+                    if (cr) {
+                        const uint2 rw = __ldg(cr + k);
+                        csr = 1;
+                        beg = rw.x;
+                        cnt = rw.y & 0xFFFFFFu;
+                        n_right += rw.y >> 24;
+                    } else {
+                        const uint64_t de = __ldg(d.desc + (size_t)(C - 1) * d.V + k);
+                        beg = (uint32_t)de;
+                        cnt = (uint32_t)(de >> 32);
+                    }
                 }
-                uint32_t incl = cap;
+                uint32_t incl = cnt;
+#pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
-                    uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
                     if (lane >= (uint32_t)o) incl += y;
                 }
-                if (j < nk) { w.koff[j] = off; w.kpre[j + 1] = total + incl; }
-                total += __shfl_sync(0xffffffffu, incl, 31);
-            }
-            __syncwarp();
-            n_left++;
-            for (uint32_t t0 = 0; t0 < total; t0 += 32) {
-                const uint32_t t = t0 + lane;
-                bool pending = false;
-                uint32_t ebase = 0;
-                Bits eb;
-                if (t < total) {
-                    // largest j with kpre[j] <= t
-                    uint32_t lo = 0, hi = nk;
-                    while (lo < hi) {
-                        uint32_t mid = (lo + hi + 1) >> 1;
-                        if (w.kpre[mid] <= t) lo = mid; else hi = mid - 1;
+                const uint32_t nitems = __shfl_sync(0xffffffffu, incl, 31);
+                for (uint32_t f0 = 0; f0 < nitems; f0 += 32) {
+                    const uint32_t f = f0 + lane;
+                    // owner lane: smallest o with incl(o) > f
+                    uint32_t lo = 0;
+#pragma unroll
+                    for (int st = 16; st; st >>= 1) {
+                        const uint32_t v = __shfl_sync(0xffffffffu, incl, lo + st - 1);
+                        if (v <= f) lo += st;
                     }
-                    const uint32_t s = w.koff[lo] + (t - w.kpre[lo]);
-                    const uint4 *ep = reinterpret_cast<const uint4 *>(d.elems + (size_t)s * 8);
-                    const uint4 e0 = ep[0], e1 = ep[1];
-                    if (e1.z != EMPTY) {
-                        pending = true;
-                        ebase = e1.z & BASE_MASK;
-                        eb.w[0] = e0.x; eb.w[1] = e0.y; eb.w[2] = e0.z; eb.w[3] = e0.w;
-                        eb.w[4] = e1.x; eb.w[5] = e1.y;
+                    const uint32_t o_incl = __shfl_sync(0xffffffffu, incl, lo);
+                    const uint32_t o_cnt = __shfl_sync(0xffffffffu, cnt, lo);
+                    const uint32_t o_beg = __shfl_sync(0xffffffffu, beg, lo);
+                    const uint32_t o_r = __shfl_sync(0xffffffffu, r, lo);
+                    const uint32_t o_C = __shfl_sync(0xffffffffu, C, lo);
+                    const uint32_t o_csr = __shfl_sync(0xffffffffu, csr, lo);
+                    bool pending = false;
+                    uint32_t ckey = 0;
+                    Bits eb;
+                    if (f < nitems) {
+                        const uint32_t item = o_beg + (f - (o_incl - o_cnt));
+                        uint32_t b2;
+#pragma unroll
+                        for (int x = 0; x < EW; x++) eb.w[x] = 0;
+                        bool valid = true;
+                        if (o_csr) {
+                            const uint32_t dst = __ldg(c_rt.csr_col[o_C] + item);
+                            b2 = dst / EIDS;
+                            const uint32_t ob = dst % EIDS;
+#pragma unroll
+                            for (int x = 0; x < EW; x++) eb.w[x] = (uint32_t)x == (ob >> 5) ? 1u << (ob & 31) : 0u;
+                        } else {
+                            const uint4 *ep = reinterpret_cast<const uint4 *>(d.elems + (size_t)item * 8);
+                            const uint4 e0 = ep[0], e1 = ep[1];
+                            valid = e1.z != EMPTY;
+                            b2 = e1.z & BASE_MASK;
+                            eb.w[0] = e0.x; eb.w[1] = e0.y; eb.w[2] = e0.z; eb.w[3] = e0.w;
+                            eb.w[4] = e1.x; eb.w[5] = e1.y;
+                        }
+                        if (valid) {
+                            n_right += o_csr ? 0 : 1;
+                            const int dd = (int)b2 - (int)w.rbase[o_r] + WIN_LO;
+                            if ((unsigned)dd < (unsigned)WIN) {
+#pragma unroll
+                                for (int x = 0; x < EW; x++)
+                                    if (eb.w[x]) atomicOr(&w.win[o_r][dd][x], eb.w[x]);
+                            } else {
+                                pending = true;
+                                ckey = (o_r << KEY_SHIFT) | b2;
+                            }
+                        }
+                    }
+                    while (__any_sync(0xffffffffu, pending)) {
+                        if (pending) pending = !acc_insert(w, ckey, eb);
+                        if (__any_sync(0xffffffffu, pending)) acc_flush(d, w, inserts);
                     }
                 }
-                n_right += __popc(__ballot_sync(0xffffffffu, pending)) * (lane == 0);
-                while (__any_sync(0xffffffffu, pending)) {
-                    if (pending) pending = !acc_insert(w, ebase, eb);
-                    if (__any_sync(0xffffffffu, pending)) ok &= acc_flush(d, w, A, row, trk, inserts);
-                }
             }
-            ok &= acc_flush(d, w, A, row, trk, inserts);
+            win_flush(d, w, inserts);
+            acc_flush(d, w, inserts);
         }
 
-        // old-left joins A ::= Bp B (this record is a delta of B at vertex `row`):
+        // old-left joins A ::= Bp B (record = delta of B at vertex `row`):
         // every h with Bp(h, row) gets the record's bits in row (A, h)
-        for (int q = c_rt.ol_start[B]; q < c_rt.ol_start[B + 1]; q++) {
-            const uint32_t A = c_rt.ol_A[q], rv = c_rt.ol_rev[q];
-            const bool trk = c_rt.track[A];
-            const uint64_t de = d.desc[(size_t)(rv - 1) * d.V + row];
-            const uint32_t off = (uint32_t)de, cap = (uint32_t)(de >> 32);
-            for (uint32_t t = lane; t < cap; t += 32) {
-                const uint4 *ep = reinterpret_cast<const uint4 *>(d.elems + (size_t)(off + t) * 8);
+        const uint32_t no = have ? c_rt.ol_start[B + 1] - c_rt.ol_start[B] : 0;
+        const uint32_t maxo = __reduce_max_sync(0xffffffffu, no);
+        for (uint32_t sg = 0; sg < maxo; sg++) {
+            const bool hs = sg < no;
+            const uint32_t q = c_rt.ol_start[B] + sg;
+            uint32_t cap = 0;
+            if (hs) {
+                const uint64_t de = d.desc[(size_t)(c_rt.ol_rev[q] - 1) * d.V + row];
+                w.rOff[lane] = (uint32_t)de;
+                cap = (uint32_t)(de >> 32);
+            }
+            w.rA[lane] = hs ? c_rt.ol_A[q] : 0;
+            const uint32_t total = warp_tasks(w, cap);
+            for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+                const uint32_t t = t0 + lane;
+                if (t >= total) continue;
+                const uint32_t r = task_record(w, t);
+                const uint4 *ep = reinterpret_cast<const uint4 *>(d.elems + (size_t)(w.rOff[r] + (t - w.kpre[r])) * 8);
                 const uint4 e0 = ep[0], e1 = ep[1];
                 if (e1.z == EMPTY) continue;
-                const uint32_t hb = e1.z & BASE_MASK;
-                const uint32_t hw[EW] = {e0.x, e0.y, e0.z, e0.w, e1.x, e1.y};
+                const uint32_t hb = e1.z & BASE_MASK, A = w.rA[r];
+                const bool trk = c_rt.track[A];
+                Bits xb;
+#pragma unroll
+                for (int x = 0; x < EW; x++) xb.w[x] = w.rbits[r][x];
+                const uint32_t xbase = w.rbase[r];
+                bool okr = true;
 #pragma unroll
                 for (int x = 0; x < EW; x++) {
-                    uint32_t bw = hw[x];
+                    uint32_t bw = x == 0 ? e0.x : x == 1 ? e0.y : x == 2 ? e0.z : x == 3 ? e0.w : x == 4 ? e1.x : e1.y;
                     while (bw) {
                         const int bit = __ffs(bw) - 1;
                         bw &= bw - 1;
-                        ok &= g_insert(d, A, hb * EIDS + x * 32 + bit, base, rb, trk);
+                        uint32_t ds;
+                        okr &= g_insert(d, A, hb * EIDS + x * 32 + bit, xbase, xb, trk, ds);
+                        if (ds != EMPTY) append_dirty(d, ds);
                         inserts++;
                     }
                 }
+                if (!okr) atomicOr(&w.fail, 1u << r);
             }
+            __syncwarp();
         }
 
-        if (__any_sync(0xffffffffu, !ok) && lane == 0) {
-            unsigned long long p = atomicAdd(&d.ctr[C_RETRY_N], 1ull);
-            retry_out[p] = (uint32_t)ri;
+        __syncwarp();
+        const bool failed = have && (!ok || ((w.fail >> lane) & 1u));
+        const unsigned fm = __ballot_sync(0xffffffffu, failed);
+        if (fm) {
+            unsigned long long p = 0;
+            if (lane == (uint32_t)(__ffs(fm) - 1)) p = atomicAdd(&d.ctr[C_RETRY_N], (unsigned long long)__popc(fm));
+            p = __shfl_sync(0xffffffffu, p, __ffs(fm) - 1);
+            if (failed) {
+                const uint64_t o = p + __popc(fm & ((1u << lane) - 1u));
+                retry_out[2 * o] = make_uint4(rb.w[0], rb.w[1], rb.w[2], rb.w[3]);
+                retry_out[2 * o + 1] = make_uint4(rb.w[4], rb.w[5], key, row);
+            }
         }
+        __syncwarp();
     }
     // per-warp work counters
-    for (int o = 16; o; o >>= 1) inserts += __shfl_xor_sync(0xffffffffu, inserts, o);
+    for (int o = 16; o; o >>= 1) {
+        inserts += __shfl_xor_sync(0xffffffffu, inserts, o);
+        n_left += __shfl_xor_sync(0xffffffffu, n_left, o);
+        n_right += __shfl_xor_sync(0xffffffffu, n_right, o);
+    }
     if (lane == 0) {
         if (n_left) atomicAdd(&d.ctr[C_LEFT], n_left);
         if (n_right) atomicAdd(&d.ctr[C_RIGHT], n_right);
         if (inserts) atomicAdd(&d.ctr[C_INSERTS], (unsigned long long)inserts);
+    }
+}
+
+// ------------------------------------------------------------ CSR of static rows
+
+// Edges per row of a packed (static) label: deg[v], and row[v].y = deg | min(elements,255) << 24.
+__global__ void k_csr_count(Dev d, uint32_t slot, uint32_t *deg, uint2 *row)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < d.V; v += gridDim.x * blockDim.x) {
+        const uint64_t de = d.desc[(size_t)(slot - 1) * d.V + v];
+        const uint32_t off = (uint32_t)de, cap = (uint32_t)(de >> 32);
+        uint32_t c = 0, nel = 0;
+        for (uint32_t j = 0; j < cap; j++) {
+            const uint32_t *p = d.elems + (size_t)(off + j) * 8;
+            if (p[6] == EMPTY) continue;
+            nel++;
+            for (int x = 0; x < EW; x++) c += __popc(p[x]);
+        }
+        deg[v] = c;
+        row[v].y = (c & 0xFFFFFFu) | (min(nel, 255u) << 24);
+        if (c > 0xFFFFFFu) atomicOr(&d.ctr[C_ERR], (unsigned long long)ERR_INTERNAL);
+    }
+}
+
+// Block-wise exclusive scan of n values (1024 per block); block totals to sums.
+__global__ void k_scan_blocks(const uint32_t *in, uint32_t *out, uint32_t *sums, uint64_t n)
+{
+    __shared__ uint32_t wsum[32];
+    const uint64_t i = blockIdx.x * 1024ull + threadIdx.x;
+    const uint32_t v = i < n ? in[i] : 0;
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31) wsum[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t s = wsum[lane], si = s;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, si, o);
+            if (lane >= (uint32_t)o) si += y;
+        }
+        wsum[lane] = si - s;
+        if (lane == 31) sums[blockIdx.x] = si;
+    }
+    __syncthreads();
+    if (i < n) out[i] = incl - v + wsum[wid];
+}
+
+// Exclusive scan of the block totals (one block, sequential over chunks of 1024); total at sums[nb].
+__global__ void k_scan_sums(uint32_t *sums, uint64_t nb)
+{
+    __shared__ uint32_t wsum[32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (uint64_t c0 = 0; c0 < nb; c0 += 1024) {
+        const uint64_t i = c0 + threadIdx.x;
+        const uint32_t v = i < nb ? sums[i] : 0;
+        uint32_t incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        if (lane == 31) wsum[wid] = incl;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t s = wsum[lane], si = s;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, si, o);
+                if (lane >= (uint32_t)o) si += y;
+            }
+            wsum[lane] = si - s;
+        }
+        __syncthreads();
+        const uint32_t base = carry;
+        if (i < nb) sums[i] = base + incl - v + wsum[wid];
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = base + wsum[wid] + incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) sums[nb] = carry;
+}
+
+__global__ void k_scan_add(uint32_t *out, const uint32_t *sums, uint64_t n)
+{
+    const uint64_t i = blockIdx.x * 1024ull + threadIdx.x;
+    if (i < n) out[i] += sums[blockIdx.x];
+}
+
+// Destination ids of every row of a packed label at ptr[v]; row[v].x = ptr[v].
+__global__ void k_csr_fill(Dev d, uint32_t slot, const uint32_t *ptr, uint2 *row, uint32_t *col)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < d.V; v += gridDim.x * blockDim.x) {
+        const uint64_t de = d.desc[(size_t)(slot - 1) * d.V + v];
+        const uint32_t off = (uint32_t)de, cap = (uint32_t)(de >> 32);
+        uint32_t pos = ptr[v];
+        row[v].x = pos;
+        for (uint32_t j = 0; j < cap; j++) {
+            const uint32_t *p = d.elems + (size_t)(off + j) * 8;
+            const uint32_t k = p[6];
+            if (k == EMPTY) continue;
+            const uint32_t b = k & BASE_MASK;
+            for (int x = 0; x < EW; x++) {
+                uint32_t bw = p[x];
+                while (bw) {
+                    const int bit = __ffs(bw) - 1;
+                    bw &= bw - 1;
+                    col[pos++] = b * EIDS + x * 32 + bit;
+                }
+            }
+        }
     }
 }
 
@@ -421,6 +762,9 @@ __global__ void k_grow(Dev d, uint64_t n)
             e[0] = make_uint4(0, 0, 0, 0);
             e[1] = make_uint4(0, 0, EMPTY, row);
             uint4 *b = reinterpret_cast<uint4 *>(d.dbits + (nb + t) * 8);
+            b[0] = make_uint4(0, 0, 0, 0);
+            b[1] = make_uint4(0, 0, 0, 0);
+            b = reinterpret_cast<uint4 *>(d.dcur + (nb + t) * 8);
             b[0] = make_uint4(0, 0, 0, 0);
             b[1] = make_uint4(0, 0, 0, 0);
         }
@@ -553,13 +897,14 @@ struct grg_ctx {
     // device memory
     uint64_t pool_bytes_req = 0;
     uint64_t pool_cap = 0;         // elements
-    uint32_t *elems = nullptr, *dbits = nullptr, *dirty = nullptr;
+    uint32_t *elems = nullptr;
+    uint32_t *dbits[2] = {nullptr, nullptr};   // delta bitmaps, by round parity
+    uint32_t *dirty[2] = {nullptr, nullptr};   // dirty lists, by round parity
+    int cur = 0;                               // parity read by the current round
     uint64_t *desc = nullptr;
     uint32_t *cnt = nullptr, *want = nullptr, *grow = nullptr;
-    uint4 *delta = nullptr;
-    uint64_t delta_cap = 0;        // records
-    uint32_t *retry[2] = {nullptr, nullptr};
-    uint64_t retry_cap = 0;
+    uint4 *rbuf[3] = {nullptr, nullptr, nullptr};   // [2]: gathered deltas; [0],[1]: retry passes
+    uint64_t rbuf_cap = 0;                     // records
     unsigned long long *ctr = nullptr;
     unsigned long long *h_ctr = nullptr;   // pinned
     uint32_t *d_in32 = nullptr;            // staged input edges (src, dst)
@@ -567,6 +912,7 @@ struct grg_ctx {
     uint64_t in_cap = 0;
     RuleTable rt{};
     uint64_t launches = 0;
+    std::vector<uint32_t *> csr_bufs;      // CSR copies of static labels (freed on reload)
 };
 
 namespace {
@@ -609,15 +955,17 @@ int grid_for(const grg_ctx *c, uint64_t n, int block, int per_sm = 8)
     return (int)std::max<uint64_t>(g, 1);
 }
 
+// Device view for a round that reads parity c->cur and writes parity c->cur ^ 1.
 Dev make_dev(const grg_ctx *c)
 {
     Dev d;
     d.elems = c->elems;
-    d.dbits = c->dbits;
+    d.dcur = c->dbits[c->cur];
+    d.dbits = c->dbits[c->cur ^ 1];
     d.desc = c->desc;
     d.cnt = c->cnt;
     d.want = c->want;
-    d.dirty = c->dirty;
+    d.dirty = c->dirty[c->cur ^ 1];
     d.grow = c->grow;
     d.ctr = c->ctr;
     d.V = c->V;
@@ -625,8 +973,15 @@ Dev make_dev(const grg_ctx *c)
     return d;
 }
 
+void free_csr(grg_ctx *c)
+{
+    for (uint32_t *p : c->csr_bufs) cudaFree(p);
+    c->csr_bufs.clear();
+}
+
 void free_graph(grg_ctx *c)
 {
+    free_csr(c);
     cudaFree(c->desc); c->desc = nullptr;
     cudaFree(c->cnt); c->cnt = nullptr;
     cudaFree(c->want); c->want = nullptr;
@@ -637,8 +992,10 @@ void free_graph(grg_ctx *c)
 void free_pool(grg_ctx *c)
 {
     cudaFree(c->elems); c->elems = nullptr;
-    cudaFree(c->dbits); c->dbits = nullptr;
-    cudaFree(c->dirty); c->dirty = nullptr;
+    for (int p = 0; p < 2; p++) {
+        cudaFree(c->dbits[p]); c->dbits[p] = nullptr;
+        cudaFree(c->dirty[p]); c->dirty[p] = nullptr;
+    }
     c->pool_cap = 0;
 }
 
@@ -650,32 +1007,40 @@ int read_ctr(grg_ctx *c)
 }
 
 
-// Pool of `elems` 32-byte slots + delta bitmaps + dirty list (68 bytes per slot).
+constexpr uint64_t POOL_BYTES_PER_SLOT = 32 + 2 * 32 + 2 * 4;
+
+// Pool of `elems` 32-byte slots + two delta-bitmap pools + two dirty lists.
 int alloc_pool(grg_ctx *c, uint64_t elems)
 {
     if (elems > 0xFFFFFFF0ull) elems = 0xFFFFFFF0ull;
-    uint32_t *e = nullptr, *b = nullptr, *dl = nullptr;
-    if (cudaMalloc(&e, elems * 32) != cudaSuccess || cudaMalloc(&b, elems * 32) != cudaSuccess ||
-        cudaMalloc(&dl, elems * 4) != cudaSuccess) {
+    uint32_t *e = nullptr, *b[2] = {nullptr, nullptr}, *dl[2] = {nullptr, nullptr};
+    auto release = [&]() {
+        cudaFree(e);
+        for (int p = 0; p < 2; p++) { cudaFree(b[p]); cudaFree(dl[p]); }
+    };
+    if (cudaMalloc(&e, elems * 32) != cudaSuccess || cudaMalloc(&b[0], elems * 32) != cudaSuccess ||
+        cudaMalloc(&b[1], elems * 32) != cudaSuccess || cudaMalloc(&dl[0], elems * 4) != cudaSuccess ||
+        cudaMalloc(&dl[1], elems * 4) != cudaSuccess) {
         cudaGetLastError();
-        cudaFree(e); cudaFree(b); cudaFree(dl);
+        release();
         return fail(c, GRG_E_NOMEM, "cannot allocate element pool of " + std::to_string(elems) + " slots");
     }
     if (c->elems) {
-        // grow: keep the used part and the pending dirty list
+        // grow: keep the used part and the dirty list being written
         int st = read_ctr(c);
-        if (st) { cudaFree(e); cudaFree(b); cudaFree(dl); return st; }
-        uint64_t used = std::min<uint64_t>(c->h_ctr[C_POOL_TOP], c->pool_cap);
-        uint64_t nd = c->h_ctr[C_DIRTY_N];
+        if (st) { release(); return st; }
+        const uint64_t used = std::min<uint64_t>(c->h_ctr[C_POOL_TOP], c->pool_cap);
+        const uint64_t nd = c->h_ctr[C_DIRTY_N];
+        const int nx = c->cur ^ 1;
         GRG_CUDA(c, cudaMemcpyAsync(e, c->elems, used * 32, cudaMemcpyDeviceToDevice, c->stream));
-        GRG_CUDA(c, cudaMemcpyAsync(b, c->dbits, used * 32, cudaMemcpyDeviceToDevice, c->stream));
-        GRG_CUDA(c, cudaMemcpyAsync(dl, c->dirty, nd * 4, cudaMemcpyDeviceToDevice, c->stream));
+        for (int p = 0; p < 2; p++)
+            GRG_CUDA(c, cudaMemcpyAsync(b[p], c->dbits[p], used * 32, cudaMemcpyDeviceToDevice, c->stream));
+        GRG_CUDA(c, cudaMemcpyAsync(dl[nx], c->dirty[nx], nd * 4, cudaMemcpyDeviceToDevice, c->stream));
         GRG_CUDA(c, cudaStreamSynchronize(c->stream));
         free_pool(c);
     }
     c->elems = e;
-    c->dbits = b;
-    c->dirty = dl;
+    for (int p = 0; p < 2; p++) { c->dbits[p] = b[p]; c->dirty[p] = dl[p]; }
     c->pool_cap = elems;
     return GRG_OK;
 }
@@ -685,24 +1050,23 @@ int grow_pool(grg_ctx *c, uint64_t min_elems)
     uint64_t want = std::max<uint64_t>(c->pool_cap * 2, min_elems);
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
-    uint64_t fit = (uint64_t)((double)fr * 0.9) / 68;
+    uint64_t fit = (uint64_t)((double)fr * 0.9) / POOL_BYTES_PER_SLOT;
     if (want > fit) want = fit;
     if (want <= c->pool_cap) return fail(c, GRG_E_NOMEM, "element pool exhausted and device memory is full");
     return alloc_pool(c, want);
 }
 
-int ensure_delta(grg_ctx *c, uint64_t n)
+// Retry buffers: every delta record of a pass may fail once, so n records each.
+int ensure_rbuf(grg_ctx *c, uint64_t n)
 {
-    if (n <= c->delta_cap) return GRG_OK;
-    uint64_t cap = std::max<uint64_t>(n + n / 2, 1 << 16);
-    cudaFree(c->delta);
-    cudaFree(c->retry[0]);
-    cudaFree(c->retry[1]);
-    c->delta = nullptr; c->retry[0] = c->retry[1] = nullptr;
-    GRG_CUDA(c, cudaMalloc(&c->delta, cap * 32));
-    GRG_CUDA(c, cudaMalloc(&c->retry[0], cap * 4));
-    GRG_CUDA(c, cudaMalloc(&c->retry[1], cap * 4));
-    c->delta_cap = cap;
+    if (n <= c->rbuf_cap) return GRG_OK;
+    const uint64_t cap = std::max<uint64_t>(n + n / 2, 1 << 16);
+    for (int i = 0; i < 3; i++) {
+        cudaFree(c->rbuf[i]);
+        c->rbuf[i] = nullptr;
+    }
+    for (int i = 0; i < 3; i++) GRG_CUDA(c, cudaMalloc(&c->rbuf[i], cap * 32));
+    c->rbuf_cap = cap;
     return GRG_OK;
 }
 
@@ -816,9 +1180,7 @@ void grg_destroy(grg_ctx *c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_graph(c);
     free_pool(c);
-    cudaFree(c->delta);
-    cudaFree(c->retry[0]);
-    cudaFree(c->retry[1]);
+    for (int i = 0; i < 3; i++) cudaFree(c->rbuf[i]);
     cudaFree(c->ctr);
     cudaFree(c->d_in32);
     cudaFree(c->d_in8);
@@ -874,11 +1236,11 @@ int grg_allocate_pool(grg_ctx *c, uint64_t pool_bytes)
     c->pool_bytes_req = pool_bytes;
     uint64_t elems;
     if (pool_bytes) {
-        elems = pool_bytes / 68;
+        elems = pool_bytes / POOL_BYTES_PER_SLOT;
     } else {
         size_t fr = 0, tot = 0;
         cudaMemGetInfo(&fr, &tot);
-        elems = (uint64_t)(fr / 8) / 68;   // start at 1/8 of free memory; grows on demand
+        elems = (uint64_t)(fr / 8) / POOL_BYTES_PER_SLOT;   // start at 1/8 of free memory; grows on demand
     }
     if (elems < 1024) elems = 1024;
     if (c->elems && c->pool_cap >= elems) return GRG_OK;
@@ -963,7 +1325,7 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
     }
     uint64_t top = c->h_ctr[C_POOL_TOP];
     if (top) {
-        k_init_region<<<grid_for(c, top, 256), 256, 0, s>>>(c->elems, c->dbits, 0, top);
+        k_init_region<<<grid_for(c, top, 256), 256, 0, s>>>(c->elems, c->dbits[0], c->dbits[1], 0, top);
         c->launches++;
     }
     if (num_edges) {
@@ -1012,14 +1374,53 @@ int grg_closure(grg_ctx *c, uint32_t filter, grg_stats *stats)
             k_compact_static<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)l);
             c->launches++;
         }
+    // CSR copies of static labels that are a binary rule's second symbol
+    free_csr(c);
+    for (int l = 1; l <= c->L; l++) {
+        bool rhs2 = false;
+        for (int q = 0; q < c->R; q++)
+            if (c->rules[3 * q + 1] && c->rules[3 * q + 2] == l) rhs2 = true;
+        if (derivable[l] || !rhs2 || c->V == 0) continue;
+        uint32_t *ptr = nullptr, *sums = nullptr, *col = nullptr, *row = nullptr;
+        const uint64_t nb = (c->V + 1023) / 1024;
+        GRG_CUDA(c, cudaMalloc(&ptr, ((uint64_t)c->V + 1) * 4));
+        c->csr_bufs.push_back(ptr);
+        GRG_CUDA(c, cudaMalloc(&row, ((uint64_t)c->V + 1) * 8));
+        c->csr_bufs.push_back(row);
+        GRG_CUDA(c, cudaMalloc(&sums, (nb + 1) * 4));
+        c->csr_bufs.push_back(sums);
+        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_ERR, 0, 8, s));
+        k_csr_count<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)l, ptr, (uint2 *)row);
+        k_scan_blocks<<<(unsigned)nb, 1024, 0, s>>>(ptr, ptr, sums, c->V);
+        k_scan_sums<<<1, 1024, 0, s>>>(sums, nb);
+        k_scan_add<<<(unsigned)nb, 1024, 0, s>>>(ptr, sums, c->V);
+        st = read_ctr(c);
+        if (st) return st;
+        if (c->h_ctr[C_ERR]) continue;                 // a row too long for the packed CSR: keep elements
+        uint32_t total = 0;
+        GRG_CUDA(c, cudaMemcpyAsync(&total, sums + nb, 4, cudaMemcpyDeviceToHost, s));
+        GRG_CUDA(c, cudaStreamSynchronize(s));
+        GRG_CUDA(c, cudaMalloc(&col, std::max<uint64_t>(total, 1) * 4));
+        c->csr_bufs.push_back(col);
+        k_csr_fill<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)l, ptr, (uint2 *)row, col);
+        c->launches += 6;
+        rt.csr_row[l] = (const uint2 *)row;
+        rt.csr_col[l] = col;
+    }
+    c->rt = rt;
+    GRG_CUDA(c, cudaMemcpyToSymbolAsync(c_rt, &rt, sizeof rt, 0, cudaMemcpyHostToDevice, s));
     st = read_ctr(c);
     if (st) return st;
     const uint64_t top = c->h_ctr[C_POOL_TOP];
     GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_DIRTY_N, 0, 8, s));
+    // every loaded element of a tracked label is a delta of round 1 (written to parity 0)
+    c->cur = 1;
+    d = make_dev(c);
     if (top) {
         k_mark_all<<<grid_for(c, top, 256), 256, 0, s>>>(d, top);
         c->launches++;
     }
+    c->cur = 0;
     double join_ms = 0;
     uint64_t joins = 0;
     for (;;) {
@@ -1027,21 +1428,24 @@ int grg_closure(grg_ctx *c, uint32_t filter, grg_stats *stats)
         if (st) return st;
         const uint64_t nd = c->h_ctr[C_DIRTY_N];
         if (nd == 0) break;
-        st = ensure_delta(c, nd);
+        st = ensure_rbuf(c, nd);
         if (st) return st;
         S.rounds++;
         S.delta_elems += nd;
-        k_gather<<<grid_for(c, nd, 256), 256, 0, s>>>(d, nd, c->delta);
+        d = make_dev(c);
+        k_gather<<<grid_for(c, nd, 256), 256, 0, s>>>(d, c->dirty[c->cur], nd, c->rbuf[2]);
         c->launches++;
         GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_DIRTY_N, 0, 8, s));
         GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_RETRY_N, 0, 16, s));   // retry + grow counters
-        const uint32_t *idx = nullptr;
         uint64_t n = nd;
         int rb = 0;
         for (int pass = 0;; pass++) {
-            const int jgrid = grid_for(c, n, JOIN_WARPS, 16);
+            const int jgrid = grid_for(c, (n + RB - 1) / RB, JOIN_WARPS, 16);
             if (c->timing) GRG_CUDA(c, cudaEventRecord(c->ev_c, s));
-            k_join<<<jgrid, JOIN_WARPS * 32, 0, s>>>(d, c->delta, n, idx, c->retry[rb]);
+            if (pass == 0)
+                k_join<<<jgrid, JOIN_WARPS * 32, 0, s>>>(d, nullptr, c->rbuf[2], n, c->rbuf[0]);
+            else
+                k_join<<<jgrid, JOIN_WARPS * 32, 0, s>>>(d, nullptr, c->rbuf[rb], n, c->rbuf[rb ^ 1]);
             c->launches++;
             joins++;
             if (c->timing) GRG_CUDA(c, cudaEventRecord(c->ev_d, s));
@@ -1072,11 +1476,11 @@ int grg_closure(grg_ctx *c, uint32_t filter, grg_stats *stats)
                 d = make_dev(c);
             }
             if (pass > 64) return fail(c, GRG_E_CUDA, "table growth did not converge");
-            idx = c->retry[rb];
+            rb = pass == 0 ? 0 : rb ^ 1;   // records that failed this pass are in rbuf[rb]
             n = nr;
-            rb ^= 1;
             GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_RETRY_N, 0, 16, s));
         }
+        c->cur ^= 1;
     }
     GRG_CUDA(c, cudaEventRecord(c->ev_b, s));
     GRG_CUDA(c, cudaEventSynchronize(c->ev_b));
@@ -1313,7 +1717,8 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
             (r[1] == 0 && r[2] != 0))
             return GRG_E_ARG;
     }
-    // scratch layout: counters | descriptors | cnt | want | grow | pool arrays (108 B per element)
+    // scratch layout: counters | descriptors | cnt | want | grow | pool arrays (168 B per element:
+    // element, two delta bitmaps, two dirty lists, two retry records)
     const uint64_t ntab = (uint64_t)(2 * num_labels) * num_vars;
     size_t off = 0;
     const size_t o_ctr = off; off = align256(off + sizeof(unsigned long long) * NCTR);
@@ -1322,14 +1727,15 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     const size_t o_want = off; off = align256(off + ntab * 4);
     const size_t o_grow = off; off = align256(off + ntab * 4);
     if (off >= NOALLOC_SCRATCH_BYTES) return GRG_E_RANGE;            // tables alone exceed the scratch
-    uint64_t pool = (NOALLOC_SCRATCH_BYTES - off - 6 * 256) / 108;
+    uint64_t pool = (NOALLOC_SCRATCH_BYTES - off - 8 * 256) / 168;
     if (pool < 4096 || num_edges > pool / 2) return GRG_E_RANGE;    // graph too large for the scratch
     const size_t o_elems = off; off = align256(off + pool * 32);
-    const size_t o_dbits = off; off = align256(off + pool * 32);
-    const size_t o_dirty = off; off = align256(off + pool * 4);
-    const size_t o_delta = off; off = align256(off + pool * 32);
-    const size_t o_retry0 = off; off = align256(off + pool * 4);
-    const size_t o_retry1 = off; off = align256(off + pool * 4);
+    const size_t o_dbits0 = off; off = align256(off + pool * 32);
+    const size_t o_dbits1 = off; off = align256(off + pool * 32);
+    const size_t o_dirty0 = off; off = align256(off + pool * 4);
+    const size_t o_dirty1 = off; off = align256(off + pool * 4);
+    const size_t o_rbuf0 = off; off = align256(off + pool * 32);
+    const size_t o_rbuf1 = off; off = align256(off + pool * 32);
     if (off > NOALLOC_SCRATCH_BYTES) return GRG_E_RANGE;
 
     RuleTable rt;
@@ -1361,12 +1767,19 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     d.want = (uint32_t *)(base + o_want);
     d.grow = (uint32_t *)(base + o_grow);
     d.elems = (uint32_t *)(base + o_elems);
-    d.dbits = (uint32_t *)(base + o_dbits);
-    d.dirty = (uint32_t *)(base + o_dirty);
+    uint32_t *dbits[2] = {(uint32_t *)(base + o_dbits0), (uint32_t *)(base + o_dbits1)};
+    uint32_t *dirty[2] = {(uint32_t *)(base + o_dirty0), (uint32_t *)(base + o_dirty1)};
+    uint4 *rbuf[2] = {(uint4 *)(base + o_rbuf0), (uint4 *)(base + o_rbuf1)};
+    // round parity cur reads dbits[cur]/dirty[cur] and writes the other pair; the
+    // initial deltas are written to parity 0
+    auto set_parity = [&](int cur) {
+        d.dcur = dbits[cur];
+        d.dbits = dbits[cur ^ 1];
+        d.dirty = dirty[cur ^ 1];
+    };
+    set_parity(1);
     d.V = num_vars;
     d.pool_cap = (uint32_t)pool;
-    uint4 *delta = (uint4 *)(base + o_delta);
-    uint32_t *retry[2] = {(uint32_t *)(base + o_retry0), (uint32_t *)(base + o_retry1)};
     unsigned long long h[NCTR];
 
     // the array keeps the previous call's contents: clear everything that must start at zero
@@ -1385,7 +1798,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     if ((st = na_read(h, d.ctr, s))) return st;
     if (h[C_ERR] & ERR_POOL) return GRG_E_NOMEM;
     const uint64_t top0 = h[C_POOL_TOP];
-    if (top0) k_init_region<<<grid(top0, 256, 8), 256, 0, s>>>(d.elems, d.dbits, 0, top0);
+    if (top0) k_init_region<<<grid(top0, 256, 8), 256, 0, s>>>(d.elems, dbits[0], dbits[1], 0, top0);
     if (num_edges) k_load_insert<<<grid(num_edges, 256, 8), 256, 0, s>>>(d, d_src, d_dst, d_label, num_edges);
     for (int q = 0; q < num_rules; q++)
         if (rules[3 * q + 1] == 0) k_eps_insert<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)rules[3 * q]);
@@ -1398,19 +1811,23 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
 
     // semi-naive rounds (grg_closure); the pool cannot grow here
     uint64_t rounds = 0;
+    int cur = 0;
     for (;;) {
         if ((st = na_read(h, d.ctr, s))) return st;
         const uint64_t nd = h[C_DIRTY_N];
         if (nd == 0) break;
         rounds++;
-        k_gather<<<grid(nd, 256, 8), 256, 0, s>>>(d, nd, delta);
+        set_parity(cur);
         NA_CUDA(cudaMemsetAsync(d.ctr + C_DIRTY_N, 0, 8, s));
         NA_CUDA(cudaMemsetAsync(d.ctr + C_RETRY_N, 0, 16, s));
-        const uint32_t *idx = nullptr;
         uint64_t n = nd;
         int rb = 0;
         for (int pass = 0;; pass++) {
-            k_join<<<grid(n, JOIN_WARPS, 16), JOIN_WARPS * 32, 0, s>>>(d, delta, n, idx, retry[rb]);
+            const int g = grid((n + RB - 1) / RB, JOIN_WARPS, 16);
+            if (pass == 0)
+                k_join<<<g, JOIN_WARPS * 32, 0, s>>>(d, dirty[cur], nullptr, n, rbuf[0]);
+            else
+                k_join<<<g, JOIN_WARPS * 32, 0, s>>>(d, nullptr, rbuf[rb], n, rbuf[rb ^ 1]);
             NA_CUDA(cudaGetLastError());
             if ((st = na_read(h, d.ctr, s))) return st;
             const uint64_t nr = h[C_RETRY_N];
@@ -1420,11 +1837,11 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
             if ((st = na_read(h, d.ctr, s))) return st;
             if (h[C_ERR] & ERR_POOL) return GRG_E_NOMEM;          // closure outgrew the scratch
             if (pass > 64) return GRG_E_CUDA;
-            idx = retry[rb];
+            rb = pass == 0 ? 0 : rb ^ 1;
             n = nr;
-            rb ^= 1;
             NA_CUDA(cudaMemsetAsync(d.ctr + C_RETRY_N, 0, 16, s));
         }
+        cur ^= 1;
     }
 
     // per-label counts and edge-set hash into the caller's device buffers

@@ -157,7 +157,7 @@ int grg_parse_graph(const char *path, int num_labels, const char *names, uint64_
  * (the legacy default stream); the call returns after the stream is idle.
  *
  * Limits: the tables take 40 bytes per (label, vertex) and the rest of the
- * array holds 108 bytes per element slot; graphs whose tables leave fewer
+ * array holds 168 bytes per element slot; graphs whose tables leave fewer
  * than 4096 slots, or with more edges than half the slots, are rejected with
  * GRG_E_RANGE before any launch; a closure that outgrows the array returns
  * GRG_E_NOMEM.
