@@ -15,13 +15,15 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
-OUT = os.path.join(HERE, "_build")
+OUT = os.environ.get("GRG_BUILD_DIR") or os.path.join(HERE, "_build")
 INC = os.path.join(ROOT, "include")
 LIB = os.path.join(OUT, "libgrg.so")
 COMP = os.path.join(OUT, "comp")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC, "-I", CSRC]
+# tuning overrides of the join kernel, e.g. GRG_NVCC_DEFS="-DGRG_WIN=4 -DGRG_JOIN_UNROLL=2"
+NVCC_FLAGS += os.environ.get("GRG_NVCC_DEFS", "").split()
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I", INC]
 
 CU_SOURCES = ["grg_engine.cu"]

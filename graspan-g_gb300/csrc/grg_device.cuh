@@ -9,12 +9,13 @@
 // row's elements are hashed by base, so a lookup is one or two probes instead
 // of a list walk and rows never need re-sorting.
 //
-// Deltas: two parallel pools of 32-byte delta bitmaps (words 0..5 = bits that
-// became set, word 6 = dirty flag) and two dirty lists of slot indices, used
-// alternately: round t reads the bitmaps and list written in round t-1 and
-// writes the next ones. The first thread that sets new bits in an element
-// appends it, so a dirty list holds each element at most once and can never
-// overflow the pool's size. This replaces the reference's tmp region and the
+// Deltas: a parallel pool of 32-byte delta bitmaps (words 0..5 = bits that
+// became set this round) and a dirty bitmap with one bit per pool slot. An
+// insert that sets new bits ORs them into the slot's delta bitmap and sets the
+// slot's dirty bit, both fire-and-forget; the next round's gather scans the
+// dirty bitmap and emits one delta record per dirty slot, in slot order (so a
+// row's records come out together). Nothing is appended to a shared list, so
+// no counter is contended and no capacity can be exceeded. This replaces the reference's tmp region and the
 // diff/merge kernels (src/kernel.cu:841-985): new edges are found by atomicOr
 // on the stored element, which returns exactly the bits that were new.
 #pragma once
@@ -35,7 +36,7 @@ constexpr int MAX_RULES = 64;
 // device counter block indices
 enum : int {
     C_POOL_TOP = 0,   // bump allocator (elements)
-    C_DIRTY_N = 1,    // dirty-list length
+    C_DIRTY_N = 1,    // delta records gathered this round
     C_RETRY_N = 2,    // retry-list length (delta records to re-run)
     C_GROW_N = 3,     // grow-list length
     C_ERR = 4,        // error bits
@@ -45,7 +46,10 @@ enum : int {
     C_TOTAL = 8,      // edge count (count kernel)
     C_HASH = 9,       // edge-set hash (hash kernel)
     C_EXPORT = 10,    // export cursor
-    C_LABEL0 = 16,    // per-label edge counts: C_LABEL0 + slot
+    C_PH0 = 11,       // join phase cycle counters (built with -DGRG_PHASE_TIMERS): 11..15
+    C_CAND_N = 16,    // candidate elements written by joins for k_apply
+    C_AFAIL = 17,     // candidates k_apply could not insert (tables to grow)
+    C_LABEL0 = 24,    // per-label edge counts: C_LABEL0 + slot
     NCTR = C_LABEL0 + MAX_SLOTS + 2
 };
 enum : unsigned long long { ERR_POOL = 1, ERR_LOAD = 2, ERR_INTERNAL = 4 };
@@ -73,13 +77,14 @@ struct RuleTable {
 
 struct Dev {
     uint32_t *elems;          // pool: 8 words per slot
-    uint32_t *dbits;          // delta bitmaps written this round: 8 words per slot
-    uint32_t *dcur;           // delta bitmaps read (and cleared) this round
+    uint32_t *dbits;          // delta bitmaps: 8 words per slot
     uint64_t *desc;           // [(slot-1)*V + row] = cap << 32 | offset
     uint32_t *cnt;            // occupied slots per table
     uint32_t *want;           // failed inserts per table since its last growth
-    uint32_t *dirty;          // dirty list (slot indices)
+    uint32_t *dmap;           // dirty bitmap: bit s = slot s has delta bits
     uint32_t *grow;           // grow list (table indices)
+    uint4 *cand;              // candidate elements (32 B: bits[6], key, row) for k_apply; may be null
+    uint64_t cand_cap;        // candidates
     unsigned long long *ctr;  // counter block
     uint32_t V;
     uint32_t pool_cap;        // elements
@@ -105,21 +110,13 @@ __device__ __forceinline__ uint64_t edge_hash(uint32_t l, uint32_t s, uint32_t d
     return splitmix64(splitmix64(((uint64_t)s << 32) | d) ^ ((uint64_t)l * 0x9E3779B97F4A7C15ull));
 }
 
-__device__ __forceinline__ void append_dirty(const Dev &d, uint32_t s)
-{
-    unsigned long long i = atomicAdd(&d.ctr[C_DIRTY_N], 1ull);
-    d.dirty[i] = s;   // capacity = pool size; each slot is appended at most once per round
-}
-
 // OR `b` into element (slot, row, base). Returns false when the table is full
 // or absent; the failure is recorded so the table grows before a retry. With
-// `track`, the bits that were new go to the element's delta bitmap, and if they
-// are the element's first new bits of the round `dirty_slot` receives the slot
-// (the caller appends it to the dirty list); otherwise dirty_slot = EMPTY.
+// `track`, the bits that were new are ORed into the element's delta bitmap and
+// its dirty bit is set (both without waiting for a reply).
 __device__ __forceinline__ bool g_insert(const Dev &d, uint32_t slot, uint32_t row, uint32_t base, const Bits b,
-                                         bool track, uint32_t &dirty_slot)
+                                         bool track)
 {
-    dirty_slot = EMPTY;
     const size_t ti = (size_t)(slot - 1) * d.V + row;
     const uint64_t de = d.desc[ti];
     const uint32_t off = (uint32_t)de, cap = (uint32_t)(de >> 32);
@@ -165,22 +162,9 @@ __device__ __forceinline__ bool g_insert(const Dev &d, uint32_t slot, uint32_t r
 #pragma unroll
         for (int w = 0; w < EW; w++)
             if (nb.w[w]) atomicOr(&db[w], nb.w[w]);
-        if (atomicExch(&db[6], 1u) == 0) dirty_slot = s;
+        atomicOr(&d.dmap[s >> 5], 1u << (s & 31));
     }
     return true;
-}
-
-// Warp-aggregated append of the lanes' dirty slots (EMPTY = none). All 32 lanes call it.
-__device__ __forceinline__ void warp_append_dirty(const Dev &d, uint32_t ds)
-{
-    const unsigned m = __ballot_sync(0xffffffffu, ds != EMPTY);
-    if (!m) return;
-    const uint32_t lane = threadIdx.x & 31;
-    const int leader = __ffs(m) - 1;
-    unsigned long long b = 0;
-    if ((int)lane == leader) b = atomicAdd(&d.ctr[C_DIRTY_N], (unsigned long long)__popc(m));
-    b = __shfl_sync(0xffffffffu, b, leader);
-    if (ds != EMPTY) d.dirty[b + __popc(m & ((1u << lane) - 1u))] = ds;
 }
 
 }  // namespace grg

@@ -29,11 +29,41 @@ namespace grg {
 
 __constant__ RuleTable c_rt;
 
-constexpr int JOIN_WARPS = 4;     // warps per join block
+// Join tuning (compile-time; -DGRG_... overrides for sweeps)
+#ifndef GRG_JOIN_WARPS
+#define GRG_JOIN_WARPS 4
+#endif
+#ifndef GRG_WIN
+#define GRG_WIN 8
+#endif
+#ifndef GRG_WIN_LO
+#define GRG_WIN_LO 3
+#endif
+#ifndef GRG_ACC_LG
+#define GRG_ACC_LG 6
+#endif
+#ifndef GRG_JOIN_MINB
+#define GRG_JOIN_MINB 6
+#endif
+#ifndef GRG_JOIN_UNROLL
+#define GRG_JOIN_UNROLL 1
+#endif
+#ifdef GRG_PHASE_TIMERS
+#define PH_MARK(i)                                   \
+    do {                                             \
+        const long long t_ = clock64();              \
+        ph[i] += (unsigned long long)(t_ - ph_t);    \
+        ph_t = t_;                                   \
+    } while (0)
+#else
+#define PH_MARK(i) do { } while (0)
+#endif
+constexpr int JOIN_WARPS = GRG_JOIN_WARPS;  // warps per join block
 constexpr int RB = 32;            // delta records per warp batch (one per lane)
-constexpr int WIN = 8;            // dense accumulator window: elements base-WIN_LO .. base+WIN-1-WIN_LO
-constexpr int WIN_LO = 3;
-constexpr int ACC_LG = 6;
+constexpr int WIN = GRG_WIN;      // dense accumulator window: elements base-WIN_LO .. base+WIN-1-WIN_LO
+constexpr int WIN_LO = GRG_WIN_LO;
+constexpr int JOIN_UNROLL = GRG_JOIN_UNROLL;
+constexpr int ACC_LG = GRG_ACC_LG;
 constexpr int ACC = 1 << ACC_LG;  // per-warp hash accumulator entries (candidates outside the window)
 constexpr int ACC_MAX = ACC * 3 / 4;
 
@@ -41,17 +71,14 @@ __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
 
 // ---------------------------------------------------------------- loader
 
-__global__ void k_init_region(uint32_t *elems, uint32_t *dbits0, uint32_t *dbits1, uint64_t begin, uint64_t end)
+__global__ void k_init_region(uint32_t *elems, uint32_t *dbits, uint64_t begin, uint64_t end)
 {
     for (uint64_t s = begin + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < end;
          s += (uint64_t)gridDim.x * blockDim.x) {
         uint4 *e = reinterpret_cast<uint4 *>(elems + s * 8);
         e[0] = make_uint4(0, 0, 0, 0);
         e[1] = make_uint4(0, 0, EMPTY, 0);
-        uint4 *b = reinterpret_cast<uint4 *>(dbits0 + s * 8);
-        b[0] = make_uint4(0, 0, 0, 0);
-        b[1] = make_uint4(0, 0, 0, 0);
-        b = reinterpret_cast<uint4 *>(dbits1 + s * 8);
+        uint4 *b = reinterpret_cast<uint4 *>(dbits + s * 8);
         b[0] = make_uint4(0, 0, 0, 0);
         b[1] = make_uint4(0, 0, 0, 0);
     }
@@ -69,16 +96,21 @@ __global__ void k_eps_hist(Dev d, uint32_t slot)
         atomicAdd(&d.cnt[(size_t)(slot - 1) * d.V + v], 1u);
 }
 
+// Minimum table capacity per label (0 = none): tables of labels that rules
+// derive start large enough to rarely grow, so they stay in row order.
+struct MinCap { uint32_t cap[MAX_LABELS + 1]; };
+
 // One thread per table: size from the edge histogram (held in cnt), bump-allocate.
-__global__ void k_load_alloc(Dev d, uint64_t ntables)
+__global__ void k_load_alloc(Dev d, uint64_t ntables, MinCap mc)
 {
     for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < ((ntables + 31) & ~31ull);
          t += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t h = t < ntables ? d.cnt[t] : 0;
-        uint32_t cap = 0;
+        const uint32_t lab = t < ntables ? (uint32_t)(t / d.V) + 1 : 1;
+        uint32_t cap = t < ntables ? mc.cap[lab] : 0;
         if (h) {
-            uint32_t need = h + h / 3 + 1;
-            cap = 4;
+            const uint32_t need = h + h / 3 + 1;
+            if (cap < 4) cap = 4;
             while (cap < need) cap <<= 1;
         }
         // warp-aggregated bump allocation
@@ -111,8 +143,7 @@ __global__ void k_load_insert(Dev d, const uint32_t *src, const uint32_t *dst, c
         const uint32_t o = v % EIDS;
 #pragma unroll
         for (int w = 0; w < EW; w++) b.w[w] = (uint32_t)w == (o >> 5) ? 1u << (o & 31) : 0u;
-        uint32_t ds;
-        if (!g_insert(d, lab[i], src[i], v / EIDS, b, false, ds)) atomicOr(&d.ctr[C_ERR], (unsigned long long)ERR_LOAD);
+        if (!g_insert(d, lab[i], src[i], v / EIDS, b, false)) atomicOr(&d.ctr[C_ERR], (unsigned long long)ERR_LOAD);
     }
 }
 
@@ -124,8 +155,7 @@ __global__ void k_eps_insert(Dev d, uint32_t slot)
         const uint32_t o = v % EIDS;
 #pragma unroll
         for (int w = 0; w < EW; w++) b.w[w] = (uint32_t)w == (o >> 5) ? 1u << (o & 31) : 0u;
-        uint32_t ds;
-        if (!g_insert(d, slot, v, v / EIDS, b, false, ds)) atomicOr(&d.ctr[C_ERR], (unsigned long long)ERR_LOAD);
+        if (!g_insert(d, slot, v, v / EIDS, b, false)) atomicOr(&d.ctr[C_ERR], (unsigned long long)ERR_LOAD);
     }
 }
 
@@ -157,36 +187,76 @@ __global__ void k_compact_static(Dev d, uint32_t slot)
     }
 }
 
-// Every loaded element of a tracked label becomes a delta of round 1.
+// Every loaded element of a tracked label becomes a delta of round 1. A warp
+// covers 32 consecutive slots, so it owns one dirty-bitmap word.
 __global__ void k_mark_all(Dev d, uint64_t end)
 {
-    for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < end; s += (uint64_t)gridDim.x * blockDim.x) {
-        const uint4 *e = reinterpret_cast<const uint4 *>(d.elems + s * 8);
-        uint4 e1 = e[1];
-        if (e1.z == EMPTY || !c_rt.track[e1.z >> KEY_SHIFT]) continue;
-        uint4 e0 = e[0];
-        uint4 *b = reinterpret_cast<uint4 *>(d.dbits + s * 8);
-        b[0] = e0;
-        b[1] = make_uint4(e1.x, e1.y, 1u, 0u);
-        append_dirty(d, (uint32_t)s);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t b0 = blockIdx.x * (uint64_t)blockDim.x + (threadIdx.x & ~31u); b0 < end; b0 += stride) {
+        const uint64_t s = b0 + lane_id();
+        bool mark = false;
+        if (s < end) {
+            const uint4 *e = reinterpret_cast<const uint4 *>(d.elems + s * 8);
+            const uint4 e1 = e[1];
+            if (e1.z != EMPTY && c_rt.track[e1.z >> KEY_SHIFT]) {
+                const uint4 e0 = e[0];
+                uint4 *b = reinterpret_cast<uint4 *>(d.dbits + s * 8);
+                b[0] = e0;
+                b[1] = make_uint4(e1.x, e1.y, 0u, 0u);
+                mark = true;
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, mark);
+        if (lane_id() == 0) d.dmap[b0 >> 5] = m;
     }
 }
 
 // ---------------------------------------------------------------- rounds
 
-// Dirty slots of the last round -> delta records (32 B: bits[6], key, row);
-// clears the slots' delta bitmaps of that parity.
-__global__ void k_gather(Dev d, const uint32_t *__restrict__ list, uint64_t n, uint4 *out)
+// Dirty records per chunk of 1024 slots (one warp per chunk of 32 bitmap words).
+__global__ void k_dcount(Dev d, uint64_t nwords, uint32_t *chunk_cnt)
 {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t s = list[i];
-        uint4 *b = reinterpret_cast<uint4 *>(d.dcur + (size_t)s * 8);
-        const uint4 b0 = b[0], b1 = b[1];
-        const uint4 e1 = reinterpret_cast<const uint4 *>(d.elems + (size_t)s * 8)[1];
-        b[0] = make_uint4(0, 0, 0, 0);
-        b[1] = make_uint4(0, 0, 0, 0);
-        out[2 * i] = b0;
-        out[2 * i + 1] = make_uint4(b1.x, b1.y, e1.z, e1.w);
+    const uint64_t nchunks = (nwords + 31) / 32;
+    const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t c = blockIdx.x * (uint64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); c < nchunks; c += nwarps) {
+        const uint64_t wi = c * 32 + lane_id();
+        uint32_t n = wi < nwords ? __popc(d.dmap[wi]) : 0;
+        for (int o = 16; o; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+        if (lane_id() == 0) chunk_cnt[c] = n;
+    }
+}
+
+// Dirty slots -> delta records (32 B: bits[6], key, row) in slot order at the
+// chunk offsets; clears the delta bitmaps and the dirty bitmap.
+__global__ void k_gather(Dev d, uint64_t nwords, const uint32_t *__restrict__ chunk_off, uint4 *out)
+{
+    const uint64_t nchunks = (nwords + 31) / 32;
+    const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    const uint32_t lane = lane_id();
+    for (uint64_t c = blockIdx.x * (uint64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); c < nchunks; c += nwarps) {
+        const uint64_t wi = c * 32 + lane;
+        uint32_t m = wi < nwords ? d.dmap[wi] : 0;
+        const uint32_t cnt = __popc(m);
+        uint32_t incl = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        uint64_t pos = chunk_off[c] + incl - cnt;
+        if (m) d.dmap[wi] = 0;
+        while (m) {
+            const int bit = __ffs(m) - 1;
+            m &= m - 1;
+            const uint64_t s = wi * 32 + bit;
+            uint4 *b = reinterpret_cast<uint4 *>(d.dbits + s * 8);
+            const uint4 b0 = b[0], b1 = b[1];
+            const uint4 e1 = reinterpret_cast<const uint4 *>(d.elems + s * 8)[1];
+            b[0] = make_uint4(0, 0, 0, 0);
+            b[1] = make_uint4(0, 0, 0, 0);
+            out[2 * pos] = b0;
+            out[2 * pos + 1] = make_uint4(b1.x, b1.y, e1.z, e1.w);
+            pos++;
+        }
     }
 }
 
@@ -299,25 +369,66 @@ __device__ __forceinline__ bool acc_insert(WarpSmem &w, uint32_t key, const Bits
     return false;
 }
 
-// Flush the hash accumulator: entry (r, base) goes to row (rA[r], rrow[r]). Warp-uniform.
+// Reserve cnt candidate slots per lane (warp-uniform). Returns the lane's first
+// slot, or ~0 for every lane when the buffer cannot take the warp's total (the
+// caller then inserts directly); slots of a reservation that straddles the end
+// of the buffer are filled with empty records.
+__device__ __forceinline__ uint64_t cand_reserve(const Dev &d, uint32_t cnt)
+{
+    const uint32_t lane = lane_id();
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    if (!total || !d.cand) return d.cand ? 0 : ~0ull;
+    unsigned long long base = 0;
+    if (lane == 31) base = atomicAdd(&d.ctr[C_CAND_N], (unsigned long long)total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    if (base + total <= d.cand_cap) return base + incl - cnt;
+    for (uint64_t i = base + incl - cnt; i < base + incl && i < d.cand_cap; i++) {
+        d.cand[2 * i] = make_uint4(0, 0, 0, 0);
+        d.cand[2 * i + 1] = make_uint4(0, 0, EMPTY, 0);
+    }
+    return ~0ull;
+}
+
+__device__ __forceinline__ void cand_write(const Dev &d, uint64_t i, const Bits &b, uint32_t key, uint32_t row)
+{
+    d.cand[2 * i] = make_uint4(b.w[0], b.w[1], b.w[2], b.w[3]);
+    d.cand[2 * i + 1] = make_uint4(b.w[4], b.w[5], key, row);
+}
+
+// Flush the hash accumulator: entry (r, base) goes to row (rA[r], rrow[r]),
+// as a candidate for k_apply or, when the candidate buffer is full, by a
+// direct insert. Warp-uniform.
 __device__ __forceinline__ void acc_flush(const Dev &d, WarpSmem &w, uint32_t &inserts)
 {
     __syncwarp();
+    uint32_t nz = 0;
+#pragma unroll
+    for (int it = 0; it < ACC / 32; it++)
+        if (w.acc_key[it * 32 + lane_id()] != EMPTY) nz |= 1u << it;
+    uint64_t ci = cand_reserve(d, __popc(nz));
 #pragma unroll 1
     for (int it = 0; it < ACC / 32; it++) {
         const int j = it * 32 + (int)lane_id();
         const uint32_t k = w.acc_key[j];
-        uint32_t ds = EMPTY;
         if (k != EMPTY) {
             Bits b;
 #pragma unroll
             for (int x = 0; x < EW; x++) { b.w[x] = w.acc_bits[j][x]; w.acc_bits[j][x] = 0; }
             w.acc_key[j] = EMPTY;
             const uint32_t r = k >> KEY_SHIFT, A = w.rA[r];
-            if (!g_insert(d, A, w.rrow[r], k & BASE_MASK, b, c_rt.track[A], ds)) atomicOr(&w.fail, 1u << r);
-            inserts++;
+            if (ci != ~0ull) {
+                cand_write(d, ci++, b, (A << KEY_SHIFT) | (k & BASE_MASK), w.rrow[r]);
+            } else {
+                if (!g_insert(d, A, w.rrow[r], k & BASE_MASK, b, c_rt.track[A])) atomicOr(&w.fail, 1u << r);
+                inserts++;
+            }
         }
-        warp_append_dirty(d, ds);
     }
     __syncwarp();
     if (lane_id() == 0) w.acc_n = 0;
@@ -328,34 +439,64 @@ __device__ __forceinline__ void acc_flush(const Dev &d, WarpSmem &w, uint32_t &i
 __device__ __forceinline__ void win_flush(const Dev &d, WarpSmem &w, uint32_t &inserts)
 {
     __syncwarp();
+    uint32_t nz = 0;
+#pragma unroll
+    for (int it = 0; it < RB * WIN / 32; it++) {
+        const uint32_t p = it * 32 + lane_id();
+        const uint32_t r = p / WIN, dd = p % WIN;
+        uint32_t any = 0;
+#pragma unroll
+        for (int x = 0; x < EW; x++) any |= w.win[r][dd][x];
+        if (any) nz |= 1u << it;
+    }
+    uint64_t ci = cand_reserve(d, __popc(nz));
 #pragma unroll 1
     for (int it = 0; it < RB * WIN / 32; it++) {
         const uint32_t p = it * 32 + lane_id();
         const uint32_t r = p / WIN, dd = p % WIN;
-        Bits b;
-        uint32_t any = 0;
+        if ((nz >> it) & 1u) {
+            Bits b;
 #pragma unroll
-        for (int x = 0; x < EW; x++) { b.w[x] = w.win[r][dd][x]; any |= b.w[x]; }
-        uint32_t ds = EMPTY;
-        if (any) {
-#pragma unroll
-            for (int x = 0; x < EW; x++) w.win[r][dd][x] = 0;
-            const uint32_t A = w.rA[r];
-            if (!g_insert(d, A, w.rrow[r], w.rbase[r] + dd - WIN_LO, b, c_rt.track[A], ds)) atomicOr(&w.fail, 1u << r);
-            inserts++;
+            for (int x = 0; x < EW; x++) { b.w[x] = w.win[r][dd][x]; w.win[r][dd][x] = 0; }
+            const uint32_t A = w.rA[r], base = w.rbase[r] + dd - WIN_LO;
+            if (ci != ~0ull) {
+                cand_write(d, ci++, b, (A << KEY_SHIFT) | base, w.rrow[r]);
+            } else {
+                if (!g_insert(d, A, w.rrow[r], base, b, c_rt.track[A])) atomicOr(&w.fail, 1u << r);
+                inserts++;
+            }
         }
-        warp_append_dirty(d, ds);
     }
     __syncwarp();
+}
+
+// Insert candidate elements (label, row, base, bits) written by k_join. One
+// thread per candidate: thousands of independent insert chains per SM.
+// Candidates whose table is full go to fail_out (C_AFAIL) for a retry after growth.
+__global__ void __launch_bounds__(256) k_apply(Dev d, const uint4 *__restrict__ cand, uint4 *fail_out)
+{
+    // the candidate count is read on the device, so the host need not wait for the join
+    const uint64_t n = min((uint64_t)d.ctr[C_CAND_N], d.cand_cap);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint4 a = cand[2 * i], b = cand[2 * i + 1];
+        if (b.z == EMPTY) continue;
+        Bits bits;
+        bits.w[0] = a.x; bits.w[1] = a.y; bits.w[2] = a.z; bits.w[3] = a.w; bits.w[4] = b.x; bits.w[5] = b.y;
+        const uint32_t A = b.z >> KEY_SHIFT;
+        if (!g_insert(d, A, b.w, b.z & BASE_MASK, bits, c_rt.track[A])) {
+            const unsigned long long f = atomicAdd(&d.ctr[C_AFAIL], 1ull);
+            fail_out[2 * f] = a;
+            fail_out[2 * f + 1] = b;
+        }
+    }
 }
 
 // One warp per batch of RB delta records (label B, row i, base, bits); lane r
 // owns record r for per-record work, and (record, k) tasks and their right-hand
 // items are flattened over the lanes so every phase keeps 32 independent memory
 // operations in flight.
-__global__ void __launch_bounds__(JOIN_WARPS * 32, 6) k_join(Dev d, const uint32_t *__restrict__ list,
-                                                             const uint4 *__restrict__ recs, uint64_t n,
-                                                             uint4 *retry_out)
+__global__ void __launch_bounds__(JOIN_WARPS * 32, GRG_JOIN_MINB) k_join(Dev d, const uint4 *__restrict__ recs,
+                                                                        uint64_t n, uint4 *retry_out)
 {
     __shared__ WarpSmem smem[JOIN_WARPS];
     WarpSmem &w = smem[threadIdx.x >> 5];
@@ -370,6 +511,10 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, 6) k_join(Dev d, const uint32
     __syncwarp();
     unsigned long long n_left = 0, n_right = 0;
     uint32_t inserts = 0;
+#ifdef GRG_PHASE_TIMERS
+    unsigned long long ph[5] = {0, 0, 0, 0, 0};
+    long long ph_t = clock64();
+#endif
     const uint64_t nwarps = (uint64_t)gridDim.x * JOIN_WARPS;
     const uint64_t nbatch = (n + RB - 1) / RB;
     for (uint64_t bt = blockIdx.x * (uint64_t)JOIN_WARPS + (threadIdx.x >> 5); bt < nbatch; bt += nwarps) {
@@ -378,21 +523,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, 6) k_join(Dev d, const uint32
         Bits rb;
         uint32_t key = EMPTY, row = 0;
         if (have) {
-            uint4 a, b;
-            if (list) {
-                // first pass: the record is the dirty slot's delta bitmap (cleared here) + its key and row
-                const uint32_t s = list[ri];
-                uint4 *db = reinterpret_cast<uint4 *>(d.dcur + (size_t)s * 8);
-                a = db[0];
-                const uint4 b1 = db[1];
-                const uint4 e1 = reinterpret_cast<const uint4 *>(d.elems + (size_t)s * 8)[1];
-                db[0] = make_uint4(0, 0, 0, 0);
-                db[1] = make_uint4(0, 0, 0, 0);
-                b = make_uint4(b1.x, b1.y, e1.z, e1.w);
-            } else {
-                a = recs[2 * ri];
-                b = recs[2 * ri + 1];
-            }
+            const uint4 a = recs[2 * ri], b = recs[2 * ri + 1];
             rb.w[0] = a.x; rb.w[1] = a.y; rb.w[2] = a.z; rb.w[3] = a.w; rb.w[4] = b.x; rb.w[5] = b.y;
             key = b.z;
             row = b.w;
@@ -410,17 +541,16 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, 6) k_join(Dev d, const uint32
         bool ok = true;
         const uint32_t nbits = popc6(rb);
 
+        PH_MARK(0);
         // unary rules A ::= B (compute10): the delta itself joins row (A, row)
         const uint32_t nu = have ? c_rt.un_start[B + 1] - c_rt.un_start[B] : 0;
         const uint32_t maxu = __reduce_max_sync(0xffffffffu, nu);
         for (uint32_t u = 0; u < maxu; u++) {
-            uint32_t ds = EMPTY;
             if (u < nu) {
                 const uint32_t A = c_rt.un_A[c_rt.un_start[B] + u];
-                ok &= g_insert(d, A, row, base, rb, c_rt.track[A], ds);
+                ok &= g_insert(d, A, row, base, rb, c_rt.track[A]);
                 inserts++;
             }
-            warp_append_dirty(d, ds);
         }
 
         // reverse index of B (needed by old-left joins): rev_B[k] gets row
@@ -437,13 +567,13 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, 6) k_join(Dev d, const uint32
                     Bits ib;
 #pragma unroll
                     for (int x = 0; x < EW; x++) ib.w[x] = (uint32_t)x == (o >> 5) ? 1u << (o & 31) : 0u;
-                    uint32_t ds;
-                    if (!g_insert(d, w.rC[r], k, rr / EIDS, ib, false, ds)) atomicOr(&w.fail, 1u << r);
+                    if (!g_insert(d, w.rC[r], k, rr / EIDS, ib, false)) atomicOr(&w.fail, 1u << r);
                     inserts++;
                 }
             }
         }
 
+        PH_MARK(1);
         // binary rules A ::= B C, delta-left: union of rows C[k] into row (A, row)
         const uint32_t nbr = have ? c_rt.bin_start[B + 1] - c_rt.bin_start[B] : 0;
         const uint32_t maxb = __reduce_max_sync(0xffffffffu, nbr);
@@ -482,65 +612,79 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, 6) k_join(Dev d, const uint32
                     if (lane >= (uint32_t)o) incl += y;
                 }
                 const uint32_t nitems = __shfl_sync(0xffffffffu, incl, 31);
-                for (uint32_t f0 = 0; f0 < nitems; f0 += 32) {
-                    const uint32_t f = f0 + lane;
-                    // owner lane: smallest o with incl(o) > f
-                    uint32_t lo = 0;
+                // JOIN_UNROLL items per lane per iteration: their loads are issued together
+                for (uint32_t f0 = 0; f0 < nitems; f0 += 32 * JOIN_UNROLL) {
+                    uint32_t it_r[JOIN_UNROLL], it_b2[JOIN_UNROLL];
+                    Bits it_b[JOIN_UNROLL];
+                    bool it_ok[JOIN_UNROLL];
 #pragma unroll
-                    for (int st = 16; st; st >>= 1) {
-                        const uint32_t v = __shfl_sync(0xffffffffu, incl, lo + st - 1);
-                        if (v <= f) lo += st;
-                    }
-                    const uint32_t o_incl = __shfl_sync(0xffffffffu, incl, lo);
-                    const uint32_t o_cnt = __shfl_sync(0xffffffffu, cnt, lo);
-                    const uint32_t o_beg = __shfl_sync(0xffffffffu, beg, lo);
-                    const uint32_t o_r = __shfl_sync(0xffffffffu, r, lo);
-                    const uint32_t o_C = __shfl_sync(0xffffffffu, C, lo);
-                    const uint32_t o_csr = __shfl_sync(0xffffffffu, csr, lo);
-                    bool pending = false;
-                    uint32_t ckey = 0;
-                    Bits eb;
-                    if (f < nitems) {
-                        const uint32_t item = o_beg + (f - (o_incl - o_cnt));
-                        uint32_t b2;
+                    for (int u = 0; u < JOIN_UNROLL; u++) {
+                        const uint32_t f = f0 + u * 32 + lane;
+                        // owner lane: smallest o with incl(o) > f
+                        uint32_t lo = 0;
 #pragma unroll
-                        for (int x = 0; x < EW; x++) eb.w[x] = 0;
-                        bool valid = true;
-                        if (o_csr) {
-                            const uint32_t dst = __ldg(c_rt.csr_col[o_C] + item);
-                            b2 = dst / EIDS;
-                            const uint32_t ob = dst % EIDS;
-#pragma unroll
-                            for (int x = 0; x < EW; x++) eb.w[x] = (uint32_t)x == (ob >> 5) ? 1u << (ob & 31) : 0u;
-                        } else {
-                            const uint4 *ep = reinterpret_cast<const uint4 *>(d.elems + (size_t)item * 8);
-                            const uint4 e0 = ep[0], e1 = ep[1];
-                            valid = e1.z != EMPTY;
-                            b2 = e1.z & BASE_MASK;
-                            eb.w[0] = e0.x; eb.w[1] = e0.y; eb.w[2] = e0.z; eb.w[3] = e0.w;
-                            eb.w[4] = e1.x; eb.w[5] = e1.y;
+                        for (int st = 16; st; st >>= 1) {
+                            const uint32_t v = __shfl_sync(0xffffffffu, incl, lo + st - 1);
+                            if (v <= f) lo += st;
                         }
-                        if (valid) {
-                            n_right += o_csr ? 0 : 1;
-                            const int dd = (int)b2 - (int)w.rbase[o_r] + WIN_LO;
-                            if ((unsigned)dd < (unsigned)WIN) {
+                        const uint32_t o_incl = __shfl_sync(0xffffffffu, incl, lo);
+                        const uint32_t o_cnt = __shfl_sync(0xffffffffu, cnt, lo);
+                        const uint32_t o_beg = __shfl_sync(0xffffffffu, beg, lo);
+                        const uint32_t o_r = __shfl_sync(0xffffffffu, r, lo);
+                        const uint32_t o_C = __shfl_sync(0xffffffffu, C, lo);
+                        const uint32_t o_csr = __shfl_sync(0xffffffffu, csr, lo);
+                        it_r[u] = o_r;
+                        it_ok[u] = false;
+                        it_b2[u] = 0;
 #pragma unroll
-                                for (int x = 0; x < EW; x++)
-                                    if (eb.w[x]) atomicOr(&w.win[o_r][dd][x], eb.w[x]);
+                        for (int x = 0; x < EW; x++) it_b[u].w[x] = 0;
+                        if (f < nitems) {
+                            const uint32_t item = o_beg + (f - (o_incl - o_cnt));
+                            if (o_csr) {
+                                const uint32_t dst = __ldg(c_rt.csr_col[o_C] + item);
+                                it_b2[u] = dst / EIDS;
+                                const uint32_t ob = dst % EIDS;
+#pragma unroll
+                                for (int x = 0; x < EW; x++) it_b[u].w[x] = (uint32_t)x == (ob >> 5) ? 1u << (ob & 31) : 0u;
+                                it_ok[u] = true;
                             } else {
-                                pending = true;
-                                ckey = (o_r << KEY_SHIFT) | b2;
+                                const uint4 *ep = reinterpret_cast<const uint4 *>(d.elems + (size_t)item * 8);
+                                const uint4 e0 = ep[0], e1 = ep[1];
+                                it_ok[u] = e1.z != EMPTY;
+                                it_b2[u] = e1.z & BASE_MASK;
+                                it_b[u].w[0] = e0.x; it_b[u].w[1] = e0.y; it_b[u].w[2] = e0.z; it_b[u].w[3] = e0.w;
+                                it_b[u].w[4] = e1.x; it_b[u].w[5] = e1.y;
+                                n_right += it_ok[u] ? 1 : 0;
                             }
                         }
                     }
-                    while (__any_sync(0xffffffffu, pending)) {
-                        if (pending) pending = !acc_insert(w, ckey, eb);
-                        if (__any_sync(0xffffffffu, pending)) acc_flush(d, w, inserts);
+#pragma unroll
+                    for (int u = 0; u < JOIN_UNROLL; u++) {
+                        bool pending = false;
+                        uint32_t ckey = 0;
+                        if (it_ok[u]) {
+                            const uint32_t o_r = it_r[u];
+                            const int dd = (int)it_b2[u] - (int)w.rbase[o_r] + WIN_LO;
+                            if ((unsigned)dd < (unsigned)WIN) {
+#pragma unroll
+                                for (int x = 0; x < EW; x++)
+                                    if (it_b[u].w[x]) atomicOr(&w.win[o_r][dd][x], it_b[u].w[x]);
+                            } else {
+                                pending = true;
+                                ckey = (o_r << KEY_SHIFT) | it_b2[u];
+                            }
+                        }
+                        while (__any_sync(0xffffffffu, pending)) {
+                            if (pending) pending = !acc_insert(w, ckey, it_b[u]);
+                            if (__any_sync(0xffffffffu, pending)) acc_flush(d, w, inserts);
+                        }
                     }
                 }
             }
+            PH_MARK(2);
             win_flush(d, w, inserts);
             acc_flush(d, w, inserts);
+            PH_MARK(3);
         }
 
         // old-left joins A ::= Bp B (record = delta of B at vertex `row`):
@@ -578,9 +722,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, 6) k_join(Dev d, const uint32
                     while (bw) {
                         const int bit = __ffs(bw) - 1;
                         bw &= bw - 1;
-                        uint32_t ds;
-                        okr &= g_insert(d, A, hb * EIDS + x * 32 + bit, xbase, xb, trk, ds);
-                        if (ds != EMPTY) append_dirty(d, ds);
+                        okr &= g_insert(d, A, hb * EIDS + x * 32 + bit, xbase, xb, trk);
                         inserts++;
                     }
                 }
@@ -603,7 +745,13 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, 6) k_join(Dev d, const uint32
             }
         }
         __syncwarp();
+        PH_MARK(4);
     }
+#ifdef GRG_PHASE_TIMERS
+
+    if (lane == 0)
+        for (int i = 0; i < 5; i++) atomicAdd(&d.ctr[C_PH0 + i], ph[i]);
+#endif
     // per-warp work counters
     for (int o = 16; o; o >>= 1) {
         inserts += __shfl_xor_sync(0xffffffffu, inserts, o);
@@ -764,9 +912,7 @@ __global__ void k_grow(Dev d, uint64_t n)
             uint4 *b = reinterpret_cast<uint4 *>(d.dbits + (nb + t) * 8);
             b[0] = make_uint4(0, 0, 0, 0);
             b[1] = make_uint4(0, 0, 0, 0);
-            b = reinterpret_cast<uint4 *>(d.dcur + (nb + t) * 8);
-            b[0] = make_uint4(0, 0, 0, 0);
-            b[1] = make_uint4(0, 0, 0, 0);
+
         }
         __syncwarp();
         const uint32_t lg = 31 - __clz(ncap);
@@ -898,13 +1044,17 @@ struct grg_ctx {
     uint64_t pool_bytes_req = 0;
     uint64_t pool_cap = 0;         // elements
     uint32_t *elems = nullptr;
-    uint32_t *dbits[2] = {nullptr, nullptr};   // delta bitmaps, by round parity
-    uint32_t *dirty[2] = {nullptr, nullptr};   // dirty lists, by round parity
-    int cur = 0;                               // parity read by the current round
+    uint32_t *dbits = nullptr;                 // delta bitmaps (32 B per slot)
+    uint32_t *dmap = nullptr;                  // dirty bitmap (1 bit per slot)
+    uint32_t *chunk = nullptr;                 // dirty counts / offsets per 1024 slots (+ scan sums)
+    uint64_t chunk_cap = 0;
     uint64_t *desc = nullptr;
     uint32_t *cnt = nullptr, *want = nullptr, *grow = nullptr;
     uint4 *rbuf[3] = {nullptr, nullptr, nullptr};   // [2]: gathered deltas; [0],[1]: retry passes
     uint64_t rbuf_cap = 0;                     // records
+    uint4 *cand[2] = {nullptr, nullptr};       // join candidates for k_apply / failed candidates
+    uint64_t cand_cap = 0;
+    int cb = 0;                                // candidate buffer the joins write
     unsigned long long *ctr = nullptr;
     unsigned long long *h_ctr = nullptr;   // pinned
     uint32_t *d_in32 = nullptr;            // staged input edges (src, dst)
@@ -955,17 +1105,17 @@ int grid_for(const grg_ctx *c, uint64_t n, int block, int per_sm = 8)
     return (int)std::max<uint64_t>(g, 1);
 }
 
-// Device view for a round that reads parity c->cur and writes parity c->cur ^ 1.
 Dev make_dev(const grg_ctx *c)
 {
     Dev d;
     d.elems = c->elems;
-    d.dcur = c->dbits[c->cur];
-    d.dbits = c->dbits[c->cur ^ 1];
+    d.dbits = c->dbits;
+    d.dmap = c->dmap;
     d.desc = c->desc;
     d.cnt = c->cnt;
     d.want = c->want;
-    d.dirty = c->dirty[c->cur ^ 1];
+    d.cand = c->cand[c->cb];
+    d.cand_cap = c->cand_cap;
     d.grow = c->grow;
     d.ctr = c->ctr;
     d.V = c->V;
@@ -992,10 +1142,8 @@ void free_graph(grg_ctx *c)
 void free_pool(grg_ctx *c)
 {
     cudaFree(c->elems); c->elems = nullptr;
-    for (int p = 0; p < 2; p++) {
-        cudaFree(c->dbits[p]); c->dbits[p] = nullptr;
-        cudaFree(c->dirty[p]); c->dirty[p] = nullptr;
-    }
+    cudaFree(c->dbits); c->dbits = nullptr;
+    cudaFree(c->dmap); c->dmap = nullptr;
     c->pool_cap = 0;
 }
 
@@ -1007,41 +1155,49 @@ int read_ctr(grg_ctx *c)
 }
 
 
-constexpr uint64_t POOL_BYTES_PER_SLOT = 32 + 2 * 32 + 2 * 4;
+constexpr uint64_t POOL_BYTES_PER_SLOT = 32 + 32 + 1;
+constexpr uint32_t DERIVED_MIN_CAP = 16;   // element, delta bitmap, dirty bit (rounded up)
 
-// Pool of `elems` 32-byte slots + two delta-bitmap pools + two dirty lists.
+// Pool of `elems` 32-byte slots + their delta bitmaps + the dirty bitmap.
 int alloc_pool(grg_ctx *c, uint64_t elems)
 {
-    if (elems > 0xFFFFFFF0ull) elems = 0xFFFFFFF0ull;
-    uint32_t *e = nullptr, *b[2] = {nullptr, nullptr}, *dl[2] = {nullptr, nullptr};
-    auto release = [&]() {
-        cudaFree(e);
-        for (int p = 0; p < 2; p++) { cudaFree(b[p]); cudaFree(dl[p]); }
-    };
-    if (cudaMalloc(&e, elems * 32) != cudaSuccess || cudaMalloc(&b[0], elems * 32) != cudaSuccess ||
-        cudaMalloc(&b[1], elems * 32) != cudaSuccess || cudaMalloc(&dl[0], elems * 4) != cudaSuccess ||
-        cudaMalloc(&dl[1], elems * 4) != cudaSuccess) {
+    if (elems > 0xFFFFFFE0ull) elems = 0xFFFFFFE0ull;
+    const uint64_t words = elems / 32 + 2;
+    uint32_t *e = nullptr, *b = nullptr, *m = nullptr;
+    if (cudaMalloc(&e, elems * 32) != cudaSuccess || cudaMalloc(&b, elems * 32) != cudaSuccess ||
+        cudaMalloc(&m, words * 4) != cudaSuccess) {
         cudaGetLastError();
-        release();
+        cudaFree(e); cudaFree(b); cudaFree(m);
         return fail(c, GRG_E_NOMEM, "cannot allocate element pool of " + std::to_string(elems) + " slots");
     }
+    GRG_CUDA(c, cudaMemsetAsync(m, 0, words * 4, c->stream));
     if (c->elems) {
-        // grow: keep the used part and the dirty list being written
+        // grow: keep the used part, its delta bitmaps and dirty bits
         int st = read_ctr(c);
-        if (st) { release(); return st; }
+        if (st) { cudaFree(e); cudaFree(b); cudaFree(m); return st; }
         const uint64_t used = std::min<uint64_t>(c->h_ctr[C_POOL_TOP], c->pool_cap);
-        const uint64_t nd = c->h_ctr[C_DIRTY_N];
-        const int nx = c->cur ^ 1;
         GRG_CUDA(c, cudaMemcpyAsync(e, c->elems, used * 32, cudaMemcpyDeviceToDevice, c->stream));
-        for (int p = 0; p < 2; p++)
-            GRG_CUDA(c, cudaMemcpyAsync(b[p], c->dbits[p], used * 32, cudaMemcpyDeviceToDevice, c->stream));
-        GRG_CUDA(c, cudaMemcpyAsync(dl[nx], c->dirty[nx], nd * 4, cudaMemcpyDeviceToDevice, c->stream));
+        GRG_CUDA(c, cudaMemcpyAsync(b, c->dbits, used * 32, cudaMemcpyDeviceToDevice, c->stream));
+        GRG_CUDA(c, cudaMemcpyAsync(m, c->dmap, (used / 32 + 1) * 4, cudaMemcpyDeviceToDevice, c->stream));
         GRG_CUDA(c, cudaStreamSynchronize(c->stream));
         free_pool(c);
     }
     c->elems = e;
-    for (int p = 0; p < 2; p++) { c->dbits[p] = b[p]; c->dirty[p] = dl[p]; }
+    c->dbits = b;
+    c->dmap = m;
     c->pool_cap = elems;
+    return GRG_OK;
+}
+
+// Chunk counters of the dirty-bitmap gather: one per 1024 slots, plus scan sums.
+int ensure_chunks(grg_ctx *c, uint64_t nchunks)
+{
+    const uint64_t need = 2 * (nchunks + 1) + (nchunks + 1023) / 1024 + 2;
+    if (need <= c->chunk_cap) return GRG_OK;
+    cudaFree(c->chunk);
+    c->chunk = nullptr;
+    GRG_CUDA(c, cudaMalloc(&c->chunk, need * 2 * 4));
+    c->chunk_cap = need * 2;
     return GRG_OK;
 }
 
@@ -1054,6 +1210,27 @@ int grow_pool(grg_ctx *c, uint64_t min_elems)
     if (want > fit) want = fit;
     if (want <= c->pool_cap) return fail(c, GRG_E_NOMEM, "element pool exhausted and device memory is full");
     return alloc_pool(c, want);
+}
+
+// Candidate buffers of a round (4 per delta record; a full buffer falls back to direct inserts).
+int ensure_cand(grg_ctx *c, uint64_t nd)
+{
+    const uint64_t want = std::max<uint64_t>(4 * nd, 1 << 20);
+    if (want <= c->cand_cap) return GRG_OK;
+    const uint64_t cap = want + want / 2;
+    cudaFree(c->cand[0]);
+    cudaFree(c->cand[1]);
+    c->cand[0] = c->cand[1] = nullptr;
+    c->cand_cap = 0;
+    if (cudaMalloc(&c->cand[0], cap * 32) != cudaSuccess || cudaMalloc(&c->cand[1], cap * 32) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(c->cand[0]);
+        cudaFree(c->cand[1]);
+        c->cand[0] = c->cand[1] = nullptr;
+        return GRG_OK;   // no candidate buffers: joins insert directly
+    }
+    c->cand_cap = cap;
+    return GRG_OK;
 }
 
 // Retry buffers: every delta record of a pass may fail once, so n records each.
@@ -1181,6 +1358,9 @@ void grg_destroy(grg_ctx *c)
     free_graph(c);
     free_pool(c);
     for (int i = 0; i < 3; i++) cudaFree(c->rbuf[i]);
+    cudaFree(c->cand[0]);
+    cudaFree(c->cand[1]);
+    cudaFree(c->chunk);
     cudaFree(c->ctr);
     cudaFree(c->d_in32);
     cudaFree(c->d_in8);
@@ -1304,10 +1484,22 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
             k_eps_hist<<<grid_for(c, num_vars, 256), 256, 0, s>>>(d, (uint32_t)c->rules[3 * q]);
             c->launches++;
         }
+    // labels on a rule's left-hand side get tables of DERIVED_MIN_CAP slots when that fits in a
+    // quarter of the pool (fewer growths, rows stay in allocation order)
+    MinCap mc;
+    memset(&mc, 0, sizeof mc);
+    {
+        int nder = 0;
+        bool lhs[MAX_LABELS + 1] = {false};
+        for (int q = 0; q < c->R; q++) lhs[c->rules[3 * q]] = true;
+        for (int l = 1; l <= c->L; l++) nder += lhs[l];
+        if ((uint64_t)nder * num_vars * DERIVED_MIN_CAP <= c->pool_cap / 4)
+            for (int l = 1; l <= c->L; l++) mc.cap[l] = lhs[l] ? DERIVED_MIN_CAP : 0;
+    }
     for (int attempt = 0;; attempt++) {
         GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_POOL_TOP, 0, 8, s));
         GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_ERR, 0, 8, s));
-        k_load_alloc<<<grid_for(c, c->ntables, 256), 256, 0, s>>>(d, c->ntables);
+        k_load_alloc<<<grid_for(c, c->ntables, 256), 256, 0, s>>>(d, c->ntables, mc);
         c->launches++;
         int st = read_ctr(c);
         if (st) return st;
@@ -1325,7 +1517,8 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
     }
     uint64_t top = c->h_ctr[C_POOL_TOP];
     if (top) {
-        k_init_region<<<grid_for(c, top, 256), 256, 0, s>>>(c->elems, c->dbits[0], c->dbits[1], 0, top);
+        GRG_CUDA(c, cudaMemsetAsync(c->dmap, 0, (c->pool_cap / 32 + 2) * 4, s));
+        k_init_region<<<grid_for(c, top, 256), 256, 0, s>>>(c->elems, c->dbits, 0, top);
         c->launches++;
     }
     if (num_edges) {
@@ -1412,42 +1605,68 @@ int grg_closure(grg_ctx *c, uint32_t filter, grg_stats *stats)
     st = read_ctr(c);
     if (st) return st;
     const uint64_t top = c->h_ctr[C_POOL_TOP];
-    GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_DIRTY_N, 0, 8, s));
-    // every loaded element of a tracked label is a delta of round 1 (written to parity 0)
-    c->cur = 1;
+    // every loaded element of a tracked label is a delta of round 1
     d = make_dev(c);
     if (top) {
         k_mark_all<<<grid_for(c, top, 256), 256, 0, s>>>(d, top);
         c->launches++;
     }
-    c->cur = 0;
     double join_ms = 0;
     uint64_t joins = 0;
+    st = read_ctr(c);
+    if (st) return st;
     for (;;) {
+        // gather the dirty slots of the last round into delta records (slot order);
+        // the pool top is the one read after the last growth
+        const uint64_t nwords = (c->h_ctr[C_POOL_TOP] + 31) / 32;
+        const uint64_t nchunks = (nwords + 31) / 32;
+        st = ensure_chunks(c, nchunks);
+        if (st) return st;
+        uint32_t *ccnt = c->chunk, *coff = c->chunk + nchunks + 1, *csum = c->chunk + 2 * (nchunks + 1);
+        const uint64_t nb = (nchunks + 1023) / 1024;
+        d = make_dev(c);
+        k_dcount<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, ccnt);
+        k_scan_blocks<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(ccnt, coff, csum, nchunks);
+        k_scan_sums<<<1, 1024, 0, s>>>(csum, nb);
+        k_scan_add<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(coff, csum, nchunks);
+        c->launches += 4;
+        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_DIRTY_N, 0, 8, s));
+        GRG_CUDA(c, cudaMemcpyAsync(c->ctr + C_DIRTY_N, csum + nb, 4, cudaMemcpyDeviceToDevice, s));
+        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_RETRY_N, 0, 16, s));   // retry + grow counters
+        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_CAND_N, 0, 16, s));    // candidates + failed candidates
         st = read_ctr(c);
         if (st) return st;
         const uint64_t nd = c->h_ctr[C_DIRTY_N];
         if (nd == 0) break;
         st = ensure_rbuf(c, nd);
         if (st) return st;
+        st = ensure_cand(c, nd);
+        if (st) return st;
         S.rounds++;
         S.delta_elems += nd;
+        c->cb = 0;
         d = make_dev(c);
-        k_gather<<<grid_for(c, nd, 256), 256, 0, s>>>(d, c->dirty[c->cur], nd, c->rbuf[2]);
+        k_gather<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->rbuf[2]);
         c->launches++;
-        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_DIRTY_N, 0, 8, s));
-        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_RETRY_N, 0, 16, s));   // retry + grow counters
-        uint64_t n = nd;
+        uint64_t n = nd;       // delta records for the next join pass (0 = none)
         int rb = 0;
+        bool first = true;
         for (int pass = 0;; pass++) {
-            const int jgrid = grid_for(c, (n + RB - 1) / RB, JOIN_WARPS, 16);
             if (c->timing) GRG_CUDA(c, cudaEventRecord(c->ev_c, s));
-            if (pass == 0)
-                k_join<<<jgrid, JOIN_WARPS * 32, 0, s>>>(d, nullptr, c->rbuf[2], n, c->rbuf[0]);
-            else
-                k_join<<<jgrid, JOIN_WARPS * 32, 0, s>>>(d, nullptr, c->rbuf[rb], n, c->rbuf[rb ^ 1]);
-            c->launches++;
-            joins++;
+            if (n) {
+                const int jgrid = grid_for(c, (n + RB - 1) / RB, JOIN_WARPS, 16);
+                if (first)
+                    k_join<<<jgrid, JOIN_WARPS * 32, 0, s>>>(d, c->rbuf[2], n, c->rbuf[0]);
+                else
+                    k_join<<<jgrid, JOIN_WARPS * 32, 0, s>>>(d, c->rbuf[rb], n, c->rbuf[rb ^ 1]);
+                c->launches++;
+                joins++;
+            }
+            // insert the candidates the joins wrote (count read on the device)
+            if (c->cand_cap) {
+                k_apply<<<c->sms * 8, 256, 0, s>>>(d, c->cand[c->cb], c->cand[c->cb ^ 1]);
+                c->launches++;
+            }
             if (c->timing) GRG_CUDA(c, cudaEventRecord(c->ev_d, s));
             GRG_CUDA(c, cudaGetLastError());
             st = read_ctr(c);
@@ -1457,10 +1676,13 @@ int grg_closure(grg_ctx *c, uint32_t filter, grg_stats *stats)
                 cudaEventElapsedTime(&ms, c->ev_c, c->ev_d);
                 join_ms += ms;
             }
-            const uint64_t nr = c->h_ctr[C_RETRY_N];
-            if (nr == 0) break;
-            S.retry_records += nr;
-            // grow every table that overflowed, then re-run the failed records
+            const uint64_t nr = n ? c->h_ctr[C_RETRY_N] : 0;
+            if (!first && n) rb ^= 1;       // the failed records of this pass are in rbuf[rb]
+            first = false;
+            const uint64_t nf = c->cand_cap ? c->h_ctr[C_AFAIL] : 0;
+            if (nr == 0 && nf == 0) break;
+            S.retry_records += nr + nf;
+            // grow every table that overflowed, then re-run the failed records and candidates
             for (int gtry = 0;; gtry++) {
                 const uint64_t ng = c->h_ctr[C_GROW_N];
                 GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_ERR, 0, 8, s));
@@ -1476,11 +1698,15 @@ int grg_closure(grg_ctx *c, uint32_t filter, grg_stats *stats)
                 d = make_dev(c);
             }
             if (pass > 64) return fail(c, GRG_E_CUDA, "table growth did not converge");
-            rb = pass == 0 ? 0 : rb ^ 1;   // records that failed this pass are in rbuf[rb]
+            // failed candidates (in cand[cb^1]) become the next candidate list; join retries append to it
+            c->cb ^= 1;
+            d = make_dev(c);
             n = nr;
+            c->h_ctr[C_CAND_N] = nf;
+            GRG_CUDA(c, cudaMemcpyAsync(c->ctr + C_CAND_N, c->h_ctr + C_CAND_N, 8, cudaMemcpyHostToDevice, s));
+            GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_AFAIL, 0, 8, s));
             GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_RETRY_N, 0, 16, s));
         }
-        c->cur ^= 1;
     }
     GRG_CUDA(c, cudaEventRecord(c->ev_b, s));
     GRG_CUDA(c, cudaEventSynchronize(c->ev_b));
@@ -1494,6 +1720,7 @@ int grg_closure(grg_ctx *c, uint32_t filter, grg_stats *stats)
     S.out_elems = S.delta_elems;
     S.pool_elems_used = c->h_ctr[C_POOL_TOP];
     S.pool_elems_cap = c->pool_cap;
+    for (int i = 0; i < 5; i++) S.join_phase_cycles[i] = c->h_ctr[C_PH0 + i];
     c->closed = true;
     // total edge count
     uint64_t counts[MAX_LABELS];
@@ -1717,8 +1944,8 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
             (r[1] == 0 && r[2] != 0))
             return GRG_E_ARG;
     }
-    // scratch layout: counters | descriptors | cnt | want | grow | pool arrays (168 B per element:
-    // element, two delta bitmaps, two dirty lists, two retry records)
+    // scratch layout: counters | descriptors | cnt | want | grow | pool arrays (161 B per element:
+    // element, delta bitmap, dirty bit, three delta-record buffers) | gather chunk counters
     const uint64_t ntab = (uint64_t)(2 * num_labels) * num_vars;
     size_t off = 0;
     const size_t o_ctr = off; off = align256(off + sizeof(unsigned long long) * NCTR);
@@ -1727,15 +1954,16 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     const size_t o_want = off; off = align256(off + ntab * 4);
     const size_t o_grow = off; off = align256(off + ntab * 4);
     if (off >= NOALLOC_SCRATCH_BYTES) return GRG_E_RANGE;            // tables alone exceed the scratch
-    uint64_t pool = (NOALLOC_SCRATCH_BYTES - off - 8 * 256) / 168;
+    uint64_t pool = (NOALLOC_SCRATCH_BYTES - off - 16 * 256) / 162;
     if (pool < 4096 || num_edges > pool / 2) return GRG_E_RANGE;    // graph too large for the scratch
+    const uint64_t pwords = pool / 32 + 2, pchunks = (pwords + 31) / 32, pnb = (pchunks + 1023) / 1024;
     const size_t o_elems = off; off = align256(off + pool * 32);
-    const size_t o_dbits0 = off; off = align256(off + pool * 32);
-    const size_t o_dbits1 = off; off = align256(off + pool * 32);
-    const size_t o_dirty0 = off; off = align256(off + pool * 4);
-    const size_t o_dirty1 = off; off = align256(off + pool * 4);
+    const size_t o_dbits = off; off = align256(off + pool * 32);
+    const size_t o_dmap = off; off = align256(off + pwords * 4);
     const size_t o_rbuf0 = off; off = align256(off + pool * 32);
     const size_t o_rbuf1 = off; off = align256(off + pool * 32);
+    const size_t o_rbuf2 = off; off = align256(off + pool * 32);
+    const size_t o_chunk = off; off = align256(off + (2 * (pchunks + 1) + pnb + 2) * 4);
     if (off > NOALLOC_SCRATCH_BYTES) return GRG_E_RANGE;
 
     RuleTable rt;
@@ -1767,19 +1995,14 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     d.want = (uint32_t *)(base + o_want);
     d.grow = (uint32_t *)(base + o_grow);
     d.elems = (uint32_t *)(base + o_elems);
-    uint32_t *dbits[2] = {(uint32_t *)(base + o_dbits0), (uint32_t *)(base + o_dbits1)};
-    uint32_t *dirty[2] = {(uint32_t *)(base + o_dirty0), (uint32_t *)(base + o_dirty1)};
-    uint4 *rbuf[2] = {(uint4 *)(base + o_rbuf0), (uint4 *)(base + o_rbuf1)};
-    // round parity cur reads dbits[cur]/dirty[cur] and writes the other pair; the
-    // initial deltas are written to parity 0
-    auto set_parity = [&](int cur) {
-        d.dcur = dbits[cur];
-        d.dbits = dbits[cur ^ 1];
-        d.dirty = dirty[cur ^ 1];
-    };
-    set_parity(1);
+    d.dbits = (uint32_t *)(base + o_dbits);
+    d.dmap = (uint32_t *)(base + o_dmap);
     d.V = num_vars;
     d.pool_cap = (uint32_t)pool;
+    d.cand = nullptr;          // no candidate buffer: joins insert directly
+    d.cand_cap = 0;
+    uint4 *rbuf[3] = {(uint4 *)(base + o_rbuf0), (uint4 *)(base + o_rbuf1), (uint4 *)(base + o_rbuf2)};
+    uint32_t *chunk = (uint32_t *)(base + o_chunk);
     unsigned long long h[NCTR];
 
     // the array keeps the previous call's contents: clear everything that must start at zero
@@ -1787,6 +2010,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     NA_CUDA(cudaMemsetAsync(d.desc, 0, ntab * 8, s));
     NA_CUDA(cudaMemsetAsync(d.cnt, 0, ntab * 4, s));
     NA_CUDA(cudaMemsetAsync(d.want, 0, ntab * 4, s));
+    NA_CUDA(cudaMemsetAsync(d.dmap, 0, pwords * 4, s));
     NA_CUDA(cudaMemcpyToSymbolAsync(c_rt, &rt, sizeof rt, 0, cudaMemcpyHostToDevice, s));
 
     // load (grg_load_edges)
@@ -1794,11 +2018,13 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     if (num_edges) k_load_hist<<<grid(num_edges, 256, 8), 256, 0, s>>>(d, d_src, d_label, num_edges);
     for (int q = 0; q < num_rules; q++)
         if (rules[3 * q + 1] == 0) k_eps_hist<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)rules[3 * q]);
-    k_load_alloc<<<grid(nlab, 256, 8), 256, 0, s>>>(d, nlab);
+    MinCap mc;
+    memset(&mc, 0, sizeof mc);
+    k_load_alloc<<<grid(nlab, 256, 8), 256, 0, s>>>(d, nlab, mc);
     if ((st = na_read(h, d.ctr, s))) return st;
     if (h[C_ERR] & ERR_POOL) return GRG_E_NOMEM;
     const uint64_t top0 = h[C_POOL_TOP];
-    if (top0) k_init_region<<<grid(top0, 256, 8), 256, 0, s>>>(d.elems, dbits[0], dbits[1], 0, top0);
+    if (top0) k_init_region<<<grid(top0, 256, 8), 256, 0, s>>>(d.elems, d.dbits, 0, top0);
     if (num_edges) k_load_insert<<<grid(num_edges, 256, 8), 256, 0, s>>>(d, d_src, d_dst, d_label, num_edges);
     for (int q = 0; q < num_rules; q++)
         if (rules[3 * q + 1] == 0) k_eps_insert<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)rules[3 * q]);
@@ -1811,23 +2037,31 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
 
     // semi-naive rounds (grg_closure); the pool cannot grow here
     uint64_t rounds = 0;
-    int cur = 0;
     for (;;) {
         if ((st = na_read(h, d.ctr, s))) return st;
-        const uint64_t nd = h[C_DIRTY_N];
+        const uint64_t nwords = (h[C_POOL_TOP] + 31) / 32, nchunks = (nwords + 31) / 32;
+        const uint64_t nb = (nchunks + 1023) / 1024;
+        uint32_t *ccnt = chunk, *coff = chunk + nchunks + 1, *csum = chunk + 2 * (nchunks + 1);
+        k_dcount<<<grid(nchunks * 32, 256, 8), 256, 0, s>>>(d, nwords, ccnt);
+        k_scan_blocks<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(ccnt, coff, csum, nchunks);
+        k_scan_sums<<<1, 1024, 0, s>>>(csum, nb);
+        k_scan_add<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(coff, csum, nchunks);
+        uint32_t nd32 = 0;
+        NA_CUDA(cudaMemcpyAsync(&nd32, csum + nb, 4, cudaMemcpyDeviceToHost, s));
+        NA_CUDA(cudaStreamSynchronize(s));
+        const uint64_t nd = nd32;
         if (nd == 0) break;
         rounds++;
-        set_parity(cur);
-        NA_CUDA(cudaMemsetAsync(d.ctr + C_DIRTY_N, 0, 8, s));
+        k_gather<<<grid(nchunks * 32, 256, 8), 256, 0, s>>>(d, nwords, coff, rbuf[2]);
         NA_CUDA(cudaMemsetAsync(d.ctr + C_RETRY_N, 0, 16, s));
         uint64_t n = nd;
         int rb = 0;
         for (int pass = 0;; pass++) {
             const int g = grid((n + RB - 1) / RB, JOIN_WARPS, 16);
             if (pass == 0)
-                k_join<<<g, JOIN_WARPS * 32, 0, s>>>(d, dirty[cur], nullptr, n, rbuf[0]);
+                k_join<<<g, JOIN_WARPS * 32, 0, s>>>(d, rbuf[2], n, rbuf[0]);
             else
-                k_join<<<g, JOIN_WARPS * 32, 0, s>>>(d, nullptr, rbuf[rb], n, rbuf[rb ^ 1]);
+                k_join<<<g, JOIN_WARPS * 32, 0, s>>>(d, rbuf[rb], n, rbuf[rb ^ 1]);
             NA_CUDA(cudaGetLastError());
             if ((st = na_read(h, d.ctr, s))) return st;
             const uint64_t nr = h[C_RETRY_N];
@@ -1841,7 +2075,6 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
             n = nr;
             NA_CUDA(cudaMemsetAsync(d.ctr + C_RETRY_N, 0, 16, s));
         }
-        cur ^= 1;
     }
 
     // per-label counts and edge-set hash into the caller's device buffers

@@ -13,7 +13,7 @@ from dataclasses import dataclass
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libgrg.so")
+LIB_PATH = os.environ.get("GRG_LIB") or os.path.join(HERE, "_build", "libgrg.so")
 COMP_PATH = os.path.join(HERE, "_build", "comp")
 
 OK = 0
@@ -45,10 +45,13 @@ class Stats(ctypes.Structure):
         ("retry_records", ctypes.c_uint64), ("grow_rows", ctypes.c_uint64), ("pool_elems_used", ctypes.c_uint64),
         ("pool_elems_cap", ctypes.c_uint64), ("closure_ms", ctypes.c_double), ("join_ms", ctypes.c_double),
         ("join_launches", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
+        ("join_phase_cycles", ctypes.c_uint64 * 5),
     ]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["join_phase_cycles"] = list(d["join_phase_cycles"])
+        return d
 
 
 _lib = None

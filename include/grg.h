@@ -60,6 +60,9 @@ typedef struct grg_stats {
     double join_ms;                /* sum of join-kernel durations (when kernel timing is on) */
     uint64_t join_launches;        /* join-kernel launches (first pass + retries) */
     uint64_t kernel_launches;      /* all kernel launches of the closure */
+    uint64_t join_phase_cycles[5]; /* join-kernel cycles per phase (record load, unary+reverse,
+                                      binary join, flush, old-left) when built with
+                                      -DGRG_PHASE_TIMERS; 0 otherwise */
 } grg_stats;
 
 /* Error text of a status code, and the last detailed message of a context. */
@@ -157,7 +160,7 @@ int grg_parse_graph(const char *path, int num_labels, const char *names, uint64_
  * (the legacy default stream); the call returns after the stream is idle.
  *
  * Limits: the tables take 40 bytes per (label, vertex) and the rest of the
- * array holds 168 bytes per element slot; graphs whose tables leave fewer
+ * array holds 162 bytes per element slot; graphs whose tables leave fewer
  * than 4096 slots, or with more edges than half the slots, are rejected with
  * GRG_E_RANGE before any launch; a closure that outgrows the array returns
  * GRG_E_NOMEM.
