@@ -226,8 +226,22 @@ __global__ void k_dcount(Dev d, uint64_t nwords, uint32_t *chunk_cnt)
     }
 }
 
+// Position of the n-th (0-based) set bit of a 32-bit word (broadword select, no loop).
+__device__ __forceinline__ uint32_t select32(uint32_t w, uint32_t n)
+{
+    uint32_t pos = 0, c;
+    c = __popc(w & 0xFFFFu); if (n >= c) { n -= c; pos += 16; w >>= 16; }
+    c = __popc(w & 0xFFu);   if (n >= c) { n -= c; pos += 8;  w >>= 8; }
+    c = __popc(w & 0xFu);    if (n >= c) { n -= c; pos += 4;  w >>= 4; }
+    c = __popc(w & 0x3u);    if (n >= c) { n -= c; pos += 2;  w >>= 2; }
+    c = w & 1u;              if (n >= c) { pos += 1; }
+    return pos;
+}
+
 // Dirty slots -> delta records (32 B: bits[6], key, row) in slot order at the
-// chunk offsets; clears the delta bitmaps and the dirty bitmap.
+// chunk offsets; clears the delta bitmaps and the dirty bitmap. One warp per
+// chunk of 32 bitmap words; lanes take consecutive dirty slots of the chunk, so
+// the copies of a warp are independent and mostly coalesced.
 __global__ void k_gather(Dev d, uint64_t nwords, const uint32_t *__restrict__ chunk_off, uint4 *out)
 {
     const uint64_t nchunks = (nwords + 31) / 32;
@@ -235,27 +249,40 @@ __global__ void k_gather(Dev d, uint64_t nwords, const uint32_t *__restrict__ ch
     const uint32_t lane = lane_id();
     for (uint64_t c = blockIdx.x * (uint64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); c < nchunks; c += nwarps) {
         const uint64_t wi = c * 32 + lane;
-        uint32_t m = wi < nwords ? d.dmap[wi] : 0;
+        const uint32_t m = wi < nwords ? d.dmap[wi] : 0;
         const uint32_t cnt = __popc(m);
         uint32_t incl = cnt;
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
             if (lane >= (uint32_t)o) incl += y;
         }
-        uint64_t pos = chunk_off[c] + incl - cnt;
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
         if (m) d.dmap[wi] = 0;
-        while (m) {
-            const int bit = __ffs(m) - 1;
-            m &= m - 1;
-            const uint64_t s = wi * 32 + bit;
-            uint4 *b = reinterpret_cast<uint4 *>(d.dbits + s * 8);
-            const uint4 b0 = b[0], b1 = b[1];
-            const uint4 e1 = reinterpret_cast<const uint4 *>(d.elems + s * 8)[1];
-            b[0] = make_uint4(0, 0, 0, 0);
-            b[1] = make_uint4(0, 0, 0, 0);
-            out[2 * pos] = b0;
-            out[2 * pos + 1] = make_uint4(b1.x, b1.y, e1.z, e1.w);
-            pos++;
+        const uint64_t base_pos = chunk_off[c];
+        for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+            const uint32_t t = t0 + lane;
+            // owner word: smallest lane o with incl(o) > t
+            uint32_t lo = 0;
+#pragma unroll
+            for (int st = 16; st; st >>= 1) {
+                const uint32_t v = __shfl_sync(0xffffffffu, incl, lo + st - 1);
+                if (v <= t) lo += st;
+            }
+            const uint32_t o_incl = __shfl_sync(0xffffffffu, incl, lo & 31);
+            const uint32_t o_cnt = __shfl_sync(0xffffffffu, cnt, lo & 31);
+            const uint32_t o_m = __shfl_sync(0xffffffffu, m, lo & 31);
+            if (t < total) {
+                const uint32_t bit = select32(o_m, t - (o_incl - o_cnt));
+                const uint64_t s = (c * 32 + lo) * 32 + bit;
+                uint4 *b = reinterpret_cast<uint4 *>(d.dbits + s * 8);
+                const uint4 b0 = b[0], b1 = b[1];
+                const uint4 e1 = reinterpret_cast<const uint4 *>(d.elems + s * 8)[1];
+                b[0] = make_uint4(0, 0, 0, 0);
+                b[1] = make_uint4(0, 0, 0, 0);
+                const uint64_t pos = base_pos + t;
+                out[2 * pos] = b0;
+                out[2 * pos + 1] = make_uint4(b1.x, b1.y, e1.z, e1.w);
+            }
         }
     }
 }
@@ -281,18 +308,6 @@ __device__ __forceinline__ uint32_t popc6(const Bits &b)
 #pragma unroll
     for (int x = 0; x < EW; x++) c += __popc(b.w[x]);
     return c;
-}
-
-// Position of the n-th (0-based) set bit of a 32-bit word (broadword select, no loop).
-__device__ __forceinline__ uint32_t select32(uint32_t w, uint32_t n)
-{
-    uint32_t pos = 0, c;
-    c = __popc(w & 0xFFFFu); if (n >= c) { n -= c; pos += 16; w >>= 16; }
-    c = __popc(w & 0xFFu);   if (n >= c) { n -= c; pos += 8;  w >>= 8; }
-    c = __popc(w & 0xFu);    if (n >= c) { n -= c; pos += 4;  w >>= 4; }
-    c = __popc(w & 0x3u);    if (n >= c) { n -= c; pos += 2;  w >>= 2; }
-    c = w & 1u;              if (n >= c) { pos += 1; }
-    return pos;
 }
 
 // Position (0..191) of the idx-th set bit of a record's bitmap in shared memory.
