@@ -256,7 +256,7 @@ def main():
         launches = s["join_launches"]
         achieved = alg_bytes / (join_ms * 1e-3) / 1e9 if join_ms > 0 else None
         traffic = None
-        tp = os.path.join(ROOT, "profiles", "k_join_traffic.json")
+        tp = os.path.join(ROOT, "profiles", "join_pass_traffic.json")
         if os.path.exists(tp):
             traffic = json.load(open(tp)).get("bytes_per_launch")
         cb = None if args.no_cpu_baseline else cpu_baseline(w)
@@ -272,7 +272,7 @@ def main():
                        "pool_elems_used": s["pool_elems_used"]},
             "e2e": {"value": world * total / (e2e_max * 1e-3), "unit": UNIT,
                     "h2d_bytes_per_step": int(w.num_edges * 9), "d2h_bytes_per_step": int(w.num_labels * 8)},
-            "roofline": {"bound": "hbm", "kernel": "k_join", "achieved": achieved, "peak": hbm,
+            "roofline": {"bound": "hbm", "kernel": "join pass (k_join + k_apply)", "achieved": achieved, "peak": hbm,
                          "peak_kind": peak_kind, "unit": "GB/s",
                          "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
                          "alg_bytes_per_launch": alg_bytes / launches, "launches_per_step": launches,
