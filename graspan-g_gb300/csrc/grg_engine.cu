@@ -84,15 +84,22 @@ __global__ void k_init_region(uint32_t *elems, uint32_t *dbits, uint64_t begin, 
     }
 }
 
-__global__ void k_load_hist(Dev d, const uint32_t *src, const uint8_t *lab, uint64_t n)
+// Input ids are local to a vertex range starting at `base` (0 for a whole graph).
+__global__ void k_fill_u32(uint32_t *p, uint64_t n, uint32_t v)
 {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        atomicAdd(&d.cnt[(size_t)(lab[i] - 1) * d.V + src[i]], 1u);
+        p[i] = v;
 }
 
-__global__ void k_eps_hist(Dev d, uint32_t slot)
+__global__ void k_load_hist(Dev d, const uint32_t *src, const uint8_t *lab, uint64_t n, uint32_t base)
 {
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < d.V; v += gridDim.x * blockDim.x)
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        atomicAdd(&d.cnt[(size_t)(lab[i] - 1) * d.V + base + src[i]], 1u);
+}
+
+__global__ void k_eps_hist(Dev d, uint32_t slot, uint32_t first, uint32_t nv)
+{
+    for (uint32_t v = first + blockIdx.x * blockDim.x + threadIdx.x; v < first + nv; v += gridDim.x * blockDim.x)
         atomicAdd(&d.cnt[(size_t)(slot - 1) * d.V + v], 1u);
 }
 
@@ -100,14 +107,17 @@ __global__ void k_eps_hist(Dev d, uint32_t slot)
 // derive start large enough to rarely grow, so they stay in row order.
 struct MinCap { uint32_t cap[MAX_LABELS + 1]; };
 
-// One thread per table: size from the edge histogram (held in cnt), bump-allocate.
-__global__ void k_load_alloc(Dev d, uint64_t ntables, MinCap mc)
+// One thread per table of labels 1..L over rows [first, first + nv): size from
+// the edge histogram (held in cnt), bump-allocate.
+__global__ void k_load_alloc(Dev d, uint32_t first, uint32_t nv, uint32_t L, MinCap mc)
 {
-    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < ((ntables + 31) & ~31ull);
-         t += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t h = t < ntables ? d.cnt[t] : 0;
-        const uint32_t lab = t < ntables ? (uint32_t)(t / d.V) + 1 : 1;
-        uint32_t cap = t < ntables ? mc.cap[lab] : 0;
+    const uint64_t ntables = (uint64_t)L * nv;
+    for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < ((ntables + 31) & ~31ull);
+         u += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t lab = u < ntables ? (uint32_t)(u / nv) + 1 : 1;
+        const uint64_t t = (uint64_t)(lab - 1) * d.V + first + (u < ntables ? u % nv : 0);
+        uint32_t h = u < ntables ? d.cnt[t] : 0;
+        uint32_t cap = u < ntables ? mc.cap[lab] : 0;
         if (h) {
             const uint32_t need = h + h / 3 + 1;
             if (cap < 4) cap = 4;
@@ -123,7 +133,7 @@ __global__ void k_load_alloc(Dev d, uint64_t ntables, MinCap mc)
         unsigned long long base = 0;
         if (lane_id() == 31 && total) base = atomicAdd(&d.ctr[C_POOL_TOP], (unsigned long long)total);
         base = __shfl_sync(0xffffffffu, base, 31);
-        if (t < ntables) {
+        if (u < ntables) {
             uint64_t off = base + incl - cap;
             if (cap && off + cap > d.pool_cap) {
                 atomicOr(&d.ctr[C_ERR], (unsigned long long)ERR_POOL);
@@ -135,22 +145,23 @@ __global__ void k_load_alloc(Dev d, uint64_t ntables, MinCap mc)
     }
 }
 
-__global__ void k_load_insert(Dev d, const uint32_t *src, const uint32_t *dst, const uint8_t *lab, uint64_t n)
+__global__ void k_load_insert(Dev d, const uint32_t *src, const uint32_t *dst, const uint8_t *lab, uint64_t n,
+                              uint32_t vbase)
 {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t v = dst[i];
+        const uint32_t v = vbase + dst[i];
         Bits b;
         const uint32_t o = v % EIDS;
 #pragma unroll
         for (int w = 0; w < EW; w++) b.w[w] = (uint32_t)w == (o >> 5) ? 1u << (o & 31) : 0u;
-        if (!g_insert(d, lab[i], src[i], v / EIDS, b, false)) atomicOr(&d.ctr[C_ERR], (unsigned long long)ERR_LOAD);
+        if (!g_insert(d, lab[i], vbase + src[i], v / EIDS, b, false)) atomicOr(&d.ctr[C_ERR], (unsigned long long)ERR_LOAD);
     }
 }
 
 // Epsilon rules A ::= eps: (v, v, A) for every vertex (compute00, src/kernel.cu:445-464).
-__global__ void k_eps_insert(Dev d, uint32_t slot)
+__global__ void k_eps_insert(Dev d, uint32_t slot, uint32_t first, uint32_t nv)
 {
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < d.V; v += gridDim.x * blockDim.x) {
+    for (uint32_t v = first + blockIdx.x * blockDim.x + threadIdx.x; v < first + nv; v += gridDim.x * blockDim.x) {
         Bits b;
         const uint32_t o = v % EIDS;
 #pragma unroll
@@ -161,9 +172,9 @@ __global__ void k_eps_insert(Dev d, uint32_t slot)
 
 // Rows of labels that are never inserted into after the load are packed:
 // occupied slots moved to the front, capacity = count (no empty slots to scan).
-__global__ void k_compact_static(Dev d, uint32_t slot)
+__global__ void k_compact_static(Dev d, uint32_t slot, uint32_t first, uint32_t nv)
 {
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < d.V; v += gridDim.x * blockDim.x) {
+    for (uint32_t v = first + blockIdx.x * blockDim.x + threadIdx.x; v < first + nv; v += gridDim.x * blockDim.x) {
         const size_t ti = (size_t)(slot - 1) * d.V + v;
         const uint64_t de = d.desc[ti];
         const uint32_t off = (uint32_t)de, cap = (uint32_t)(de >> 32);
@@ -189,10 +200,10 @@ __global__ void k_compact_static(Dev d, uint32_t slot)
 
 // Every loaded element of a tracked label becomes a delta of round 1. A warp
 // covers 32 consecutive slots, so it owns one dirty-bitmap word.
-__global__ void k_mark_all(Dev d, uint64_t end)
+__global__ void k_mark_all(Dev d, uint64_t begin, uint64_t end)   // begin: multiple of 32
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t b0 = blockIdx.x * (uint64_t)blockDim.x + (threadIdx.x & ~31u); b0 < end; b0 += stride) {
+    for (uint64_t b0 = begin + blockIdx.x * (uint64_t)blockDim.x + (threadIdx.x & ~31u); b0 < end; b0 += stride) {
         const uint64_t s = b0 + lane_id();
         bool mark = false;
         if (s < end) {
@@ -242,7 +253,8 @@ __device__ __forceinline__ uint32_t select32(uint32_t w, uint32_t n)
 // chunk offsets; clears the delta bitmaps and the dirty bitmap. One warp per
 // chunk of 32 bitmap words; lanes take consecutive dirty slots of the chunk, so
 // the copies of a warp are independent and mostly coalesced.
-__global__ void k_gather(Dev d, uint64_t nwords, const uint32_t *__restrict__ chunk_off, uint4 *out)
+__global__ void k_gather(Dev d, uint64_t nwords, const uint32_t *__restrict__ chunk_off, uint4 *out,
+                         const uint32_t *__restrict__ row_job, uint32_t *job_cnt)
 {
     const uint64_t nchunks = (nwords + 31) / 32;
     const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
@@ -282,6 +294,16 @@ __global__ void k_gather(Dev d, uint64_t nwords, const uint32_t *__restrict__ ch
                 const uint64_t pos = base_pos + t;
                 out[2 * pos] = b0;
                 out[2 * pos + 1] = make_uint4(b1.x, b1.y, e1.z, e1.w);
+            }
+            if (row_job) {
+                // batched jobs: records per job (a job with none has reached its fixpoint)
+                uint32_t job = EMPTY;
+                if (t < total) {
+                    const uint32_t *e = d.elems + ((c * 32 + lo) * 32 + select32(o_m, t - (o_incl - o_cnt))) * 8;
+                    job = row_job[e[7]];
+                }
+                const unsigned g = __match_any_sync(0xffffffffu, job);
+                if (job != EMPTY && (int)lane == __ffs(g) - 1) atomicAdd(&job_cnt[job], (uint32_t)__popc(g));
             }
         }
     }
@@ -959,12 +981,12 @@ __global__ void k_grow(Dev d, uint64_t n)
 
 // One warp per table of a label slot: edge/element counts, optional degree and hash.
 __global__ void k_count(Dev d, uint32_t slot, uint32_t *deg_edges, uint32_t *deg_elems, uint32_t first,
-                        uint32_t last, int do_hash)
+                        uint32_t last, int do_hash, uint32_t r0, uint32_t r1, uint32_t hash_base)
 {
     const uint32_t lane = lane_id();
     const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
     unsigned long long my_edges = 0, my_hash = 0;
-    for (uint64_t v = blockIdx.x * (uint64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); v < d.V; v += nwarps) {
+    for (uint64_t v = r0 + blockIdx.x * (uint64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); v < r1; v += nwarps) {
         const uint64_t de = d.desc[(size_t)(slot - 1) * d.V + v];
         const uint32_t off = (uint32_t)de, cap = (uint32_t)(de >> 32);
         uint32_t e = 0, el = 0;
@@ -981,7 +1003,7 @@ __global__ void k_count(Dev d, uint32_t slot, uint32_t *deg_edges, uint32_t *deg
                     while (bw) {
                         const int bit = __ffs(bw) - 1;
                         bw &= bw - 1;
-                        my_hash += edge_hash(slot, (uint32_t)v, hb * EIDS + x * 32 + bit);
+                        my_hash += edge_hash(slot - hash_base, (uint32_t)v - r0, hb * EIDS + x * 32 + bit - r0);
                     }
             }
         }
@@ -1078,6 +1100,15 @@ struct grg_ctx {
     RuleTable rt{};
     uint64_t launches = 0;
     std::vector<uint32_t *> csr_bufs;      // CSR copies of static labels (freed on reload)
+    // batched jobs (continuous batching): each job owns a vertex range
+    uint32_t *row_job = nullptr;           // vertex -> job slot (EMPTY = free)
+    uint32_t *job_cnt = nullptr;           // delta records per job slot in the last gather
+    uint32_t max_jobs = 0;
+    bool batch = false;
+    uint32_t filter = 0;
+    // pending: delta records of the job in the last gather (UINT32_MAX until a step has run)
+    struct JobRange { uint32_t base = 0, nv = 0; bool active = false; uint32_t pending = 0xFFFFFFFFu; };
+    std::vector<JobRange> jobs;
 };
 
 namespace {
@@ -1147,6 +1178,11 @@ void free_csr(grg_ctx *c)
 void free_graph(grg_ctx *c)
 {
     free_csr(c);
+    cudaFree(c->row_job); c->row_job = nullptr;
+    cudaFree(c->job_cnt); c->job_cnt = nullptr;
+    c->max_jobs = 0;
+    c->batch = false;
+    c->jobs.clear();
     cudaFree(c->desc); c->desc = nullptr;
     cudaFree(c->cnt); c->cnt = nullptr;
     cudaFree(c->want); c->want = nullptr;
@@ -1458,7 +1494,7 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
     c->V = num_vars;
     c->ntables = (uint64_t)c->L * num_vars;
     const uint64_t nt_all = (uint64_t)(2 * c->L) * num_vars;
-    if (c->ntables_alloc != nt_all) {
+    if (c->ntables_alloc != nt_all || c->batch) {
         free_graph(c);
         GRG_CUDA(c, cudaMalloc(&c->desc, std::max<uint64_t>(nt_all, 1) * 8));
         GRG_CUDA(c, cudaMalloc(&c->cnt, std::max<uint64_t>(nt_all, 1) * 4));
@@ -1491,12 +1527,12 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
     Dev d = make_dev(c);
     c->launches = 0;
     if (num_edges) {
-        k_load_hist<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, dlab, num_edges);
+        k_load_hist<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, dlab, num_edges, 0);
         c->launches++;
     }
     for (int q = 0; q < c->R; q++)
         if (c->rules[3 * q + 1] == 0) {
-            k_eps_hist<<<grid_for(c, num_vars, 256), 256, 0, s>>>(d, (uint32_t)c->rules[3 * q]);
+            k_eps_hist<<<grid_for(c, num_vars, 256), 256, 0, s>>>(d, (uint32_t)c->rules[3 * q], 0, num_vars);
             c->launches++;
         }
     // labels on a rule's left-hand side get tables of DERIVED_MIN_CAP slots when that fits in a
@@ -1514,7 +1550,7 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
     for (int attempt = 0;; attempt++) {
         GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_POOL_TOP, 0, 8, s));
         GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_ERR, 0, 8, s));
-        k_load_alloc<<<grid_for(c, c->ntables, 256), 256, 0, s>>>(d, c->ntables, mc);
+        k_load_alloc<<<grid_for(c, c->ntables, 256), 256, 0, s>>>(d, 0, num_vars, (uint32_t)c->L, mc);
         c->launches++;
         int st = read_ctr(c);
         if (st) return st;
@@ -1525,10 +1561,10 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
         if (st) return st;
         d = make_dev(c);
         GRG_CUDA(c, cudaMemsetAsync(c->cnt, 0, nt_all * 4, s));
-        if (num_edges) k_load_hist<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, dlab, num_edges);
+        if (num_edges) k_load_hist<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, dlab, num_edges, 0);
         for (int q = 0; q < c->R; q++)
             if (c->rules[3 * q + 1] == 0)
-                k_eps_hist<<<grid_for(c, num_vars, 256), 256, 0, s>>>(d, (uint32_t)c->rules[3 * q]);
+                k_eps_hist<<<grid_for(c, num_vars, 256), 256, 0, s>>>(d, (uint32_t)c->rules[3 * q], 0, num_vars);
     }
     uint64_t top = c->h_ctr[C_POOL_TOP];
     if (top) {
@@ -1537,12 +1573,12 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
         c->launches++;
     }
     if (num_edges) {
-        k_load_insert<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges);
+        k_load_insert<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges, 0);
         c->launches++;
     }
     for (int q = 0; q < c->R; q++)
         if (c->rules[3 * q + 1] == 0) {
-            k_eps_insert<<<grid_for(c, num_vars, 256), 256, 0, s>>>(d, (uint32_t)c->rules[3 * q]);
+            k_eps_insert<<<grid_for(c, num_vars, 256), 256, 0, s>>>(d, (uint32_t)c->rules[3 * q], 0, num_vars);
             c->launches++;
         }
     GRG_CUDA(c, cudaGetLastError());
@@ -1554,83 +1590,20 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
     return GRG_OK;
 }
 
-int grg_closure(grg_ctx *c, uint32_t filter, grg_stats *stats)
+// Semi-naive rounds: gather the dirty slots of the last round into delta
+// records, join them, insert the candidates. Stops when a gather finds no delta
+// (the fixpoint: *idle = true) or after max_rounds rounds (0 = no limit).
+static int run_rounds(grg_ctx *c, uint64_t max_rounds, grg_stats &S, double &join_ms, uint64_t &joins, bool *idle)
 {
-    if (!c || filter > 1) return GRG_E_ARG;
-    if (!c->loaded) return fail(c, GRG_E_STATE, "grg_load_edges must come first");
-    if (c->closed) return fail(c, GRG_E_STATE, "closure already computed; reload the graph");
-    cudaSetDevice(c->device);
-    RuleTable rt;
-    int st = build_rules(c, filter, rt);
-    if (st) return st;
-    c->rt = rt;
     cudaStream_t s = c->stream;
-    GRG_CUDA(c, cudaMemcpyToSymbolAsync(c_rt, &rt, sizeof rt, 0, cudaMemcpyHostToDevice, s));
-    grg_stats S;
-    memset(&S, 0, sizeof S);
-    GRG_CUDA(c, cudaEventRecord(c->ev_a, s));
     Dev d = make_dev(c);
-    // labels never inserted into after the load are packed
-    bool derivable[MAX_LABELS + 1] = {false};
-    for (int q = 0; q < c->R; q++) {
-        const int *r = &c->rules[3 * q];
-        bool unary = r[1] && !r[2];
-        if (!(filter && unary)) derivable[r[0]] = true;
-    }
-    for (int l = 1; l <= c->L; l++)
-        if (!derivable[l]) {
-            k_compact_static<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)l);
-            c->launches++;
-        }
-    // CSR copies of static labels that are a binary rule's second symbol
-    free_csr(c);
-    for (int l = 1; l <= c->L; l++) {
-        bool rhs2 = false;
-        for (int q = 0; q < c->R; q++)
-            if (c->rules[3 * q + 1] && c->rules[3 * q + 2] == l) rhs2 = true;
-        if (derivable[l] || !rhs2 || c->V == 0) continue;
-        uint32_t *ptr = nullptr, *sums = nullptr, *col = nullptr, *row = nullptr;
-        const uint64_t nb = (c->V + 1023) / 1024;
-        GRG_CUDA(c, cudaMalloc(&ptr, ((uint64_t)c->V + 1) * 4));
-        c->csr_bufs.push_back(ptr);
-        GRG_CUDA(c, cudaMalloc(&row, ((uint64_t)c->V + 1) * 8));
-        c->csr_bufs.push_back(row);
-        GRG_CUDA(c, cudaMalloc(&sums, (nb + 1) * 4));
-        c->csr_bufs.push_back(sums);
-        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_ERR, 0, 8, s));
-        k_csr_count<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)l, ptr, (uint2 *)row);
-        k_scan_blocks<<<(unsigned)nb, 1024, 0, s>>>(ptr, ptr, sums, c->V);
-        k_scan_sums<<<1, 1024, 0, s>>>(sums, nb);
-        k_scan_add<<<(unsigned)nb, 1024, 0, s>>>(ptr, sums, c->V);
-        st = read_ctr(c);
-        if (st) return st;
-        if (c->h_ctr[C_ERR]) continue;                 // a row too long for the packed CSR: keep elements
-        uint32_t total = 0;
-        GRG_CUDA(c, cudaMemcpyAsync(&total, sums + nb, 4, cudaMemcpyDeviceToHost, s));
-        GRG_CUDA(c, cudaStreamSynchronize(s));
-        GRG_CUDA(c, cudaMalloc(&col, std::max<uint64_t>(total, 1) * 4));
-        c->csr_bufs.push_back(col);
-        k_csr_fill<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)l, ptr, (uint2 *)row, col);
-        c->launches += 6;
-        rt.csr_row[l] = (const uint2 *)row;
-        rt.csr_col[l] = col;
-    }
-    c->rt = rt;
-    GRG_CUDA(c, cudaMemcpyToSymbolAsync(c_rt, &rt, sizeof rt, 0, cudaMemcpyHostToDevice, s));
-    st = read_ctr(c);
+    int st = read_ctr(c);
     if (st) return st;
-    const uint64_t top = c->h_ctr[C_POOL_TOP];
-    // every loaded element of a tracked label is a delta of round 1
-    d = make_dev(c);
-    if (top) {
-        k_mark_all<<<grid_for(c, top, 256), 256, 0, s>>>(d, top);
-        c->launches++;
-    }
-    double join_ms = 0;
-    uint64_t joins = 0;
-    st = read_ctr(c);
-    if (st) return st;
+    *idle = false;
+    uint64_t done_rounds = 0;
     for (;;) {
+        if (max_rounds && done_rounds >= max_rounds) break;
+        if (c->job_cnt) GRG_CUDA(c, cudaMemsetAsync(c->job_cnt, 0, (size_t)c->max_jobs * 4, s));
         // gather the dirty slots of the last round into delta records (slot order);
         // the pool top is the one read after the last growth
         const uint64_t nwords = (c->h_ctr[C_POOL_TOP] + 31) / 32;
@@ -1652,7 +1625,11 @@ int grg_closure(grg_ctx *c, uint32_t filter, grg_stats *stats)
         st = read_ctr(c);
         if (st) return st;
         const uint64_t nd = c->h_ctr[C_DIRTY_N];
-        if (nd == 0) break;
+        if (nd == 0) {
+            *idle = true;
+            break;
+        }
+        done_rounds++;
         st = ensure_rbuf(c, nd);
         if (st) return st;
         st = ensure_cand(c, nd);
@@ -1661,7 +1638,7 @@ int grg_closure(grg_ctx *c, uint32_t filter, grg_stats *stats)
         S.delta_elems += nd;
         c->cb = 0;
         d = make_dev(c);
-        k_gather<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->rbuf[2]);
+        k_gather<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->rbuf[2], c->row_job, c->job_cnt);
         c->launches++;
         uint64_t n = nd;       // delta records for the next join pass (0 = none)
         int rb = 0;
@@ -1723,6 +1700,86 @@ int grg_closure(grg_ctx *c, uint32_t filter, grg_stats *stats)
             GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_RETRY_N, 0, 16, s));
         }
     }
+    return GRG_OK;
+}
+
+int grg_closure(grg_ctx *c, uint32_t filter, grg_stats *stats)
+{
+    if (!c || filter > 1) return GRG_E_ARG;
+    if (!c->loaded) return fail(c, GRG_E_STATE, "grg_load_edges must come first");
+    if (c->closed) return fail(c, GRG_E_STATE, "closure already computed; reload the graph");
+    cudaSetDevice(c->device);
+    RuleTable rt;
+    int st = build_rules(c, filter, rt);
+    if (st) return st;
+    c->rt = rt;
+    cudaStream_t s = c->stream;
+    GRG_CUDA(c, cudaMemcpyToSymbolAsync(c_rt, &rt, sizeof rt, 0, cudaMemcpyHostToDevice, s));
+    grg_stats S;
+    memset(&S, 0, sizeof S);
+    GRG_CUDA(c, cudaEventRecord(c->ev_a, s));
+    Dev d = make_dev(c);
+    // labels never inserted into after the load are packed
+    bool derivable[MAX_LABELS + 1] = {false};
+    for (int q = 0; q < c->R; q++) {
+        const int *r = &c->rules[3 * q];
+        bool unary = r[1] && !r[2];
+        if (!(filter && unary)) derivable[r[0]] = true;
+    }
+    for (int l = 1; l <= c->L; l++)
+        if (!derivable[l]) {
+            k_compact_static<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)l, 0, c->V);
+            c->launches++;
+        }
+    // CSR copies of static labels that are a binary rule's second symbol
+    free_csr(c);
+    for (int l = 1; l <= c->L; l++) {
+        bool rhs2 = false;
+        for (int q = 0; q < c->R; q++)
+            if (c->rules[3 * q + 1] && c->rules[3 * q + 2] == l) rhs2 = true;
+        if (derivable[l] || !rhs2 || c->V == 0) continue;
+        uint32_t *ptr = nullptr, *sums = nullptr, *col = nullptr, *row = nullptr;
+        const uint64_t nb = (c->V + 1023) / 1024;
+        GRG_CUDA(c, cudaMalloc(&ptr, ((uint64_t)c->V + 1) * 4));
+        c->csr_bufs.push_back(ptr);
+        GRG_CUDA(c, cudaMalloc(&row, ((uint64_t)c->V + 1) * 8));
+        c->csr_bufs.push_back(row);
+        GRG_CUDA(c, cudaMalloc(&sums, (nb + 1) * 4));
+        c->csr_bufs.push_back(sums);
+        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_ERR, 0, 8, s));
+        k_csr_count<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)l, ptr, (uint2 *)row);
+        k_scan_blocks<<<(unsigned)nb, 1024, 0, s>>>(ptr, ptr, sums, c->V);
+        k_scan_sums<<<1, 1024, 0, s>>>(sums, nb);
+        k_scan_add<<<(unsigned)nb, 1024, 0, s>>>(ptr, sums, c->V);
+        st = read_ctr(c);
+        if (st) return st;
+        if (c->h_ctr[C_ERR]) continue;                 // a row too long for the packed CSR: keep elements
+        uint32_t total = 0;
+        GRG_CUDA(c, cudaMemcpyAsync(&total, sums + nb, 4, cudaMemcpyDeviceToHost, s));
+        GRG_CUDA(c, cudaStreamSynchronize(s));
+        GRG_CUDA(c, cudaMalloc(&col, std::max<uint64_t>(total, 1) * 4));
+        c->csr_bufs.push_back(col);
+        k_csr_fill<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)l, ptr, (uint2 *)row, col);
+        c->launches += 6;
+        rt.csr_row[l] = (const uint2 *)row;
+        rt.csr_col[l] = col;
+    }
+    c->rt = rt;
+    GRG_CUDA(c, cudaMemcpyToSymbolAsync(c_rt, &rt, sizeof rt, 0, cudaMemcpyHostToDevice, s));
+    st = read_ctr(c);
+    if (st) return st;
+    const uint64_t top = c->h_ctr[C_POOL_TOP];
+    // every loaded element of a tracked label is a delta of round 1
+    d = make_dev(c);
+    if (top) {
+        k_mark_all<<<grid_for(c, top, 256), 256, 0, s>>>(d, 0, top);
+        c->launches++;
+    }
+    double join_ms = 0;
+    uint64_t joins = 0;
+    bool idle = false;
+    st = run_rounds(c, 0, S, join_ms, joins, &idle);
+    if (st) return st;
     GRG_CUDA(c, cudaEventRecord(c->ev_b, s));
     GRG_CUDA(c, cudaEventSynchronize(c->ev_b));
     float ms = 0;
@@ -1754,7 +1811,7 @@ static int count_pass(grg_ctx *c, uint32_t *deg_e, uint32_t *deg_el, uint32_t fi
     GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_LABEL0, 0, sizeof(unsigned long long) * (MAX_SLOTS + 2), s));
     GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_HASH, 0, 8, s));
     for (int l = 1; l <= c->L; l++)
-        k_count<<<grid_for(c, (uint64_t)c->V * 32, 256), 256, 0, s>>>(d, (uint32_t)l, deg_e, deg_el, first, last, do_hash);
+        k_count<<<grid_for(c, (uint64_t)c->V * 32, 256), 256, 0, s>>>(d, (uint32_t)l, deg_e, deg_el, first, last, do_hash, 0, c->V, 0);
     GRG_CUDA(c, cudaGetLastError());
     return read_ctr(c);
 }
@@ -1829,6 +1886,208 @@ int grg_export_edges(grg_ctx *c, uint64_t cap, uint32_t *src, uint32_t *dst, uin
         cudaFree(d8);
     }
     GRG_CUDA(c, cudaGetLastError());
+    return GRG_OK;
+}
+
+}  // extern "C"
+
+// ====================================================================== batched jobs
+
+extern "C" {
+
+int grg_batch_begin(grg_ctx *c, uint32_t max_vars, uint32_t max_jobs, int num_rules, const int *rules,
+                    int num_labels, uint32_t filter)
+{
+    if (!c || filter > 1 || max_jobs == 0 || max_vars == 0) return GRG_E_ARG;
+    int st = grg_transfer_rules(c, num_rules, rules, num_labels);
+    if (st) return st;
+    cudaSetDevice(c->device);
+    RuleTable rt;
+    st = build_rules(c, filter, rt);
+    if (st) return st;
+    if (!c->elems) {
+        st = grg_allocate_pool(c, c->pool_bytes_req);
+        if (st) return st;
+    }
+    if ((uint64_t)max_vars * (uint64_t)(2 * c->L) >= 0xFFFFFFFFull)
+        return fail(c, GRG_E_RANGE, "max_vars x 2 x numLabels must stay below 2^32");
+    free_graph(c);
+    cudaStream_t s = c->stream;
+    c->V = max_vars;
+    c->ntables = (uint64_t)c->L * max_vars;
+    const uint64_t nt_all = (uint64_t)(2 * c->L) * max_vars;
+    GRG_CUDA(c, cudaMalloc(&c->desc, nt_all * 8));
+    GRG_CUDA(c, cudaMalloc(&c->cnt, nt_all * 4));
+    GRG_CUDA(c, cudaMalloc(&c->want, nt_all * 4));
+    GRG_CUDA(c, cudaMalloc(&c->grow, nt_all * 4));
+    c->ntables_alloc = nt_all;
+    GRG_CUDA(c, cudaMalloc(&c->row_job, (uint64_t)max_vars * 4));
+    GRG_CUDA(c, cudaMalloc(&c->job_cnt, (uint64_t)max_jobs * 4));
+    c->max_jobs = max_jobs;
+    c->jobs.assign(max_jobs, grg_ctx::JobRange());
+    GRG_CUDA(c, cudaMemsetAsync(c->desc, 0, nt_all * 8, s));
+    GRG_CUDA(c, cudaMemsetAsync(c->cnt, 0, nt_all * 4, s));
+    GRG_CUDA(c, cudaMemsetAsync(c->want, 0, nt_all * 4, s));
+    GRG_CUDA(c, cudaMemsetAsync(c->row_job, 0xFF, (uint64_t)max_vars * 4, s));
+    GRG_CUDA(c, cudaMemsetAsync(c->job_cnt, 0, (uint64_t)max_jobs * 4, s));
+    GRG_CUDA(c, cudaMemsetAsync(c->ctr, 0, sizeof(unsigned long long) * NCTR, s));
+    GRG_CUDA(c, cudaMemsetAsync(c->dmap, 0, (c->pool_cap / 32 + 2) * 4, s));
+    c->rt = rt;   // batch mode keeps every label in hash tables (no CSR copies)
+    GRG_CUDA(c, cudaMemcpyToSymbolAsync(c_rt, &rt, sizeof rt, 0, cudaMemcpyHostToDevice, s));
+    c->batch = true;
+    c->filter = filter;
+    c->loaded = true;
+    c->closed = false;
+    return read_ctr(c);
+}
+
+int grg_batch_admit(grg_ctx *c, uint32_t job, uint32_t base, uint32_t num_vars, uint64_t num_edges,
+                    const uint32_t *src, const uint32_t *dst, const uint8_t *label, int on_device, uint64_t eps_mask)
+{
+    if (!c || (num_edges && (!src || !dst || !label))) return GRG_E_ARG;
+    if (!c->batch) return fail(c, GRG_E_STATE, "grg_batch_begin must come first");
+    if (job >= c->max_jobs || c->jobs[job].active) return fail(c, GRG_E_ARG, "job slot in use or out of range");
+    if (num_vars == 0 || (uint64_t)base + num_vars > c->V) return fail(c, GRG_E_RANGE, "vertex range outside max_vars");
+    for (const auto &j : c->jobs)
+        if (j.active && base < j.base + j.nv && j.base < base + num_vars)
+            return fail(c, GRG_E_ARG, "vertex range overlaps an admitted job");
+    cudaSetDevice(c->device);
+    cudaStream_t s = c->stream;
+    const uint32_t *dsrc = src, *ddst = dst;
+    const uint8_t *dlab = label;
+    if (!on_device && num_edges) {
+        if (c->in_cap < num_edges) {
+            cudaFree(c->d_in32); cudaFree(c->d_in8);
+            c->d_in32 = nullptr; c->d_in8 = nullptr;
+            GRG_CUDA(c, cudaMalloc(&c->d_in32, num_edges * 8));
+            GRG_CUDA(c, cudaMalloc(&c->d_in8, num_edges));
+            c->in_cap = num_edges;
+        }
+        GRG_CUDA(c, cudaMemcpyAsync(c->d_in32, src, num_edges * 4, cudaMemcpyHostToDevice, s));
+        GRG_CUDA(c, cudaMemcpyAsync(c->d_in32 + num_edges, dst, num_edges * 4, cudaMemcpyHostToDevice, s));
+        GRG_CUDA(c, cudaMemcpyAsync(c->d_in8, label, num_edges, cudaMemcpyHostToDevice, s));
+        dsrc = c->d_in32;
+        ddst = c->d_in32 + num_edges;
+        dlab = c->d_in8;
+    }
+    // room for the job's tables: edges x 4/3 plus presized derived rows
+    MinCap mc;
+    memset(&mc, 0, sizeof mc);
+    bool lhs[MAX_LABELS + 1] = {false};
+    int nder = 0;
+    for (int q = 0; q < c->R; q++) lhs[c->rules[3 * q]] = true;
+    for (int l = 1; l <= c->L; l++) nder += lhs[l];
+    int st = read_ctr(c);
+    if (st) return st;
+    const uint64_t top0 = (c->h_ctr[C_POOL_TOP] + 31) & ~31ull;   // the job's slots start on a dirty-bitmap word
+    const uint64_t est = 2 * num_edges + (uint64_t)num_vars * (64 + 4 * __builtin_popcountll(eps_mask)) +
+                         (uint64_t)nder * num_vars * DERIVED_MIN_CAP;
+    if (top0 + est > c->pool_cap) {
+        st = grow_pool(c, top0 + est + c->pool_cap / 2);
+        if (st) return st;
+    }
+    if ((uint64_t)nder * num_vars * DERIVED_MIN_CAP <= (c->pool_cap - top0) / 4)
+        for (int l = 1; l <= c->L; l++) mc.cap[l] = lhs[l] ? DERIVED_MIN_CAP : 0;
+    c->h_ctr[C_POOL_TOP] = top0;
+    GRG_CUDA(c, cudaMemcpyAsync(c->ctr + C_POOL_TOP, c->h_ctr + C_POOL_TOP, 8, cudaMemcpyHostToDevice, s));
+    GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_ERR, 0, 8, s));
+    Dev d = make_dev(c);
+    if (num_edges) k_load_hist<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, dlab, num_edges, base);
+    for (int l = 1; l <= c->L; l++)
+        if ((eps_mask >> (l - 1)) & 1ull) k_eps_hist<<<grid_for(c, num_vars, 256), 256, 0, s>>>(d, (uint32_t)l, base, num_vars);
+    k_load_alloc<<<grid_for(c, (uint64_t)c->L * num_vars, 256), 256, 0, s>>>(d, base, num_vars, (uint32_t)c->L, mc);
+    st = read_ctr(c);
+    if (st) return st;
+    if (c->h_ctr[C_ERR] & ERR_POOL) return fail(c, GRG_E_NOMEM, "element pool too small for the job");
+    const uint64_t top1 = c->h_ctr[C_POOL_TOP];
+    if (top1 > top0) k_init_region<<<grid_for(c, top1 - top0, 256), 256, 0, s>>>(c->elems, c->dbits, top0, top1);
+    if (num_edges) k_load_insert<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges, base);
+    for (int l = 1; l <= c->L; l++)
+        if ((eps_mask >> (l - 1)) & 1ull) k_eps_insert<<<grid_for(c, num_vars, 256), 256, 0, s>>>(d, (uint32_t)l, base, num_vars);
+    // rows of labels that no active rule derives are packed (as grg_closure does)
+    bool derivable[MAX_LABELS + 1] = {false};
+    for (int q = 0; q < c->R; q++) {
+        const int *r = &c->rules[3 * q];
+        const bool unary = r[1] && !r[2];
+        if (!(c->filter && unary)) derivable[r[0]] = true;
+    }
+    for (int l = 1; l <= c->L; l++)
+        if (!derivable[l]) k_compact_static<<<grid_for(c, num_vars, 256), 256, 0, s>>>(d, (uint32_t)l, base, num_vars);
+    if (top1 > top0) k_mark_all<<<grid_for(c, top1 - top0, 256), 256, 0, s>>>(d, top0, top1);
+    k_fill_u32<<<grid_for(c, num_vars, 256), 256, 0, s>>>(c->row_job + base, num_vars, job);
+    GRG_CUDA(c, cudaGetLastError());
+    st = read_ctr(c);
+    if (st) return st;
+    if (c->h_ctr[C_ERR]) return fail(c, GRG_E_CUDA, "internal error while admitting a job");
+    c->jobs[job].base = base;
+    c->jobs[job].nv = num_vars;
+    c->jobs[job].active = true;
+    c->jobs[job].pending = 0xFFFFFFFFu;
+    return GRG_OK;
+}
+
+int grg_batch_step(grg_ctx *c, uint32_t max_rounds, uint32_t *job_records, uint64_t *rounds_run)
+{
+    if (!c) return GRG_E_ARG;
+    if (!c->batch) return fail(c, GRG_E_STATE, "grg_batch_begin must come first");
+    cudaSetDevice(c->device);
+    grg_stats S;
+    memset(&S, 0, sizeof S);
+    double join_ms = 0;
+    uint64_t joins = 0;
+    bool idle = false;
+    int st = run_rounds(c, max_rounds, S, join_ms, joins, &idle);
+    if (st) return st;
+    std::vector<uint32_t> cnt(c->max_jobs, 0);
+    if (!idle) GRG_CUDA(c, cudaMemcpy(cnt.data(), c->job_cnt, sizeof(uint32_t) * c->max_jobs, cudaMemcpyDeviceToHost));
+    for (uint32_t j = 0; j < c->max_jobs; j++)
+        if (c->jobs[j].active) c->jobs[j].pending = cnt[j];
+    if (job_records) memcpy(job_records, cnt.data(), sizeof(uint32_t) * c->max_jobs);
+    if (rounds_run) *rounds_run = S.rounds;
+    return GRG_OK;
+}
+
+int grg_batch_result(grg_ctx *c, uint32_t job, uint32_t label_offset, uint32_t num_labels, uint64_t *counts,
+                     uint64_t *hash)
+{
+    if (!c || !counts) return GRG_E_ARG;
+    if (!c->batch || job >= c->max_jobs || !c->jobs[job].active) return fail(c, GRG_E_STATE, "no such job");
+    if (label_offset + num_labels > (uint32_t)c->L) return GRG_E_RANGE;
+    cudaSetDevice(c->device);
+    cudaStream_t s = c->stream;
+    Dev d = make_dev(c);
+    const uint32_t r0 = c->jobs[job].base, r1 = r0 + c->jobs[job].nv;
+    GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_LABEL0, 0, sizeof(unsigned long long) * (MAX_SLOTS + 2), s));
+    GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_HASH, 0, 8, s));
+    for (uint32_t l = label_offset + 1; l <= label_offset + num_labels; l++)
+        k_count<<<grid_for(c, (uint64_t)(r1 - r0) * 32, 256), 256, 0, s>>>(d, l, nullptr, nullptr, 0, 0, hash ? 1 : 0,
+                                                                           r0, r1, label_offset);
+    GRG_CUDA(c, cudaGetLastError());
+    int st = read_ctr(c);
+    if (st) return st;
+    for (uint32_t l = 0; l < num_labels; l++) counts[l] = c->h_ctr[C_LABEL0 + label_offset + 1 + l];
+    if (hash) *hash = c->h_ctr[C_HASH];
+    return GRG_OK;
+}
+
+int grg_batch_release(grg_ctx *c, uint32_t job)
+{
+    if (!c) return GRG_E_ARG;
+    if (!c->batch || job >= c->max_jobs || !c->jobs[job].active) return fail(c, GRG_E_STATE, "no such job");
+    if (c->jobs[job].pending != 0)
+        return fail(c, GRG_E_STATE, "job has not reached its fixpoint (its last step gathered delta records)");
+    cudaSetDevice(c->device);
+    cudaStream_t s = c->stream;
+    const uint32_t base = c->jobs[job].base, nv = c->jobs[job].nv;
+    for (int slot = 1; slot <= 2 * c->L; slot++) {
+        const size_t t0 = (size_t)(slot - 1) * c->V + base;
+        GRG_CUDA(c, cudaMemsetAsync(c->desc + t0, 0, (size_t)nv * 8, s));
+        GRG_CUDA(c, cudaMemsetAsync(c->cnt + t0, 0, (size_t)nv * 4, s));
+        GRG_CUDA(c, cudaMemsetAsync(c->want + t0, 0, (size_t)nv * 4, s));
+    }
+    GRG_CUDA(c, cudaMemsetAsync(c->row_job + base, 0xFF, (size_t)nv * 4, s));
+    GRG_CUDA(c, cudaStreamSynchronize(s));
+    c->jobs[job].active = false;
     return GRG_OK;
 }
 
@@ -2030,22 +2289,22 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
 
     // load (grg_load_edges)
     const uint64_t nlab = (uint64_t)num_labels * num_vars;
-    if (num_edges) k_load_hist<<<grid(num_edges, 256, 8), 256, 0, s>>>(d, d_src, d_label, num_edges);
+    if (num_edges) k_load_hist<<<grid(num_edges, 256, 8), 256, 0, s>>>(d, d_src, d_label, num_edges, 0);
     for (int q = 0; q < num_rules; q++)
-        if (rules[3 * q + 1] == 0) k_eps_hist<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)rules[3 * q]);
+        if (rules[3 * q + 1] == 0) k_eps_hist<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)rules[3 * q], 0, num_vars);
     MinCap mc;
     memset(&mc, 0, sizeof mc);
-    k_load_alloc<<<grid(nlab, 256, 8), 256, 0, s>>>(d, nlab, mc);
+    k_load_alloc<<<grid(nlab, 256, 8), 256, 0, s>>>(d, 0, num_vars, (uint32_t)num_labels, mc);
     if ((st = na_read(h, d.ctr, s))) return st;
     if (h[C_ERR] & ERR_POOL) return GRG_E_NOMEM;
     const uint64_t top0 = h[C_POOL_TOP];
     if (top0) k_init_region<<<grid(top0, 256, 8), 256, 0, s>>>(d.elems, d.dbits, 0, top0);
-    if (num_edges) k_load_insert<<<grid(num_edges, 256, 8), 256, 0, s>>>(d, d_src, d_dst, d_label, num_edges);
+    if (num_edges) k_load_insert<<<grid(num_edges, 256, 8), 256, 0, s>>>(d, d_src, d_dst, d_label, num_edges, 0);
     for (int q = 0; q < num_rules; q++)
-        if (rules[3 * q + 1] == 0) k_eps_insert<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)rules[3 * q]);
+        if (rules[3 * q + 1] == 0) k_eps_insert<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)rules[3 * q], 0, num_vars);
     for (int l = 1; l <= num_labels; l++)
-        if (!derivable[l]) k_compact_static<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)l);
-    if (top0) k_mark_all<<<grid(top0, 256, 8), 256, 0, s>>>(d, top0);
+        if (!derivable[l]) k_compact_static<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)l, 0, num_vars);
+    if (top0) k_mark_all<<<grid(top0, 256, 8), 256, 0, s>>>(d, 0, top0);
     NA_CUDA(cudaGetLastError());
     if ((st = na_read(h, d.ctr, s))) return st;
     if (h[C_ERR]) return GRG_E_CUDA;
@@ -2067,7 +2326,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
         const uint64_t nd = nd32;
         if (nd == 0) break;
         rounds++;
-        k_gather<<<grid(nchunks * 32, 256, 8), 256, 0, s>>>(d, nwords, coff, rbuf[2]);
+        k_gather<<<grid(nchunks * 32, 256, 8), 256, 0, s>>>(d, nwords, coff, rbuf[2], nullptr, nullptr);
         NA_CUDA(cudaMemsetAsync(d.ctr + C_RETRY_N, 0, 16, s));
         uint64_t n = nd;
         int rb = 0;
@@ -2096,8 +2355,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     NA_CUDA(cudaMemsetAsync(d.ctr + C_LABEL0, 0, sizeof(unsigned long long) * (MAX_SLOTS + 2), s));
     NA_CUDA(cudaMemsetAsync(d.ctr + C_HASH, 0, 8, s));
     for (int l = 1; l <= num_labels; l++)
-        k_count<<<grid((uint64_t)num_vars * 32, 256, 8), 256, 0, s>>>(d, (uint32_t)l, nullptr, nullptr, 0, 0,
-                                                                     d_set_hash ? 1 : 0);
+        k_count<<<grid((uint64_t)num_vars * 32, 256, 8), 256, 0, s>>>(d, (uint32_t)l, nullptr, nullptr, 0, 0, d_set_hash ? 1 : 0, 0, num_vars, 0);
     NA_CUDA(cudaMemcpyAsync(d_label_counts, d.ctr + C_LABEL0 + 1, sizeof(uint64_t) * num_labels,
                             cudaMemcpyDeviceToDevice, s));
     if (d_set_hash) NA_CUDA(cudaMemcpyAsync(d_set_hash, d.ctr + C_HASH, 8, cudaMemcpyDeviceToDevice, s));

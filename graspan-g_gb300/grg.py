@@ -28,7 +28,8 @@ EXPORTS = (
     "grg_error_string", "grg_last_error", "grg_create", "grg_destroy", "grg_device", "grg_set_stream",
     "grg_set_kernel_timing", "grg_transfer_rules", "grg_allocate_pool", "grg_load_edges", "grg_closure",
     "grg_label_counts", "grg_get_degree", "grg_set_hash", "grg_export_edges", "grg_parse_grammar",
-    "grg_parse_graph_header", "grg_parse_graph", "grg_closure_noalloc",
+    "grg_parse_graph_header", "grg_parse_graph", "grg_closure_noalloc", "grg_batch_begin", "grg_batch_admit",
+    "grg_batch_step", "grg_batch_result", "grg_batch_release",
 )
 
 
@@ -88,6 +89,11 @@ def load_library(path: str = LIB_PATH):
     L.grg_parse_graph_header.argtypes = [ctypes.c_char_p, ctypes.POINTER(U64), ctypes.POINTER(U32)]
     L.grg_parse_graph.argtypes = [ctypes.c_char_p, I, P, U64, U32, P, P, P]
     L.grg_closure_noalloc.argtypes = [I, P, I, P, I, U32, U32, U64, P, P, P, P, P, ctypes.POINTER(U64)]
+    L.grg_batch_begin.argtypes = [P, U32, U32, I, P, I, U32]
+    L.grg_batch_admit.argtypes = [P, U32, U32, U32, U64, P, P, P, I, U64]
+    L.grg_batch_step.argtypes = [P, U32, P, ctypes.POINTER(U64)]
+    L.grg_batch_result.argtypes = [P, U32, U32, U32, P, ctypes.POINTER(U64)]
+    L.grg_batch_release.argtypes = [P, U32]
     _lib = L
     return L
 
@@ -259,3 +265,61 @@ def run_closure(num_vars, rules, num_labels, filter_flag, src, dst, lab, device=
     ctx.load_edges(num_vars, src, dst, lab)
     stats = ctx.closure(filter_flag)
     return ctx, stats
+
+
+class Batch:
+    """Many independent closures in one context (grg_batch_*).
+
+    grammars: list of (rules, labels) with rules as tuples of label names (LHS
+    first, as in grg_gen). Each grammar gets its own label range in the union
+    grammar; a job names its grammar by index and uses that grammar's label ids
+    (1-based, first-appearance order)."""
+
+    def __init__(self, ctx: Context, max_vars: int, max_jobs: int, grammars, filter_flag: int = 0):
+        self.ctx = ctx
+        self.max_jobs = max_jobs
+        self.offsets, self.sizes, self.eps = [], [], []
+        union = []
+        off = 0
+        for rules, labels in grammars:
+            ids = {n: i + 1 + off for i, n in enumerate(labels)}
+            eps = 0
+            for r in rules:
+                row = [ids[r[0]], ids[r[1]] if len(r) > 1 else 0, ids[r[2]] if len(r) > 2 else 0]
+                union.append(row)
+                if len(r) == 1:
+                    eps |= 1 << (ids[r[0]] - 1)
+            self.offsets.append(off)
+            self.sizes.append(len(labels))
+            self.eps.append(eps)
+            off += len(labels)
+        self.num_labels = off
+        r = np.ascontiguousarray(np.array(union, dtype=np.int32).reshape(-1))
+        ctx._check(ctx._L.grg_batch_begin(ctx._h, max_vars, max_jobs, len(r) // 3, _ptr(r), off, filter_flag),
+                   "batch_begin")
+        self._rec = np.zeros(max_jobs, dtype=np.uint32)
+
+    def admit(self, job: int, base: int, grammar: int, num_vars: int, src, dst, lab):
+        """Host arrays with job-local vertex ids and the grammar's label ids."""
+        src = np.ascontiguousarray(src, dtype=np.uint32)
+        dst = np.ascontiguousarray(dst, dtype=np.uint32)
+        lab = np.ascontiguousarray(np.asarray(lab, dtype=np.int64) + self.offsets[grammar], dtype=np.uint8)
+        self.ctx._check(self.ctx._L.grg_batch_admit(self.ctx._h, job, base, num_vars, len(src), _ptr(src), _ptr(dst),
+                                                    _ptr(lab), 0, self.eps[grammar]), "batch_admit")
+
+    def step(self, max_rounds: int = 1):
+        """Returns (records per job slot in the last round, rounds with work)."""
+        n = ctypes.c_uint64()
+        self.ctx._check(self.ctx._L.grg_batch_step(self.ctx._h, max_rounds, _ptr(self._rec), ctypes.byref(n)),
+                        "batch_step")
+        return self._rec.copy(), n.value
+
+    def result(self, job: int, grammar: int):
+        counts = np.zeros(self.sizes[grammar], dtype=np.uint64)
+        h = ctypes.c_uint64()
+        self.ctx._check(self.ctx._L.grg_batch_result(self.ctx._h, job, self.offsets[grammar], self.sizes[grammar],
+                                                     _ptr(counts), ctypes.byref(h)), "batch_result")
+        return counts, h.value
+
+    def release(self, job: int):
+        self.ctx._check(self.ctx._L.grg_batch_release(self.ctx._h, job), "batch_release")

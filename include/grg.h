@@ -142,6 +142,39 @@ int grg_parse_graph_header(const char *path, uint64_t *num_edges, uint32_t *num_
 int grg_parse_graph(const char *path, int num_labels, const char *names, uint64_t num_edges,
                     uint32_t num_vars, uint32_t *src, uint32_t *dst, uint8_t *label);
 
+/* ---- Batched closure of many independent graphs (continuous batching). The
+ * reference closes one graph per process; these entry points close many in
+ * one context: each job owns a vertex range [base, base+num_vars) of a
+ * context-wide vertex space, all jobs share one union grammar (callers give
+ * every grammar its own label range), and every round's kernels process the
+ * delta records of all admitted jobs together. New jobs can be admitted
+ * between steps while others are in flight. */
+
+/* Open a batch: vertex space [0, max_vars), up to max_jobs job slots, the union
+ * grammar (as grg_transfer_rules) and the filter shared by all jobs. Epsilon
+ * rules are applied per job (see eps_mask of grg_batch_admit). */
+int grg_batch_begin(grg_ctx *ctx, uint32_t max_vars, uint32_t max_jobs, int num_rules, const int *rules,
+                    int num_labels, uint32_t filter);
+/* Admit a job in slot `job`: its edges use job-local vertex ids [0, num_vars)
+ * placed at `base`, labels of the union grammar. eps_mask bit l-1 = apply the
+ * epsilon rule of label l to this job's vertices. on_device as for
+ * grg_load_edges. The range must not overlap another admitted job. */
+int grg_batch_admit(grg_ctx *ctx, uint32_t job, uint32_t base, uint32_t num_vars, uint64_t num_edges,
+                    const uint32_t *src, const uint32_t *dst, const uint8_t *label, int on_device,
+                    uint64_t eps_mask);
+/* Run up to max_rounds semi-naive rounds over all admitted jobs (0 = until no
+ * job has deltas). job_records[j] (max_jobs values, may be NULL) = delta
+ * records job j had in the last round; 0 for an admitted job means it has
+ * reached its fixpoint. *rounds_run = rounds that had work. */
+int grg_batch_step(grg_ctx *ctx, uint32_t max_rounds, uint32_t *job_records, uint64_t *rounds_run);
+/* Per-label edge counts of job `job` for the num_labels labels after
+ * label_offset (its grammar's range in the union), and the edge-set hash over
+ * job-local ids and labels (equal to grg_set_hash of the job closed alone). */
+int grg_batch_result(grg_ctx *ctx, uint32_t job, uint32_t label_offset, uint32_t num_labels, uint64_t *counts,
+                     uint64_t *hash);
+/* Free a job's vertex range for reuse; only once its last step reported 0 records. */
+int grg_batch_release(grg_ctx *ctx, uint32_t job);
+
 /* Allocation-free closure. No counterpart in the reference.
  *
  * For callers that cannot allocate device memory while they run: a serving

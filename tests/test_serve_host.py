@@ -1,0 +1,33 @@
+"""CPU tests of the serving host logic (no GPU)."""
+import numpy as np
+
+import grg_gen as G
+import serve
+
+
+def test_range_allocator_first_fit_and_merge():
+    ra = serve.RangeAllocator(100)
+    a = ra.alloc(30)
+    b = ra.alloc(30)
+    c = ra.alloc(30)
+    assert (a, b, c) == (0, 30, 60)
+    assert ra.alloc(20) is None
+    ra.release(b, 30)
+    assert ra.alloc(40) is None
+    ra.release(a, 30)
+    assert ra.free[0] == (0, 60)          # merged
+    assert ra.alloc(50) == 0
+    ra.release(0, 50)
+    ra.release(c, 30)
+    assert ra.free == [(0, 100)]
+
+
+def test_make_jobs_and_footprint():
+    specs = G.batch_mix(seed=3, jobs=6, vmin=300, vmax=2000)
+    jobs = serve.make_jobs(specs, block=250)
+    assert [j.kind for j in jobs] == ["dataflow", "alias"] * 3
+    for j in jobs:
+        assert j.src.max() < j.num_vars and j.dst.max() < j.num_vars
+        assert 3 <= len(j.src) / j.num_vars <= 10
+        assert serve.footprint_bytes(j) > 65 * 64 * j.num_vars
+    assert all(np.diff([j.arrival_s for j in jobs]) > 0)
