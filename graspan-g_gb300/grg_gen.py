@@ -97,7 +97,9 @@ def write_graph(path, w: Workload):
 
 
 def _zipf_degrees(rng, n, s, cap, total):
-    """Out-degrees ~ Zipf(s) capped at cap (min 1), trimmed/padded at random to sum to total."""
+    """Out-degrees ~ Zipf(s) capped at cap (min 1), trimmed/padded at random to
+    sum to total (at most n * cap)."""
+    total = min(int(total), int(n) * int(cap))
     deg = np.minimum(rng.zipf(s, size=n), cap).astype(np.int64)
     diff = int(total - deg.sum())
     while diff != 0:
@@ -169,6 +171,11 @@ def dataflow_blocks(seed=0x5EED0002, num_blocks=2000, block=1000, num_edges=6_00
     num_vars = num_blocks * block
     n_intra = int(round(num_edges * intra_frac))
     n_cross = num_edges - n_intra
+    # cross edges leave the exits only: at most exits x call_window x entries per block
+    max_cross = num_blocks * exits * call_window * entries
+    if n_cross > max_cross:
+        n_intra += n_cross - max_cross
+        n_cross = max_cross
     pos = np.arange(num_vars, dtype=np.int64) % block
     body = np.nonzero(pos < block - exits)[0]          # intra-block sources: all but the exits
     deg = np.zeros(num_vars, dtype=np.int64)

@@ -31,3 +31,15 @@ def test_make_jobs_and_footprint():
         assert 3 <= len(j.src) / j.num_vars <= 10
         assert serve.footprint_bytes(j) > 65 * 64 * j.num_vars
     assert all(np.diff([j.arrival_s for j in jobs]) > 0)
+
+
+def test_dense_block_graphs_generate():
+    """5 x V edges on 1000-vertex blocks ask for more cross-block edges than the
+    exits can hold; the generator moves the excess to intra-block edges."""
+    w = G.dataflow_blocks(seed=9, num_blocks=4, num_edges=20_000, seed_n=False)
+    assert 19_000 <= w.num_edges <= 20_000
+    e = w.src.astype(np.int64)
+    cross = (e // 1000) != (w.dst.astype(np.int64) // 1000)
+    assert cross.sum() <= 4 * 10 * 50
+    jobs = serve.make_jobs(G.batch_mix(seed=4, jobs=6, vmin=1000, vmax=5000))
+    assert len(jobs) == 6
