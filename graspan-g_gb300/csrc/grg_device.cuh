@@ -32,6 +32,7 @@ constexpr uint32_t BASE_MASK = (1u << KEY_SHIFT) - 1;
 constexpr int MAX_LABELS = 63;
 constexpr int MAX_SLOTS = 2 * MAX_LABELS;  // label slots 1..L, reverse-index slots L+1..2L
 constexpr int MAX_RULES = 64;
+constexpr uint32_t OL_SLOT0 = 64;          // label slots >= 64 in a delta record: old-left rule (slot - 64)
 
 // device counter block indices
 enum : int {
@@ -49,6 +50,7 @@ enum : int {
     C_PH0 = 11,       // join phase cycle counters (built with -DGRG_PHASE_TIMERS): 11..15
     C_CAND_N = 16,    // candidate elements written by joins for k_apply
     C_AFAIL = 17,     // candidates k_apply could not insert (tables to grow)
+    C_VN = 18,        // virtual old-left records written
     C_LABEL0 = 24,    // per-label edge counts: C_LABEL0 + slot
     NCTR = C_LABEL0 + MAX_SLOTS + 2
 };
@@ -56,17 +58,19 @@ enum : unsigned long long { ERR_POOL = 1, ERR_LOAD = 2, ERR_INTERNAL = 4 };
 
 struct RuleTable {
     int L;                                   // labels
-    int num_slots;                           // L + number of reverse slots in use (max index)
     // binary rules A ::= B C grouped by B
     uint8_t bin_start[MAX_LABELS + 2];
     uint8_t bin_A[MAX_RULES], bin_C[MAX_RULES];
     // unary rules A ::= B grouped by B (empty under filter 1)
     uint8_t un_start[MAX_LABELS + 2];
     uint8_t un_A[MAX_RULES];
-    // old-left joins O_B o D_C for A ::= B C grouped by C: (A, reverse slot of B)
-    uint8_t ol_start[MAX_LABELS + 2];
-    uint8_t ol_A[MAX_RULES], ol_rev[MAX_RULES];
-    uint8_t rev_slot[MAX_LABELS + 1];        // reverse-index slot of label B (0 = none)
+    // old-left joins O_B o D_C of rules A ::= B C whose C is derivable (filter 0):
+    // rule q (0..nol-1) = (ol_A[q], ol_B[q], ol_C[q]); a virtual delta record
+    // with label slot OL_SLOT0 + q carries an O_B element masked to the
+    // vertices k whose row C[k] has deltas this round
+    int nol;
+    uint8_t ol_A[MAX_RULES], ol_B[MAX_RULES], ol_C[MAX_RULES];
+    uint8_t dindex[MAX_LABELS + 1];          // label C: index this round's deltas per row
     uint8_t track[MAX_SLOTS + 2];            // slot: new bits become deltas
     // labels never inserted into after the load that are a rule's second
     // symbol also get a CSR copy (row pointers + destination ids): joins read
@@ -85,6 +89,14 @@ struct Dev {
     uint32_t *grow;           // grow list (table indices)
     uint4 *cand;              // candidate elements (32 B: bits[6], key, row) for k_apply; may be null
     uint64_t cand_cap;        // candidates
+    // this round's delta index (labels with dindex): records [drs, drs+drc) of
+    // the gathered delta buffer drec belong to table (label, row); dvm = vertex
+    // bitmap per label of rows with deltas (vwords words per label)
+    uint32_t *drs;
+    uint32_t *drc;
+    uint32_t *dvm;
+    const uint4 *drec;
+    uint32_t vwords;
     unsigned long long *ctr;  // counter block
     uint32_t V;
     uint32_t pool_cap;        // elements

@@ -2,7 +2,8 @@
 //
 // Hot path (reference: src/kernel.cu):
 //   k_join    binary joins A ::= B C for a round's delta records, delta-left
-//             (D_B o O_C) and old-left (O_B o D_C through a reverse index),
+//             (D_B o O_C) and old-left (O_B o D_C, pulled through this round's
+//             delta index: virtual records from k_oldleft),
 //             unary rules A ::= B, and dedup of every candidate against the
 //             stored rows. Replaces compute11/compute10 (src/kernel.cu:403-442)
 //             and diff/merge (src/kernel.cu:841-985).
@@ -28,6 +29,62 @@
 namespace grg {
 
 __constant__ RuleTable c_rt;
+
+// Rule table of a grammar under a filter (filter semantics: src/kernel.cu:490-494,
+// 499-503): binary rules by first symbol, unary rules (filter 0 only), old-left
+// joins for binary rules whose second symbol is derivable (filter 0; refused
+// under filter 1), tracked and delta-indexed labels.
+static int make_rule_table(const int *rules, int R, int L, uint32_t filter, RuleTable &rt, bool *derivable)
+{
+    memset(&rt, 0, sizeof rt);
+    rt.L = L;
+    for (int l = 0; l <= MAX_LABELS; l++) derivable[l] = false;
+    for (int q = 0; q < R; q++) {
+        const int *r = &rules[3 * q];
+        const bool unary = r[1] && !r[2];
+        if (!(filter && unary)) derivable[r[0]] = true;
+    }
+    int nol = 0;
+    for (int q = 0; q < R; q++) {
+        const int *r = &rules[3 * q];
+        if (r[1] && r[2] && derivable[r[2]]) {
+            if (filter) return GRG_E_FILTER;
+            rt.ol_A[nol] = (uint8_t)r[0];
+            rt.ol_B[nol] = (uint8_t)r[1];
+            rt.ol_C[nol] = (uint8_t)r[2];
+            rt.dindex[r[2]] = 1;
+            rt.track[r[2]] = 1;
+            nol++;
+        }
+    }
+    rt.nol = nol;
+    int k = 0;
+    for (int B = 1; B <= L + 1; B++) {
+        rt.bin_start[B] = (uint8_t)k;
+        if (B > L) break;
+        for (int q = 0; q < R; q++)
+            if (rules[3 * q + 1] == B && rules[3 * q + 2]) {
+                rt.bin_A[k] = (uint8_t)rules[3 * q];
+                rt.bin_C[k] = (uint8_t)rules[3 * q + 2];
+                k++;
+            }
+    }
+    k = 0;
+    for (int B = 1; B <= L + 1; B++) {
+        rt.un_start[B] = (uint8_t)k;
+        if (B > L || filter) continue;
+        for (int q = 0; q < R; q++)
+            if (rules[3 * q + 1] == B && !rules[3 * q + 2]) rt.un_A[k++] = (uint8_t)rules[3 * q];
+    }
+    // tracked labels: left operand of an active binary/unary rule, or right operand of an old-left join
+    for (int q = 0; q < R; q++) {
+        const int *r = &rules[3 * q];
+        const bool unary = r[1] && !r[2];
+        if (r[1] && !(filter && unary)) rt.track[r[1]] = 1;
+    }
+    return GRG_OK;
+}
+
 
 // Join tuning (compile-time; -DGRG_... overrides for sweeps)
 #ifndef GRG_JOIN_WARPS
@@ -294,6 +351,14 @@ __global__ void k_gather(Dev d, uint64_t nwords, const uint32_t *__restrict__ ch
                 const uint64_t pos = base_pos + t;
                 out[2 * pos] = b0;
                 out[2 * pos + 1] = make_uint4(b1.x, b1.y, e1.z, e1.w);
+                const uint32_t lab = e1.z >> KEY_SHIFT;
+                if (c_rt.dindex[lab]) {
+                    // a table's records are contiguous (slot order; growth moves dirty bits along)
+                    const size_t ti = (size_t)(lab - 1) * d.V + e1.w;
+                    atomicMin(&d.drs[ti], (uint32_t)pos);
+                    atomicAdd(&d.drc[ti], 1u);
+                    atomicOr(&d.dvm[(size_t)(lab - 1) * d.vwords + (e1.w >> 5)], 1u << (e1.w & 31));
+                }
             }
             if (row_job) {
                 // batched jobs: records per job (a job with none has reached its fixpoint)
@@ -309,6 +374,55 @@ __global__ void k_gather(Dev d, uint64_t nwords, const uint32_t *__restrict__ ch
     }
 }
 
+// Old-left join q (A ::= B C, C derivable): every element of every row of B,
+// masked to the vertices k whose row C[k] has deltas this round, becomes a
+// virtual delta record (label slot OL_SLOT0 + q). The 192 ids of an element are
+// exactly 6 words of the dirty-vertex bitmap. Records past cap are counted only.
+__global__ void k_oldleft(Dev d, uint32_t q, uint4 *out, uint64_t cap)
+{
+    const uint32_t B = c_rt.ol_B[q], C = c_rt.ol_C[q];
+    const uint32_t *dv = d.dvm + (size_t)(C - 1) * d.vwords;
+    const uint32_t vkey = (OL_SLOT0 + q) << KEY_SHIFT;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t b0 = blockIdx.x * (uint64_t)blockDim.x + (threadIdx.x & ~31u); b0 < d.V; b0 += stride) {
+        const uint64_t v = b0 + lane_id();
+        const uint64_t de = v < d.V ? d.desc[(size_t)(B - 1) * d.V + v] : 0ull;
+        const uint32_t off = (uint32_t)de, cap_v = (uint32_t)(de >> 32);
+        const uint32_t maxc = __reduce_max_sync(0xffffffffu, cap_v);
+        for (uint32_t j = 0; j < maxc; j++) {
+            Bits m;
+            uint32_t any = 0, base = 0;
+            if (j < cap_v) {
+                const uint4 *e = reinterpret_cast<const uint4 *>(d.elems + (size_t)(off + j) * 8);
+                const uint4 e0 = e[0], e1 = e[1];
+                if (e1.z != EMPTY) {
+                    base = e1.z & BASE_MASK;
+                    const uint64_t w0 = (uint64_t)base * EW;
+                    const uint32_t ew[EW] = {e0.x, e0.y, e0.z, e0.w, e1.x, e1.y};
+#pragma unroll
+                    for (int x = 0; x < EW; x++) {
+                        m.w[x] = (w0 + x < d.vwords) ? ew[x] & __ldg(dv + w0 + x) : 0u;
+                        any |= m.w[x];
+                    }
+                }
+            }
+            const unsigned em = __ballot_sync(0xffffffffu, any != 0);
+            if (!em) continue;
+            unsigned long long p0 = 0;
+            const int leader = __ffs(em) - 1;
+            if ((int)lane_id() == leader) p0 = atomicAdd(&d.ctr[C_VN], (unsigned long long)__popc(em));
+            p0 = __shfl_sync(0xffffffffu, p0, leader);
+            if (any) {
+                const uint64_t p = p0 + __popc(em & ((1u << lane_id()) - 1u));
+                if (p < cap) {
+                    out[2 * p] = make_uint4(m.w[0], m.w[1], m.w[2], m.w[3]);
+                    out[2 * p + 1] = make_uint4(m.w[4], m.w[5], vkey | base, (uint32_t)v);
+                }
+            }
+        }
+    }
+}
+
 struct __align__(16) WarpSmem {
     uint32_t win[RB][WIN][EW];    // dense window accumulator per record
     uint32_t acc_bits[ACC][EW];   // hash accumulator: OR of candidate bitmaps
@@ -317,8 +431,8 @@ struct __align__(16) WarpSmem {
     uint32_t rrow[RB];
     uint32_t rbase[RB];
     uint32_t rA[RB];              // per record: output label of the current rule pass
-    uint32_t rC[RB];              // per record: right operand label / reverse slot
-    uint32_t rOff[RB];            // per record: row offset (old-left pass)
+    uint32_t rC[RB];              // per record: right operand label
+    uint32_t rOff[RB];            // per record: 1 = virtual old-left record
     uint32_t kpre[RB + 1];        // exclusive prefix of per-record task counts
     uint32_t acc_n;
     uint32_t fail;                // records with a failed insert (retry after growth)
@@ -580,7 +694,8 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, GRG_JOIN_MINB) k_join(Dev d, 
 
         PH_MARK(0);
         // unary rules A ::= B (compute10): the delta itself joins row (A, row)
-        const uint32_t nu = have ? c_rt.un_start[B + 1] - c_rt.un_start[B] : 0;
+        const bool virt = have && B >= OL_SLOT0;      // virtual record of an old-left join
+        const uint32_t nu = have && !virt ? c_rt.un_start[B + 1] - c_rt.un_start[B] : 0;
         const uint32_t maxu = __reduce_max_sync(0xffffffffu, nu);
         for (uint32_t u = 0; u < maxu; u++) {
             if (u < nu) {
@@ -590,47 +705,38 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, GRG_JOIN_MINB) k_join(Dev d, 
             }
         }
 
-        // reverse index of B (needed by old-left joins): rev_B[k] gets row
-        {
-            const uint32_t rs = have ? c_rt.rev_slot[B] : 0;
-            w.rC[lane] = rs;
-            const uint32_t total = warp_tasks(w, rs ? nbits : 0);
-            for (uint32_t t0 = 0; t0 < total; t0 += 32) {
-                const uint32_t t = t0 + lane;
-                if (t < total) {
-                    const uint32_t r = task_record(w, t);
-                    const uint32_t k = w.rbase[r] * EIDS + select_bit(w.rbits[r], t - w.kpre[r]);
-                    const uint32_t rr = w.rrow[r], o = rr % EIDS;
-                    Bits ib;
-#pragma unroll
-                    for (int x = 0; x < EW; x++) ib.w[x] = (uint32_t)x == (o >> 5) ? 1u << (o & 31) : 0u;
-                    if (!g_insert(d, w.rC[r], k, rr / EIDS, ib, false)) atomicOr(&w.fail, 1u << r);
-                    inserts++;
-                }
-            }
-        }
-
         PH_MARK(1);
-        // binary rules A ::= B C, delta-left: union of rows C[k] into row (A, row)
-        const uint32_t nbr = have ? c_rt.bin_start[B + 1] - c_rt.bin_start[B] : 0;
+        // binary rules A ::= B C: union of rows C[k] into row (A, row). Delta-left
+        // (D_B o O_C): right rows from the tables (or their CSR copy). Old-left
+        // (O_B o D_C, virtual record of rule q): right rows are this round's delta
+        // records of C[k], found through the delta index.
+        const uint32_t qv = virt ? B - OL_SLOT0 : 0;
+        const uint32_t nbr = !have ? 0 : virt ? 1 : c_rt.bin_start[B + 1] - c_rt.bin_start[B];
         const uint32_t maxb = __reduce_max_sync(0xffffffffu, nbr);
+        w.rOff[lane] = virt;
         for (uint32_t rho = 0; rho < maxb; rho++) {
             const bool hr = rho < nbr;
-            const uint32_t q = c_rt.bin_start[B] + rho;
-            w.rA[lane] = hr ? c_rt.bin_A[q] : 0;
-            w.rC[lane] = hr ? c_rt.bin_C[q] : 0;
+            const uint32_t q = virt ? qv : c_rt.bin_start[B] + rho;
+            w.rA[lane] = !hr ? 0 : virt ? c_rt.ol_A[q] : c_rt.bin_A[q];
+            w.rC[lane] = !hr ? 0 : virt ? c_rt.ol_C[q] : c_rt.bin_C[q];
             n_left += hr;
             const uint32_t total = warp_tasks(w, hr ? nbits : 0);
             for (uint32_t t0 = 0; t0 < total; t0 += 32) {
                 // task (record r, intermediate k) -> items of row C[k]
                 const uint32_t t = t0 + lane;
-                uint32_t r = 0, C = 0, beg = 0, cnt = 0, csr = 0;
+                uint32_t r = 0, C = 0, beg = 0, cnt = 0, csr = 0;   // csr: item source 0 table, 1 CSR, 2 delta records
                 if (t < total) {
                     r = task_record(w, t);
                     C = w.rC[r];
                     const uint32_t k = w.rbase[r] * EIDS + select_bit(w.rbits[r], t - w.kpre[r]);
                     const uint2 *cr = c_rt.csr_row[C];
-                    if (cr) {
+                    if (w.rOff[r]) {
+                        const size_t ti = (size_t)(C - 1) * d.V + k;
+                        const uint32_t s0 = __ldg(d.drs + ti);
+                        csr = 2;
+                        beg = s0;
+                        cnt = s0 == EMPTY ? 0 : __ldg(d.drc + ti);
+                    } else if (cr) {
                         const uint2 rw = __ldg(cr + k);
                         csr = 1;
                         beg = rw.x;
@@ -677,7 +783,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, GRG_JOIN_MINB) k_join(Dev d, 
                         for (int x = 0; x < EW; x++) it_b[u].w[x] = 0;
                         if (f < nitems) {
                             const uint32_t item = o_beg + (f - (o_incl - o_cnt));
-                            if (o_csr) {
+                            if (o_csr == 1) {
                                 const uint32_t dst = __ldg(c_rt.csr_col[o_C] + item);
                                 it_b2[u] = dst / EIDS;
                                 const uint32_t ob = dst % EIDS;
@@ -685,7 +791,8 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, GRG_JOIN_MINB) k_join(Dev d, 
                                 for (int x = 0; x < EW; x++) it_b[u].w[x] = (uint32_t)x == (ob >> 5) ? 1u << (ob & 31) : 0u;
                                 it_ok[u] = true;
                             } else {
-                                const uint4 *ep = reinterpret_cast<const uint4 *>(d.elems + (size_t)item * 8);
+                                const uint4 *ep = o_csr == 2 ? d.drec + 2 * (size_t)item
+                                                             : reinterpret_cast<const uint4 *>(d.elems + (size_t)item * 8);
                                 const uint4 e0 = ep[0], e1 = ep[1];
                                 it_ok[u] = e1.z != EMPTY;
                                 it_b2[u] = e1.z & BASE_MASK;
@@ -722,50 +829,6 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, GRG_JOIN_MINB) k_join(Dev d, 
             win_flush(d, w, inserts);
             acc_flush(d, w, inserts);
             PH_MARK(3);
-        }
-
-        // old-left joins A ::= Bp B (record = delta of B at vertex `row`):
-        // every h with Bp(h, row) gets the record's bits in row (A, h)
-        const uint32_t no = have ? c_rt.ol_start[B + 1] - c_rt.ol_start[B] : 0;
-        const uint32_t maxo = __reduce_max_sync(0xffffffffu, no);
-        for (uint32_t sg = 0; sg < maxo; sg++) {
-            const bool hs = sg < no;
-            const uint32_t q = c_rt.ol_start[B] + sg;
-            uint32_t cap = 0;
-            if (hs) {
-                const uint64_t de = d.desc[(size_t)(c_rt.ol_rev[q] - 1) * d.V + row];
-                w.rOff[lane] = (uint32_t)de;
-                cap = (uint32_t)(de >> 32);
-            }
-            w.rA[lane] = hs ? c_rt.ol_A[q] : 0;
-            const uint32_t total = warp_tasks(w, cap);
-            for (uint32_t t0 = 0; t0 < total; t0 += 32) {
-                const uint32_t t = t0 + lane;
-                if (t >= total) continue;
-                const uint32_t r = task_record(w, t);
-                const uint4 *ep = reinterpret_cast<const uint4 *>(d.elems + (size_t)(w.rOff[r] + (t - w.kpre[r])) * 8);
-                const uint4 e0 = ep[0], e1 = ep[1];
-                if (e1.z == EMPTY) continue;
-                const uint32_t hb = e1.z & BASE_MASK, A = w.rA[r];
-                const bool trk = c_rt.track[A];
-                Bits xb;
-#pragma unroll
-                for (int x = 0; x < EW; x++) xb.w[x] = w.rbits[r][x];
-                const uint32_t xbase = w.rbase[r];
-                bool okr = true;
-#pragma unroll
-                for (int x = 0; x < EW; x++) {
-                    uint32_t bw = x == 0 ? e0.x : x == 1 ? e0.y : x == 2 ? e0.z : x == 3 ? e0.w : x == 4 ? e1.x : e1.y;
-                    while (bw) {
-                        const int bit = __ffs(bw) - 1;
-                        bw &= bw - 1;
-                        okr &= g_insert(d, A, hb * EIDS + x * 32 + bit, xbase, xb, trk);
-                        inserts++;
-                    }
-                }
-                if (!okr) atomicOr(&w.fail, 1u << r);
-            }
-            __syncwarp();
         }
 
         __syncwarp();
@@ -965,6 +1028,18 @@ __global__ void k_grow(Dev d, uint64_t n)
                     t2[0] = e0;
                     d.elems[q * 8 + 4] = e1.x;
                     d.elems[q * 8 + 5] = e1.y;
+                    // pending delta bits move along, so a table's delta records stay contiguous
+                    const uint64_t os = (uint64_t)off + t;
+                    if ((d.dmap[os >> 5] >> (os & 31)) & 1u) {
+                        uint4 *ob = reinterpret_cast<uint4 *>(d.dbits + os * 8);
+                        uint4 *nbp = reinterpret_cast<uint4 *>(d.dbits + q * 8);
+                        nbp[0] = ob[0];
+                        nbp[1] = ob[1];
+                        ob[0] = make_uint4(0, 0, 0, 0);
+                        ob[1] = make_uint4(0, 0, 0, 0);
+                        atomicAnd(&d.dmap[os >> 5], ~(1u << (os & 31)));
+                        atomicOr(&d.dmap[q >> 5], 1u << (q & 31));
+                    }
                     break;
                 }
             }
@@ -1076,7 +1151,7 @@ struct grg_ctx {
     bool closed = false;
     uint32_t V = 0;
     uint64_t ntables = 0;          // L * V (label slots 1..L)
-    uint64_t ntables_alloc = 0;    // 2L * V (with reverse slots)
+    uint64_t ntables_alloc = 0;    // L * V
     // device memory
     uint64_t pool_bytes_req = 0;
     uint64_t pool_cap = 0;         // elements
@@ -1087,8 +1162,13 @@ struct grg_ctx {
     uint64_t chunk_cap = 0;
     uint64_t *desc = nullptr;
     uint32_t *cnt = nullptr, *want = nullptr, *grow = nullptr;
-    uint4 *rbuf[3] = {nullptr, nullptr, nullptr};   // [2]: gathered deltas; [0],[1]: retry passes
+    uint4 *rbuf[2] = {nullptr, nullptr};       // delta records of retry passes
     uint64_t rbuf_cap = 0;                     // records
+    uint4 *gbuf = nullptr;                     // gathered delta records of the round
+    uint64_t gbuf_cap = 0;
+    uint4 *vbuf = nullptr;                     // virtual records of old-left joins
+    uint64_t vbuf_cap = 0;
+    uint32_t *drs = nullptr, *drc = nullptr, *dvm = nullptr;   // delta index (per label x row / vertex bitmap)
     uint4 *cand[2] = {nullptr, nullptr};       // join candidates for k_apply / failed candidates
     uint64_t cand_cap = 0;
     int cb = 0;                                // candidate buffer the joins write
@@ -1162,6 +1242,11 @@ Dev make_dev(const grg_ctx *c)
     d.want = c->want;
     d.cand = c->cand[c->cb];
     d.cand_cap = c->cand_cap;
+    d.drs = c->drs;
+    d.drc = c->drc;
+    d.dvm = c->dvm;
+    d.drec = c->gbuf;
+    d.vwords = (c->V + 31) / 32;
     d.grow = c->grow;
     d.ctr = c->ctr;
     d.V = c->V;
@@ -1178,6 +1263,9 @@ void free_csr(grg_ctx *c)
 void free_graph(grg_ctx *c)
 {
     free_csr(c);
+    cudaFree(c->drs); c->drs = nullptr;
+    cudaFree(c->drc); c->drc = nullptr;
+    cudaFree(c->dvm); c->dvm = nullptr;
     cudaFree(c->row_job); c->row_job = nullptr;
     cudaFree(c->job_cnt); c->job_cnt = nullptr;
     c->max_jobs = 0;
@@ -1284,81 +1372,53 @@ int ensure_cand(grg_ctx *c, uint64_t nd)
     return GRG_OK;
 }
 
+// Grow a record buffer (32 B per record) to hold n records (contents not kept).
+int ensure_buf(grg_ctx *c, uint4 **buf, uint64_t *cap, uint64_t n)
+{
+    if (n <= *cap) return GRG_OK;
+    const uint64_t nc = std::max<uint64_t>(n + n / 2, 1 << 16);
+    cudaFree(*buf);
+    *buf = nullptr;
+    *cap = 0;
+    GRG_CUDA(c, cudaMalloc(buf, nc * 32));
+    *cap = nc;
+    return GRG_OK;
+}
+
 // Retry buffers: every delta record of a pass may fail once, so n records each.
 int ensure_rbuf(grg_ctx *c, uint64_t n)
 {
     if (n <= c->rbuf_cap) return GRG_OK;
     const uint64_t cap = std::max<uint64_t>(n + n / 2, 1 << 16);
-    for (int i = 0; i < 3; i++) {
+    for (int i = 0; i < 2; i++) {
         cudaFree(c->rbuf[i]);
         c->rbuf[i] = nullptr;
     }
-    for (int i = 0; i < 3; i++) GRG_CUDA(c, cudaMalloc(&c->rbuf[i], cap * 32));
+    c->rbuf_cap = 0;
+    for (int i = 0; i < 2; i++) GRG_CUDA(c, cudaMalloc(&c->rbuf[i], cap * 32));
     c->rbuf_cap = cap;
     return GRG_OK;
 }
 
-// Build the rule table for a filter (filter semantics: src/kernel.cu:490-494, 499-503 ...).
+// Delta index of the labels old-left joins read: table start/count and vertex bitmap.
+int alloc_dindex(grg_ctx *c)
+{
+    const uint64_t nt = (uint64_t)c->L * c->V, vw = (uint64_t)c->L * ((c->V + 31) / 32);
+    GRG_CUDA(c, cudaMalloc(&c->drs, std::max<uint64_t>(nt, 1) * 4));
+    GRG_CUDA(c, cudaMalloc(&c->drc, std::max<uint64_t>(nt, 1) * 4));
+    GRG_CUDA(c, cudaMalloc(&c->dvm, std::max<uint64_t>(vw, 1) * 4));
+    GRG_CUDA(c, cudaMemsetAsync(c->drs, 0xFF, std::max<uint64_t>(nt, 1) * 4, c->stream));
+    GRG_CUDA(c, cudaMemsetAsync(c->drc, 0, std::max<uint64_t>(nt, 1) * 4, c->stream));
+    GRG_CUDA(c, cudaMemsetAsync(c->dvm, 0, std::max<uint64_t>(vw, 1) * 4, c->stream));
+    return GRG_OK;
+}
+
+// Rule table of the context's grammar for a filter.
 int build_rules(grg_ctx *c, uint32_t filter, RuleTable &rt)
 {
-    memset(&rt, 0, sizeof rt);
-    const int L = c->L;
-    rt.L = L;
-    bool derivable[MAX_LABELS + 1] = {false};
-    for (int q = 0; q < c->R; q++) {
-        const int *r = &c->rules[3 * q];
-        bool unary = r[1] && !r[2];
-        if (!(filter && unary)) derivable[r[0]] = true;
-    }
-    bool need_ol[GRG_MAX_RULES] = {false};
-    for (int q = 0; q < c->R; q++) {
-        const int *r = &c->rules[3 * q];
-        if (r[1] && r[2] && derivable[r[2]]) {
-            if (filter) return fail(c, GRG_E_FILTER, status_text(GRG_E_FILTER));
-            need_ol[q] = true;
-        }
-    }
-    int next_rev = L + 1;
-    for (int q = 0; q < c->R; q++)
-        if (need_ol[q] && !rt.rev_slot[c->rules[3 * q + 1]]) rt.rev_slot[c->rules[3 * q + 1]] = (uint8_t)next_rev++;
-    rt.num_slots = next_rev - 1;
-    // binary rules grouped by RHS1
-    int k = 0;
-    for (int B = 1; B <= L + 1; B++) {
-        rt.bin_start[B] = (uint8_t)k;
-        if (B > L) break;
-        for (int q = 0; q < c->R; q++) {
-            const int *r = &c->rules[3 * q];
-            if (r[1] == B && r[2]) { rt.bin_A[k] = (uint8_t)r[0]; rt.bin_C[k] = (uint8_t)r[2]; k++; }
-        }
-    }
-    rt.bin_start[0] = 0;
-    k = 0;
-    for (int B = 1; B <= L + 1; B++) {
-        rt.un_start[B] = (uint8_t)k;
-        if (B > L) break;
-        if (filter) continue;
-        for (int q = 0; q < c->R; q++) {
-            const int *r = &c->rules[3 * q];
-            if (r[1] == B && !r[2]) rt.un_A[k++] = (uint8_t)r[0];
-        }
-    }
-    k = 0;
-    for (int C = 1; C <= L + 1; C++) {
-        rt.ol_start[C] = (uint8_t)k;
-        if (C > L) break;
-        for (int q = 0; q < c->R; q++) {
-            const int *r = &c->rules[3 * q];
-            if (need_ol[q] && r[2] == C) { rt.ol_A[k] = (uint8_t)r[0]; rt.ol_rev[k] = rt.rev_slot[r[1]]; k++; }
-        }
-    }
-    // tracked labels: left operand of an active binary/unary rule, or right operand of an old-left join
-    for (int q = 0; q < c->R; q++) {
-        const int *r = &c->rules[3 * q];
-        bool unary = r[1] && !r[2];
-        if (r[1] && !(filter && unary)) rt.track[r[1]] = 1;
-        if (need_ol[q]) rt.track[r[2]] = 1;
-    }
+    bool derivable[MAX_LABELS + 1];
+    const int st = make_rule_table(c->rules, c->R, c->L, filter, rt, derivable);
+    if (st) return fail(c, st, status_text(st));
     return GRG_OK;
 }
 
@@ -1408,7 +1468,9 @@ void grg_destroy(grg_ctx *c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_graph(c);
     free_pool(c);
-    for (int i = 0; i < 3; i++) cudaFree(c->rbuf[i]);
+    for (int i = 0; i < 2; i++) cudaFree(c->rbuf[i]);
+    cudaFree(c->gbuf);
+    cudaFree(c->vbuf);
     cudaFree(c->cand[0]);
     cudaFree(c->cand[1]);
     cudaFree(c->chunk);
@@ -1489,11 +1551,11 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
         int st = grg_allocate_pool(c, c->pool_bytes_req);
         if (st) return st;
     }
-    if ((uint64_t)num_vars * (uint64_t)(2 * c->L) >= 0xFFFFFFFFull)
+    if ((uint64_t)num_vars * (uint64_t)c->L >= 0xFFFFFFFFull)
         return fail(c, GRG_E_RANGE, "numVars x 2 x numLabels must stay below 2^32");
     c->V = num_vars;
     c->ntables = (uint64_t)c->L * num_vars;
-    const uint64_t nt_all = (uint64_t)(2 * c->L) * num_vars;
+    const uint64_t nt_all = (uint64_t)c->L * num_vars;
     if (c->ntables_alloc != nt_all || c->batch) {
         free_graph(c);
         GRG_CUDA(c, cudaMalloc(&c->desc, std::max<uint64_t>(nt_all, 1) * 8));
@@ -1501,6 +1563,8 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
         GRG_CUDA(c, cudaMalloc(&c->want, std::max<uint64_t>(nt_all, 1) * 4));
         GRG_CUDA(c, cudaMalloc(&c->grow, std::max<uint64_t>(nt_all, 1) * 4));
         c->ntables_alloc = nt_all;
+        int st0 = alloc_dindex(c);
+        if (st0) return st0;
     }
     cudaStream_t s = c->stream;
     GRG_CUDA(c, cudaMemsetAsync(c->desc, 0, nt_all * 8, s));
@@ -1630,7 +1694,7 @@ static int run_rounds(grg_ctx *c, uint64_t max_rounds, grg_stats &S, double &joi
             break;
         }
         done_rounds++;
-        st = ensure_rbuf(c, nd);
+        st = ensure_buf(c, &c->gbuf, &c->gbuf_cap, nd);
         if (st) return st;
         st = ensure_cand(c, nd);
         if (st) return st;
@@ -1638,19 +1702,54 @@ static int run_rounds(grg_ctx *c, uint64_t max_rounds, grg_stats &S, double &joi
         S.delta_elems += nd;
         c->cb = 0;
         d = make_dev(c);
-        k_gather<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->rbuf[2], c->row_job, c->job_cnt);
+        // the delta index of the last round is cleared for the labels old-left joins read
+        for (int l = 1; l <= c->L; l++)
+            if (c->rt.dindex[l]) {
+                const size_t t0 = (size_t)(l - 1) * c->V, vw = (c->V + 31) / 32;
+                GRG_CUDA(c, cudaMemsetAsync(c->drs + t0, 0xFF, (size_t)c->V * 4, s));
+                GRG_CUDA(c, cudaMemsetAsync(c->drc + t0, 0, (size_t)c->V * 4, s));
+                GRG_CUDA(c, cudaMemsetAsync(c->dvm + (size_t)(l - 1) * vw, 0, vw * 4, s));
+            }
+        k_gather<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->gbuf, c->row_job, c->job_cnt);
         c->launches++;
+        // old-left joins: virtual records of O_B masked to the vertices with deltas of C
+        uint64_t nv = 0;
+        if (c->rt.nol) {
+            for (int attempt = 0; attempt < 2; attempt++) {
+                GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_VN, 0, 8, s));
+                for (int q = 0; q < c->rt.nol; q++) {
+                    k_oldleft<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)q, c->vbuf, c->vbuf_cap);
+                    c->launches++;
+                }
+                st = read_ctr(c);
+                if (st) return st;
+                nv = c->h_ctr[C_VN];
+                if (nv <= c->vbuf_cap) break;
+                st = ensure_buf(c, &c->vbuf, &c->vbuf_cap, nv);
+                if (st) return st;
+            }
+        }
+        st = ensure_rbuf(c, nd + nv);
+        if (st) return st;
         uint64_t n = nd;       // delta records for the next join pass (0 = none)
         int rb = 0;
         bool first = true;
         for (int pass = 0;; pass++) {
             if (c->timing) GRG_CUDA(c, cudaEventRecord(c->ev_c, s));
-            if (n) {
+            if (first) {
+                k_join<<<grid_for(c, (nd + RB - 1) / RB, JOIN_WARPS, 16), JOIN_WARPS * 32, 0, s>>>(d, c->gbuf, nd,
+                                                                                                 c->rbuf[0]);
+                c->launches++;
+                joins++;
+                if (nv) {
+                    k_join<<<grid_for(c, (nv + RB - 1) / RB, JOIN_WARPS, 16), JOIN_WARPS * 32, 0, s>>>(d, c->vbuf, nv,
+                                                                                                     c->rbuf[0]);
+                    c->launches++;
+                    joins++;
+                }
+            } else if (n) {
                 const int jgrid = grid_for(c, (n + RB - 1) / RB, JOIN_WARPS, 16);
-                if (first)
-                    k_join<<<jgrid, JOIN_WARPS * 32, 0, s>>>(d, c->rbuf[2], n, c->rbuf[0]);
-                else
-                    k_join<<<jgrid, JOIN_WARPS * 32, 0, s>>>(d, c->rbuf[rb], n, c->rbuf[rb ^ 1]);
+                k_join<<<jgrid, JOIN_WARPS * 32, 0, s>>>(d, c->rbuf[rb], n, c->rbuf[rb ^ 1]);
                 c->launches++;
                 joins++;
             }
@@ -1668,8 +1767,9 @@ static int run_rounds(grg_ctx *c, uint64_t max_rounds, grg_stats &S, double &joi
                 cudaEventElapsedTime(&ms, c->ev_c, c->ev_d);
                 join_ms += ms;
             }
-            const uint64_t nr = n ? c->h_ctr[C_RETRY_N] : 0;
+            const uint64_t nr = (first || n) ? c->h_ctr[C_RETRY_N] : 0;
             if (!first && n) rb ^= 1;       // the failed records of this pass are in rbuf[rb]
+            if (first) n = nd;
             first = false;
             const uint64_t nf = c->cand_cap ? c->h_ctr[C_AFAIL] : 0;
             if (nr == 0 && nf == 0) break;
@@ -1909,18 +2009,20 @@ int grg_batch_begin(grg_ctx *c, uint32_t max_vars, uint32_t max_jobs, int num_ru
         st = grg_allocate_pool(c, c->pool_bytes_req);
         if (st) return st;
     }
-    if ((uint64_t)max_vars * (uint64_t)(2 * c->L) >= 0xFFFFFFFFull)
+    if ((uint64_t)max_vars * (uint64_t)c->L >= 0xFFFFFFFFull)
         return fail(c, GRG_E_RANGE, "max_vars x 2 x numLabels must stay below 2^32");
     free_graph(c);
     cudaStream_t s = c->stream;
     c->V = max_vars;
     c->ntables = (uint64_t)c->L * max_vars;
-    const uint64_t nt_all = (uint64_t)(2 * c->L) * max_vars;
+    const uint64_t nt_all = (uint64_t)c->L * max_vars;
     GRG_CUDA(c, cudaMalloc(&c->desc, nt_all * 8));
     GRG_CUDA(c, cudaMalloc(&c->cnt, nt_all * 4));
     GRG_CUDA(c, cudaMalloc(&c->want, nt_all * 4));
     GRG_CUDA(c, cudaMalloc(&c->grow, nt_all * 4));
     c->ntables_alloc = nt_all;
+    st = alloc_dindex(c);
+    if (st) return st;
     GRG_CUDA(c, cudaMalloc(&c->row_job, (uint64_t)max_vars * 4));
     GRG_CUDA(c, cudaMalloc(&c->job_cnt, (uint64_t)max_jobs * 4));
     c->max_jobs = max_jobs;
@@ -2079,7 +2181,7 @@ int grg_batch_release(grg_ctx *c, uint32_t job)
     cudaSetDevice(c->device);
     cudaStream_t s = c->stream;
     const uint32_t base = c->jobs[job].base, nv = c->jobs[job].nv;
-    for (int slot = 1; slot <= 2 * c->L; slot++) {
+    for (int slot = 1; slot <= c->L; slot++) {
         const size_t t0 = (size_t)(slot - 1) * c->V + base;
         GRG_CUDA(c, cudaMemsetAsync(c->desc + t0, 0, (size_t)nv * 8, s));
         GRG_CUDA(c, cudaMemsetAsync(c->cnt + t0, 0, (size_t)nv * 4, s));
@@ -2115,67 +2217,6 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH
 static void *g_noalloc_addr[256];
 
 static inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
-
-// Rule table for the allocation-free path (same rules as build_rules, without a context).
-static int noalloc_rules(const int *rules, int R, int L, uint32_t filter, RuleTable &rt, bool *derivable)
-{
-    memset(&rt, 0, sizeof rt);
-    rt.L = L;
-    for (int l = 0; l <= MAX_LABELS; l++) derivable[l] = false;
-    for (int q = 0; q < R; q++) {
-        const int *r = &rules[3 * q];
-        const bool unary = r[1] && !r[2];
-        if (!(filter && unary)) derivable[r[0]] = true;
-    }
-    bool need_ol[GRG_MAX_RULES] = {false};
-    for (int q = 0; q < R; q++) {
-        const int *r = &rules[3 * q];
-        if (r[1] && r[2] && derivable[r[2]]) {
-            if (filter) return GRG_E_FILTER;
-            need_ol[q] = true;
-        }
-    }
-    int next_rev = L + 1;
-    for (int q = 0; q < R; q++)
-        if (need_ol[q] && !rt.rev_slot[rules[3 * q + 1]]) rt.rev_slot[rules[3 * q + 1]] = (uint8_t)next_rev++;
-    rt.num_slots = next_rev - 1;
-    int k = 0;
-    for (int B = 1; B <= L + 1; B++) {
-        rt.bin_start[B] = (uint8_t)k;
-        if (B > L) break;
-        for (int q = 0; q < R; q++)
-            if (rules[3 * q + 1] == B && rules[3 * q + 2]) {
-                rt.bin_A[k] = (uint8_t)rules[3 * q];
-                rt.bin_C[k] = (uint8_t)rules[3 * q + 2];
-                k++;
-            }
-    }
-    k = 0;
-    for (int B = 1; B <= L + 1; B++) {
-        rt.un_start[B] = (uint8_t)k;
-        if (B > L || filter) continue;
-        for (int q = 0; q < R; q++)
-            if (rules[3 * q + 1] == B && !rules[3 * q + 2]) rt.un_A[k++] = (uint8_t)rules[3 * q];
-    }
-    k = 0;
-    for (int C = 1; C <= L + 1; C++) {
-        rt.ol_start[C] = (uint8_t)k;
-        if (C > L) break;
-        for (int q = 0; q < R; q++)
-            if (need_ol[q] && rules[3 * q + 2] == C) {
-                rt.ol_A[k] = (uint8_t)rules[3 * q];
-                rt.ol_rev[k] = rt.rev_slot[rules[3 * q + 1]];
-                k++;
-            }
-    }
-    for (int q = 0; q < R; q++) {
-        const int *r = &rules[3 * q];
-        const bool unary = r[1] && !r[2];
-        if (r[1] && !(filter && unary)) rt.track[r[1]] = 1;
-        if (need_ol[q]) rt.track[r[2]] = 1;
-    }
-    return GRG_OK;
-}
 
 }  // namespace grg
 
@@ -2218,31 +2259,37 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
             (r[1] == 0 && r[2] != 0))
             return GRG_E_ARG;
     }
-    // scratch layout: counters | descriptors | cnt | want | grow | pool arrays (161 B per element:
-    // element, delta bitmap, dirty bit, three delta-record buffers) | gather chunk counters
-    const uint64_t ntab = (uint64_t)(2 * num_labels) * num_vars;
+    // scratch layout: counters | descriptors | cnt | want | grow | delta index | pool arrays
+    // (194 B per element slot: element, delta bitmap, dirty bit, four delta-record buffers) |
+    // gather chunk counters. A round has at most one delta record per slot, old-left virtual
+    // records at most one per (old-left rule, element), retries at most one per record.
+    const uint64_t ntab = (uint64_t)num_labels * num_vars, vwords = (num_vars + 31) / 32;
     size_t off = 0;
     const size_t o_ctr = off; off = align256(off + sizeof(unsigned long long) * NCTR);
     const size_t o_desc = off; off = align256(off + ntab * 8);
     const size_t o_cnt = off; off = align256(off + ntab * 4);
     const size_t o_want = off; off = align256(off + ntab * 4);
     const size_t o_grow = off; off = align256(off + ntab * 4);
+    const size_t o_drs = off; off = align256(off + ntab * 4);
+    const size_t o_drc = off; off = align256(off + ntab * 4);
+    const size_t o_dvm = off; off = align256(off + (uint64_t)num_labels * vwords * 4);
     if (off >= NOALLOC_SCRATCH_BYTES) return GRG_E_RANGE;            // tables alone exceed the scratch
-    uint64_t pool = (NOALLOC_SCRATCH_BYTES - off - 16 * 256) / 162;
+    uint64_t pool = (NOALLOC_SCRATCH_BYTES - off - 16 * 256) / 194;
     if (pool < 4096 || num_edges > pool / 2) return GRG_E_RANGE;    // graph too large for the scratch
     const uint64_t pwords = pool / 32 + 2, pchunks = (pwords + 31) / 32, pnb = (pchunks + 1023) / 1024;
     const size_t o_elems = off; off = align256(off + pool * 32);
     const size_t o_dbits = off; off = align256(off + pool * 32);
     const size_t o_dmap = off; off = align256(off + pwords * 4);
+    const size_t o_gbuf = off; off = align256(off + pool * 32);
+    const size_t o_vbuf = off; off = align256(off + pool * 32);
     const size_t o_rbuf0 = off; off = align256(off + pool * 32);
     const size_t o_rbuf1 = off; off = align256(off + pool * 32);
-    const size_t o_rbuf2 = off; off = align256(off + pool * 32);
     const size_t o_chunk = off; off = align256(off + (2 * (pchunks + 1) + pnb + 2) * 4);
     if (off > NOALLOC_SCRATCH_BYTES) return GRG_E_RANGE;
 
     RuleTable rt;
     bool derivable[MAX_LABELS + 1];
-    int st = noalloc_rules(rules, num_rules, num_labels, filter, rt, derivable);
+    int st = make_rule_table(rules, num_rules, num_labels, filter, rt, derivable);
     if (st) return st;
 
     DeviceGuard guard;
@@ -2275,7 +2322,13 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     d.pool_cap = (uint32_t)pool;
     d.cand = nullptr;          // no candidate buffer: joins insert directly
     d.cand_cap = 0;
-    uint4 *rbuf[3] = {(uint4 *)(base + o_rbuf0), (uint4 *)(base + o_rbuf1), (uint4 *)(base + o_rbuf2)};
+    d.drs = (uint32_t *)(base + o_drs);
+    d.drc = (uint32_t *)(base + o_drc);
+    d.dvm = (uint32_t *)(base + o_dvm);
+    d.vwords = (uint32_t)vwords;
+    uint4 *gbuf = (uint4 *)(base + o_gbuf), *vbuf = (uint4 *)(base + o_vbuf);
+    d.drec = gbuf;
+    uint4 *rbuf[2] = {(uint4 *)(base + o_rbuf0), (uint4 *)(base + o_rbuf1)};
     uint32_t *chunk = (uint32_t *)(base + o_chunk);
     unsigned long long h[NCTR];
 
@@ -2285,6 +2338,9 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     NA_CUDA(cudaMemsetAsync(d.cnt, 0, ntab * 4, s));
     NA_CUDA(cudaMemsetAsync(d.want, 0, ntab * 4, s));
     NA_CUDA(cudaMemsetAsync(d.dmap, 0, pwords * 4, s));
+    NA_CUDA(cudaMemsetAsync(d.drs, 0xFF, ntab * 4, s));
+    NA_CUDA(cudaMemsetAsync(d.drc, 0, ntab * 4, s));
+    NA_CUDA(cudaMemsetAsync(d.dvm, 0, (uint64_t)num_labels * vwords * 4, s));
     NA_CUDA(cudaMemcpyToSymbolAsync(c_rt, &rt, sizeof rt, 0, cudaMemcpyHostToDevice, s));
 
     // load (grg_load_edges)
@@ -2326,16 +2382,33 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
         const uint64_t nd = nd32;
         if (nd == 0) break;
         rounds++;
-        k_gather<<<grid(nchunks * 32, 256, 8), 256, 0, s>>>(d, nwords, coff, rbuf[2], nullptr, nullptr);
+        for (int l = 1; l <= num_labels; l++)
+            if (rt.dindex[l]) {
+                NA_CUDA(cudaMemsetAsync(d.drs + (size_t)(l - 1) * num_vars, 0xFF, (size_t)num_vars * 4, s));
+                NA_CUDA(cudaMemsetAsync(d.drc + (size_t)(l - 1) * num_vars, 0, (size_t)num_vars * 4, s));
+                NA_CUDA(cudaMemsetAsync(d.dvm + (size_t)(l - 1) * vwords, 0, vwords * 4, s));
+            }
+        k_gather<<<grid(nchunks * 32, 256, 8), 256, 0, s>>>(d, nwords, coff, gbuf, nullptr, nullptr);
+        uint64_t nv = 0;
+        if (rt.nol) {
+            NA_CUDA(cudaMemsetAsync(d.ctr + C_VN, 0, 8, s));
+            for (int q = 0; q < rt.nol; q++)
+                k_oldleft<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)q, vbuf, pool);
+            if ((st = na_read(h, d.ctr, s))) return st;
+            nv = h[C_VN];
+            if (nd + nv > pool) return GRG_E_NOMEM;                // records (and their retries) outgrew the scratch
+        }
         NA_CUDA(cudaMemsetAsync(d.ctr + C_RETRY_N, 0, 16, s));
         uint64_t n = nd;
         int rb = 0;
         for (int pass = 0;; pass++) {
             const int g = grid((n + RB - 1) / RB, JOIN_WARPS, 16);
-            if (pass == 0)
-                k_join<<<g, JOIN_WARPS * 32, 0, s>>>(d, rbuf[2], n, rbuf[0]);
-            else
+            if (pass == 0) {
+                k_join<<<g, JOIN_WARPS * 32, 0, s>>>(d, gbuf, nd, rbuf[0]);
+                if (nv) k_join<<<grid((nv + RB - 1) / RB, JOIN_WARPS, 16), JOIN_WARPS * 32, 0, s>>>(d, vbuf, nv, rbuf[0]);
+            } else {
                 k_join<<<g, JOIN_WARPS * 32, 0, s>>>(d, rbuf[rb], n, rbuf[rb ^ 1]);
+            }
             NA_CUDA(cudaGetLastError());
             if ((st = na_read(h, d.ctr, s))) return st;
             const uint64_t nr = h[C_RETRY_N];

@@ -28,7 +28,7 @@ import grg_gen as G
 GRAMMARS = [(G.DATAFLOW_RULES, G.grammar_labels(G.DATAFLOW_RULES)),
             (G.ALIAS_RULES, G.grammar_labels(G.ALIAS_RULES))]
 KIND = {"dataflow": 0, "alias": 1}
-DERIVED = {0: 1, 1: 5}        # derived label tables per vertex (incl. reverse indexes) for the footprint model
+DERIVED = {0: 1, 1: 3}        # derived label tables per vertex for the footprint model
 
 
 @dataclass

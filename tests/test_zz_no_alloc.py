@@ -68,7 +68,7 @@ def test_noalloc_rejects_oversized_graphs(grg_mod):
     torch = pytest.importorskip("torch")
     lib = grg_mod.load_library()
     big = G.dataflow_blocks(seed=3, num_blocks=900, num_edges=90_000)
-    # 900k vertices x 2 labels of tables exceed the 64 MiB scratch: rejected before any launch
+    # 900k vertices of tables plus 90k edges exceed the 64 MiB scratch: rejected before any launch
     st, counts, _, _ = _noalloc(lib, torch, big, 1)
     assert st == grg_mod.E_RANGE
     assert counts == [2**64 - 1] * big.num_labels       # outputs untouched
