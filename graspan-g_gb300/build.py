@@ -25,9 +25,10 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-
 # tuning overrides of the join kernel, e.g. GRG_NVCC_DEFS="-DGRG_WIN=4 -DGRG_JOIN_UNROLL=2"
 NVCC_FLAGS += os.environ.get("GRG_NVCC_DEFS", "").split()
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I", INC]
+CUDA_INC = ["-I", os.path.join(os.path.dirname(os.path.dirname(shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")), "include")]
 
 CU_SOURCES = ["grg_engine.cu"]
-CXX_SOURCES = ["grg_parse.cpp"]
+CXX_SOURCES = ["grg_parse.cpp", "grg_part.cpp"]
 
 
 def _nvcc():
@@ -68,7 +69,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         obj = os.path.join(OUT, f + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
-            jobs.append(["g++"] + CXX_FLAGS + ["-c", src, "-o", obj])
+            jobs.append(["g++"] + CXX_FLAGS + CUDA_INC + ["-c", src, "-o", obj])
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         logs = list(ex.map(_run, jobs))
     if verbose:

@@ -97,6 +97,10 @@ struct Dev {
     uint32_t *dvm;
     const uint4 *drec;
     uint32_t vwords;
+    // per-slot stamps of a graph loaded from element images (null otherwise):
+    // the run in which the element last gained bits, carried through growth,
+    // compaction and export; the out-of-core schedule marks deltas from them
+    uint32_t *stamp;
     unsigned long long *ctr;  // counter block
     uint32_t V;
     uint32_t pool_cap;        // elements

@@ -128,7 +128,7 @@ __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
 
 // ---------------------------------------------------------------- loader
 
-__global__ void k_init_region(uint32_t *elems, uint32_t *dbits, uint64_t begin, uint64_t end)
+__global__ void k_init_region(uint32_t *elems, uint32_t *dbits, uint32_t *stamp, uint64_t begin, uint64_t end)
 {
     for (uint64_t s = begin + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < end;
          s += (uint64_t)gridDim.x * blockDim.x) {
@@ -138,6 +138,7 @@ __global__ void k_init_region(uint32_t *elems, uint32_t *dbits, uint64_t begin, 
         uint4 *b = reinterpret_cast<uint4 *>(dbits + s * 8);
         b[0] = make_uint4(0, 0, 0, 0);
         b[1] = make_uint4(0, 0, 0, 0);
+        if (stamp) stamp[s] = 0;
     }
 }
 
@@ -242,11 +243,24 @@ __global__ void k_compact_static(Dev d, uint32_t slot, uint32_t first, uint32_t 
             uint4 e1 = e[1];
             if (e1.z == EMPTY) continue;
             if (j != wpos) {
-                uint4 *t = reinterpret_cast<uint4 *>(d.elems + (size_t)(off + wpos) * 8);
+                const uint64_t os = (uint64_t)off + j, ns = (uint64_t)off + wpos;
+                uint4 *t = reinterpret_cast<uint4 *>(d.elems + ns * 8);
                 t[0] = e[0];
                 t[1] = e1;
                 e[0] = make_uint4(0, 0, 0, 0);
                 e[1] = make_uint4(0, 0, EMPTY, 0);
+                if (d.stamp) d.stamp[ns] = d.stamp[os];
+                // a delta mark set at the load (element images) moves with its element
+                if ((d.dmap[os >> 5] >> (os & 31)) & 1u) {
+                    uint4 *ob = reinterpret_cast<uint4 *>(d.dbits + os * 8);
+                    uint4 *nbp = reinterpret_cast<uint4 *>(d.dbits + ns * 8);
+                    nbp[0] = ob[0];
+                    nbp[1] = ob[1];
+                    ob[0] = make_uint4(0, 0, 0, 0);
+                    ob[1] = make_uint4(0, 0, 0, 0);
+                    atomicAnd(&d.dmap[os >> 5], ~(1u << (os & 31)));
+                    atomicOr(&d.dmap[ns >> 5], 1u << (ns & 31));
+                }
             }
             wpos++;
         }
@@ -311,7 +325,7 @@ __device__ __forceinline__ uint32_t select32(uint32_t w, uint32_t n)
 // chunk of 32 bitmap words; lanes take consecutive dirty slots of the chunk, so
 // the copies of a warp are independent and mostly coalesced.
 __global__ void k_gather(Dev d, uint64_t nwords, const uint32_t *__restrict__ chunk_off, uint4 *out,
-                         const uint32_t *__restrict__ row_job, uint32_t *job_cnt)
+                         const uint32_t *__restrict__ row_job, uint32_t *job_cnt, uint32_t run_stamp)
 {
     const uint64_t nchunks = (nwords + 31) / 32;
     const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
@@ -349,10 +363,11 @@ __global__ void k_gather(Dev d, uint64_t nwords, const uint32_t *__restrict__ ch
                 b[0] = make_uint4(0, 0, 0, 0);
                 b[1] = make_uint4(0, 0, 0, 0);
                 const uint64_t pos = base_pos + t;
+                if (run_stamp) d.stamp[s] = run_stamp;     // gained bits during this run
                 out[2 * pos] = b0;
                 out[2 * pos + 1] = make_uint4(b1.x, b1.y, e1.z, e1.w);
                 const uint32_t lab = e1.z >> KEY_SHIFT;
-                if (c_rt.dindex[lab]) {
+                if (lab <= (uint32_t)MAX_LABELS && c_rt.dindex[lab]) {
                     // a table's records are contiguous (slot order; growth moves dirty bits along)
                     const size_t ti = (size_t)(lab - 1) * d.V + e1.w;
                     atomicMin(&d.drs[ti], (uint32_t)pos);
@@ -694,8 +709,10 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, GRG_JOIN_MINB) k_join(Dev d, 
 
         PH_MARK(0);
         // unary rules A ::= B (compute10): the delta itself joins row (A, row)
-        const bool virt = have && B >= OL_SLOT0;      // virtual record of an old-left join
-        const uint32_t nu = have && !virt ? c_rt.un_start[B + 1] - c_rt.un_start[B] : 0;
+        // a record names a label 1..L or an old-left rule; anything else joins nothing
+        const bool virt = have && B >= OL_SLOT0 && B < OL_SLOT0 + (uint32_t)c_rt.nol;
+        const bool real = have && B >= 1 && B <= (uint32_t)c_rt.L;
+        const uint32_t nu = real ? c_rt.un_start[B + 1] - c_rt.un_start[B] : 0;
         const uint32_t maxu = __reduce_max_sync(0xffffffffu, nu);
         for (uint32_t u = 0; u < maxu; u++) {
             if (u < nu) {
@@ -711,7 +728,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, GRG_JOIN_MINB) k_join(Dev d, 
         // (O_B o D_C, virtual record of rule q): right rows are this round's delta
         // records of C[k], found through the delta index.
         const uint32_t qv = virt ? B - OL_SLOT0 : 0;
-        const uint32_t nbr = !have ? 0 : virt ? 1 : c_rt.bin_start[B + 1] - c_rt.bin_start[B];
+        const uint32_t nbr = virt ? 1 : real ? c_rt.bin_start[B + 1] - c_rt.bin_start[B] : 0;
         const uint32_t maxb = __reduce_max_sync(0xffffffffu, nbr);
         w.rOff[lane] = virt;
         for (uint32_t rho = 0; rho < maxb; rho++) {
@@ -1012,7 +1029,7 @@ __global__ void k_grow(Dev d, uint64_t n)
             uint4 *b = reinterpret_cast<uint4 *>(d.dbits + (nb + t) * 8);
             b[0] = make_uint4(0, 0, 0, 0);
             b[1] = make_uint4(0, 0, 0, 0);
-
+            if (d.stamp) d.stamp[nb + t] = 0;
         }
         __syncwarp();
         const uint32_t lg = 31 - __clz(ncap);
@@ -1030,6 +1047,7 @@ __global__ void k_grow(Dev d, uint64_t n)
                     d.elems[q * 8 + 5] = e1.y;
                     // pending delta bits move along, so a table's delta records stay contiguous
                     const uint64_t os = (uint64_t)off + t;
+                    if (d.stamp) d.stamp[q] = d.stamp[os];
                     if ((d.dmap[os >> 5] >> (os & 31)) & 1u) {
                         uint4 *ob = reinterpret_cast<uint4 *>(d.dbits + os * 8);
                         uint4 *nbp = reinterpret_cast<uint4 *>(d.dbits + q * 8);
@@ -1056,7 +1074,7 @@ __global__ void k_grow(Dev d, uint64_t n)
 
 // One warp per table of a label slot: edge/element counts, optional degree and hash.
 __global__ void k_count(Dev d, uint32_t slot, uint32_t *deg_edges, uint32_t *deg_elems, uint32_t first,
-                        uint32_t last, int do_hash, uint32_t r0, uint32_t r1, uint32_t hash_base)
+                        uint32_t last, int do_hash, uint32_t r0, uint32_t r1, uint32_t hash_base, uint32_t id0)
 {
     const uint32_t lane = lane_id();
     const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
@@ -1078,7 +1096,7 @@ __global__ void k_count(Dev d, uint32_t slot, uint32_t *deg_edges, uint32_t *deg
                     while (bw) {
                         const int bit = __ffs(bw) - 1;
                         bw &= bw - 1;
-                        my_hash += edge_hash(slot - hash_base, (uint32_t)v - r0, hb * EIDS + x * 32 + bit - r0);
+                        my_hash += edge_hash(slot - hash_base, (uint32_t)v - id0, hb * EIDS + x * 32 + bit - id0);
                     }
             }
         }
@@ -1122,6 +1140,116 @@ __global__ void k_export(Dev d, uint32_t slot, uint32_t *src, uint32_t *dst, uin
                         lab[pos] = (uint8_t)slot;
                     }
                     pos++;
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- element images
+//
+// An element image is the list of a vertex range's occupied elements, 32 bytes
+// each (words 0-5 bitmap, word 6 key = label << 25 | base, word 7 row), with
+// a stamp per element: the reference's partition pool dump (transferElements
+// / transferBackElements, src/kernel.cu:42-52, src/main.cpp:477-483) with its
+// linked-list words replaced by the key, and the stamps that let an
+// out-of-core schedule mark only what a pair of partitions has not seen.
+
+__device__ __forceinline__ bool elem_ok(const Dev &d, uint32_t L, uint32_t key, uint32_t row)
+{
+    const uint32_t lab = key >> KEY_SHIFT, base = key & BASE_MASK;
+    return lab >= 1 && lab <= L && row < d.V && (uint64_t)base * EIDS < d.V;
+}
+
+__global__ void k_elem_hist(Dev d, const uint4 *recs, uint64_t n, uint32_t L)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint4 e1 = recs[2 * i + 1];
+        if (!elem_ok(d, L, e1.z, e1.w)) {
+            atomicOr(&d.ctr[C_ERR], (unsigned long long)ERR_LOAD);
+            continue;
+        }
+        atomicAdd(&d.cnt[(size_t)((e1.z >> KEY_SHIFT) - 1) * d.V + e1.w], 1u);
+    }
+}
+
+// Place every record in its (fresh, histogram-sized) table; records stamped
+// after mark_after become deltas of round 1.
+__global__ void k_elem_insert(Dev d, const uint4 *recs, const uint32_t *stamps, uint64_t n, uint32_t mark_after,
+                              uint32_t L)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint4 e0 = recs[2 * i], e1 = recs[2 * i + 1];
+        if (!elem_ok(d, L, e1.z, e1.w)) {
+            atomicOr(&d.ctr[C_ERR], (unsigned long long)ERR_LOAD);
+            continue;
+        }
+        const uint32_t lab = e1.z >> KEY_SHIFT, base = e1.z & BASE_MASK;
+        const size_t ti = (size_t)(lab - 1) * d.V + e1.w;
+        const uint64_t de = d.desc[ti];
+        const uint32_t off = (uint32_t)de, cap = (uint32_t)(de >> 32);
+        uint32_t q = EMPTY;
+        if (cap && (cap & (cap - 1)) == 0) {
+            const uint32_t h = hash_slot(base, 31 - __clz(cap));
+            for (uint32_t p = 0; p < cap; p++) {
+                const uint32_t t = off + ((h + p) & (cap - 1));
+                const uint32_t prev = atomicCAS(d.elems + (size_t)t * 8 + 6, EMPTY, e1.z);
+                if (prev == EMPTY) { q = t; break; }
+                if (prev == e1.z) break;               // repeated record
+            }
+        }
+        if (q == EMPTY) {
+            atomicOr(&d.ctr[C_ERR], (unsigned long long)ERR_LOAD);
+            continue;
+        }
+        uint4 *e = reinterpret_cast<uint4 *>(d.elems + (size_t)q * 8);
+        e[0] = e0;
+        d.elems[(size_t)q * 8 + 4] = e1.x;
+        d.elems[(size_t)q * 8 + 5] = e1.y;
+        d.elems[(size_t)q * 8 + 7] = e1.w;
+        atomicAdd(&d.cnt[ti], 1u);
+        const uint32_t st = stamps[i];
+        d.stamp[q] = st;
+        if (st > mark_after) {
+            uint4 *b = reinterpret_cast<uint4 *>(d.dbits + (size_t)q * 8);
+            b[0] = e0;
+            b[1] = make_uint4(e1.x, e1.y, 0u, 0u);
+            atomicOr(&d.dmap[q >> 5], 1u << (q & 31));
+        }
+    }
+}
+
+// Image of rows [v0, v1): one warp per table (label, row); out == null counts only.
+__global__ void k_export_elems(Dev d, uint32_t v0, uint32_t v1, uint32_t L, uint4 *out, uint32_t *st_out,
+                               uint64_t cap_out)
+{
+    const uint32_t lane = lane_id();
+    const uint64_t nv = v1 - v0, ntab = (uint64_t)L * nv;
+    const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t u = blockIdx.x * (uint64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); u < ntab; u += nwarps) {
+        const uint32_t lab = (uint32_t)(u / nv) + 1, row = v0 + (uint32_t)(u % nv);
+        const uint64_t de = d.desc[(size_t)(lab - 1) * d.V + row];
+        const uint32_t off = (uint32_t)de, cap = (uint32_t)(de >> 32);
+        for (uint32_t t0 = 0; t0 < cap; t0 += 32) {
+            const uint32_t t = t0 + lane;
+            uint4 e0 = make_uint4(0, 0, 0, 0), e1 = make_uint4(0, 0, EMPTY, 0);
+            if (t < cap) {
+                const uint4 *e = reinterpret_cast<const uint4 *>(d.elems + (size_t)(off + t) * 8);
+                e1 = e[1];
+                if (e1.z != EMPTY) e0 = e[0];
+            }
+            const bool have = e1.z != EMPTY;
+            const unsigned m = __ballot_sync(0xffffffffu, have);
+            if (!m) continue;
+            unsigned long long p0 = 0;
+            if (lane == 0) p0 = atomicAdd(&d.ctr[C_EXPORT], (unsigned long long)__popc(m));
+            p0 = __shfl_sync(0xffffffffu, p0, 0);
+            if (have && out) {
+                const uint64_t p = p0 + __popc(m & ((1u << lane) - 1u));
+                if (p < cap_out) {
+                    out[2 * p] = e0;
+                    out[2 * p + 1] = make_uint4(e1.x, e1.y, e1.z, row);
+                    st_out[p] = d.stamp ? d.stamp[off + t] : 0u;
                 }
             }
         }
@@ -1177,6 +1305,15 @@ struct grg_ctx {
     uint32_t *d_in32 = nullptr;            // staged input edges (src, dst)
     uint8_t *d_in8 = nullptr;
     uint64_t in_cap = 0;
+    // element images (out-of-core partitions): graph loaded from element records with stamps
+    bool stamp_on = false;                 // the pool carries a stamp per slot
+    bool elem_loaded = false;              // the current graph came from grg_load_elements
+    uint32_t *stamp = nullptr;             // per-slot stamps (pool_cap entries)
+    uint32_t run_stamp = 0;                // stamp given to elements that gain bits in this closure
+    uint4 *xbuf = nullptr;                 // staged element records (load input / export output)
+    uint32_t *xst = nullptr;               // staged stamps
+    uint64_t xcap = 0;
+    uint64_t pool_limit = 0;               // maximum pool slots (0 = what the device holds)
     RuleTable rt{};
     uint64_t launches = 0;
     std::vector<uint32_t *> csr_bufs;      // CSR copies of static labels (freed on reload)
@@ -1251,6 +1388,7 @@ Dev make_dev(const grg_ctx *c)
     d.ctr = c->ctr;
     d.V = c->V;
     d.pool_cap = (uint32_t)c->pool_cap;
+    d.stamp = c->elem_loaded ? c->stamp : nullptr;
     return d;
 }
 
@@ -1283,6 +1421,7 @@ void free_pool(grg_ctx *c)
     cudaFree(c->elems); c->elems = nullptr;
     cudaFree(c->dbits); c->dbits = nullptr;
     cudaFree(c->dmap); c->dmap = nullptr;
+    cudaFree(c->stamp); c->stamp = nullptr;
     c->pool_cap = 0;
 }
 
@@ -1302,28 +1441,30 @@ int alloc_pool(grg_ctx *c, uint64_t elems)
 {
     if (elems > 0xFFFFFFE0ull) elems = 0xFFFFFFE0ull;
     const uint64_t words = elems / 32 + 2;
-    uint32_t *e = nullptr, *b = nullptr, *m = nullptr;
+    uint32_t *e = nullptr, *b = nullptr, *m = nullptr, *t = nullptr;
     if (cudaMalloc(&e, elems * 32) != cudaSuccess || cudaMalloc(&b, elems * 32) != cudaSuccess ||
-        cudaMalloc(&m, words * 4) != cudaSuccess) {
+        cudaMalloc(&m, words * 4) != cudaSuccess || (c->stamp_on && cudaMalloc(&t, elems * 4) != cudaSuccess)) {
         cudaGetLastError();
-        cudaFree(e); cudaFree(b); cudaFree(m);
+        cudaFree(e); cudaFree(b); cudaFree(m); cudaFree(t);
         return fail(c, GRG_E_NOMEM, "cannot allocate element pool of " + std::to_string(elems) + " slots");
     }
     GRG_CUDA(c, cudaMemsetAsync(m, 0, words * 4, c->stream));
     if (c->elems) {
-        // grow: keep the used part, its delta bitmaps and dirty bits
+        // grow: keep the used part, its delta bitmaps, dirty bits and stamps
         int st = read_ctr(c);
-        if (st) { cudaFree(e); cudaFree(b); cudaFree(m); return st; }
+        if (st) { cudaFree(e); cudaFree(b); cudaFree(m); cudaFree(t); return st; }
         const uint64_t used = std::min<uint64_t>(c->h_ctr[C_POOL_TOP], c->pool_cap);
         GRG_CUDA(c, cudaMemcpyAsync(e, c->elems, used * 32, cudaMemcpyDeviceToDevice, c->stream));
         GRG_CUDA(c, cudaMemcpyAsync(b, c->dbits, used * 32, cudaMemcpyDeviceToDevice, c->stream));
         GRG_CUDA(c, cudaMemcpyAsync(m, c->dmap, (used / 32 + 1) * 4, cudaMemcpyDeviceToDevice, c->stream));
+        if (t && c->stamp) GRG_CUDA(c, cudaMemcpyAsync(t, c->stamp, used * 4, cudaMemcpyDeviceToDevice, c->stream));
         GRG_CUDA(c, cudaStreamSynchronize(c->stream));
         free_pool(c);
     }
     c->elems = e;
     c->dbits = b;
     c->dmap = m;
+    c->stamp = t;
     c->pool_cap = elems;
     return GRG_OK;
 }
@@ -1347,6 +1488,7 @@ int grow_pool(grg_ctx *c, uint64_t min_elems)
     cudaMemGetInfo(&fr, &tot);
     uint64_t fit = (uint64_t)((double)fr * 0.9) / POOL_BYTES_PER_SLOT;
     if (want > fit) want = fit;
+    if (c->pool_limit && want > c->pool_limit) want = c->pool_limit;
     if (want <= c->pool_cap) return fail(c, GRG_E_NOMEM, "element pool exhausted and device memory is full");
     return alloc_pool(c, want);
 }
@@ -1471,6 +1613,8 @@ void grg_destroy(grg_ctx *c)
     for (int i = 0; i < 2; i++) cudaFree(c->rbuf[i]);
     cudaFree(c->gbuf);
     cudaFree(c->vbuf);
+    cudaFree(c->xbuf);
+    cudaFree(c->xst);
     cudaFree(c->cand[0]);
     cudaFree(c->cand[1]);
     cudaFree(c->chunk);
@@ -1522,6 +1666,16 @@ int grg_transfer_rules(grg_ctx *c, int num_rules, const int *rules, int num_labe
     return GRG_OK;
 }
 
+int grg_get_rules(const grg_ctx *c, int *num_rules, int *rules, int *num_labels)
+{
+    if (!c || !num_rules || !rules || !num_labels) return GRG_E_ARG;
+    if (!c->have_rules) return GRG_E_STATE;
+    *num_rules = c->R;
+    *num_labels = c->L;
+    memcpy(rules, c->rules, sizeof(int) * 3 * c->R);
+    return GRG_OK;
+}
+
 int grg_allocate_pool(grg_ctx *c, uint64_t pool_bytes)
 {
     if (!c) return GRG_E_ARG;
@@ -1536,26 +1690,29 @@ int grg_allocate_pool(grg_ctx *c, uint64_t pool_bytes)
         elems = (uint64_t)(fr / 8) / POOL_BYTES_PER_SLOT;   // start at 1/8 of free memory; grows on demand
     }
     if (elems < 1024) elems = 1024;
+    if (c->pool_limit && elems > c->pool_limit) elems = c->pool_limit;
     if (c->elems && c->pool_cap >= elems) return GRG_OK;
     free_pool(c);
     return alloc_pool(c, elems);
 }
 
-int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint32_t *src, const uint32_t *dst,
-                   const uint8_t *label, int on_device)
+}  // extern "C"
+
+namespace {
+
+// Tables for a new graph of num_vars vertices: descriptors, counts and the
+// delta index (re)allocated when the size changes, everything cleared.
+int setup_tables(grg_ctx *c, uint32_t num_vars)
 {
-    if (!c || (num_edges && (!src || !dst || !label))) return GRG_E_ARG;
-    if (!c->have_rules) return fail(c, GRG_E_STATE, "grg_transfer_rules must come first");
-    cudaSetDevice(c->device);
     if (!c->elems) {
         int st = grg_allocate_pool(c, c->pool_bytes_req);
         if (st) return st;
     }
     if ((uint64_t)num_vars * (uint64_t)c->L >= 0xFFFFFFFFull)
-        return fail(c, GRG_E_RANGE, "numVars x 2 x numLabels must stay below 2^32");
+        return fail(c, GRG_E_RANGE, "numVars x numLabels must stay below 2^32");
     c->V = num_vars;
     c->ntables = (uint64_t)c->L * num_vars;
-    const uint64_t nt_all = (uint64_t)c->L * num_vars;
+    const uint64_t nt_all = c->ntables;
     if (c->ntables_alloc != nt_all || c->batch) {
         free_graph(c);
         GRG_CUDA(c, cudaMalloc(&c->desc, std::max<uint64_t>(nt_all, 1) * 8));
@@ -1571,12 +1728,80 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
     GRG_CUDA(c, cudaMemsetAsync(c->cnt, 0, nt_all * 4, s));
     GRG_CUDA(c, cudaMemsetAsync(c->want, 0, nt_all * 4, s));
     GRG_CUDA(c, cudaMemsetAsync(c->ctr, 0, sizeof(unsigned long long) * NCTR, s));
+    c->loaded = false;
+    c->closed = false;
+    return GRG_OK;
+}
+
+// Labels on a rule's left-hand side get tables of DERIVED_MIN_CAP slots when
+// that fits in a quarter of the pool (fewer growths, rows stay in allocation order).
+MinCap derived_min_cap(const grg_ctx *c)
+{
+    MinCap mc;
+    memset(&mc, 0, sizeof mc);
+    int nder = 0;
+    bool lhs[MAX_LABELS + 1] = {false};
+    for (int q = 0; q < c->R; q++) lhs[c->rules[3 * q]] = true;
+    for (int l = 1; l <= c->L; l++) nder += lhs[l];
+    if ((uint64_t)nder * c->V * DERIVED_MIN_CAP <= c->pool_cap / 4)
+        for (int l = 1; l <= c->L; l++) mc.cap[l] = lhs[l] ? DERIVED_MIN_CAP : 0;
+    return mc;
+}
+
+// Size and bump-allocate every table from the histogram that `hist` builds in
+// cnt; the pool grows (and the histogram is rebuilt) until the tables fit.
+// Clears the allocated region. Returns the pool top in *top.
+template <class Hist>
+int alloc_tables(grg_ctx *c, const MinCap &mc, Hist hist, uint64_t *top)
+{
+    cudaStream_t s = c->stream;
+    hist(make_dev(c));
+    for (int attempt = 0;; attempt++) {
+        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_POOL_TOP, 0, 8, s));
+        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_ERR, 0, 8, s));
+        k_load_alloc<<<grid_for(c, c->ntables, 256), 256, 0, s>>>(make_dev(c), 0, c->V, (uint32_t)c->L, mc);
+        c->launches++;
+        int st = read_ctr(c);
+        if (st) return st;
+        if (!(c->h_ctr[C_ERR] & ERR_POOL)) break;
+        if (attempt > 8) return fail(c, GRG_E_NOMEM, "element pool too small for the input graph");
+        // the histogram was consumed: rebuild it after growing the pool
+        st = grow_pool(c, c->h_ctr[C_POOL_TOP] + c->h_ctr[C_POOL_TOP] / 2);
+        if (st) return st;
+        GRG_CUDA(c, cudaMemsetAsync(c->cnt, 0, c->ntables * 4, s));
+        hist(make_dev(c));
+    }
+    *top = c->h_ctr[C_POOL_TOP];
+    GRG_CUDA(c, cudaMemsetAsync(c->dmap, 0, (c->pool_cap / 32 + 2) * 4, s));
+    if (*top) {
+        k_init_region<<<grid_for(c, *top, 256), 256, 0, s>>>(c->elems, c->dbits, c->elem_loaded ? c->stamp : nullptr,
+                                                             0, *top);
+        c->launches++;
+    }
+    return GRG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint32_t *src, const uint32_t *dst,
+                   const uint8_t *label, int on_device)
+{
+    if (!c || (num_edges && (!src || !dst || !label))) return GRG_E_ARG;
+    if (!c->have_rules) return fail(c, GRG_E_STATE, "grg_transfer_rules must come first");
+    cudaSetDevice(c->device);
+    c->elem_loaded = false;
+    int st = setup_tables(c, num_vars);
+    if (st) return st;
+    cudaStream_t s = c->stream;
     const uint32_t *dsrc = src, *ddst = dst;
     const uint8_t *dlab = label;
     if (!on_device && num_edges) {
         if (c->in_cap < num_edges) {
             cudaFree(c->d_in32); cudaFree(c->d_in8);
             c->d_in32 = nullptr; c->d_in8 = nullptr;
+            c->in_cap = 0;
             GRG_CUDA(c, cudaMalloc(&c->d_in32, num_edges * 8));
             GRG_CUDA(c, cudaMalloc(&c->d_in8, num_edges));
             c->in_cap = num_edges;
@@ -1588,54 +1813,22 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
         ddst = c->d_in32 + num_edges;
         dlab = c->d_in8;
     }
-    Dev d = make_dev(c);
     c->launches = 0;
-    if (num_edges) {
-        k_load_hist<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, dlab, num_edges, 0);
-        c->launches++;
-    }
-    for (int q = 0; q < c->R; q++)
-        if (c->rules[3 * q + 1] == 0) {
-            k_eps_hist<<<grid_for(c, num_vars, 256), 256, 0, s>>>(d, (uint32_t)c->rules[3 * q], 0, num_vars);
+    auto hist = [&](Dev d) {
+        if (num_edges) {
+            k_load_hist<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, dlab, num_edges, 0);
             c->launches++;
         }
-    // labels on a rule's left-hand side get tables of DERIVED_MIN_CAP slots when that fits in a
-    // quarter of the pool (fewer growths, rows stay in allocation order)
-    MinCap mc;
-    memset(&mc, 0, sizeof mc);
-    {
-        int nder = 0;
-        bool lhs[MAX_LABELS + 1] = {false};
-        for (int q = 0; q < c->R; q++) lhs[c->rules[3 * q]] = true;
-        for (int l = 1; l <= c->L; l++) nder += lhs[l];
-        if ((uint64_t)nder * num_vars * DERIVED_MIN_CAP <= c->pool_cap / 4)
-            for (int l = 1; l <= c->L; l++) mc.cap[l] = lhs[l] ? DERIVED_MIN_CAP : 0;
-    }
-    for (int attempt = 0;; attempt++) {
-        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_POOL_TOP, 0, 8, s));
-        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_ERR, 0, 8, s));
-        k_load_alloc<<<grid_for(c, c->ntables, 256), 256, 0, s>>>(d, 0, num_vars, (uint32_t)c->L, mc);
-        c->launches++;
-        int st = read_ctr(c);
-        if (st) return st;
-        if (!(c->h_ctr[C_ERR] & ERR_POOL)) break;
-        if (attempt > 8) return fail(c, GRG_E_NOMEM, "element pool too small for the input graph");
-        // histogram was consumed: rebuild it after growing the pool
-        st = grow_pool(c, c->h_ctr[C_POOL_TOP] + c->h_ctr[C_POOL_TOP] / 2);
-        if (st) return st;
-        d = make_dev(c);
-        GRG_CUDA(c, cudaMemsetAsync(c->cnt, 0, nt_all * 4, s));
-        if (num_edges) k_load_hist<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, dlab, num_edges, 0);
         for (int q = 0; q < c->R; q++)
-            if (c->rules[3 * q + 1] == 0)
+            if (c->rules[3 * q + 1] == 0) {
                 k_eps_hist<<<grid_for(c, num_vars, 256), 256, 0, s>>>(d, (uint32_t)c->rules[3 * q], 0, num_vars);
-    }
-    uint64_t top = c->h_ctr[C_POOL_TOP];
-    if (top) {
-        GRG_CUDA(c, cudaMemsetAsync(c->dmap, 0, (c->pool_cap / 32 + 2) * 4, s));
-        k_init_region<<<grid_for(c, top, 256), 256, 0, s>>>(c->elems, c->dbits, 0, top);
-        c->launches++;
-    }
+                c->launches++;
+            }
+    };
+    uint64_t top = 0;
+    st = alloc_tables(c, derived_min_cap(c), hist, &top);
+    if (st) return st;
+    Dev d = make_dev(c);
     if (num_edges) {
         k_load_insert<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges, 0);
         c->launches++;
@@ -1646,9 +1839,72 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
             c->launches++;
         }
     GRG_CUDA(c, cudaGetLastError());
-    int st = read_ctr(c);
+    st = read_ctr(c);
     if (st) return st;
     if (c->h_ctr[C_ERR]) return fail(c, GRG_E_CUDA, "internal error while loading edges");
+    c->loaded = true;
+    c->closed = false;
+    return GRG_OK;
+}
+
+int grg_load_elements(grg_ctx *c, uint32_t num_vars, uint64_t num_elems, const uint32_t *elems,
+                      const uint32_t *stamps, uint32_t mark_after, int on_device)
+{
+    if (!c || (num_elems && (!elems || !stamps))) return GRG_E_ARG;
+    if (!c->have_rules) return fail(c, GRG_E_STATE, "grg_transfer_rules must come first");
+    cudaSetDevice(c->device);
+    if (!c->stamp_on) {
+        // the pool gains a stamp per slot from now on
+        c->stamp_on = true;
+        if (c->elems && !c->stamp) {
+            if (cudaMalloc(&c->stamp, c->pool_cap * 4) != cudaSuccess) {
+                cudaGetLastError();
+                c->stamp = nullptr;
+                c->stamp_on = false;
+                return fail(c, GRG_E_NOMEM, "cannot allocate element stamps");
+            }
+        }
+    }
+    c->elem_loaded = true;
+    int st = setup_tables(c, num_vars);
+    if (st) return st;
+    cudaStream_t s = c->stream;
+    const uint4 *drec = reinterpret_cast<const uint4 *>(elems);
+    const uint32_t *dst_ = stamps;
+    if (!on_device && num_elems) {
+        if (c->xcap < num_elems) {
+            cudaFree(c->xbuf); cudaFree(c->xst);
+            c->xbuf = nullptr; c->xst = nullptr;
+            c->xcap = 0;
+            const uint64_t cap = num_elems + num_elems / 4;
+            GRG_CUDA(c, cudaMalloc(&c->xbuf, cap * 32));
+            GRG_CUDA(c, cudaMalloc(&c->xst, cap * 4));
+            c->xcap = cap;
+        }
+        GRG_CUDA(c, cudaMemcpyAsync(c->xbuf, elems, num_elems * 32, cudaMemcpyHostToDevice, s));
+        GRG_CUDA(c, cudaMemcpyAsync(c->xst, stamps, num_elems * 4, cudaMemcpyHostToDevice, s));
+        drec = c->xbuf;
+        dst_ = c->xst;
+    }
+    c->launches = 0;
+    auto hist = [&](Dev d) {
+        if (num_elems) {
+            k_elem_hist<<<grid_for(c, num_elems, 256), 256, 0, s>>>(d, drec, num_elems, (uint32_t)c->L);
+            c->launches++;
+        }
+    };
+    uint64_t top = 0;
+    st = alloc_tables(c, derived_min_cap(c), hist, &top);
+    if (st) return st;
+    if (num_elems) {
+        k_elem_insert<<<grid_for(c, num_elems, 256), 256, 0, s>>>(make_dev(c), drec, dst_, num_elems, mark_after,
+                                                                  (uint32_t)c->L);
+        c->launches++;
+    }
+    GRG_CUDA(c, cudaGetLastError());
+    st = read_ctr(c);
+    if (st) return st;
+    if (c->h_ctr[C_ERR]) return fail(c, GRG_E_ARG, "element records out of range or repeated");
     c->loaded = true;
     c->closed = false;
     return GRG_OK;
@@ -1710,7 +1966,9 @@ static int run_rounds(grg_ctx *c, uint64_t max_rounds, grg_stats &S, double &joi
                 GRG_CUDA(c, cudaMemsetAsync(c->drc + t0, 0, (size_t)c->V * 4, s));
                 GRG_CUDA(c, cudaMemsetAsync(c->dvm + (size_t)(l - 1) * vw, 0, vw * 4, s));
             }
-        k_gather<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->gbuf, c->row_job, c->job_cnt);
+        // elements that gain bits in this run get its stamp; round 1 gathers the load marks
+        const uint32_t rs = (c->elem_loaded && done_rounds > 1) ? c->run_stamp : 0u;
+        k_gather<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->gbuf, c->row_job, c->job_cnt, rs);
         c->launches++;
         // old-left joins: virtual records of O_B masked to the vertices with deltas of C
         uint64_t nv = 0;
@@ -1803,10 +2061,13 @@ static int run_rounds(grg_ctx *c, uint64_t max_rounds, grg_stats &S, double &joi
     return GRG_OK;
 }
 
-int grg_closure(grg_ctx *c, uint32_t filter, grg_stats *stats)
+int grg_closure(grg_ctx *c, uint32_t filter, grg_stats *stats) { return grg_closure_ex(c, filter, 0, stats); }
+
+int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *stats)
 {
     if (!c || filter > 1) return GRG_E_ARG;
     if (!c->loaded) return fail(c, GRG_E_STATE, "grg_load_edges must come first");
+    c->run_stamp = run_stamp;
     if (c->closed) return fail(c, GRG_E_STATE, "closure already computed; reload the graph");
     cudaSetDevice(c->device);
     RuleTable rt;
@@ -1869,9 +2130,10 @@ int grg_closure(grg_ctx *c, uint32_t filter, grg_stats *stats)
     st = read_ctr(c);
     if (st) return st;
     const uint64_t top = c->h_ctr[C_POOL_TOP];
-    // every loaded element of a tracked label is a delta of round 1
+    // every loaded element of a tracked label is a delta of round 1 (element images
+    // carry their own marks instead)
     d = make_dev(c);
-    if (top) {
+    if (top && !c->elem_loaded) {
         k_mark_all<<<grid_for(c, top, 256), 256, 0, s>>>(d, 0, top);
         c->launches++;
     }
@@ -1911,7 +2173,7 @@ static int count_pass(grg_ctx *c, uint32_t *deg_e, uint32_t *deg_el, uint32_t fi
     GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_LABEL0, 0, sizeof(unsigned long long) * (MAX_SLOTS + 2), s));
     GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_HASH, 0, 8, s));
     for (int l = 1; l <= c->L; l++)
-        k_count<<<grid_for(c, (uint64_t)c->V * 32, 256), 256, 0, s>>>(d, (uint32_t)l, deg_e, deg_el, first, last, do_hash, 0, c->V, 0);
+        k_count<<<grid_for(c, (uint64_t)c->V * 32, 256), 256, 0, s>>>(d, (uint32_t)l, deg_e, deg_el, first, last, do_hash, 0, c->V, 0, 0);
     GRG_CUDA(c, cudaGetLastError());
     return read_ctr(c);
 }
@@ -1989,6 +2251,79 @@ int grg_export_edges(grg_ctx *c, uint64_t cap, uint32_t *src, uint32_t *dst, uin
     return GRG_OK;
 }
 
+int grg_export_elements(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t cap, uint32_t *elems,
+                        uint32_t *stamps, uint64_t *num_out)
+{
+    if (!c || v_begin > v_end || (cap && (!elems || !stamps))) return GRG_E_ARG;
+    if (!c->loaded) return fail(c, GRG_E_STATE, "no graph loaded");
+    if (v_end > c->V) return fail(c, GRG_E_RANGE, "vertex range beyond the graph");
+    cudaSetDevice(c->device);
+    cudaStream_t s = c->stream;
+    Dev d = make_dev(c);
+    const uint64_t ntab = (uint64_t)c->L * (v_end - v_begin);
+    // count, then write into a staging buffer of exactly that size
+    GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_EXPORT, 0, 8, s));
+    if (ntab) k_export_elems<<<grid_for(c, ntab * 32, 256), 256, 0, s>>>(d, v_begin, v_end, (uint32_t)c->L, nullptr, nullptr, 0);
+    int st = read_ctr(c);
+    if (st) return st;
+    const uint64_t n = c->h_ctr[C_EXPORT];
+    if (num_out) *num_out = n;
+    if (n > cap) return fail(c, GRG_E_RANGE, "export buffer too small");
+    if (!n) return GRG_OK;
+    if (c->xcap < n) {
+        cudaFree(c->xbuf); cudaFree(c->xst);
+        c->xbuf = nullptr; c->xst = nullptr;
+        c->xcap = 0;
+        const uint64_t xc = n + n / 4;
+        GRG_CUDA(c, cudaMalloc(&c->xbuf, xc * 32));
+        GRG_CUDA(c, cudaMalloc(&c->xst, xc * 4));
+        c->xcap = xc;
+    }
+    GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_EXPORT, 0, 8, s));
+    k_export_elems<<<grid_for(c, ntab * 32, 256), 256, 0, s>>>(d, v_begin, v_end, (uint32_t)c->L, c->xbuf, c->xst, n);
+    GRG_CUDA(c, cudaMemcpyAsync(elems, c->xbuf, n * 32, cudaMemcpyDeviceToHost, s));
+    GRG_CUDA(c, cudaMemcpyAsync(stamps, c->xst, n * 4, cudaMemcpyDeviceToHost, s));
+    GRG_CUDA(c, cudaStreamSynchronize(s));
+    GRG_CUDA(c, cudaGetLastError());
+    return GRG_OK;
+}
+
+int grg_range_counts(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t *counts, uint64_t *hash)
+{
+    if (!c || !counts || v_begin > v_end) return GRG_E_ARG;
+    if (!c->loaded) return fail(c, GRG_E_STATE, "no graph loaded");
+    if (v_end > c->V) return fail(c, GRG_E_RANGE, "vertex range beyond the graph");
+    cudaSetDevice(c->device);
+    cudaStream_t s = c->stream;
+    Dev d = make_dev(c);
+    GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_LABEL0, 0, sizeof(unsigned long long) * (MAX_SLOTS + 2), s));
+    GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_HASH, 0, 8, s));
+    if (v_end > v_begin)
+        for (int l = 1; l <= c->L; l++)
+            k_count<<<grid_for(c, (uint64_t)(v_end - v_begin) * 32, 256), 256, 0, s>>>(
+                d, (uint32_t)l, nullptr, nullptr, 0, 0, hash ? 1 : 0, v_begin, v_end, 0, 0);
+    GRG_CUDA(c, cudaGetLastError());
+    int st = read_ctr(c);
+    if (st) return st;
+    for (int l = 1; l <= c->L; l++) counts[l - 1] = c->h_ctr[C_LABEL0 + l];
+    if (hash) *hash = c->h_ctr[C_HASH];
+    return GRG_OK;
+}
+
+int grg_set_pool_limit(grg_ctx *c, uint64_t pool_bytes)
+{
+    if (!c) return GRG_E_ARG;
+    cudaSetDevice(c->device);
+    c->pool_limit = pool_bytes ? std::max<uint64_t>(pool_bytes / (POOL_BYTES_PER_SLOT + 4), 1024) : 0;
+    if (c->pool_limit && c->elems && c->pool_cap > c->pool_limit) {
+        // the pool shrinks on the next load; the loaded graph is dropped
+        free_pool(c);
+        c->loaded = false;
+        c->closed = false;
+    }
+    return GRG_OK;
+}
+
 }  // extern "C"
 
 // ====================================================================== batched jobs
@@ -2002,6 +2337,7 @@ int grg_batch_begin(grg_ctx *c, uint32_t max_vars, uint32_t max_jobs, int num_ru
     int st = grg_transfer_rules(c, num_rules, rules, num_labels);
     if (st) return st;
     cudaSetDevice(c->device);
+    c->elem_loaded = false;
     RuleTable rt;
     st = build_rules(c, filter, rt);
     if (st) return st;
@@ -2102,7 +2438,7 @@ int grg_batch_admit(grg_ctx *c, uint32_t job, uint32_t base, uint32_t num_vars, 
     if (st) return st;
     if (c->h_ctr[C_ERR] & ERR_POOL) return fail(c, GRG_E_NOMEM, "element pool too small for the job");
     const uint64_t top1 = c->h_ctr[C_POOL_TOP];
-    if (top1 > top0) k_init_region<<<grid_for(c, top1 - top0, 256), 256, 0, s>>>(c->elems, c->dbits, top0, top1);
+    if (top1 > top0) k_init_region<<<grid_for(c, top1 - top0, 256), 256, 0, s>>>(c->elems, c->dbits, nullptr, top0, top1);
     if (num_edges) k_load_insert<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges, base);
     for (int l = 1; l <= c->L; l++)
         if ((eps_mask >> (l - 1)) & 1ull) k_eps_insert<<<grid_for(c, num_vars, 256), 256, 0, s>>>(d, (uint32_t)l, base, num_vars);
@@ -2163,7 +2499,7 @@ int grg_batch_result(grg_ctx *c, uint32_t job, uint32_t label_offset, uint32_t n
     GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_HASH, 0, 8, s));
     for (uint32_t l = label_offset + 1; l <= label_offset + num_labels; l++)
         k_count<<<grid_for(c, (uint64_t)(r1 - r0) * 32, 256), 256, 0, s>>>(d, l, nullptr, nullptr, 0, 0, hash ? 1 : 0,
-                                                                           r0, r1, label_offset);
+                                                                           r0, r1, label_offset, r0);
     GRG_CUDA(c, cudaGetLastError());
     int st = read_ctr(c);
     if (st) return st;
@@ -2326,6 +2662,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     d.drc = (uint32_t *)(base + o_drc);
     d.dvm = (uint32_t *)(base + o_dvm);
     d.vwords = (uint32_t)vwords;
+    d.stamp = nullptr;
     uint4 *gbuf = (uint4 *)(base + o_gbuf), *vbuf = (uint4 *)(base + o_vbuf);
     d.drec = gbuf;
     uint4 *rbuf[2] = {(uint4 *)(base + o_rbuf0), (uint4 *)(base + o_rbuf1)};
@@ -2354,7 +2691,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     if ((st = na_read(h, d.ctr, s))) return st;
     if (h[C_ERR] & ERR_POOL) return GRG_E_NOMEM;
     const uint64_t top0 = h[C_POOL_TOP];
-    if (top0) k_init_region<<<grid(top0, 256, 8), 256, 0, s>>>(d.elems, d.dbits, 0, top0);
+    if (top0) k_init_region<<<grid(top0, 256, 8), 256, 0, s>>>(d.elems, d.dbits, nullptr, 0, top0);
     if (num_edges) k_load_insert<<<grid(num_edges, 256, 8), 256, 0, s>>>(d, d_src, d_dst, d_label, num_edges, 0);
     for (int q = 0; q < num_rules; q++)
         if (rules[3 * q + 1] == 0) k_eps_insert<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)rules[3 * q], 0, num_vars);
@@ -2388,7 +2725,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
                 NA_CUDA(cudaMemsetAsync(d.drc + (size_t)(l - 1) * num_vars, 0, (size_t)num_vars * 4, s));
                 NA_CUDA(cudaMemsetAsync(d.dvm + (size_t)(l - 1) * vwords, 0, vwords * 4, s));
             }
-        k_gather<<<grid(nchunks * 32, 256, 8), 256, 0, s>>>(d, nwords, coff, gbuf, nullptr, nullptr);
+        k_gather<<<grid(nchunks * 32, 256, 8), 256, 0, s>>>(d, nwords, coff, gbuf, nullptr, nullptr, 0);
         uint64_t nv = 0;
         if (rt.nol) {
             NA_CUDA(cudaMemsetAsync(d.ctr + C_VN, 0, 8, s));
@@ -2428,7 +2765,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     NA_CUDA(cudaMemsetAsync(d.ctr + C_LABEL0, 0, sizeof(unsigned long long) * (MAX_SLOTS + 2), s));
     NA_CUDA(cudaMemsetAsync(d.ctr + C_HASH, 0, 8, s));
     for (int l = 1; l <= num_labels; l++)
-        k_count<<<grid((uint64_t)num_vars * 32, 256, 8), 256, 0, s>>>(d, (uint32_t)l, nullptr, nullptr, 0, 0, d_set_hash ? 1 : 0, 0, num_vars, 0);
+        k_count<<<grid((uint64_t)num_vars * 32, 256, 8), 256, 0, s>>>(d, (uint32_t)l, nullptr, nullptr, 0, 0, d_set_hash ? 1 : 0, 0, num_vars, 0, 0);
     NA_CUDA(cudaMemcpyAsync(d_label_counts, d.ctr + C_LABEL0 + 1, sizeof(uint64_t) * num_labels,
                             cudaMemcpyDeviceToDevice, s));
     if (d_set_hash) NA_CUDA(cudaMemcpyAsync(d_set_hash, d.ctr + C_HASH, 8, cudaMemcpyDeviceToDevice, s));

@@ -1,0 +1,462 @@
+// grg_part.cpp -- out-of-core closure over vertex-range partitions.
+//
+// The reference always runs partitioned (src/main.cpp:141-175: at least two
+// vertex-range partitions), spilling partition pools to files and computing
+// supersteps over all partition pairs until no pair has new edges
+// (precomputation / run_computation, src/main.cpp:764-858), splitting a
+// partition that overflows the GPU heap (src/main.cpp:633-762). Here the
+// in-core closure (grg_closure) is the normal path -- the GPU's memory holds
+// graphs the reference had to partition -- and this scheduler takes over when
+// a graph's closure does not fit the context's pool limit. It is host code on
+// the C ABI: partition images live in host memory (the spill files), the
+// device closes one partition or one pair at a time.
+//
+// Two schedules:
+//   stream  every binary rule's second symbol is never derived, so a row's
+//           closure needs only its own rows and static rows: the static
+//           labels of the whole graph stay in the load, each partition's rows
+//           are closed once, in turn (no supersteps).
+//   pairs   otherwise: supersteps over pairs (a, b). Every element carries a
+//           stamp (the run that last gave it bits); a pair's run marks as
+//           round-1 deltas exactly the elements stamped after the pair's last
+//           run, and a pair none of whose elements is newer is skipped. A
+//           superstep without a run is the fixpoint.
+// A run that does not fit (GRG_E_NOMEM) splits the larger partition at its
+// median element and is repeated.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <utility>
+#include <vector>
+
+#include "grg.h"
+
+namespace {
+
+constexpr uint32_t KEY_SHIFT = 25;
+
+struct Image {
+    uint32_t id = 0;                 // unique per partition (splits make new ids)
+    uint32_t lo = 0, hi = 0;         // source vertices [lo, hi)
+    std::vector<uint32_t> rec;       // 8 words per element
+    std::vector<uint32_t> st;        // stamp per element
+    uint32_t max_stamp = 0;
+    uint32_t last_run = 0;           // last run that held this partition
+    bool counted = false;            // counts/hash are those of the current image
+    std::vector<uint64_t> counts;
+    uint64_t hash = 0;
+
+    uint64_t size() const { return st.size(); }
+    void refresh()
+    {
+        max_stamp = 0;
+        for (uint32_t s : st) max_stamp = std::max(max_stamp, s);
+    }
+};
+
+// Pinned staging buffer for records and stamps.
+struct Pinned {
+    uint32_t *rec = nullptr;
+    uint32_t *st = nullptr;
+    uint64_t cap = 0;
+    ~Pinned() { release(); }
+    void release()
+    {
+        if (rec) cudaFreeHost(rec);
+        if (st) cudaFreeHost(st);
+        rec = st = nullptr;
+        cap = 0;
+    }
+    int ensure(uint64_t n)
+    {
+        if (n <= cap) return GRG_OK;
+        release();
+        const uint64_t c = std::max<uint64_t>(n + n / 4, 1024);
+        if (cudaHostAlloc((void **)&rec, c * 32, cudaHostAllocDefault) != cudaSuccess ||
+            cudaHostAlloc((void **)&st, c * 4, cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            release();
+            return GRG_E_NOMEM;
+        }
+        cap = c;
+        return GRG_OK;
+    }
+};
+
+}  // namespace
+
+struct grg_part {
+    grg_ctx *ctx = nullptr;
+    uint32_t V = 0;
+    int R = 0, L = 0;
+    int rules[3 * GRG_MAX_RULES] = {0};
+    std::vector<Image> parts;                                  // ordered by lo
+    std::map<std::pair<uint32_t, uint32_t>, uint32_t> seen;    // (id, id) -> run after which the pair is closed
+    uint32_t next_id = 1;
+    uint32_t run_id = 1;                                       // stamps of loaded edges are 1
+    bool loaded = false;
+    bool closed = false;
+    Pinned in, out;
+    grg_part_stats S{};
+};
+
+namespace {
+
+std::pair<uint32_t, uint32_t> pkey(uint32_t a, uint32_t b) { return a < b ? std::make_pair(a, b) : std::make_pair(b, a); }
+
+// Labels any rule can add edges to under the filter (epsilon rules count: they
+// add edges at the load), as the engine classifies them.
+void derivable_labels(const grg_part *p, uint32_t filter, bool *der)
+{
+    for (int l = 0; l <= GRG_MAX_LABELS; l++) der[l] = false;
+    for (int q = 0; q < p->R; q++) {
+        const int *r = &p->rules[3 * q];
+        const bool unary = r[1] && !r[2];
+        if (!(filter && unary)) der[r[0]] = true;
+    }
+}
+
+// Export rows [lo, hi) of the loaded graph into img (records + device stamps).
+int export_image(grg_part *p, Image &img)
+{
+    int st = p->out.ensure(1024);
+    if (st) return st;
+    uint64_t n2 = 0;
+    st = grg_export_elements(p->ctx, img.lo, img.hi, p->out.cap, p->out.rec, p->out.st, &n2);
+    if (st == GRG_E_RANGE && n2 > p->out.cap) {
+        if ((st = p->out.ensure(n2))) return st;
+        st = grg_export_elements(p->ctx, img.lo, img.hi, p->out.cap, p->out.rec, p->out.st, &n2);
+    }
+    if (st) return st;
+    img.rec.assign(p->out.rec, p->out.rec + n2 * 8);
+    img.st.assign(p->out.st, p->out.st + n2);
+    p->S.d2h_bytes += n2 * 36;
+    return GRG_OK;
+}
+
+int count_image(grg_part *p, Image &img)
+{
+    img.counts.assign(p->L, 0);
+    int st = grg_range_counts(p->ctx, img.lo, img.hi, img.counts.data(), &img.hash);
+    if (st) return st;
+    img.counted = true;
+    return GRG_OK;
+}
+
+// Split parts[i] at its median element (by source row); false when it is one row.
+bool split(grg_part *p, size_t i)
+{
+    Image &x = p->parts[i];
+    if (x.hi - x.lo < 2) return false;
+    std::vector<uint64_t> per(x.hi - x.lo, 0);
+    for (uint64_t e = 0; e < x.size(); e++) per[x.rec[8 * e + 7] - x.lo]++;
+    uint64_t half = x.size() / 2, acc = 0;
+    uint32_t mid = x.lo + (x.hi - x.lo) / 2;
+    if (x.size()) {
+        for (uint32_t v = x.lo; v < x.hi; v++) {
+            acc += per[v - x.lo];
+            if (acc >= half) { mid = v + 1; break; }
+        }
+        mid = std::min(std::max(mid, x.lo + 1), x.hi - 1);
+    }
+    Image a, b;
+    a.id = p->next_id++;
+    b.id = p->next_id++;
+    a.lo = x.lo; a.hi = mid;
+    b.lo = mid; b.hi = x.hi;
+    for (uint64_t e = 0; e < x.size(); e++) {
+        Image &t = x.rec[8 * e + 7] < mid ? a : b;
+        t.rec.insert(t.rec.end(), x.rec.begin() + 8 * e, x.rec.begin() + 8 * e + 8);
+        t.st.push_back(x.st[e]);
+    }
+    a.refresh();
+    b.refresh();
+    a.last_run = b.last_run = x.last_run;
+    // the halves have seen what the whole had seen, with every other partition and with each other
+    std::map<std::pair<uint32_t, uint32_t>, uint32_t> add;
+    for (const auto &kv : p->seen) {
+        uint32_t other = kv.first.first == x.id ? kv.first.second : kv.first.second == x.id ? kv.first.first : 0;
+        if (!other) continue;
+        if (other == x.id) continue;
+        add[pkey(a.id, other)] = kv.second;
+        add[pkey(b.id, other)] = kv.second;
+    }
+    for (const auto &kv : add) p->seen[kv.first] = kv.second;
+    p->seen[pkey(a.id, b.id)] = x.last_run;
+    p->parts[i] = std::move(a);
+    p->parts.insert(p->parts.begin() + i + 1, std::move(b));
+    p->S.splits++;
+    return true;
+}
+
+// Load one partition's image (nothing marked) and count its rows.
+int recount(grg_part *p, Image &x)
+{
+    int st = p->in.ensure(x.size());
+    if (st) return st;
+    memcpy(p->in.rec, x.rec.data(), x.size() * 32);
+    memcpy(p->in.st, x.st.data(), x.size() * 4);
+    p->S.h2d_bytes += x.size() * 36;
+    if ((st = grg_load_elements(p->ctx, p->V, x.size(), p->in.rec, p->in.st, ~0u, 0))) return st;
+    return count_image(p, x);
+}
+
+// One device run over the given partitions; the load holds `extra` first (static
+// records of the stream schedule, stamps as given) then the partitions' images.
+// Partitions' records are marked when their stamp is above mark_after.
+int run_once(grg_part *p, uint32_t filter, const std::vector<size_t> &idx, const Image *extra,
+             const bool *keep_label, uint32_t mark_after, uint32_t run_stamp)
+{
+    uint64_t n = extra ? extra->size() : 0;
+    for (size_t i : idx)
+        for (uint64_t e = 0; e < p->parts[i].size(); e++)
+            if (!keep_label || keep_label[p->parts[i].rec[8 * e + 6] >> KEY_SHIFT]) n++;
+    int st = p->in.ensure(n);
+    if (st) return st;
+    uint64_t k = 0;
+    if (extra && extra->size()) {
+        memcpy(p->in.rec, extra->rec.data(), extra->size() * 32);
+        memcpy(p->in.st, extra->st.data(), extra->size() * 4);
+        k = extra->size();
+    }
+    for (size_t i : idx) {
+        const Image &x = p->parts[i];
+        for (uint64_t e = 0; e < x.size(); e++) {
+            if (keep_label && !keep_label[x.rec[8 * e + 6] >> KEY_SHIFT]) continue;
+            memcpy(p->in.rec + 8 * k, x.rec.data() + 8 * e, 32);
+            p->in.st[k] = x.st[e];
+            k++;
+        }
+    }
+    p->S.h2d_bytes += n * 36;
+    if ((st = grg_load_elements(p->ctx, p->V, n, p->in.rec, p->in.st, mark_after, 0))) return st;
+    grg_stats cs;
+    if ((st = grg_closure_ex(p->ctx, filter, run_stamp, &cs))) return st;
+    p->S.runs++;
+    p->S.rounds += cs.rounds;
+    return GRG_OK;
+}
+
+int run_stream(grg_part *p, uint32_t filter, const bool *der)
+{
+    bool derived[GRG_MAX_LABELS + 1];
+    for (int l = 0; l <= GRG_MAX_LABELS; l++) derived[l] = der[l];
+    for (size_t i = 0; i < p->parts.size();) {
+        // static records of every partition, marked only for partition i's rows
+        Image stat;
+        for (size_t j = 0; j < p->parts.size(); j++) {
+            const Image &x = p->parts[j];
+            for (uint64_t e = 0; e < x.size(); e++) {
+                if (derived[x.rec[8 * e + 6] >> KEY_SHIFT]) continue;
+                stat.rec.insert(stat.rec.end(), x.rec.begin() + 8 * e, x.rec.begin() + 8 * e + 8);
+                stat.st.push_back(j == i ? 1u : 0u);
+            }
+        }
+        Image &x = p->parts[i];
+        for (uint32_t &s : x.st) s = 1;
+        const int st = run_once(p, filter, {i}, &stat, derived, 0, 0);
+        if (st == GRG_E_NOMEM) {
+            if (!split(p, i)) return GRG_E_NOMEM;
+            continue;
+        }
+        if (st) return st;
+        int s2 = export_image(p, p->parts[i]);
+        if (s2) return s2;
+        if ((s2 = count_image(p, p->parts[i]))) return s2;
+        i++;
+    }
+    return GRG_OK;
+}
+
+int run_pairs(grg_part *p, uint32_t filter)
+{
+    for (;;) {
+        bool ran = false, restart = false;
+        const size_t m = p->parts.size();
+        for (size_t i = 0; i < m && !restart; i++) {
+            for (size_t j = (m == 1 ? i : i + 1); j < m && !restart; j++) {
+                Image &a = p->parts[i], &b = p->parts[j];
+                const auto key = pkey(a.id, b.id);
+                const uint32_t t = p->seen.count(key) ? p->seen[key] : 0;
+                if (a.max_stamp <= t && b.max_stamp <= t) {
+                    p->S.skipped++;
+                    continue;
+                }
+                const uint32_t r = ++p->run_id;
+                std::vector<size_t> idx = {i};
+                if (j != i) idx.push_back(j);
+                const int st = run_once(p, filter, idx, nullptr, nullptr, t, r);
+                if (st == GRG_E_NOMEM) {
+                    const size_t big = (j != i && b.size() > a.size()) ? j : i;
+                    if (!split(p, big)) return GRG_E_NOMEM;
+                    restart = true;
+                    break;
+                }
+                if (st) return st;
+                for (size_t q : idx) {
+                    Image &x = p->parts[q];
+                    int s2 = export_image(p, x);
+                    if (s2) return s2;
+                    if ((s2 = count_image(p, x))) return s2;
+                    x.refresh();
+                    x.last_run = r;
+                }
+                p->seen[key] = r;
+                ran = true;
+            }
+        }
+        if (restart) continue;
+        p->S.supersteps++;
+        if (!ran) return GRG_OK;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int grg_part_create(grg_part **out, grg_ctx *ctx, uint32_t num_vars, uint32_t num_parts)
+{
+    if (!out || !ctx || num_parts == 0) return GRG_E_ARG;
+    *out = nullptr;
+    grg_part *p = new grg_part;
+    p->ctx = ctx;
+    p->V = num_vars;
+    int st = grg_get_rules(ctx, &p->R, p->rules, &p->L);
+    if (st) {
+        delete p;
+        return st;
+    }
+    const uint32_t m = std::max<uint32_t>(1, std::min<uint32_t>(num_parts, std::max<uint32_t>(num_vars, 1)));
+    for (uint32_t i = 0; i < m; i++) {
+        Image x;
+        x.id = p->next_id++;
+        x.lo = (uint32_t)((uint64_t)num_vars * i / m);
+        x.hi = (uint32_t)((uint64_t)num_vars * (i + 1) / m);
+        p->parts.push_back(std::move(x));
+    }
+    *out = p;
+    return GRG_OK;
+}
+
+void grg_part_destroy(grg_part *p) { delete p; }
+
+int grg_part_load_edges(grg_part *p, uint64_t num_edges, const uint32_t *src, const uint32_t *dst,
+                        const uint8_t *label)
+{
+    if (!p || (num_edges && (!src || !dst || !label))) return GRG_E_ARG;
+    for (uint64_t e = 0; e < num_edges; e++)
+        if (src[e] >= p->V || dst[e] >= p->V) return GRG_E_RANGE;
+    // bucket the edges by source partition, then build each image on the device
+    struct Bucket { std::vector<uint32_t> s, d; std::vector<uint8_t> l; };
+    std::vector<Bucket> bk(p->parts.size());
+    std::vector<uint32_t> lo;
+    for (const Image &x : p->parts) lo.push_back(x.lo);
+    for (uint64_t e = 0; e < num_edges; e++) {
+        const size_t i = std::upper_bound(lo.begin(), lo.end(), src[e]) - lo.begin() - 1;
+        bk[i].s.push_back(src[e]);
+        bk[i].d.push_back(dst[e]);
+        bk[i].l.push_back(label[e]);
+    }
+    for (size_t i = 0; i < p->parts.size();) {
+        Image &x = p->parts[i];
+        Bucket &b0 = bk[i];
+        int st = grg_load_edges(p->ctx, p->V, b0.s.size(), b0.s.data(), b0.d.data(), b0.l.data(), 0);
+        if (st == GRG_E_NOMEM) {
+            // halve the vertex range (its image does not exist yet)
+            if (x.hi - x.lo < 2) return GRG_E_NOMEM;
+            Image b;
+            b.id = p->next_id++;
+            b.lo = x.lo + (x.hi - x.lo) / 2;
+            b.hi = x.hi;
+            x.hi = b.lo;
+            Bucket lo_b, hi_b;
+            for (size_t e = 0; e < b0.s.size(); e++) {
+                Bucket &t = b0.s[e] < b.lo ? lo_b : hi_b;
+                t.s.push_back(b0.s[e]);
+                t.d.push_back(b0.d[e]);
+                t.l.push_back(b0.l[e]);
+            }
+            bk[i] = std::move(lo_b);
+            bk.insert(bk.begin() + i + 1, std::move(hi_b));
+            p->parts.insert(p->parts.begin() + i + 1, std::move(b));
+            p->S.splits++;
+            continue;
+        }
+        if (st) return st;
+        p->S.h2d_bytes += b0.s.size() * 9;
+        if ((st = export_image(p, p->parts[i]))) return st;
+        Image &y = p->parts[i];
+        for (uint32_t &t : y.st) t = 1;
+        y.refresh();
+        y.counted = false;
+        i++;
+    }
+    p->loaded = true;
+    p->closed = false;
+    return GRG_OK;
+}
+
+int grg_part_run(grg_part *p, uint32_t filter, grg_part_stats *stats)
+{
+    if (!p || filter > 1) return GRG_E_ARG;
+    if (!p->loaded) return GRG_E_STATE;
+    if (p->closed) return GRG_E_STATE;
+    const auto t0 = std::chrono::steady_clock::now();
+    const uint64_t splits0 = p->S.splits;
+    p->S = grg_part_stats{};
+    p->S.splits = splits0;
+    bool der[GRG_MAX_LABELS + 1];
+    derivable_labels(p, filter, der);
+    bool coupled = false;
+    for (int q = 0; q < p->R; q++) {
+        const int *r = &p->rules[3 * q];
+        if (r[1] && r[2] && der[r[2]]) coupled = true;
+    }
+    p->S.schedule = coupled ? 1 : 0;
+    int st = coupled ? run_pairs(p, filter) : run_stream(p, filter, der);
+    if (st) return st;
+    // partitions whose counts predate a split are counted from their images
+    for (size_t i = 0; i < p->parts.size(); i++) {
+        Image &x = p->parts[i];
+        if (x.counted) continue;
+        if ((st = recount(p, x))) return st;
+    }
+    for (const Image &x : p->parts)
+        for (int l = 0; l < p->L; l++) p->S.total_edges += x.counts[l];
+    p->S.num_parts = (uint32_t)p->parts.size();
+    p->S.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    p->closed = true;
+    if (stats) *stats = p->S;
+    return GRG_OK;
+}
+
+int grg_part_label_counts(grg_part *p, uint64_t *counts, uint64_t *hash)
+{
+    if (!p || !counts) return GRG_E_ARG;
+    if (!p->closed) return GRG_E_STATE;
+    uint64_t h = 0;
+    for (int l = 0; l < p->L; l++) counts[l] = 0;
+    for (const Image &x : p->parts) {
+        for (int l = 0; l < p->L; l++) counts[l] += x.counts[l];
+        h += x.hash;
+    }
+    if (hash) *hash = h;
+    return GRG_OK;
+}
+
+int grg_part_bounds(grg_part *p, uint32_t cap, uint32_t *bounds, uint32_t *num_parts)
+{
+    if (!p || !num_parts) return GRG_E_ARG;
+    *num_parts = (uint32_t)p->parts.size();
+    if (cap < p->parts.size() + 1 || !bounds) return cap ? GRG_E_RANGE : GRG_OK;
+    for (size_t i = 0; i < p->parts.size(); i++) bounds[i] = p->parts[i].lo;
+    bounds[p->parts.size()] = p->parts.empty() ? 0 : p->parts.back().hi;
+    return GRG_OK;
+}
+
+}  // extern "C"

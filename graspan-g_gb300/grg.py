@@ -29,7 +29,9 @@ EXPORTS = (
     "grg_set_kernel_timing", "grg_transfer_rules", "grg_allocate_pool", "grg_load_edges", "grg_closure",
     "grg_label_counts", "grg_get_degree", "grg_set_hash", "grg_export_edges", "grg_parse_grammar",
     "grg_parse_graph_header", "grg_parse_graph", "grg_closure_noalloc", "grg_batch_begin", "grg_batch_admit",
-    "grg_batch_step", "grg_batch_result", "grg_batch_release",
+    "grg_batch_step", "grg_batch_result", "grg_batch_release", "grg_get_rules", "grg_closure_ex",
+    "grg_load_elements", "grg_export_elements", "grg_range_counts", "grg_set_pool_limit", "grg_part_create",
+    "grg_part_destroy", "grg_part_load_edges", "grg_part_run", "grg_part_label_counts", "grg_part_bounds",
 )
 
 
@@ -52,6 +54,20 @@ class Stats(ctypes.Structure):
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
         d["join_phase_cycles"] = list(d["join_phase_cycles"])
+        return d
+
+
+class PartStats(ctypes.Structure):
+    _fields_ = [
+        ("total_edges", ctypes.c_uint64), ("num_parts", ctypes.c_uint32), ("schedule", ctypes.c_uint32),
+        ("supersteps", ctypes.c_uint64), ("runs", ctypes.c_uint64), ("skipped", ctypes.c_uint64),
+        ("splits", ctypes.c_uint64), ("rounds", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64),
+        ("d2h_bytes", ctypes.c_uint64), ("ms", ctypes.c_double),
+    ]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["schedule"] = ("stream", "pairs")[d["schedule"]]
         return d
 
 
@@ -94,6 +110,19 @@ def load_library(path: str = LIB_PATH):
     L.grg_batch_step.argtypes = [P, U32, P, ctypes.POINTER(U64)]
     L.grg_batch_result.argtypes = [P, U32, U32, U32, P, ctypes.POINTER(U64)]
     L.grg_batch_release.argtypes = [P, U32]
+    L.grg_get_rules.argtypes = [P, ctypes.POINTER(I), P, ctypes.POINTER(I)]
+    L.grg_closure_ex.argtypes = [P, U32, U32, ctypes.POINTER(Stats)]
+    L.grg_load_elements.argtypes = [P, U32, U64, P, P, U32, I]
+    L.grg_export_elements.argtypes = [P, U32, U32, U64, P, P, ctypes.POINTER(U64)]
+    L.grg_range_counts.argtypes = [P, U32, U32, P, ctypes.POINTER(U64)]
+    L.grg_set_pool_limit.argtypes = [P, U64]
+    L.grg_part_create.argtypes = [ctypes.POINTER(P), P, U32, U32]
+    L.grg_part_destroy.argtypes = [P]
+    L.grg_part_destroy.restype = None
+    L.grg_part_load_edges.argtypes = [P, U64, P, P, P]
+    L.grg_part_run.argtypes = [P, U32, ctypes.POINTER(PartStats)]
+    L.grg_part_label_counts.argtypes = [P, P, ctypes.POINTER(U64)]
+    L.grg_part_bounds.argtypes = [P, U32, P, ctypes.POINTER(U32)]
     _lib = L
     return L
 
@@ -255,6 +284,42 @@ class Context:
         order = np.lexsort((dst, src, lab))
         return src[order], dst[order], lab[order]
 
+    # ---- element images (out-of-core partitions)
+    def set_pool_limit(self, pool_bytes: int):
+        self._check(self._L.grg_set_pool_limit(self._h, pool_bytes), "set_pool_limit")
+
+    def load_elements(self, num_vars, recs, stamps, mark_after=0):
+        """recs: uint32 [n, 8] element records; stamps: uint32 [n]."""
+        recs = np.ascontiguousarray(recs, dtype=np.uint32).reshape(-1, 8)
+        stamps = np.ascontiguousarray(stamps, dtype=np.uint32)
+        self._check(self._L.grg_load_elements(self._h, num_vars, len(stamps), _ptr(recs), _ptr(stamps), mark_after, 0),
+                    "load_elements")
+        self.num_vars = num_vars
+
+    def closure_ex(self, filter_flag: int, run_stamp: int) -> dict:
+        s = Stats()
+        self._check(self._L.grg_closure_ex(self._h, filter_flag, run_stamp, ctypes.byref(s)), "closure_ex")
+        return s.as_dict()
+
+    def export_elements(self, v_begin=0, v_end=None):
+        if v_end is None:
+            v_end = self.num_vars
+        n = ctypes.c_uint64()
+        st = self._L.grg_export_elements(self._h, v_begin, v_end, 0, None, None, ctypes.byref(n))
+        if st not in (OK, E_RANGE):
+            self._check(st, "export_elements")
+        recs = np.zeros((n.value, 8), np.uint32)
+        stamps = np.zeros(n.value, np.uint32)
+        self._check(self._L.grg_export_elements(self._h, v_begin, v_end, n.value, _ptr(recs), _ptr(stamps),
+                                                ctypes.byref(n)), "export_elements")
+        return recs, stamps
+
+    def range_counts(self, v_begin, v_end):
+        counts = np.zeros(self.num_labels, dtype=np.uint64)
+        h = ctypes.c_uint64()
+        self._check(self._L.grg_range_counts(self._h, v_begin, v_end, _ptr(counts), ctypes.byref(h)), "range_counts")
+        return counts, h.value
+
 
 def run_closure(num_vars, rules, num_labels, filter_flag, src, dst, lab, device=0, pool_bytes=0, timing=False):
     """Convenience: one context, one closure. Returns (context, stats)."""
@@ -265,6 +330,51 @@ def run_closure(num_vars, rules, num_labels, filter_flag, src, dst, lab, device=
     ctx.load_edges(num_vars, src, dst, lab)
     stats = ctx.closure(filter_flag)
     return ctx, stats
+
+
+class Partitioned:
+    """Out-of-core closure over vertex-range partitions (grg_part_*) on a
+    context that holds the grammar (and, optionally, a pool limit)."""
+
+    def __init__(self, ctx: Context, num_vars: int, num_parts: int):
+        self.ctx = ctx
+        self.num_vars = num_vars
+        h = ctypes.c_void_p()
+        ctx._check(ctx._L.grg_part_create(ctypes.byref(h), ctx._h, num_vars, num_parts), "part_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.ctx._L.grg_part_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def load_edges(self, src, dst, lab):
+        src = np.ascontiguousarray(src, dtype=np.uint32)
+        dst = np.ascontiguousarray(dst, dtype=np.uint32)
+        lab = np.ascontiguousarray(lab, dtype=np.uint8)
+        self.ctx._check(self.ctx._L.grg_part_load_edges(self._h, len(src), _ptr(src), _ptr(dst), _ptr(lab)),
+                        "part_load_edges")
+
+    def run(self, filter_flag: int) -> dict:
+        s = PartStats()
+        self.ctx._check(self.ctx._L.grg_part_run(self._h, filter_flag, ctypes.byref(s)), "part_run")
+        return s.as_dict()
+
+    def label_counts(self):
+        counts = np.zeros(self.ctx.num_labels, dtype=np.uint64)
+        h = ctypes.c_uint64()
+        self.ctx._check(self.ctx._L.grg_part_label_counts(self._h, _ptr(counts), ctypes.byref(h)), "part_label_counts")
+        return counts, h.value
+
+    def bounds(self):
+        n = ctypes.c_uint32()
+        self.ctx._check(self.ctx._L.grg_part_bounds(self._h, 0, None, ctypes.byref(n)), "part_bounds")
+        b = np.zeros(n.value + 1, np.uint32)
+        self.ctx._check(self.ctx._L.grg_part_bounds(self._h, len(b), _ptr(b), ctypes.byref(n)), "part_bounds")
+        return b
 
 
 class Batch:

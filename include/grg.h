@@ -60,8 +60,8 @@ typedef struct grg_stats {
     double join_ms;                /* sum of join-kernel durations (when kernel timing is on) */
     uint64_t join_launches;        /* join-kernel launches (first pass + retries) */
     uint64_t kernel_launches;      /* all kernel launches of the closure */
-    uint64_t join_phase_cycles[5]; /* join-kernel cycles per phase (record load, unary+reverse,
-                                      binary join, flush, old-left) when built with
+    uint64_t join_phase_cycles[5]; /* join-kernel cycles per phase (record load, unary,
+                                      binary join, flush, retry list) when built with
                                       -DGRG_PHASE_TIMERS; 0 otherwise */
 } grg_stats;
 
@@ -86,6 +86,8 @@ int grg_set_kernel_timing(grg_ctx *ctx, int on);
  * (src/kernel.cu:22-31), which takes rules from readAndTransferRules
  * (src/main.cpp:69-97). The caller keeps ownership of rules. */
 int grg_transfer_rules(grg_ctx *ctx, int num_rules, const int *rules, int num_labels);
+/* The context's grammar as given to grg_transfer_rules (rules: 3*GRG_MAX_RULES ints). */
+int grg_get_rules(const grg_ctx *ctx, int *num_rules, int *rules, int *num_labels);
 
 /* Reserve the element pool: pool_bytes of device memory for 32-byte elements
  * plus their delta bitmaps (0 = size it from the free device memory).
@@ -111,6 +113,13 @@ int grg_load_edges(grg_ctx *ctx, uint32_t num_vars, uint64_t num_edges, const ui
  * (src/kernel.cu:466-780, 943-985). stats may be NULL. */
 int grg_closure(grg_ctx *ctx, uint32_t filter, grg_stats *stats);
 
+/* grg_closure for a graph loaded with grg_load_elements: the round-1 deltas
+ * are the records marked at the load, and every element that gains bits
+ * during this closure gets stamp run_stamp (0 = stamps unchanged). One call
+ * closes the loaded vertex ranges together, like one spagpu_s/spagpu_b/spagpu
+ * pass over a partition or a pair of partitions (src/kernel.cu:466-780). */
+int grg_closure_ex(grg_ctx *ctx, uint32_t filter, uint32_t run_stamp, grg_stats *stats);
+
 /* Per-label closure edge counts: counts[l-1] for label l (num_labels values). */
 int grg_label_counts(grg_ctx *ctx, uint64_t *counts);
 
@@ -129,6 +138,75 @@ int grg_set_hash(grg_ctx *ctx, uint64_t *hash);
  * most cap are written. */
 int grg_export_edges(grg_ctx *ctx, uint64_t cap, uint32_t *src, uint32_t *dst, uint8_t *label,
                      uint64_t *num_out);
+
+/* ---- Element images: the pool contents of a vertex range, for out-of-core
+ * schedules. An image is num_elems records of 8 uint32 words (words 0-5: bitmap
+ * of 192 destination ids base*192.., word 6: label << 25 | base, word 7: source
+ * vertex) plus one uint32 stamp per record. Replaces transferElements
+ * (src/kernel.cu:42-52) and transferBackElements (src/main.cpp:477-483),
+ * whose images are raw pool words with linked-list heads. */
+
+/* Load a graph over [0, num_vars) from element records (no epsilon rules are
+ * applied: images already hold their epsilon edges). Records whose stamp is
+ * above mark_after are the deltas of round 1 of the next grg_closure_ex.
+ * Records must be distinct per (label, source, base); out-of-range or repeated
+ * records fail with GRG_E_ARG. on_device as for grg_load_edges. */
+int grg_load_elements(grg_ctx *ctx, uint32_t num_vars, uint64_t num_elems, const uint32_t *elems,
+                      const uint32_t *stamps, uint32_t mark_after, int on_device);
+/* Image of source vertices [v_begin, v_end), all labels, into HOST arrays of
+ * cap records (8 words each) and cap stamps. *num_out = records in the range;
+ * GRG_E_RANGE (nothing written) when that exceeds cap. */
+int grg_export_elements(grg_ctx *ctx, uint32_t v_begin, uint32_t v_end, uint64_t cap, uint32_t *elems,
+                        uint32_t *stamps, uint64_t *num_out);
+/* Per-label edge counts (num_labels values) and edge-set hash (may be NULL;
+ * same hash terms as grg_set_hash) of the rows [v_begin, v_end). */
+int grg_range_counts(grg_ctx *ctx, uint32_t v_begin, uint32_t v_end, uint64_t *counts, uint64_t *hash);
+/* Cap the element pool at pool_bytes of device memory (0 = no cap): a load or
+ * closure that needs more fails with GRG_E_NOMEM instead of growing the pool.
+ * A pool already larger is freed (the loaded graph is dropped). */
+int grg_set_pool_limit(grg_ctx *ctx, uint64_t pool_bytes);
+
+/* ---- Out-of-core closure over vertex-range partitions (host scheduler on
+ * the calls above). Replaces the reference's partitioned driver: partition
+ * set-up (src/main.cpp:141-175), precomputation / run_computation supersteps
+ * over partition pairs (src/main.cpp:764-858), repartitioning
+ * (src/main.cpp:633-762) and the partition spill files (src/main.cpp:447-456,
+ * 602-610). Partition images live in host memory; the device holds one pair
+ * of partitions (or, when every binary rule's second symbol is never derived,
+ * the static labels of the whole graph plus one partition) at a time, within
+ * the context's pool limit (grg_set_pool_limit). A partition whose run does
+ * not fit is split in two at its median element and the run is repeated. */
+typedef struct grg_part grg_part;
+typedef struct {
+    uint64_t total_edges;     /* closure edges, all labels */
+    uint32_t num_parts;       /* partitions at the end (after splits) */
+    uint32_t schedule;        /* 0 = stream (independent rows), 1 = pairs */
+    uint64_t supersteps;      /* sweeps over the partition pairs (pairs schedule) */
+    uint64_t runs;            /* closures run on the device */
+    uint64_t skipped;         /* pairs skipped: nothing new since their last run */
+    uint64_t splits;          /* partitions split because a run did not fit */
+    uint64_t rounds;          /* semi-naive rounds over all runs */
+    uint64_t h2d_bytes;       /* image bytes loaded to the device */
+    uint64_t d2h_bytes;       /* image bytes read back */
+    double ms;                /* wall time of grg_part_run */
+} grg_part_stats;
+
+/* A partitioned graph over [0, num_vars) on context ctx (which holds the
+ * grammar, from grg_transfer_rules, and the pool limit), split into num_parts
+ * vertex ranges of equal size (at least 1 vertex each). */
+int grg_part_create(grg_part **part, grg_ctx *ctx, uint32_t num_vars, uint32_t num_parts);
+void grg_part_destroy(grg_part *part);
+/* Input edges (HOST arrays) with the conventions of grg_load_edges; builds the
+ * partition images on the device one partition at a time. */
+int grg_part_load_edges(grg_part *part, uint64_t num_edges, const uint32_t *src, const uint32_t *dst,
+                        const uint8_t *label);
+/* Close the graph (filter as for grg_closure). stats may be NULL. */
+int grg_part_run(grg_part *part, uint32_t filter, grg_part_stats *stats);
+/* Per-label closure edge counts (num_labels values) and the edge-set hash
+ * (may be NULL), equal to grg_label_counts / grg_set_hash of the in-core closure. */
+int grg_part_label_counts(grg_part *part, uint64_t *counts, uint64_t *hash);
+/* Current partition bounds: bounds[0..num_parts] (cap entries at most). */
+int grg_part_bounds(grg_part *part, uint32_t cap, uint32_t *bounds, uint32_t *num_parts);
 
 /* Text formats (host). Grammar: readAndTransferRules (src/main.cpp:60-97);
  * names must hold GRG_MAX_LABELS*GRG_NAME_LEN bytes, label l at
