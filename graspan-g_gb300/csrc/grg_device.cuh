@@ -51,8 +51,14 @@ enum : int {
     C_CAND_N = 16,    // candidate elements written by joins for k_apply
     C_AFAIL = 17,     // candidates k_apply could not insert (tables to grow)
     C_VN = 18,        // virtual old-left records written
+    C_HALT = 19,      // device-driven rounds: why the round loop stopped (0 = running)
+    C_ITERS = 20,     // device-driven round iterations started
+    C_GROUNDS = 21,   // device-driven rounds that had delta records
+    C_GDSUM = 22,     // delta records of those rounds
+    C_JNS = 23,       // join-pass nanoseconds of those rounds (with kernel timing)
     C_LABEL0 = 24,    // per-label edge counts: C_LABEL0 + slot
-    NCTR = C_LABEL0 + MAX_SLOTS + 2
+    C_JT0 = C_LABEL0 + MAX_SLOTS + 2,   // start time of the current join pass (device-driven rounds)
+    NCTR = C_LABEL0 + MAX_SLOTS + 3
 };
 enum : unsigned long long { ERR_POOL = 1, ERR_LOAD = 2, ERR_INTERNAL = 4 };
 

@@ -296,8 +296,18 @@ __global__ void k_mark_all(Dev d, uint64_t begin, uint64_t end)   // begin: mult
 // ---------------------------------------------------------------- rounds
 
 // Dirty records per chunk of 1024 slots (one warp per chunk of 32 bitmap words).
-__global__ void k_dcount(Dev d, uint64_t nwords, uint32_t *chunk_cnt)
+// Dirty-bitmap words below the pool top. Launches recorded once and replayed
+// (round graphs, dyn != 0) read the top from the device counter, bounded by
+// nwords = the words the buffers were sized for; others get the host's figure.
+__device__ __forceinline__ uint64_t dyn_words(uint64_t nwords, const unsigned long long *ctr, int dyn)
 {
+    return dyn ? min(nwords, (uint64_t)(ctr[C_POOL_TOP] + 31) / 32) : nwords;
+}
+
+__global__ void k_dcount(Dev d, uint64_t nwords, uint32_t *chunk_cnt, int dyn)
+{
+    if (d.ctr[C_HALT]) return;
+    nwords = dyn_words(nwords, d.ctr, dyn);
     const uint64_t nchunks = (nwords + 31) / 32;
     const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
     for (uint64_t c = blockIdx.x * (uint64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); c < nchunks; c += nwarps) {
@@ -325,8 +335,10 @@ __device__ __forceinline__ uint32_t select32(uint32_t w, uint32_t n)
 // chunk of 32 bitmap words; lanes take consecutive dirty slots of the chunk, so
 // the copies of a warp are independent and mostly coalesced.
 __global__ void k_gather(Dev d, uint64_t nwords, const uint32_t *__restrict__ chunk_off, uint4 *out,
-                         const uint32_t *__restrict__ row_job, uint32_t *job_cnt, uint32_t run_stamp)
+                         const uint32_t *__restrict__ row_job, uint32_t *job_cnt, uint32_t run_stamp, int dyn)
 {
+    if (d.ctr[C_HALT]) return;
+    nwords = dyn_words(nwords, d.ctr, dyn);
     const uint64_t nchunks = (nwords + 31) / 32;
     const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
     const uint32_t lane = lane_id();
@@ -395,6 +407,7 @@ __global__ void k_gather(Dev d, uint64_t nwords, const uint32_t *__restrict__ ch
 // exactly 6 words of the dirty-vertex bitmap. Records past cap are counted only.
 __global__ void k_oldleft(Dev d, uint32_t q, uint4 *out, uint64_t cap)
 {
+    if (d.ctr[C_HALT]) return;
     const uint32_t B = c_rt.ol_B[q], C = c_rt.ol_C[q];
     const uint32_t *dv = d.dvm + (size_t)(C - 1) * d.vwords;
     const uint32_t vkey = (OL_SLOT0 + q) << KEY_SHIFT;
@@ -641,6 +654,7 @@ __device__ __forceinline__ void win_flush(const Dev &d, WarpSmem &w, uint32_t &i
 // Candidates whose table is full go to fail_out (C_AFAIL) for a retry after growth.
 __global__ void __launch_bounds__(256) k_apply(Dev d, const uint4 *__restrict__ cand, uint4 *fail_out)
 {
+    if (d.ctr[C_HALT]) return;
     // the candidate count is read on the device, so the host need not wait for the join
     const uint64_t n = min((uint64_t)d.ctr[C_CAND_N], d.cand_cap);
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -661,9 +675,12 @@ __global__ void __launch_bounds__(256) k_apply(Dev d, const uint4 *__restrict__ 
 // owns record r for per-record work, and (record, k) tasks and their right-hand
 // items are flattened over the lanes so every phase keeps 32 independent memory
 // operations in flight.
+// n_ctr >= 0: the record count is device counter n_ctr (round graphs).
 __global__ void __launch_bounds__(JOIN_WARPS * 32, GRG_JOIN_MINB) k_join(Dev d, const uint4 *__restrict__ recs,
-                                                                        uint64_t n, uint4 *retry_out)
+                                                                        uint64_t n, int n_ctr, uint4 *retry_out)
 {
+    if (d.ctr[C_HALT]) return;
+    if (n_ctr >= 0) n = d.ctr[n_ctr];
     __shared__ WarpSmem smem[JOIN_WARPS];
     WarpSmem &w = smem[threadIdx.x >> 5];
     const uint32_t lane = lane_id();
@@ -904,8 +921,19 @@ __global__ void k_csr_count(Dev d, uint32_t slot, uint32_t *deg, uint2 *row)
 }
 
 // Block-wise exclusive scan of n values (1024 per block); block totals to sums.
-__global__ void k_scan_blocks(const uint32_t *in, uint32_t *out, uint32_t *sums, uint64_t n)
+// dyn != null: a scan of the gather's chunk counts whose length follows the
+// pool top in the device counters (round graphs), at most n; blocks past it return.
+__device__ __forceinline__ uint64_t dyn_chunks(uint64_t n, const unsigned long long *dyn)
 {
+    return dyn ? min(n, (uint64_t)(dyn[C_POOL_TOP] + 1023) / 1024) : n;
+}
+
+__global__ void k_scan_blocks(const uint32_t *in, uint32_t *out, uint32_t *sums, uint64_t n,
+                              const unsigned long long *dyn)
+{
+    if (dyn && dyn[C_HALT]) return;
+    n = dyn_chunks(n, dyn);
+    if (blockIdx.x * 1024ull >= n && n) return;
     __shared__ uint32_t wsum[32];
     const uint64_t i = blockIdx.x * 1024ull + threadIdx.x;
     const uint32_t v = i < n ? in[i] : 0;
@@ -931,8 +959,10 @@ __global__ void k_scan_blocks(const uint32_t *in, uint32_t *out, uint32_t *sums,
 }
 
 // Exclusive scan of the block totals (one block, sequential over chunks of 1024); total at sums[nb].
-__global__ void k_scan_sums(uint32_t *sums, uint64_t nb)
+__global__ void k_scan_sums(uint32_t *sums, uint64_t nb, const unsigned long long *dyn)
 {
+    if (dyn && dyn[C_HALT]) return;
+    if (dyn) nb = min(nb, (dyn_chunks(~0ull, dyn) + 1023) / 1024);
     __shared__ uint32_t wsum[32];
     __shared__ uint32_t carry;
     if (threadIdx.x == 0) carry = 0;
@@ -966,8 +996,10 @@ __global__ void k_scan_sums(uint32_t *sums, uint64_t nb)
     if (threadIdx.x == 0) sums[nb] = carry;
 }
 
-__global__ void k_scan_add(uint32_t *out, const uint32_t *sums, uint64_t n)
+__global__ void k_scan_add(uint32_t *out, const uint32_t *sums, uint64_t n, const unsigned long long *dyn)
 {
+    if (dyn && dyn[C_HALT]) return;
+    n = dyn_chunks(n, dyn);
     const uint64_t i = blockIdx.x * 1024ull + threadIdx.x;
     if (i < n) out[i] += sums[blockIdx.x];
 }
@@ -1314,6 +1346,13 @@ struct grg_ctx {
     uint32_t *xst = nullptr;               // staged stamps
     uint64_t xcap = 0;
     uint64_t pool_limit = 0;               // maximum pool slots (0 = what the device holds)
+    // device-driven rounds: a CUDA graph whose WHILE node repeats one closure round
+    bool device_rounds = true;
+    cudaStream_t cap_stream = nullptr;     // stream the round graph is recorded on
+    cudaGraph_t rg_graph = nullptr;
+    cudaGraphExec_t rg_exec = nullptr;
+    std::vector<uint64_t> rg_key;          // pointers and sizes the recorded launches hold
+    int rg_kernels = 0;                    // kernels per recorded round
     RuleTable rt{};
     uint64_t launches = 0;
     std::vector<uint32_t *> csr_bufs;      // CSR copies of static labels (freed on reload)
@@ -1327,6 +1366,8 @@ struct grg_ctx {
     struct JobRange { uint32_t base = 0, nv = 0; bool active = false; uint32_t pending = 0xFFFFFFFFu; };
     std::vector<JobRange> jobs;
 };
+
+static void free_round_graph(grg_ctx *c);
 
 namespace {
 
@@ -1599,6 +1640,8 @@ int grg_create(grg_ctx **out, int device)
         return GRG_E_CUDA;
     }
     c->stream = c->own_stream;
+    const char *dr = getenv("GRG_DEVICE_ROUNDS");      // "0": every round driven from the host
+    c->device_rounds = !(dr && dr[0] == '0');
     *out = c;
     return GRG_OK;
 }
@@ -1626,6 +1669,8 @@ void grg_destroy(grg_ctx *c)
     if (c->ev_b) cudaEventDestroy(c->ev_b);
     if (c->ev_c) cudaEventDestroy(c->ev_c);
     if (c->ev_d) cudaEventDestroy(c->ev_d);
+    free_round_graph(c);
+    if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
 }
@@ -1636,6 +1681,13 @@ int grg_set_stream(grg_ctx *c, void *stream)
 {
     if (!c) return GRG_E_ARG;
     c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    return GRG_OK;
+}
+
+int grg_set_device_rounds(grg_ctx *c, int on)
+{
+    if (!c) return GRG_E_ARG;
+    c->device_rounds = on != 0;
     return GRG_OK;
 }
 
@@ -1910,156 +1962,439 @@ int grg_load_elements(grg_ctx *c, uint32_t num_vars, uint64_t num_elems, const u
     return GRG_OK;
 }
 
-// Semi-naive rounds: gather the dirty slots of the last round into delta
-// records, join them, insert the candidates. Stops when a gather finds no delta
-// (the fixpoint: *idle = true) or after max_rounds rounds (0 = no limit).
+}  // extern "C"
+
+// Semi-naive rounds on the host's side: gather the dirty slots of the last
+// round into delta records, join them, insert the candidates, re-run what did
+// not fit after growing its tables. The pieces are separate so a round the
+// device-driven loop hands back can be finished where it stopped.
+
+// Round head: count and gather the dirty slots (rs: stamp for elements that
+// gained bits, 0 = none). *nd = delta records (0 = fixpoint).
+static int round_head(grg_ctx *c, uint32_t rs, grg_stats &S, uint64_t *nd_out)
+{
+    cudaStream_t s = c->stream;
+    if (c->job_cnt) GRG_CUDA(c, cudaMemsetAsync(c->job_cnt, 0, (size_t)c->max_jobs * 4, s));
+    // the pool top is the one read after the last growth
+    const uint64_t nwords = (c->h_ctr[C_POOL_TOP] + 31) / 32;
+    const uint64_t nchunks = (nwords + 31) / 32;
+    int st = ensure_chunks(c, nchunks);
+    if (st) return st;
+    uint32_t *ccnt = c->chunk, *coff = c->chunk + nchunks + 1, *csum = c->chunk + 2 * (nchunks + 1);
+    const uint64_t nb = (nchunks + 1023) / 1024;
+    Dev d = make_dev(c);
+    k_dcount<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, ccnt, 0);
+    k_scan_blocks<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(ccnt, coff, csum, nchunks, nullptr);
+    k_scan_sums<<<1, 1024, 0, s>>>(csum, nb, nullptr);
+    k_scan_add<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(coff, csum, nchunks, nullptr);
+    c->launches += 4;
+    GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_DIRTY_N, 0, 8, s));
+    GRG_CUDA(c, cudaMemcpyAsync(c->ctr + C_DIRTY_N, csum + nb, 4, cudaMemcpyDeviceToDevice, s));
+    GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_RETRY_N, 0, 16, s));   // retry + grow counters
+    GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_CAND_N, 0, 16, s));    // candidates + failed candidates
+    st = read_ctr(c);
+    if (st) return st;
+    const uint64_t nd = c->h_ctr[C_DIRTY_N];
+    *nd_out = nd;
+    if (nd == 0) return GRG_OK;
+    st = ensure_buf(c, &c->gbuf, &c->gbuf_cap, nd);
+    if (st) return st;
+    st = ensure_cand(c, nd);
+    if (st) return st;
+    S.rounds++;
+    S.delta_elems += nd;
+    c->cb = 0;
+    d = make_dev(c);
+    // the delta index of the last round is cleared for the labels old-left joins read
+    for (int l = 1; l <= c->L; l++)
+        if (c->rt.dindex[l]) {
+            const size_t t0 = (size_t)(l - 1) * c->V, vw = (c->V + 31) / 32;
+            GRG_CUDA(c, cudaMemsetAsync(c->drs + t0, 0xFF, (size_t)c->V * 4, s));
+            GRG_CUDA(c, cudaMemsetAsync(c->drc + t0, 0, (size_t)c->V * 4, s));
+            GRG_CUDA(c, cudaMemsetAsync(c->dvm + (size_t)(l - 1) * vw, 0, vw * 4, s));
+        }
+    k_gather<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->gbuf, c->row_job, c->job_cnt, rs, 0);
+    c->launches++;
+    return GRG_OK;
+}
+
+// Old-left joins: virtual records of O_B masked to the vertices with deltas of C.
+static int round_oldleft(grg_ctx *c, uint64_t *nv_out)
+{
+    cudaStream_t s = c->stream;
+    uint64_t nv = 0;
+    if (c->rt.nol) {
+        for (int attempt = 0; attempt < 2; attempt++) {
+            Dev d = make_dev(c);
+            GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_VN, 0, 8, s));
+            for (int q = 0; q < c->rt.nol; q++) {
+                k_oldleft<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)q, c->vbuf, c->vbuf_cap);
+                c->launches++;
+            }
+            int st = read_ctr(c);
+            if (st) return st;
+            nv = c->h_ctr[C_VN];
+            if (nv <= c->vbuf_cap) break;
+            st = ensure_buf(c, &c->vbuf, &c->vbuf_cap, nv);
+            if (st) return st;
+        }
+    }
+    *nv_out = nv;
+    return GRG_OK;
+}
+
+// Tables that overflowed grow (the pool too, when it is full); then the failed
+// records (rbuf[0]) and failed candidates (cand[cb ^ 1]) of the round's first
+// pass are re-run until nothing fails.
+static int round_retries(grg_ctx *c, uint64_t nr, uint64_t nf, grg_stats &S, double &join_ms, uint64_t &joins)
+{
+    cudaStream_t s = c->stream;
+    int rb = 0;    // the failed records of the last pass are in rbuf[rb]
+    for (int pass = 1;; pass++) {
+        if (nr == 0 && nf == 0) return GRG_OK;
+        S.retry_records += nr + nf;
+        Dev d = make_dev(c);
+        for (int gtry = 0;; gtry++) {
+            const uint64_t ng = c->h_ctr[C_GROW_N];
+            GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_ERR, 0, 8, s));
+            k_grow<<<grid_for(c, ng * 32, 256), 256, 0, s>>>(d, ng);
+            c->launches++;
+            S.grow_rows += ng;
+            int st = read_ctr(c);
+            if (st) return st;
+            if (!(c->h_ctr[C_ERR] & ERR_POOL)) break;
+            if (gtry > 16) return fail(c, GRG_E_NOMEM, "element pool exhausted");
+            st = grow_pool(c, c->pool_cap * 2);
+            if (st) return st;
+            d = make_dev(c);
+        }
+        if (pass > 64) return fail(c, GRG_E_CUDA, "table growth did not converge");
+        // failed candidates (in cand[cb^1]) become the candidate list; join retries append to it
+        c->cb ^= 1;
+        d = make_dev(c);
+        c->h_ctr[C_CAND_N] = nf;
+        GRG_CUDA(c, cudaMemcpyAsync(c->ctr + C_CAND_N, c->h_ctr + C_CAND_N, 8, cudaMemcpyHostToDevice, s));
+        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_AFAIL, 0, 8, s));
+        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_RETRY_N, 0, 16, s));
+        if (c->timing) GRG_CUDA(c, cudaEventRecord(c->ev_c, s));
+        if (nr) {
+            k_join<<<grid_for(c, (nr + RB - 1) / RB, JOIN_WARPS, 16), JOIN_WARPS * 32, 0, s>>>(d, c->rbuf[rb], nr, -1,
+                                                                                             c->rbuf[rb ^ 1]);
+            c->launches++;
+            joins++;
+        }
+        if (c->cand_cap) {
+            k_apply<<<c->sms * 8, 256, 0, s>>>(d, c->cand[c->cb], c->cand[c->cb ^ 1]);
+            c->launches++;
+        }
+        if (c->timing) GRG_CUDA(c, cudaEventRecord(c->ev_d, s));
+        GRG_CUDA(c, cudaGetLastError());
+        int st = read_ctr(c);
+        if (st) return st;
+        if (c->timing) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, c->ev_c, c->ev_d);
+            join_ms += ms;
+        }
+        if (nr) rb ^= 1;
+        nr = c->h_ctr[C_RETRY_N];
+        nf = c->cand_cap ? c->h_ctr[C_AFAIL] : 0;
+    }
+}
+
+// First join pass of a round over its nd gathered and nv virtual records, then retries.
+static int round_joins(grg_ctx *c, uint64_t nd, uint64_t nv, grg_stats &S, double &join_ms, uint64_t &joins)
+{
+    cudaStream_t s = c->stream;
+    int st = ensure_rbuf(c, nd + nv);
+    if (st) return st;
+    Dev d = make_dev(c);
+    if (c->timing) GRG_CUDA(c, cudaEventRecord(c->ev_c, s));
+    k_join<<<grid_for(c, (nd + RB - 1) / RB, JOIN_WARPS, 16), JOIN_WARPS * 32, 0, s>>>(d, c->gbuf, nd, -1, c->rbuf[0]);
+    c->launches++;
+    joins++;
+    if (nv) {
+        k_join<<<grid_for(c, (nv + RB - 1) / RB, JOIN_WARPS, 16), JOIN_WARPS * 32, 0, s>>>(d, c->vbuf, nv, -1,
+                                                                                         c->rbuf[0]);
+        c->launches++;
+        joins++;
+    }
+    // insert the candidates the joins wrote (count read on the device)
+    if (c->cand_cap) {
+        k_apply<<<c->sms * 8, 256, 0, s>>>(d, c->cand[c->cb], c->cand[c->cb ^ 1]);
+        c->launches++;
+    }
+    if (c->timing) GRG_CUDA(c, cudaEventRecord(c->ev_d, s));
+    GRG_CUDA(c, cudaGetLastError());
+    st = read_ctr(c);
+    if (st) return st;
+    if (c->timing) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c->ev_c, c->ev_d);
+        join_ms += ms;
+    }
+    return round_retries(c, c->h_ctr[C_RETRY_N], c->cand_cap ? c->h_ctr[C_AFAIL] : 0, S, join_ms, joins);
+}
+
+// ---------------------------------------------------------------- device-driven rounds
+//
+// After the first round, closure rounds run from a CUDA graph whose WHILE node
+// repeats one round -- count/scan/gather, old-left records, joins, apply --
+// with every size read on the device, so the host neither waits nor launches
+// per round. Gate kernels end the loop when the host is needed: the fixpoint,
+// a buffer too small for the round, or tables to grow (the rare retry path);
+// the host then finishes that round with the functions above and relaunches.
+
+enum : unsigned long long { HALT_FIXPOINT = 1, HALT_CAPACITY = 2, HALT_OLDLEFT = 3, HALT_RETRY = 4, HALT_LIMIT = 5 };
+constexpr uint64_t GATE_MAX_ITERS = 1u << 20;   // iterations of one graph launch; past it the host takes over
+
+__global__ void k_gate_gather(unsigned long long *ctr, const uint32_t *csum, uint64_t max_chunks, uint64_t gbuf_cap,
+                              uint64_t rbuf_cap, uint64_t max_iters, cudaGraphConditionalHandle h)
+{
+    if (threadIdx.x != 0) return;
+    const unsigned long long it = ++ctr[C_ITERS];
+    if (ctr[C_HALT] || it > max_iters) {
+        if (!ctr[C_HALT]) ctr[C_HALT] = HALT_LIMIT;
+        cudaGraphSetConditional(h, 0);
+        return;
+    }
+    const uint64_t nb = (dyn_chunks(max_chunks, ctr) + 1023) / 1024;
+    const uint64_t nd = csum[nb];
+    ctr[C_DIRTY_N] = nd;
+    const unsigned long long halt = nd == 0 ? HALT_FIXPOINT : (nd > gbuf_cap || nd > rbuf_cap) ? HALT_CAPACITY : 0;
+    if (halt) {
+        ctr[C_HALT] = halt;                  // later kernels of this iteration return at once
+        cudaGraphSetConditional(h, 0);
+        return;
+    }
+    ctr[C_GROUNDS]++;
+    ctr[C_GDSUM] += nd;
+}
+
+__global__ void k_gate_oldleft(unsigned long long *ctr, uint64_t vbuf_cap, uint64_t rbuf_cap,
+                               cudaGraphConditionalHandle h)
+{
+    if (threadIdx.x != 0 || ctr[C_HALT]) return;
+    const uint64_t nv = ctr[C_VN];
+    if (nv > vbuf_cap || ctr[C_DIRTY_N] + nv > rbuf_cap) {
+        ctr[C_HALT] = HALT_OLDLEFT;
+        cudaGraphSetConditional(h, 0);
+    }
+}
+
+__global__ void k_gate_end(unsigned long long *ctr, cudaGraphConditionalHandle h)
+{
+    if (threadIdx.x != 0 || ctr[C_HALT]) return;
+    if (ctr[C_RETRY_N] || ctr[C_AFAIL]) {
+        ctr[C_HALT] = HALT_RETRY;
+        cudaGraphSetConditional(h, 0);
+    }
+}
+
+// Join-pass time of device-driven rounds (kernel timing on): global nanosecond timer.
+__global__ void k_tmark(unsigned long long *ctr, int end)
+{
+    if (threadIdx.x != 0 || ctr[C_HALT]) return;
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (!end)
+        ctr[C_JT0] = t;
+    else
+        ctr[C_JNS] += t - ctr[C_JT0];
+}
+
+static void free_round_graph(grg_ctx *c)
+{
+    if (c->rg_exec) cudaGraphExecDestroy(c->rg_exec);
+    if (c->rg_graph) cudaGraphDestroy(c->rg_graph);
+    c->rg_exec = nullptr;
+    c->rg_graph = nullptr;
+    c->rg_key.clear();
+}
+
+// Everything the recorded launches hold by value.
+static std::vector<uint64_t> round_graph_key(const grg_ctx *c, uint32_t rs, uint64_t nchunks)
+{
+    std::vector<uint64_t> k = {(uint64_t)c->elems, (uint64_t)c->dbits, (uint64_t)c->dmap, (uint64_t)c->stamp,
+                               (uint64_t)c->desc, (uint64_t)c->cnt, (uint64_t)c->want, (uint64_t)c->grow,
+                               (uint64_t)c->gbuf, c->gbuf_cap, (uint64_t)c->vbuf, c->vbuf_cap,
+                               (uint64_t)c->rbuf[0], (uint64_t)c->rbuf[1], c->rbuf_cap, (uint64_t)c->cand[0],
+                               (uint64_t)c->cand[1], c->cand_cap, (uint64_t)c->chunk, nchunks, (uint64_t)c->drs,
+                               (uint64_t)c->drc, (uint64_t)c->dvm, c->pool_cap, c->V, rs, (uint64_t)c->timing,
+                               (uint64_t)c->elem_loaded, (uint64_t)c->rt.nol};
+    for (int l = 1; l <= c->L; l++) k.push_back(c->rt.dindex[l]);
+    return k;
+}
+
+static int build_round_graph(grg_ctx *c, uint32_t rs)
+{
+    const uint64_t nwords = c->pool_cap / 32 + 2, nchunks = (nwords + 31) / 32, nb = (nchunks + 1023) / 1024;
+    int st = ensure_chunks(c, nchunks);
+    if (st) return st;
+    std::vector<uint64_t> key = round_graph_key(c, rs, nchunks);
+    if (c->rg_exec && key == c->rg_key) return GRG_OK;
+    free_round_graph(c);
+    if (!c->cap_stream) GRG_CUDA(c, cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking));
+    cudaStream_t s = c->cap_stream;
+    GRG_CUDA(c, cudaGraphCreate(&c->rg_graph, 0));
+    cudaGraphConditionalHandle h;
+    GRG_CUDA(c, cudaGraphConditionalHandleCreate(&h, c->rg_graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    GRG_CUDA(c, cudaGraphAddNode(&node, c->rg_graph, nullptr, nullptr, 0, &p));
+    cudaGraph_t body = p.conditional.phGraph_out[0];
+    GRG_CUDA(c, cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    const int saved_cb = c->cb;
+    c->cb = 0;
+    Dev d = make_dev(c);
+    c->cb = saved_cb;
+    uint32_t *ccnt = c->chunk, *coff = c->chunk + nchunks + 1, *csum = c->chunk + 2 * (nchunks + 1);
+    unsigned long long *ctr = c->ctr;
+    int nk = 0;
+    cudaMemsetAsync(ctr + C_RETRY_N, 0, 16, s);
+    cudaMemsetAsync(ctr + C_CAND_N, 0, 16, s);
+    k_dcount<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, ccnt, 1);
+    k_scan_blocks<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(ccnt, coff, csum, nchunks, ctr);
+    k_scan_sums<<<1, 1024, 0, s>>>(csum, nb, ctr);
+    k_scan_add<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(coff, csum, nchunks, ctr);
+    k_gate_gather<<<1, 32, 0, s>>>(ctr, csum, nchunks, c->gbuf_cap, c->rbuf_cap, GATE_MAX_ITERS, h);
+    nk += 5;
+    for (int l = 1; l <= c->L; l++)
+        if (c->rt.dindex[l]) {
+            const size_t t0 = (size_t)(l - 1) * c->V, vw = (c->V + 31) / 32;
+            cudaMemsetAsync(c->drs + t0, 0xFF, (size_t)c->V * 4, s);
+            cudaMemsetAsync(c->drc + t0, 0, (size_t)c->V * 4, s);
+            cudaMemsetAsync(c->dvm + (size_t)(l - 1) * vw, 0, vw * 4, s);
+        }
+    cudaMemsetAsync(ctr + C_VN, 0, 8, s);
+    k_gather<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->gbuf, nullptr, nullptr, rs, 1);
+    nk++;
+    if (c->rt.nol) {
+        for (int q = 0; q < c->rt.nol; q++)
+            k_oldleft<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)q, c->vbuf, c->vbuf_cap);
+        k_gate_oldleft<<<1, 32, 0, s>>>(ctr, c->vbuf_cap, c->rbuf_cap, h);
+        nk += c->rt.nol + 1;
+    }
+    if (c->timing) {
+        k_tmark<<<1, 32, 0, s>>>(ctr, 0);
+        nk++;
+    }
+    const int jgrid = grid_for(c, ~0u, JOIN_WARPS, 16);
+    k_join<<<jgrid, JOIN_WARPS * 32, 0, s>>>(d, c->gbuf, 0, C_DIRTY_N, c->rbuf[0]);
+    nk++;
+    if (c->rt.nol) {
+        k_join<<<jgrid, JOIN_WARPS * 32, 0, s>>>(d, c->vbuf, 0, C_VN, c->rbuf[0]);
+        nk++;
+    }
+    if (c->cand_cap) {
+        k_apply<<<c->sms * 8, 256, 0, s>>>(d, c->cand[0], c->cand[1]);
+        nk++;
+    }
+    if (c->timing) {
+        k_tmark<<<1, 32, 0, s>>>(ctr, 1);
+        nk++;
+    }
+    k_gate_end<<<1, 32, 0, s>>>(ctr, h);
+    nk++;
+    cudaGraph_t captured = body;
+    const cudaError_t ce = cudaStreamEndCapture(s, &captured);
+    if (ce != cudaSuccess) {
+        free_round_graph(c);
+        return fail(c, GRG_E_CUDA, std::string("round graph capture: ") + cudaGetErrorString(ce));
+    }
+    GRG_CUDA(c, cudaGraphInstantiate(&c->rg_exec, c->rg_graph, 0));
+    c->rg_key = key;
+    c->rg_kernels = nk;
+    return GRG_OK;
+}
+
+// Rounds until the fixpoint (max_rounds = 0) or max_rounds rounds with work;
+// *idle = the last gather found no delta.
 static int run_rounds(grg_ctx *c, uint64_t max_rounds, grg_stats &S, double &join_ms, uint64_t &joins, bool *idle)
 {
     cudaStream_t s = c->stream;
-    Dev d = make_dev(c);
     int st = read_ctr(c);
     if (st) return st;
     *idle = false;
     uint64_t done_rounds = 0;
+    bool graphs = c->device_rounds && max_rounds == 0 && !c->batch && c->V > 0;
     for (;;) {
         if (max_rounds && done_rounds >= max_rounds) break;
-        if (c->job_cnt) GRG_CUDA(c, cudaMemsetAsync(c->job_cnt, 0, (size_t)c->max_jobs * 4, s));
-        // gather the dirty slots of the last round into delta records (slot order);
-        // the pool top is the one read after the last growth
-        const uint64_t nwords = (c->h_ctr[C_POOL_TOP] + 31) / 32;
-        const uint64_t nchunks = (nwords + 31) / 32;
-        st = ensure_chunks(c, nchunks);
-        if (st) return st;
-        uint32_t *ccnt = c->chunk, *coff = c->chunk + nchunks + 1, *csum = c->chunk + 2 * (nchunks + 1);
-        const uint64_t nb = (nchunks + 1023) / 1024;
-        d = make_dev(c);
-        k_dcount<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, ccnt);
-        k_scan_blocks<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(ccnt, coff, csum, nchunks);
-        k_scan_sums<<<1, 1024, 0, s>>>(csum, nb);
-        k_scan_add<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(coff, csum, nchunks);
-        c->launches += 4;
-        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_DIRTY_N, 0, 8, s));
-        GRG_CUDA(c, cudaMemcpyAsync(c->ctr + C_DIRTY_N, csum + nb, 4, cudaMemcpyDeviceToDevice, s));
-        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_RETRY_N, 0, 16, s));   // retry + grow counters
-        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_CAND_N, 0, 16, s));    // candidates + failed candidates
-        st = read_ctr(c);
-        if (st) return st;
-        const uint64_t nd = c->h_ctr[C_DIRTY_N];
-        if (nd == 0) {
+        // elements that gain bits in this run get its stamp; round 1 gathers the load marks
+        const uint32_t rs = (c->elem_loaded && done_rounds > 0) ? c->run_stamp : 0u;
+        if (!graphs || done_rounds == 0) {
+            uint64_t nd = 0, nv = 0;
+            if ((st = round_head(c, rs, S, &nd))) return st;
+            if (nd == 0) {
+                *idle = true;
+                break;
+            }
+            done_rounds++;
+            if ((st = round_oldleft(c, &nv))) return st;
+            if ((st = round_joins(c, nd, nv, S, join_ms, joins))) return st;
+            continue;
+        }
+        // device-driven rounds: buffers sized with room to grow, then the graph loop
+        const uint64_t nd_last = std::max<uint64_t>(c->h_ctr[C_DIRTY_N], 1);
+        if ((st = ensure_buf(c, &c->gbuf, &c->gbuf_cap, 2 * nd_last))) return st;
+        if (c->rt.nol && (st = ensure_buf(c, &c->vbuf, &c->vbuf_cap, std::max<uint64_t>(c->h_ctr[C_VN], 1) * 4)))
+            return st;
+        if ((st = ensure_cand(c, 2 * nd_last))) return st;    // a full candidate buffer falls back to direct inserts
+        if ((st = ensure_rbuf(c, c->gbuf_cap + (c->rt.nol ? c->vbuf_cap : 0)))) return st;
+        if ((st = build_round_graph(c, rs))) return st;
+        c->cb = 0;
+        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_HALT, 0, 8 * 5, s));   // halt, iterations, rounds, deltas, join ns
+        GRG_CUDA(c, cudaGraphLaunch(c->rg_exec, s));
+        if ((st = read_ctr(c))) return st;
+        const unsigned long long halt = c->h_ctr[C_HALT], rounds = c->h_ctr[C_GROUNDS];
+        S.rounds += rounds;
+        S.delta_elems += c->h_ctr[C_GDSUM];
+        joins += rounds * (c->rt.nol ? 2 : 1);
+        c->launches += c->h_ctr[C_ITERS] * c->rg_kernels;
+        join_ms += c->h_ctr[C_JNS] * 1e-6;
+        done_rounds += rounds;
+        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_HALT, 0, 8, s));
+        c->h_ctr[C_HALT] = 0;
+        if (halt == HALT_FIXPOINT) {
             *idle = true;
             break;
         }
-        done_rounds++;
-        st = ensure_buf(c, &c->gbuf, &c->gbuf_cap, nd);
-        if (st) return st;
-        st = ensure_cand(c, nd);
-        if (st) return st;
-        S.rounds++;
-        S.delta_elems += nd;
-        c->cb = 0;
-        d = make_dev(c);
-        // the delta index of the last round is cleared for the labels old-left joins read
-        for (int l = 1; l <= c->L; l++)
-            if (c->rt.dindex[l]) {
-                const size_t t0 = (size_t)(l - 1) * c->V, vw = (c->V + 31) / 32;
-                GRG_CUDA(c, cudaMemsetAsync(c->drs + t0, 0xFF, (size_t)c->V * 4, s));
-                GRG_CUDA(c, cudaMemsetAsync(c->drc + t0, 0, (size_t)c->V * 4, s));
-                GRG_CUDA(c, cudaMemsetAsync(c->dvm + (size_t)(l - 1) * vw, 0, vw * 4, s));
+        if (halt == HALT_CAPACITY) {
+            // this round's dirty bits are untouched: the host runs it from the start
+            uint64_t nd = 0, nv = 0;
+            if ((st = round_head(c, rs, S, &nd))) return st;
+            if (nd == 0) {
+                *idle = true;
+                break;
             }
-        // elements that gain bits in this run get its stamp; round 1 gathers the load marks
-        const uint32_t rs = (c->elem_loaded && done_rounds > 1) ? c->run_stamp : 0u;
-        k_gather<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->gbuf, c->row_job, c->job_cnt, rs);
-        c->launches++;
-        // old-left joins: virtual records of O_B masked to the vertices with deltas of C
-        uint64_t nv = 0;
-        if (c->rt.nol) {
-            for (int attempt = 0; attempt < 2; attempt++) {
-                GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_VN, 0, 8, s));
-                for (int q = 0; q < c->rt.nol; q++) {
-                    k_oldleft<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)q, c->vbuf, c->vbuf_cap);
-                    c->launches++;
-                }
-                st = read_ctr(c);
-                if (st) return st;
-                nv = c->h_ctr[C_VN];
-                if (nv <= c->vbuf_cap) break;
-                st = ensure_buf(c, &c->vbuf, &c->vbuf_cap, nv);
-                if (st) return st;
-            }
-        }
-        st = ensure_rbuf(c, nd + nv);
-        if (st) return st;
-        uint64_t n = nd;       // delta records for the next join pass (0 = none)
-        int rb = 0;
-        bool first = true;
-        for (int pass = 0;; pass++) {
-            if (c->timing) GRG_CUDA(c, cudaEventRecord(c->ev_c, s));
-            if (first) {
-                k_join<<<grid_for(c, (nd + RB - 1) / RB, JOIN_WARPS, 16), JOIN_WARPS * 32, 0, s>>>(d, c->gbuf, nd,
-                                                                                                 c->rbuf[0]);
-                c->launches++;
-                joins++;
-                if (nv) {
-                    k_join<<<grid_for(c, (nv + RB - 1) / RB, JOIN_WARPS, 16), JOIN_WARPS * 32, 0, s>>>(d, c->vbuf, nv,
-                                                                                                     c->rbuf[0]);
-                    c->launches++;
-                    joins++;
-                }
-            } else if (n) {
-                const int jgrid = grid_for(c, (n + RB - 1) / RB, JOIN_WARPS, 16);
-                k_join<<<jgrid, JOIN_WARPS * 32, 0, s>>>(d, c->rbuf[rb], n, c->rbuf[rb ^ 1]);
-                c->launches++;
-                joins++;
-            }
-            // insert the candidates the joins wrote (count read on the device)
-            if (c->cand_cap) {
-                k_apply<<<c->sms * 8, 256, 0, s>>>(d, c->cand[c->cb], c->cand[c->cb ^ 1]);
-                c->launches++;
-            }
-            if (c->timing) GRG_CUDA(c, cudaEventRecord(c->ev_d, s));
-            GRG_CUDA(c, cudaGetLastError());
-            st = read_ctr(c);
-            if (st) return st;
-            if (c->timing) {
-                float ms = 0;
-                cudaEventElapsedTime(&ms, c->ev_c, c->ev_d);
-                join_ms += ms;
-            }
-            const uint64_t nr = (first || n) ? c->h_ctr[C_RETRY_N] : 0;
-            if (!first && n) rb ^= 1;       // the failed records of this pass are in rbuf[rb]
-            if (first) n = nd;
-            first = false;
-            const uint64_t nf = c->cand_cap ? c->h_ctr[C_AFAIL] : 0;
-            if (nr == 0 && nf == 0) break;
-            S.retry_records += nr + nf;
-            // grow every table that overflowed, then re-run the failed records and candidates
-            for (int gtry = 0;; gtry++) {
-                const uint64_t ng = c->h_ctr[C_GROW_N];
-                GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_ERR, 0, 8, s));
-                k_grow<<<grid_for(c, ng * 32, 256), 256, 0, s>>>(d, ng);
-                c->launches++;
-                S.grow_rows += ng;
-                st = read_ctr(c);
-                if (st) return st;
-                if (!(c->h_ctr[C_ERR] & ERR_POOL)) break;
-                if (gtry > 16) return fail(c, GRG_E_NOMEM, "element pool exhausted");
-                st = grow_pool(c, c->pool_cap * 2);
-                if (st) return st;
-                d = make_dev(c);
-            }
-            if (pass > 64) return fail(c, GRG_E_CUDA, "table growth did not converge");
-            // failed candidates (in cand[cb^1]) become the next candidate list; join retries append to it
-            c->cb ^= 1;
-            d = make_dev(c);
-            n = nr;
-            c->h_ctr[C_CAND_N] = nf;
-            GRG_CUDA(c, cudaMemcpyAsync(c->ctr + C_CAND_N, c->h_ctr + C_CAND_N, 8, cudaMemcpyHostToDevice, s));
-            GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_AFAIL, 0, 8, s));
-            GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_RETRY_N, 0, 16, s));
+            done_rounds++;
+            if ((st = round_oldleft(c, &nv))) return st;
+            if ((st = round_joins(c, nd, nv, S, join_ms, joins))) return st;
+        } else if (halt == HALT_OLDLEFT) {
+            // gathered and indexed: the host redoes the virtual records with more room, then joins
+            uint64_t nv = 0;
+            if ((st = ensure_buf(c, &c->vbuf, &c->vbuf_cap, c->h_ctr[C_VN]))) return st;
+            if ((st = round_oldleft(c, &nv))) return st;
+            if ((st = round_joins(c, c->h_ctr[C_DIRTY_N], nv, S, join_ms, joins))) return st;
+        } else if (halt == HALT_RETRY) {
+            if ((st = round_retries(c, c->h_ctr[C_RETRY_N], c->cand_cap ? c->h_ctr[C_AFAIL] : 0, S, join_ms, joins)))
+                return st;
+        } else if (halt == HALT_LIMIT) {
+            // a launch that ran this long without a halt is not trusted: host-driven rounds from here
+            c->device_rounds = false;
+            graphs = false;
+        } else {
+            return fail(c, GRG_E_CUDA, "device-driven rounds stopped without a reason");
         }
     }
     return GRG_OK;
 }
+
+extern "C" {
 
 int grg_closure(grg_ctx *c, uint32_t filter, grg_stats *stats) { return grg_closure_ex(c, filter, 0, stats); }
 
@@ -2109,9 +2444,9 @@ int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *s
         c->csr_bufs.push_back(sums);
         GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_ERR, 0, 8, s));
         k_csr_count<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)l, ptr, (uint2 *)row);
-        k_scan_blocks<<<(unsigned)nb, 1024, 0, s>>>(ptr, ptr, sums, c->V);
-        k_scan_sums<<<1, 1024, 0, s>>>(sums, nb);
-        k_scan_add<<<(unsigned)nb, 1024, 0, s>>>(ptr, sums, c->V);
+        k_scan_blocks<<<(unsigned)nb, 1024, 0, s>>>(ptr, ptr, sums, c->V, nullptr);
+        k_scan_sums<<<1, 1024, 0, s>>>(sums, nb, nullptr);
+        k_scan_add<<<(unsigned)nb, 1024, 0, s>>>(ptr, sums, c->V, nullptr);
         st = read_ctr(c);
         if (st) return st;
         if (c->h_ctr[C_ERR]) continue;                 // a row too long for the packed CSR: keep elements
@@ -2709,10 +3044,10 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
         const uint64_t nwords = (h[C_POOL_TOP] + 31) / 32, nchunks = (nwords + 31) / 32;
         const uint64_t nb = (nchunks + 1023) / 1024;
         uint32_t *ccnt = chunk, *coff = chunk + nchunks + 1, *csum = chunk + 2 * (nchunks + 1);
-        k_dcount<<<grid(nchunks * 32, 256, 8), 256, 0, s>>>(d, nwords, ccnt);
-        k_scan_blocks<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(ccnt, coff, csum, nchunks);
-        k_scan_sums<<<1, 1024, 0, s>>>(csum, nb);
-        k_scan_add<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(coff, csum, nchunks);
+        k_dcount<<<grid(nchunks * 32, 256, 8), 256, 0, s>>>(d, nwords, ccnt, 0);
+        k_scan_blocks<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(ccnt, coff, csum, nchunks, nullptr);
+        k_scan_sums<<<1, 1024, 0, s>>>(csum, nb, nullptr);
+        k_scan_add<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(coff, csum, nchunks, nullptr);
         uint32_t nd32 = 0;
         NA_CUDA(cudaMemcpyAsync(&nd32, csum + nb, 4, cudaMemcpyDeviceToHost, s));
         NA_CUDA(cudaStreamSynchronize(s));
@@ -2725,7 +3060,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
                 NA_CUDA(cudaMemsetAsync(d.drc + (size_t)(l - 1) * num_vars, 0, (size_t)num_vars * 4, s));
                 NA_CUDA(cudaMemsetAsync(d.dvm + (size_t)(l - 1) * vwords, 0, vwords * 4, s));
             }
-        k_gather<<<grid(nchunks * 32, 256, 8), 256, 0, s>>>(d, nwords, coff, gbuf, nullptr, nullptr, 0);
+        k_gather<<<grid(nchunks * 32, 256, 8), 256, 0, s>>>(d, nwords, coff, gbuf, nullptr, nullptr, 0, 0);
         uint64_t nv = 0;
         if (rt.nol) {
             NA_CUDA(cudaMemsetAsync(d.ctr + C_VN, 0, 8, s));
@@ -2741,10 +3076,10 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
         for (int pass = 0;; pass++) {
             const int g = grid((n + RB - 1) / RB, JOIN_WARPS, 16);
             if (pass == 0) {
-                k_join<<<g, JOIN_WARPS * 32, 0, s>>>(d, gbuf, nd, rbuf[0]);
-                if (nv) k_join<<<grid((nv + RB - 1) / RB, JOIN_WARPS, 16), JOIN_WARPS * 32, 0, s>>>(d, vbuf, nv, rbuf[0]);
+                k_join<<<g, JOIN_WARPS * 32, 0, s>>>(d, gbuf, nd, -1, rbuf[0]);
+                if (nv) k_join<<<grid((nv + RB - 1) / RB, JOIN_WARPS, 16), JOIN_WARPS * 32, 0, s>>>(d, vbuf, nv, -1, rbuf[0]);
             } else {
-                k_join<<<g, JOIN_WARPS * 32, 0, s>>>(d, rbuf[rb], n, rbuf[rb ^ 1]);
+                k_join<<<g, JOIN_WARPS * 32, 0, s>>>(d, rbuf[rb], n, -1, rbuf[rb ^ 1]);
             }
             NA_CUDA(cudaGetLastError());
             if ((st = na_read(h, d.ctr, s))) return st;

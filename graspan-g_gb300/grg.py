@@ -32,6 +32,7 @@ EXPORTS = (
     "grg_batch_step", "grg_batch_result", "grg_batch_release", "grg_get_rules", "grg_closure_ex",
     "grg_load_elements", "grg_export_elements", "grg_range_counts", "grg_set_pool_limit", "grg_part_create",
     "grg_part_destroy", "grg_part_load_edges", "grg_part_run", "grg_part_label_counts", "grg_part_bounds",
+    "grg_set_device_rounds",
 )
 
 
@@ -93,6 +94,7 @@ def load_library(path: str = LIB_PATH):
     L.grg_device.argtypes = [P]
     L.grg_set_stream.argtypes = [P, P]
     L.grg_set_kernel_timing.argtypes = [P, I]
+    L.grg_set_device_rounds.argtypes = [P, I]
     L.grg_transfer_rules.argtypes = [P, I, P, I]
     L.grg_allocate_pool.argtypes = [P, U64]
     L.grg_load_edges.argtypes = [P, U32, U64, P, P, P, I]
@@ -224,6 +226,9 @@ class Context:
 
     def set_kernel_timing(self, on: bool):
         self._check(self._L.grg_set_kernel_timing(self._h, int(bool(on))), "set_kernel_timing")
+
+    def set_device_rounds(self, on: bool):
+        self._check(self._L.grg_set_device_rounds(self._h, int(bool(on))), "set_device_rounds")
 
     def transfer_rules(self, rules, num_labels: int):
         r = np.ascontiguousarray(np.asarray(rules, dtype=np.int32).reshape(-1))

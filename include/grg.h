@@ -78,8 +78,16 @@ void grg_destroy(grg_ctx *ctx);
 int grg_device(const grg_ctx *ctx);
 /* Issue all work of the context on this cudaStream_t (NULL = the context's own stream). */
 int grg_set_stream(grg_ctx *ctx, void *stream);
-/* Measure each join launch with CUDA events (adds a little host overhead). */
+/* Measure the join pass of every round (adds a little host overhead): CUDA
+ * events around host-driven passes, the global nanosecond timer inside
+ * device-driven rounds. */
 int grg_set_kernel_timing(grg_ctx *ctx, int on);
+/* Device-driven rounds (default on; environment GRG_DEVICE_ROUNDS=0 turns the
+ * default off): after the first round, grg_closure replays one round from a
+ * CUDA graph with a WHILE node until the fixpoint or until a round needs the
+ * host (table growth, buffer room), instead of launching and waiting per
+ * round. The results are identical either way. */
+int grg_set_device_rounds(grg_ctx *ctx, int on);
 
 /* Grammar: rules[3*i+{0,1,2}] = LHS, RHS1, RHS2 label ids (1-based, 0 = absent),
  * num_labels = number of distinct labels. Replaces transferRules

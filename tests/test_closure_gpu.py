@@ -187,3 +187,34 @@ def test_device_load_equals_host_load(grg_mod):
         ha = ctx.set_hash()
     ctx2, st = gpu_closure(grg_mod, w)
     assert a == st["total_edges"] and ha == ctx2.set_hash()
+
+
+@pytest.mark.parametrize("name", ["pointsto", "alias", "dataflow", "chain"])
+def test_device_rounds_equal_host_rounds(grg_mod, oracle_mod, name):
+    """Rounds replayed from the CUDA graph's WHILE node give the same closure
+    as rounds driven from the host. (How new edges split over rounds depends on
+    the timing of a round's concurrent inserts, so round and delta counts may
+    differ; the closure may not.)"""
+    w = {"pointsto": lambda: G.pointsto(seed=31, num_vars=900, num_edges=2200),
+         "alias": lambda: G.alias(seed=32, num_vars=4000, num_base_edges=9000, block=500),
+         "dataflow": lambda: G.dataflow_blocks(seed=33, num_blocks=20, block=500, num_edges=30000),
+         "chain": lambda: G.random_grammar_graph(34, num_vars=600, num_edges=599, num_labels=2, num_rules=2)}[name]()
+    if name == "chain":
+        w.rules = [("L0", "L0", "L1"), ("L0", "L1")]
+        w.labels = ["L0", "L1"]
+        w.src = np.arange(599, dtype=np.uint32)
+        w.dst = w.src + 1
+        w.lab = np.full(599, 2, np.uint8)
+        w.filter_flag = 0
+    r = oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, w.filter_flag, w.src, w.dst, w.lab)
+    out = []
+    for dev in (False, True):
+        ctx = grg_mod.Context(0)
+        ctx.set_device_rounds(dev)
+        ctx.transfer_rules(w.rule_ids(), w.num_labels)
+        ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
+        st = ctx.closure(w.filter_flag)
+        out.append((ctx.label_counts().tolist(), ctx.set_hash()))
+        ctx.close()
+    assert out[0] == out[1]
+    assert out[1][0] == r.label_counts().tolist() and out[1][1] == r.set_hash
