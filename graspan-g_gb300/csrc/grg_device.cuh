@@ -10,7 +10,9 @@
 // of a list walk and rows never need re-sorting.
 //
 // Deltas: a parallel pool of 32-byte delta bitmaps (words 0..5 = bits that
-// became set this round) and a dirty bitmap with one bit per pool slot. An
+// became set this round; words 6..7 = the slot's key and row, written when the
+// slot is filled, so the gather reads one sector per record) and a dirty
+// bitmap with one bit per pool slot. An
 // insert that sets new bits ORs them into the slot's delta bitmap and sets the
 // slot's dirty bit, both fire-and-forget; the next round's gather scans the
 // dirty bitmap and emits one delta record per dirty slot, in slot order (so a
@@ -155,7 +157,13 @@ __device__ __forceinline__ bool g_insert(const Dev &d, uint32_t slot, uint32_t r
             if (k != EMPTY) continue;
             if (atomicAdd(&d.cnt[ti], 1u) >= max_load(cap)) { atomicSub(&d.cnt[ti], 1u); break; }
             const uint32_t prev = atomicCAS(kp, EMPTY, key);
-            if (prev == EMPTY) { d.elems[(size_t)q * 8 + 7] = row; s = q; break; }
+            if (prev == EMPTY) {
+                d.elems[(size_t)q * 8 + 7] = row;
+                // the delta bitmap's spare words carry the slot's key and row for the gather
+                reinterpret_cast<uint2 *>(d.dbits + (size_t)q * 8)[3] = make_uint2(key, row);
+                s = q;
+                break;
+            }
             atomicSub(&d.cnt[ti], 1u);
             if (prev == key) { s = q; break; }
         }

@@ -261,6 +261,7 @@ __global__ void k_compact_static(Dev d, uint32_t slot, uint32_t first, uint32_t 
                     atomicAnd(&d.dmap[os >> 5], ~(1u << (os & 31)));
                     atomicOr(&d.dmap[ns >> 5], 1u << (ns & 31));
                 }
+                reinterpret_cast<uint2 *>(d.dbits + ns * 8)[3] = make_uint2(e1.z, e1.w);
             }
             wpos++;
         }
@@ -284,7 +285,7 @@ __global__ void k_mark_all(Dev d, uint64_t begin, uint64_t end)   // begin: mult
                 const uint4 e0 = e[0];
                 uint4 *b = reinterpret_cast<uint4 *>(d.dbits + s * 8);
                 b[0] = e0;
-                b[1] = make_uint4(e1.x, e1.y, 0u, 0u);
+                b[1] = e1;                 // words 6-7: key and row
                 mark = true;
             }
         }
@@ -334,8 +335,11 @@ __device__ __forceinline__ uint32_t select32(uint32_t w, uint32_t n)
 // chunk offsets; clears the delta bitmaps and the dirty bitmap. One warp per
 // chunk of 32 bitmap words; lanes take consecutive dirty slots of the chunk, so
 // the copies of a warp are independent and mostly coalesced.
-__global__ void k_gather(Dev d, uint64_t nwords, const uint32_t *__restrict__ chunk_off, uint4 *out,
-                         const uint32_t *__restrict__ row_job, uint32_t *job_cnt, uint32_t run_stamp, int dyn)
+// Gather, pass 1: the dirty slots of the round, in slot order (a table's
+// records stay contiguous), each slot id written to word 7 of its record's
+// place in `out`; the dirty bits are cleared. Lanes walk their own bitmap word:
+// stores only, nothing to wait for.
+__global__ void k_gather_slots(Dev d, uint64_t nwords, const uint32_t *__restrict__ chunk_off, uint4 *out, int dyn)
 {
     if (d.ctr[C_HALT]) return;
     nwords = dyn_words(nwords, d.ctr, dyn);
@@ -344,59 +348,55 @@ __global__ void k_gather(Dev d, uint64_t nwords, const uint32_t *__restrict__ ch
     const uint32_t lane = lane_id();
     for (uint64_t c = blockIdx.x * (uint64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); c < nchunks; c += nwarps) {
         const uint64_t wi = c * 32 + lane;
-        const uint32_t m = wi < nwords ? d.dmap[wi] : 0;
+        uint32_t m = wi < nwords ? d.dmap[wi] : 0;
+        const uint64_t base_pos = chunk_off[c];
         const uint32_t cnt = __popc(m);
         uint32_t incl = cnt;
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
             if (lane >= (uint32_t)o) incl += y;
         }
-        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
         if (m) d.dmap[wi] = 0;
-        const uint64_t base_pos = chunk_off[c];
-        for (uint32_t t0 = 0; t0 < total; t0 += 32) {
-            const uint32_t t = t0 + lane;
-            // owner word: smallest lane o with incl(o) > t
-            uint32_t lo = 0;
-#pragma unroll
-            for (int st = 16; st; st >>= 1) {
-                const uint32_t v = __shfl_sync(0xffffffffu, incl, lo + st - 1);
-                if (v <= t) lo += st;
-            }
-            const uint32_t o_incl = __shfl_sync(0xffffffffu, incl, lo & 31);
-            const uint32_t o_cnt = __shfl_sync(0xffffffffu, cnt, lo & 31);
-            const uint32_t o_m = __shfl_sync(0xffffffffu, m, lo & 31);
-            if (t < total) {
-                const uint32_t bit = select32(o_m, t - (o_incl - o_cnt));
-                const uint64_t s = (c * 32 + lo) * 32 + bit;
-                uint4 *b = reinterpret_cast<uint4 *>(d.dbits + s * 8);
-                const uint4 b0 = b[0], b1 = b[1];
-                const uint4 e1 = reinterpret_cast<const uint4 *>(d.elems + s * 8)[1];
-                b[0] = make_uint4(0, 0, 0, 0);
-                b[1] = make_uint4(0, 0, 0, 0);
-                const uint64_t pos = base_pos + t;
-                if (run_stamp) d.stamp[s] = run_stamp;     // gained bits during this run
-                out[2 * pos] = b0;
-                out[2 * pos + 1] = make_uint4(b1.x, b1.y, e1.z, e1.w);
-                const uint32_t lab = e1.z >> KEY_SHIFT;
-                if (lab <= (uint32_t)MAX_LABELS && c_rt.dindex[lab]) {
-                    // a table's records are contiguous (slot order; growth moves dirty bits along)
-                    const size_t ti = (size_t)(lab - 1) * d.V + e1.w;
-                    atomicMin(&d.drs[ti], (uint32_t)pos);
-                    atomicAdd(&d.drc[ti], 1u);
-                    atomicOr(&d.dvm[(size_t)(lab - 1) * d.vwords + (e1.w >> 5)], 1u << (e1.w & 31));
-                }
-            }
-            if (row_job) {
-                // batched jobs: records per job (a job with none has reached its fixpoint)
-                uint32_t job = EMPTY;
-                if (t < total) {
-                    const uint32_t *e = d.elems + ((c * 32 + lo) * 32 + select32(o_m, t - (o_incl - o_cnt))) * 8;
-                    job = row_job[e[7]];
-                }
-                const unsigned g = __match_any_sync(0xffffffffu, job);
-                if (job != EMPTY && (int)lane == __ffs(g) - 1) atomicAdd(&job_cnt[job], (uint32_t)__popc(g));
-            }
+        uint32_t *w7 = reinterpret_cast<uint32_t *>(out) + (base_pos + incl - cnt) * 8 + 7;
+        while (m) {
+            *w7 = (uint32_t)(wi * 32 + (__ffs(m) - 1));
+            m &= m - 1;
+            w7 += 8;
+        }
+    }
+}
+
+// Gather, pass 2: one thread per record. The slot's delta bitmap (words 0-5:
+// bits new since the last gather; 6-7: the slot's key and row) becomes the
+// record and is cleared; the delta index and per-job counts are filled.
+// n_ctr >= 0: the record count is device counter n_ctr (round graphs).
+__global__ void k_gather_recs(Dev d, uint4 *out, uint64_t n, int n_ctr, const uint32_t *__restrict__ row_job,
+                              uint32_t *job_cnt, uint32_t run_stamp)
+{
+    if (d.ctr[C_HALT]) return;
+    if (n_ctr >= 0) n = d.ctr[n_ctr];
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t s = reinterpret_cast<const uint32_t *>(out)[i * 8 + 7];
+        uint4 *b = reinterpret_cast<uint4 *>(d.dbits + s * 8);
+        const uint4 b0 = b[0], b1 = b[1];
+        b[0] = make_uint4(0, 0, 0, 0);
+        reinterpret_cast<uint2 *>(b + 1)[0] = make_uint2(0, 0);
+        if (run_stamp) d.stamp[s] = run_stamp;         // gained bits during this run
+        out[2 * i] = b0;
+        out[2 * i + 1] = b1;
+        const uint32_t lab = b1.z >> KEY_SHIFT, row = b1.w;
+        if (lab <= (uint32_t)MAX_LABELS && c_rt.dindex[lab]) {
+            const size_t ti = (size_t)(lab - 1) * d.V + row;
+            atomicMin(&d.drs[ti], (uint32_t)i);
+            atomicAdd(&d.drc[ti], 1u);
+            atomicOr(&d.dvm[(size_t)(lab - 1) * d.vwords + (row >> 5)], 1u << (row & 31));
+        }
+        if (row_job) {
+            // batched jobs: records per job (a job with none has reached its fixpoint)
+            const uint32_t job = row_job[row];
+            const unsigned act = __activemask();
+            const unsigned g = __match_any_sync(act, job);
+            if (job != EMPTY && lane_id() == (uint32_t)(__ffs(g) - 1)) atomicAdd(&job_cnt[job], (uint32_t)__popc(g));
         }
     }
 }
@@ -1080,6 +1080,7 @@ __global__ void k_grow(Dev d, uint64_t n)
                     // pending delta bits move along, so a table's delta records stay contiguous
                     const uint64_t os = (uint64_t)off + t;
                     if (d.stamp) d.stamp[q] = d.stamp[os];
+                    reinterpret_cast<uint2 *>(d.dbits + q * 8)[3] = make_uint2(e1.z, e1.w);
                     if ((d.dmap[os >> 5] >> (os & 31)) & 1u) {
                         uint4 *ob = reinterpret_cast<uint4 *>(d.dbits + os * 8);
                         uint4 *nbp = reinterpret_cast<uint4 *>(d.dbits + q * 8);
@@ -1242,11 +1243,13 @@ __global__ void k_elem_insert(Dev d, const uint4 *recs, const uint32_t *stamps, 
         atomicAdd(&d.cnt[ti], 1u);
         const uint32_t st = stamps[i];
         d.stamp[q] = st;
+        uint4 *b = reinterpret_cast<uint4 *>(d.dbits + (size_t)q * 8);
         if (st > mark_after) {
-            uint4 *b = reinterpret_cast<uint4 *>(d.dbits + (size_t)q * 8);
             b[0] = e0;
-            b[1] = make_uint4(e1.x, e1.y, 0u, 0u);
+            b[1] = e1;                     // words 6-7: key and row
             atomicOr(&d.dmap[q >> 5], 1u << (q & 31));
+        } else {
+            reinterpret_cast<uint2 *>(b)[3] = make_uint2(e1.z, e1.w);
         }
     }
 }
@@ -2013,8 +2016,9 @@ static int round_head(grg_ctx *c, uint32_t rs, grg_stats &S, uint64_t *nd_out)
             GRG_CUDA(c, cudaMemsetAsync(c->drc + t0, 0, (size_t)c->V * 4, s));
             GRG_CUDA(c, cudaMemsetAsync(c->dvm + (size_t)(l - 1) * vw, 0, vw * 4, s));
         }
-    k_gather<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->gbuf, c->row_job, c->job_cnt, rs, 0);
-    c->launches++;
+    k_gather_slots<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->gbuf, 0);
+    k_gather_recs<<<grid_for(c, nd, 256), 256, 0, s>>>(d, c->gbuf, nd, -1, c->row_job, c->job_cnt, rs);
+    c->launches += 2;
     return GRG_OK;
 }
 
@@ -2271,8 +2275,9 @@ static int build_round_graph(grg_ctx *c, uint32_t rs)
             cudaMemsetAsync(c->dvm + (size_t)(l - 1) * vw, 0, vw * 4, s);
         }
     cudaMemsetAsync(ctr + C_VN, 0, 8, s);
-    k_gather<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->gbuf, nullptr, nullptr, rs, 1);
-    nk++;
+    k_gather_slots<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->gbuf, 1);
+    k_gather_recs<<<grid_for(c, c->gbuf_cap, 256), 256, 0, s>>>(d, c->gbuf, 0, C_DIRTY_N, nullptr, nullptr, rs);
+    nk += 2;
     if (c->rt.nol) {
         for (int q = 0; q < c->rt.nol; q++)
             k_oldleft<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)q, c->vbuf, c->vbuf_cap);
@@ -3060,7 +3065,8 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
                 NA_CUDA(cudaMemsetAsync(d.drc + (size_t)(l - 1) * num_vars, 0, (size_t)num_vars * 4, s));
                 NA_CUDA(cudaMemsetAsync(d.dvm + (size_t)(l - 1) * vwords, 0, vwords * 4, s));
             }
-        k_gather<<<grid(nchunks * 32, 256, 8), 256, 0, s>>>(d, nwords, coff, gbuf, nullptr, nullptr, 0, 0);
+        k_gather_slots<<<grid(nchunks * 32, 256, 8), 256, 0, s>>>(d, nwords, coff, gbuf, 0);
+        k_gather_recs<<<grid(nd, 256, 8), 256, 0, s>>>(d, gbuf, nd, -1, nullptr, nullptr, 0);
         uint64_t nv = 0;
         if (rt.nol) {
             NA_CUDA(cudaMemsetAsync(d.ctr + C_VN, 0, 8, s));
