@@ -161,9 +161,11 @@ def serving_measurement(args):
     import grg_gen as G
     specs = G.batch_mix(jobs=args.serve_jobs, vmax=args.serve_vmax)
     jobs = serve.make_jobs(specs)
-    max_vars = max(4 * args.serve_vmax, 2_000_000)
-    batched = serve.serve(jobs, max_vars=max_vars, max_jobs=256, realtime=False)     # all jobs available at t=0
-    served = serve.serve(jobs, max_vars=max_vars, max_jobs=256, realtime=True)       # Poisson arrivals
+    # vertex space for the whole mix (HBM holds it: tables take ~250 B per vertex of the union grammar)
+    max_vars = min(sum(j.num_vars for j in jobs) + args.serve_vmax, 32_000_000)
+    max_jobs = min(len(jobs), 512)
+    batched = serve.serve(jobs, max_vars=max_vars, max_jobs=max_jobs, realtime=False)  # all jobs available at t=0
+    served = serve.serve(jobs, max_vars=max_vars, max_jobs=max_jobs, realtime=True)    # Poisson arrivals
     plain = serve.plain(jobs)
     assert served["total_edges"] == plain["total_edges"] == batched["total_edges"]
     return {"workload": f"{args.serve_jobs} jobs, V log-uniform 1000..{args.serve_vmax}, edges 3-5 x V, "

@@ -60,7 +60,8 @@ enum : int {
     C_JNS = 23,       // join-pass nanoseconds of those rounds (with kernel timing)
     C_LABEL0 = 24,    // per-label edge counts: C_LABEL0 + slot
     C_JT0 = C_LABEL0 + MAX_SLOTS + 2,   // start time of the current join pass (device-driven rounds)
-    NCTR = C_LABEL0 + MAX_SLOTS + 3
+    C_MAXR = C_LABEL0 + MAX_SLOTS + 3,  // rounds a device-driven launch may run (0 = until the fixpoint)
+    NCTR = C_LABEL0 + MAX_SLOTS + 4
 };
 enum : unsigned long long { ERR_POOL = 1, ERR_LOAD = 2, ERR_INTERNAL = 4 };
 
@@ -176,12 +177,17 @@ __device__ __forceinline__ bool g_insert(const Dev &d, uint32_t slot, uint32_t r
         return false;
     }
     uint32_t *e = d.elems + (size_t)s * 8;
+    // words whose candidate bits are all present already need no atomic: bits are
+    // only ever set during a round, so a stale read can only show fewer of them
+    const uint4 c0 = __ldcg(reinterpret_cast<const uint4 *>(e));
+    const uint2 c1 = __ldcg(reinterpret_cast<const uint2 *>(e + 4));
+    const uint32_t cur[EW] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y};
     Bits nb;
     uint32_t any = 0;
 #pragma unroll
     for (int w = 0; w < EW; w++) {
         nb.w[w] = 0;
-        if (b.w[w]) {
+        if (b.w[w] & ~cur[w]) {
             const uint32_t old = atomicOr(&e[w], b.w[w]);
             nb.w[w] = b.w[w] & ~old;
             any |= nb.w[w];

@@ -1291,6 +1291,48 @@ __global__ void k_export_elems(Dev d, uint32_t v0, uint32_t v1, uint32_t L, uint
     }
 }
 
+// Partitions that rows [v0, v1) reach through labels in label_mask:
+// flags[p] = 1 when an element's destinations overlap [bounds[p], bounds[p+1])
+// (every partition between an element's lowest and highest destination: a
+// superset, which only ever schedules a pair too many).
+__global__ void k_range_reach(Dev d, uint32_t v0, uint32_t v1, uint32_t L, unsigned long long label_mask,
+                              const uint32_t *bounds, uint32_t np, uint32_t *flags)
+{
+    const uint32_t lane = lane_id();
+    const uint64_t nv = v1 - v0, ntab = (uint64_t)L * nv;
+    const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t u = blockIdx.x * (uint64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); u < ntab; u += nwarps) {
+        const uint32_t lab = (uint32_t)(u / nv) + 1, row = v0 + (uint32_t)(u % nv);
+        if (!((label_mask >> (lab - 1)) & 1ull)) continue;
+        const uint64_t de = d.desc[(size_t)(lab - 1) * d.V + row];
+        const uint32_t off = (uint32_t)de, cap = (uint32_t)(de >> 32);
+        for (uint32_t t = lane; t < cap; t += 32) {
+            const uint32_t *e = d.elems + (size_t)(off + t) * 8;
+            const uint32_t key = e[6];
+            if (key == EMPTY) continue;
+            int lo = -1, hi = -1;
+#pragma unroll
+            for (int x = 0; x < EW; x++) {
+                const uint32_t w = e[x];
+                if (w && lo < 0) lo = x * 32 + __ffs(w) - 1;
+                if (w) hi = x * 32 + 31 - __clz(w);
+            }
+            if (lo < 0) continue;
+            const uint64_t b0 = (uint64_t)(key & BASE_MASK) * EIDS;
+            const uint64_t dmin = b0 + lo, dmax = b0 + hi;
+            // last p with bounds[p] <= dest
+            uint32_t a = 0, z = np;
+            while (z - a > 1) {
+                const uint32_t m = (a + z) / 2;
+                if (bounds[m] <= dmin) a = m; else z = m;
+            }
+            uint32_t p = a;
+            for (; p < np && bounds[p] <= dmax; p++)
+                if (!flags[p]) flags[p] = 1;
+        }
+    }
+}
+
 }  // namespace grg
 
 // ====================================================================== host
@@ -1880,6 +1922,23 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
                 c->launches++;
             }
     };
+    // derived rows start presized when the device can hold them: grow the pool for it
+    {
+        int nder = 0;
+        bool lhs[MAX_LABELS + 1] = {false};
+        for (int q = 0; q < c->R; q++) lhs[c->rules[3 * q]] = true;
+        for (int l = 1; l <= c->L; l++) nder += lhs[l];
+        const uint64_t want = 4ull * nder * num_vars * DERIVED_MIN_CAP + 2 * num_edges;
+        if (want > c->pool_cap) {
+            size_t fr = 0, tot = 0;
+            cudaMemGetInfo(&fr, &tot);
+            const uint64_t fit = (uint64_t)((double)fr * 0.6) / (POOL_BYTES_PER_SLOT + 4);
+            if (fit > c->pool_cap && (!c->pool_limit || c->pool_limit > c->pool_cap)) {
+                st = grow_pool(c, std::min(want, fit));
+                if (st) return st;
+            }
+        }
+    }
     uint64_t top = 0;
     st = alloc_tables(c, derived_min_cap(c), hist, &top);
     if (st) return st;
@@ -2149,7 +2208,9 @@ static int round_joins(grg_ctx *c, uint64_t nd, uint64_t nv, grg_stats &S, doubl
 // a buffer too small for the round, or tables to grow (the rare retry path);
 // the host then finishes that round with the functions above and relaunches.
 
-enum : unsigned long long { HALT_FIXPOINT = 1, HALT_CAPACITY = 2, HALT_OLDLEFT = 3, HALT_RETRY = 4, HALT_LIMIT = 5 };
+enum : unsigned long long {
+    HALT_FIXPOINT = 1, HALT_CAPACITY = 2, HALT_OLDLEFT = 3, HALT_RETRY = 4, HALT_LIMIT = 5, HALT_ROUNDS = 6
+};
 constexpr uint64_t GATE_MAX_ITERS = 1u << 20;   // iterations of one graph launch; past it the host takes over
 
 __global__ void k_gate_gather(unsigned long long *ctr, const uint32_t *csum, uint64_t max_chunks, uint64_t gbuf_cap,
@@ -2192,6 +2253,10 @@ __global__ void k_gate_end(unsigned long long *ctr, cudaGraphConditionalHandle h
     if (ctr[C_RETRY_N] || ctr[C_AFAIL]) {
         ctr[C_HALT] = HALT_RETRY;
         cudaGraphSetConditional(h, 0);
+    } else if (ctr[C_MAXR] && ctr[C_GROUNDS] >= ctr[C_MAXR]) {
+        // the round budget of this launch is spent; per-job counts of this round stay for the host
+        ctr[C_HALT] = HALT_ROUNDS;
+        cudaGraphSetConditional(h, 0);
     }
 }
 
@@ -2225,7 +2290,8 @@ static std::vector<uint64_t> round_graph_key(const grg_ctx *c, uint32_t rs, uint
                                (uint64_t)c->rbuf[0], (uint64_t)c->rbuf[1], c->rbuf_cap, (uint64_t)c->cand[0],
                                (uint64_t)c->cand[1], c->cand_cap, (uint64_t)c->chunk, nchunks, (uint64_t)c->drs,
                                (uint64_t)c->drc, (uint64_t)c->dvm, c->pool_cap, c->V, rs, (uint64_t)c->timing,
-                               (uint64_t)c->elem_loaded, (uint64_t)c->rt.nol};
+                               (uint64_t)c->elem_loaded, (uint64_t)c->rt.nol, (uint64_t)c->row_job,
+                               (uint64_t)c->job_cnt, c->max_jobs};
     for (int l = 1; l <= c->L; l++) k.push_back(c->rt.dindex[l]);
     return k;
 }
@@ -2261,6 +2327,7 @@ static int build_round_graph(grg_ctx *c, uint32_t rs)
     int nk = 0;
     cudaMemsetAsync(ctr + C_RETRY_N, 0, 16, s);
     cudaMemsetAsync(ctr + C_CAND_N, 0, 16, s);
+    if (c->job_cnt) cudaMemsetAsync(c->job_cnt, 0, (size_t)c->max_jobs * 4, s);
     k_dcount<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, ccnt, 1);
     k_scan_blocks<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(ccnt, coff, csum, nchunks, ctr);
     k_scan_sums<<<1, 1024, 0, s>>>(csum, nb, ctr);
@@ -2276,7 +2343,7 @@ static int build_round_graph(grg_ctx *c, uint32_t rs)
         }
     cudaMemsetAsync(ctr + C_VN, 0, 8, s);
     k_gather_slots<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->gbuf, 1);
-    k_gather_recs<<<grid_for(c, c->gbuf_cap, 256), 256, 0, s>>>(d, c->gbuf, 0, C_DIRTY_N, nullptr, nullptr, rs);
+    k_gather_recs<<<grid_for(c, c->gbuf_cap, 256), 256, 0, s>>>(d, c->gbuf, 0, C_DIRTY_N, c->row_job, c->job_cnt, rs);
     nk += 2;
     if (c->rt.nol) {
         for (int q = 0; q < c->rt.nol; q++)
@@ -2326,7 +2393,7 @@ static int run_rounds(grg_ctx *c, uint64_t max_rounds, grg_stats &S, double &joi
     if (st) return st;
     *idle = false;
     uint64_t done_rounds = 0;
-    bool graphs = c->device_rounds && max_rounds == 0 && !c->batch && c->V > 0;
+    bool graphs = c->device_rounds && max_rounds != 1 && c->V > 0;
     for (;;) {
         if (max_rounds && done_rounds >= max_rounds) break;
         // elements that gain bits in this run get its stamp; round 1 gathers the load marks
@@ -2353,6 +2420,8 @@ static int run_rounds(grg_ctx *c, uint64_t max_rounds, grg_stats &S, double &joi
         if ((st = build_round_graph(c, rs))) return st;
         c->cb = 0;
         GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_HALT, 0, 8 * 5, s));   // halt, iterations, rounds, deltas, join ns
+        c->h_ctr[C_MAXR] = max_rounds ? max_rounds - done_rounds : 0;
+        GRG_CUDA(c, cudaMemcpyAsync(c->ctr + C_MAXR, c->h_ctr + C_MAXR, 8, cudaMemcpyHostToDevice, s));
         GRG_CUDA(c, cudaGraphLaunch(c->rg_exec, s));
         if ((st = read_ctr(c))) return st;
         const unsigned long long halt = c->h_ctr[C_HALT], rounds = c->h_ctr[C_GROUNDS];
@@ -2368,6 +2437,7 @@ static int run_rounds(grg_ctx *c, uint64_t max_rounds, grg_stats &S, double &joi
             *idle = true;
             break;
         }
+        if (halt == HALT_ROUNDS) continue;      // the loop head ends the step
         if (halt == HALT_CAPACITY) {
             // this round's dirty bits are untouched: the host runs it from the start
             uint64_t nd = 0, nv = 0;
@@ -2650,6 +2720,33 @@ int grg_range_counts(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t *cou
     return GRG_OK;
 }
 
+int grg_range_reach(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t label_mask, uint32_t num_parts,
+                    const uint32_t *bounds, uint8_t *reach)
+{
+    if (!c || v_begin > v_end || num_parts == 0 || !bounds || !reach) return GRG_E_ARG;
+    if (!c->loaded) return fail(c, GRG_E_STATE, "no graph loaded");
+    if (v_end > c->V) return fail(c, GRG_E_RANGE, "vertex range beyond the graph");
+    for (uint32_t p = 0; p < num_parts; p++)
+        if (bounds[p] > bounds[p + 1]) return fail(c, GRG_E_ARG, "partition bounds must not decrease");
+    cudaSetDevice(c->device);
+    cudaStream_t s = c->stream;
+    uint32_t *db = nullptr;                      // bounds, then one flag per partition
+    GRG_CUDA(c, cudaMallocAsync((void **)&db, (2 * (size_t)num_parts + 1) * 4, s));
+    GRG_CUDA(c, cudaMemcpyAsync(db, bounds, ((size_t)num_parts + 1) * 4, cudaMemcpyHostToDevice, s));
+    GRG_CUDA(c, cudaMemsetAsync(db + num_parts + 1, 0, (size_t)num_parts * 4, s));
+    const uint64_t ntab = (uint64_t)c->L * (v_end - v_begin);
+    if (ntab)
+        k_range_reach<<<grid_for(c, ntab * 32, 256), 256, 0, s>>>(make_dev(c), v_begin, v_end, (uint32_t)c->L,
+                                                                  label_mask, db, num_parts, db + num_parts + 1);
+    std::vector<uint32_t> f(num_parts);
+    GRG_CUDA(c, cudaMemcpyAsync(f.data(), db + num_parts + 1, (size_t)num_parts * 4, cudaMemcpyDeviceToHost, s));
+    GRG_CUDA(c, cudaFreeAsync(db, s));
+    GRG_CUDA(c, cudaStreamSynchronize(s));
+    GRG_CUDA(c, cudaGetLastError());
+    for (uint32_t p = 0; p < num_parts; p++) reach[p] = f[p] ? 1 : 0;
+    return GRG_OK;
+}
+
 int grg_set_pool_limit(grg_ctx *c, uint64_t pool_bytes)
 {
     if (!c) return GRG_E_ARG;
@@ -2748,12 +2845,30 @@ int grg_batch_admit(grg_ctx *c, uint32_t job, uint32_t base, uint32_t num_vars, 
         ddst = c->d_in32 + num_edges;
         dlab = c->d_in8;
     }
-    // room for the job's tables: edges x 4/3 plus presized derived rows
+    // room for the job's tables: edges x 4/3 plus presized derived rows -- only of the
+    // labels the job's own edges can derive (host inputs), else of every derived label
     MinCap mc;
     memset(&mc, 0, sizeof mc);
     bool lhs[MAX_LABELS + 1] = {false};
     int nder = 0;
-    for (int q = 0; q < c->R; q++) lhs[c->rules[3 * q]] = true;
+    if (!on_device) {
+        bool have[MAX_LABELS + 1] = {false};
+        for (uint64_t e = 0; e < num_edges; e++)
+            if (label[e] >= 1 && label[e] <= c->L) have[label[e]] = true;
+        for (int l = 1; l <= c->L; l++)
+            if ((eps_mask >> (l - 1)) & 1ull) have[l] = true;
+        for (bool grew = true; grew;) {
+            grew = false;
+            for (int q = 0; q < c->R; q++) {
+                const int *r = &c->rules[3 * q];
+                if (r[1] && have[r[1]] && (!r[2] || have[r[2]]) && !have[r[0]]) have[r[0]] = grew = true;
+            }
+        }
+        for (int q = 0; q < c->R; q++)
+            if (have[c->rules[3 * q]]) lhs[c->rules[3 * q]] = true;
+    } else {
+        for (int q = 0; q < c->R; q++) lhs[c->rules[3 * q]] = true;
+    }
     for (int l = 1; l <= c->L; l++) nder += lhs[l];
     int st = read_ctr(c);
     if (st) return st;

@@ -16,10 +16,15 @@
 //           closure needs only its own rows and static rows: the static
 //           labels of the whole graph stay in the load, each partition's rows
 //           are closed once, in turn (no supersteps).
-//   pairs   otherwise: supersteps over pairs (a, b). Every element carries a
-//           stamp (the run that last gave it bits); a pair's run marks as
-//           round-1 deltas exactly the elements stamped after the pair's last
-//           run, and a pair none of whose elements is newer is skipped. A
+//   pairs   otherwise: supersteps over pairs (a, b). A join A(i,j) <- B(i,k)
+//           C(k,j) involves rows i and k only, so a run that holds a closes
+//           a's own rows, and a pair (a, b) adds something only if a B-edge
+//           crosses between them (each partition's reach set, computed on the
+//           device after every run; the reference's data-dependence manager,
+//           src/ddm.cpp:9-132, never called there). Every element carries a
+//           stamp (the run that last gave it bits); a run marks as round-1
+//           deltas exactly the elements stamped after the last run that held
+//           the same partitions, and is skipped when none is newer. A
 //           superstep without a run is the fixpoint.
 // A run that does not fit (GRG_E_NOMEM) splits the larger partition at its
 // median element and is repeated.
@@ -47,6 +52,7 @@ struct Image {
     uint32_t max_stamp = 0;
     uint32_t last_run = 0;           // last run that held this partition
     bool counted = false;            // counts/hash are those of the current image
+    std::vector<uint32_t> reach;     // ids of partitions this one's B-edges may end in (sorted)
     std::vector<uint64_t> counts;
     uint64_t hash = 0;
 
@@ -102,6 +108,7 @@ struct grg_part {
     bool closed = false;
     Pinned in, out;
     grg_part_stats S{};
+    uint64_t bmask = 0;              // labels that are a binary rule's first symbol
 };
 
 namespace {
@@ -147,6 +154,24 @@ int count_image(grg_part *p, Image &img)
     return GRG_OK;
 }
 
+// Reach set of parts[i] over the current partition bounds (graph loaded on the device).
+int reach_image(grg_part *p, size_t i)
+{
+    const size_t m = p->parts.size();
+    std::vector<uint32_t> bounds(m + 1);
+    for (size_t q = 0; q < m; q++) bounds[q] = p->parts[q].lo;
+    bounds[m] = p->parts[m - 1].hi;
+    std::vector<uint8_t> r(m);
+    Image &x = p->parts[i];
+    int st = grg_range_reach(p->ctx, x.lo, x.hi, p->bmask, (uint32_t)m, bounds.data(), r.data());
+    if (st) return st;
+    x.reach.clear();
+    for (size_t q = 0; q < m; q++)
+        if (r[q]) x.reach.push_back(p->parts[q].id);
+    std::sort(x.reach.begin(), x.reach.end());
+    return GRG_OK;
+}
+
 // Split parts[i] at its median element (by source row); false when it is one row.
 bool split(grg_part *p, size_t i)
 {
@@ -187,6 +212,21 @@ bool split(grg_part *p, size_t i)
     }
     for (const auto &kv : add) p->seen[kv.first] = kv.second;
     p->seen[pkey(a.id, b.id)] = x.last_run;
+    p->seen[pkey(a.id, a.id)] = p->seen.count(pkey(x.id, x.id)) ? p->seen[pkey(x.id, x.id)] : 0;
+    p->seen[pkey(b.id, b.id)] = p->seen[pkey(a.id, a.id)];
+    // reach: what reached x (or x itself) may now reach either half
+    auto widen = [&](std::vector<uint32_t> &r) {
+        if (std::binary_search(r.begin(), r.end(), x.id)) {
+            r.push_back(a.id);
+            r.push_back(b.id);
+            std::sort(r.begin(), r.end());
+        }
+    };
+    a.reach = x.reach;
+    widen(a.reach);
+    b.reach = a.reach;
+    for (Image &y : p->parts)
+        if (y.id != x.id) widen(y.reach);
     p->parts[i] = std::move(a);
     p->parts.insert(p->parts.begin() + i + 1, std::move(b));
     p->S.splits++;
@@ -272,42 +312,64 @@ int run_stream(grg_part *p, uint32_t filter, const bool *der)
     return GRG_OK;
 }
 
+uint32_t seen_of(grg_part *p, uint32_t a, uint32_t b)
+{
+    auto it = p->seen.find(pkey(a, b));
+    return it == p->seen.end() ? 0 : it->second;
+}
+
+bool reaches(const Image &a, const Image &b)
+{
+    return std::binary_search(a.reach.begin(), a.reach.end(), b.id) ||
+           std::binary_search(b.reach.begin(), b.reach.end(), a.id);
+}
+
 int run_pairs(grg_part *p, uint32_t filter)
 {
     for (;;) {
         bool ran = false, restart = false;
+        // pairs whose B-edges cross, then partitions no run has closed since their last change
+        std::vector<std::pair<size_t, size_t>> order;
         const size_t m = p->parts.size();
-        for (size_t i = 0; i < m && !restart; i++) {
-            for (size_t j = (m == 1 ? i : i + 1); j < m && !restart; j++) {
-                Image &a = p->parts[i], &b = p->parts[j];
-                const auto key = pkey(a.id, b.id);
-                const uint32_t t = p->seen.count(key) ? p->seen[key] : 0;
-                if (a.max_stamp <= t && b.max_stamp <= t) {
-                    p->S.skipped++;
-                    continue;
-                }
-                const uint32_t r = ++p->run_id;
-                std::vector<size_t> idx = {i};
-                if (j != i) idx.push_back(j);
-                const int st = run_once(p, filter, idx, nullptr, nullptr, t, r);
-                if (st == GRG_E_NOMEM) {
-                    const size_t big = (j != i && b.size() > a.size()) ? j : i;
-                    if (!split(p, big)) return GRG_E_NOMEM;
-                    restart = true;
-                    break;
-                }
-                if (st) return st;
-                for (size_t q : idx) {
-                    Image &x = p->parts[q];
-                    int s2 = export_image(p, x);
-                    if (s2) return s2;
-                    if ((s2 = count_image(p, x))) return s2;
-                    x.refresh();
-                    x.last_run = r;
-                }
-                p->seen[key] = r;
-                ran = true;
+        for (size_t i = 0; i < m; i++)
+            for (size_t j = i + 1; j < m; j++) order.emplace_back(i, j);
+        for (size_t i = 0; i < m; i++) order.emplace_back(i, i);
+        for (const auto &ij : order) {
+            const size_t i = ij.first, j = ij.second;
+            Image &a = p->parts[i], &b = p->parts[j];
+            const uint32_t t = seen_of(p, a.id, b.id);
+            bool need;
+            if (i == j)
+                need = a.max_stamp > t;
+            else
+                need = reaches(a, b) && (a.max_stamp > t || b.max_stamp > t);
+            if (!need) {
+                p->S.skipped++;
+                continue;
             }
+            const uint32_t r = ++p->run_id;
+            std::vector<size_t> idx = {i};
+            if (j != i) idx.push_back(j);
+            const int st = run_once(p, filter, idx, nullptr, nullptr, t, r);
+            if (st == GRG_E_NOMEM) {
+                const size_t big = (j != i && b.size() > a.size()) ? j : i;
+                if (!split(p, big)) return GRG_E_NOMEM;
+                restart = true;
+                break;
+            }
+            if (st) return st;
+            for (size_t q : idx) {
+                int s2 = export_image(p, p->parts[q]);
+                if (s2) return s2;
+                if ((s2 = count_image(p, p->parts[q]))) return s2;
+                if ((s2 = reach_image(p, q))) return s2;
+                Image &x = p->parts[q];
+                x.refresh();
+                x.last_run = r;
+                p->seen[pkey(x.id, x.id)] = r;   // a run that holds x closes x's own rows
+            }
+            p->seen[pkey(a.id, b.id)] = r;
+            ran = true;
         }
         if (restart) continue;
         p->S.supersteps++;
@@ -331,6 +393,8 @@ int grg_part_create(grg_part **out, grg_ctx *ctx, uint32_t num_vars, uint32_t nu
         delete p;
         return st;
     }
+    for (int q = 0; q < p->R; q++)
+        if (p->rules[3 * q + 1] && p->rules[3 * q + 2]) p->bmask |= 1ull << (p->rules[3 * q + 1] - 1);
     const uint32_t m = std::max<uint32_t>(1, std::min<uint32_t>(num_parts, std::max<uint32_t>(num_vars, 1)));
     for (uint32_t i = 0; i < m; i++) {
         Image x;
@@ -383,6 +447,12 @@ int grg_part_load_edges(grg_part *p, uint64_t num_edges, const uint32_t *src, co
             }
             bk[i] = std::move(lo_b);
             bk.insert(bk.begin() + i + 1, std::move(hi_b));
+            // partitions already loaded that reach x may reach its upper half
+            for (Image &y : p->parts)
+                if (std::binary_search(y.reach.begin(), y.reach.end(), x.id)) {
+                    y.reach.push_back(b.id);
+                    std::sort(y.reach.begin(), y.reach.end());
+                }
             p->parts.insert(p->parts.begin() + i + 1, std::move(b));
             p->S.splits++;
             continue;
@@ -390,6 +460,7 @@ int grg_part_load_edges(grg_part *p, uint64_t num_edges, const uint32_t *src, co
         if (st) return st;
         p->S.h2d_bytes += b0.s.size() * 9;
         if ((st = export_image(p, p->parts[i]))) return st;
+        if ((st = reach_image(p, i))) return st;
         Image &y = p->parts[i];
         for (uint32_t &t : y.st) t = 1;
         y.refresh();

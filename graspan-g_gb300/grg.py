@@ -32,7 +32,7 @@ EXPORTS = (
     "grg_batch_step", "grg_batch_result", "grg_batch_release", "grg_get_rules", "grg_closure_ex",
     "grg_load_elements", "grg_export_elements", "grg_range_counts", "grg_set_pool_limit", "grg_part_create",
     "grg_part_destroy", "grg_part_load_edges", "grg_part_run", "grg_part_label_counts", "grg_part_bounds",
-    "grg_set_device_rounds",
+    "grg_set_device_rounds", "grg_range_reach",
 )
 
 
@@ -118,6 +118,7 @@ def load_library(path: str = LIB_PATH):
     L.grg_export_elements.argtypes = [P, U32, U32, U64, P, P, ctypes.POINTER(U64)]
     L.grg_range_counts.argtypes = [P, U32, U32, P, ctypes.POINTER(U64)]
     L.grg_set_pool_limit.argtypes = [P, U64]
+    L.grg_range_reach.argtypes = [P, U32, U32, U64, U32, P, P]
     L.grg_part_create.argtypes = [ctypes.POINTER(P), P, U32, U32]
     L.grg_part_destroy.argtypes = [P]
     L.grg_part_destroy.restype = None
@@ -318,6 +319,13 @@ class Context:
         self._check(self._L.grg_export_elements(self._h, v_begin, v_end, n.value, _ptr(recs), _ptr(stamps),
                                                 ctypes.byref(n)), "export_elements")
         return recs, stamps
+
+    def range_reach(self, v_begin, v_end, label_mask, bounds):
+        bounds = np.ascontiguousarray(bounds, dtype=np.uint32)
+        out = np.zeros(len(bounds) - 1, np.uint8)
+        self._check(self._L.grg_range_reach(self._h, v_begin, v_end, label_mask, len(out), _ptr(bounds), _ptr(out)),
+                    "range_reach")
+        return out
 
     def range_counts(self, v_begin, v_end):
         counts = np.zeros(self.num_labels, dtype=np.uint64)

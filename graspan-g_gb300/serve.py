@@ -107,9 +107,13 @@ class RangeAllocator:
         self.free = merged
 
 
-def serve(jobs, max_vars, max_jobs=256, budget_bytes=None, device=0, realtime=True, rounds_per_step=1):
+def serve(jobs, max_vars, max_jobs=256, budget_bytes=None, device=0, realtime=True, rounds_per_step=4,
+          drain_rounds=0):
     """Run the service over `jobs` (arrival_s relative to the start). With
-    realtime=False every job is available at t=0 (a pure batch)."""
+    realtime=False every job is available at t=0 (a pure batch). A step runs
+    rounds_per_step rounds while jobs wait for admission, else drain_rounds
+    (0 = until every admitted job has reached its fixpoint); the rounds of a
+    step run on the device without host round trips."""
     ctx = grg.Context(device)
     ctx.allocate_pool(0)
     batch = grg.Batch(ctx, max_vars, max_jobs, GRAMMARS, 0)
@@ -145,7 +149,7 @@ def serve(jobs, max_vars, max_jobs=256, budget_bytes=None, device=0, realtime=Tr
             if pending:
                 time.sleep(max(0.0, pending[0].arrival_s - (time.perf_counter() - t0)))
             continue
-        rec, _ = batch.step(rounds_per_step)
+        rec, _ = batch.step(rounds_per_step if pending else drain_rounds)
         steps += 1
         now = time.perf_counter() - t0
         for slot in [s for s, j in active.items() if rec[s] == 0]:

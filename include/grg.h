@@ -169,6 +169,14 @@ int grg_export_elements(grg_ctx *ctx, uint32_t v_begin, uint32_t v_end, uint64_t
 /* Per-label edge counts (num_labels values) and edge-set hash (may be NULL;
  * same hash terms as grg_set_hash) of the rows [v_begin, v_end). */
 int grg_range_counts(grg_ctx *ctx, uint32_t v_begin, uint32_t v_end, uint64_t *counts, uint64_t *hash);
+/* Partitions that rows [v_begin, v_end) reach: reach[p] = 1 (num_parts
+ * values) when an edge of a label in label_mask (bit l-1 = label l) from those
+ * rows may end in [bounds[p], bounds[p+1]) (bounds: num_parts+1 non-decreasing
+ * vertex ids). May report a partition too many, never one too few. A pair
+ * of partitions neither of which reaches the other has no join across them
+ * (the reference's data-dependence manager idea, src/ddm.cpp:9-132). */
+int grg_range_reach(grg_ctx *ctx, uint32_t v_begin, uint32_t v_end, uint64_t label_mask, uint32_t num_parts,
+                    const uint32_t *bounds, uint8_t *reach);
 /* Cap the element pool at pool_bytes of device memory (0 = no cap): a load or
  * closure that needs more fails with GRG_E_NOMEM instead of growing the pool.
  * A pool already larger is freed (the loaded graph is dropped). */

@@ -144,3 +144,34 @@ def test_element_image_round_trip(grg_mod, oracle_mod):
     assert ei.value.status == grg_mod.E_ARG
     ctx.close()
     ctx2.close()
+
+
+def test_range_reach_matches_edges(grg_mod):
+    # reach of a vertex range = the partitions its B-label edges end in (a superset at most)
+    w = G.pointsto(seed=17, num_vars=700, num_edges=1600)
+    ctx = grg_mod.Context(0)
+    ctx.transfer_rules(w.rule_ids(), w.num_labels)
+    ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
+    bounds = np.array([0, 100, 250, 251, 400, 700], np.uint32)
+    ids = w.rule_ids()
+    bmask = 0
+    for r in ids:
+        if r[1] and r[2]:
+            bmask |= 1 << (int(r[1]) - 1)
+    for lo, hi in [(0, 100), (100, 400), (250, 251), (0, 700)]:
+        got = ctx.range_reach(lo, hi, bmask, bounds)
+        sel = (w.src >= lo) & (w.src < hi) & (((bmask >> (w.lab.astype(np.int64) - 1)) & 1) == 1)
+        want = np.zeros(len(bounds) - 1, bool)
+        for d in w.dst[sel]:
+            want[np.searchsorted(bounds, d, side="right") - 1] = True
+        assert np.all(got[want] == 1), (lo, hi)          # never one too few
+    ctx.close()
+
+
+def test_block_graph_needs_no_cross_pairs(grg_mod, oracle_mod):
+    # block-confined alias graph, partitions on block boundaries: self-runs only, no pair runs
+    w = G.alias(seed=19, num_vars=4000, num_base_edges=8000, block=500)
+    want = oracle_result(oracle_mod, w, 0)
+    counts, h, st, bounds = part_closure(grg_mod, w, 0, 8)
+    assert (counts, h) == want
+    assert st["runs"] == 8 and st["supersteps"] == 2
