@@ -61,7 +61,8 @@ enum : int {
     C_LABEL0 = 24,    // per-label edge counts: C_LABEL0 + slot
     C_JT0 = C_LABEL0 + MAX_SLOTS + 2,   // start time of the current join pass (device-driven rounds)
     C_MAXR = C_LABEL0 + MAX_SLOTS + 3,  // rounds a device-driven launch may run (0 = until the fixpoint)
-    NCTR = C_LABEL0 + MAX_SLOTS + 4
+    C_WOUT = C_LABEL0 + MAX_SLOTS + 4,  // right-hand items the join's dense window could not hold
+    NCTR = C_LABEL0 + MAX_SLOTS + 5
 };
 enum : unsigned long long { ERR_POOL = 1, ERR_LOAD = 2, ERR_INTERNAL = 4 };
 

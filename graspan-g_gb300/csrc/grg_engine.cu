@@ -119,6 +119,14 @@ constexpr int JOIN_WARPS = GRG_JOIN_WARPS;  // warps per join block
 constexpr int RB = 32;            // delta records per warp batch (one per lane)
 constexpr int WIN = GRG_WIN;      // dense accumulator window: elements base-WIN_LO .. base+WIN-1-WIN_LO
 constexpr int WIN_LO = GRG_WIN_LO;
+#ifndef GRG_WIN2
+#define GRG_WIN2 12
+#endif
+#ifndef GRG_WIN2_LO
+#define GRG_WIN2_LO 6
+#endif
+constexpr int WIN2 = GRG_WIN2;    // wide window: rows whose destinations spread over many elements
+constexpr int WIN2_LO = GRG_WIN2_LO;
 constexpr int JOIN_UNROLL = GRG_JOIN_UNROLL;
 constexpr int ACC_LG = GRG_ACC_LG;
 constexpr int ACC = 1 << ACC_LG;  // per-warp hash accumulator entries (candidates outside the window)
@@ -451,8 +459,12 @@ __global__ void k_oldleft(Dev d, uint32_t q, uint4 *out, uint64_t cap)
     }
 }
 
-struct __align__(16) WarpSmem {
-    uint32_t win[RB][WIN][EW];    // dense window accumulator per record
+// Per-warp shared memory of the join, for a dense window of W elements per
+// record covering bases rbase-LO .. rbase+W-1-LO.
+template <int W, int LO>
+struct __align__(16) WarpSmemT {
+    static constexpr int kWin = W, kLo = LO;
+    uint32_t win[RB][W][EW];      // dense window accumulator per record
     uint32_t acc_bits[ACC][EW];   // hash accumulator: OR of candidate bitmaps
     uint32_t acc_key[ACC];        // key = record << 25 | base (EMPTY = free)
     uint32_t rbits[RB][EW];       // the batch's delta records
@@ -490,7 +502,8 @@ __device__ __forceinline__ uint32_t select_bit(const uint32_t *bits, uint32_t id
 }
 
 // Exclusive warp prefix of per-lane task counts into kpre[0..RB]; returns the total.
-__device__ __forceinline__ uint32_t warp_tasks(WarpSmem &w, uint32_t cnt)
+template <class WS>
+__device__ __forceinline__ uint32_t warp_tasks(WS &w, uint32_t cnt)
 {
     const uint32_t lane = lane_id();
     uint32_t incl = cnt;
@@ -507,7 +520,8 @@ __device__ __forceinline__ uint32_t warp_tasks(WarpSmem &w, uint32_t cnt)
 }
 
 // Record owning flattened task t: largest r with kpre[r] <= t.
-__device__ __forceinline__ uint32_t task_record(const WarpSmem &w, uint32_t t)
+template <class WS>
+__device__ __forceinline__ uint32_t task_record(const WS &w, uint32_t t)
 {
     uint32_t lo = 0, hi = RB - 1;
     while (lo < hi) {
@@ -518,7 +532,8 @@ __device__ __forceinline__ uint32_t task_record(const WarpSmem &w, uint32_t t)
 }
 
 // OR (key, b) into the warp's hash accumulator; false when it is full.
-__device__ __forceinline__ bool acc_insert(WarpSmem &w, uint32_t key, const Bits b)
+template <class WS>
+__device__ __forceinline__ bool acc_insert(WS &w, uint32_t key, const Bits b)
 {
     volatile uint32_t *keys = w.acc_key;
     const uint32_t h = (key * 0x9E3779B1u) >> (32 - ACC_LG);
@@ -583,7 +598,8 @@ __device__ __forceinline__ void cand_write(const Dev &d, uint64_t i, const Bits 
 // Flush the hash accumulator: entry (r, base) goes to row (rA[r], rrow[r]),
 // as a candidate for k_apply or, when the candidate buffer is full, by a
 // direct insert. Warp-uniform.
-__device__ __forceinline__ void acc_flush(const Dev &d, WarpSmem &w, uint32_t &inserts)
+template <class WS>
+__device__ __forceinline__ void acc_flush(const Dev &d, WS &w, uint32_t &inserts)
 {
     __syncwarp();
     uint32_t nz = 0;
@@ -615,8 +631,10 @@ __device__ __forceinline__ void acc_flush(const Dev &d, WarpSmem &w, uint32_t &i
 }
 
 // Flush every record's window into row (rA[r], rrow[r]) and clear it. Warp-uniform.
-__device__ __forceinline__ void win_flush(const Dev &d, WarpSmem &w, uint32_t &inserts)
+template <class WS>
+__device__ __forceinline__ void win_flush(const Dev &d, WS &w, uint32_t &inserts)
 {
+    constexpr int WIN = WS::kWin, WIN_LO = WS::kLo;
     __syncwarp();
     uint32_t nz = 0;
 #pragma unroll
@@ -676,9 +694,13 @@ __global__ void __launch_bounds__(256) k_apply(Dev d, const uint4 *__restrict__ 
 // items are flattened over the lanes so every phase keeps 32 independent memory
 // operations in flight.
 // n_ctr >= 0: the record count is device counter n_ctr (round graphs).
-__global__ void __launch_bounds__(JOIN_WARPS * 32, GRG_JOIN_MINB) k_join(Dev d, const uint4 *__restrict__ recs,
-                                                                        uint64_t n, int n_ctr, uint4 *retry_out)
+// W, LO: the dense window (instantiated for narrow and wide rows; see join_wide).
+template <int W, int LO>
+__global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : 4))
+    k_join(Dev d, const uint4 *__restrict__ recs, uint64_t n, int n_ctr, uint4 *retry_out)
 {
+    constexpr int WIN = W, WIN_LO = LO;
+    using WarpSmem = WarpSmemT<W, LO>;
     if (d.ctr[C_HALT]) return;
     if (n_ctr >= 0) n = d.ctr[n_ctr];
     __shared__ WarpSmem smem[JOIN_WARPS];
@@ -692,7 +714,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, GRG_JOIN_MINB) k_join(Dev d, 
     for (int j = lane; j < RB * WIN * EW; j += 32) (&w.win[0][0][0])[j] = 0;
     if (lane == 0) w.acc_n = 0;
     __syncwarp();
-    unsigned long long n_left = 0, n_right = 0;
+    unsigned long long n_left = 0, n_right = 0, n_out = 0;
     uint32_t inserts = 0;
 #ifdef GRG_PHASE_TIMERS
     unsigned long long ph[5] = {0, 0, 0, 0, 0};
@@ -843,6 +865,8 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, GRG_JOIN_MINB) k_join(Dev d, 
                         if (it_ok[u]) {
                             const uint32_t o_r = it_r[u];
                             const int dd = (int)it_b2[u] - (int)w.rbase[o_r] + WIN_LO;
+                            // the statistic the window choice is keyed on: items beyond the narrow window
+                            n_out += (unsigned)(dd - WIN_LO + grg::WIN_LO) >= (unsigned)grg::WIN;
                             if ((unsigned)dd < (unsigned)WIN) {
 #pragma unroll
                                 for (int x = 0; x < EW; x++)
@@ -891,10 +915,12 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, GRG_JOIN_MINB) k_join(Dev d, 
         inserts += __shfl_xor_sync(0xffffffffu, inserts, o);
         n_left += __shfl_xor_sync(0xffffffffu, n_left, o);
         n_right += __shfl_xor_sync(0xffffffffu, n_right, o);
+        n_out += __shfl_xor_sync(0xffffffffu, n_out, o);
     }
     if (lane == 0) {
         if (n_left) atomicAdd(&d.ctr[C_LEFT], n_left);
         if (n_right) atomicAdd(&d.ctr[C_RIGHT], n_right);
+        if (n_out) atomicAdd(&d.ctr[C_WOUT], n_out);
         if (inserts) atomicAdd(&d.ctr[C_INSERTS], (unsigned long long)inserts);
     }
 }
@@ -1356,7 +1382,8 @@ struct grg_ctx {
     bool closed = false;
     uint32_t V = 0;
     uint64_t ntables = 0;          // L * V (label slots 1..L)
-    uint64_t ntables_alloc = 0;    // L * V
+    uint64_t ntables_alloc = 0;    // table entries allocated (>= L * V)
+    uint64_t dvm_alloc = 0;        // dirty-vertex bitmap words allocated
     // device memory
     uint64_t pool_bytes_req = 0;
     uint64_t pool_cap = 0;         // elements
@@ -1391,6 +1418,9 @@ struct grg_ctx {
     uint32_t *xst = nullptr;               // staged stamps
     uint64_t xcap = 0;
     uint64_t pool_limit = 0;               // maximum pool slots (0 = what the device holds)
+    // join window: narrow (WIN) or wide (WIN2, the default)
+    bool join_wide = true;
+    int join_window_mode = 1;              // 0 = narrow, 1 = wide
     // device-driven rounds: a CUDA graph whose WHILE node repeats one closure round
     bool device_rounds = true;
     cudaStream_t cap_stream = nullptr;     // stream the round graph is recorded on
@@ -1400,7 +1430,12 @@ struct grg_ctx {
     int rg_kernels = 0;                    // kernels per recorded round
     RuleTable rt{};
     uint64_t launches = 0;
-    std::vector<uint32_t *> csr_bufs;      // CSR copies of static labels (freed on reload)
+    // CSR copies of static labels, per label; reused by later closures while they fit
+    struct CsrBuf {
+        uint32_t *ptr = nullptr, *sums = nullptr, *col = nullptr;
+        uint2 *row = nullptr;
+        uint64_t vcap = 0, colcap = 0;
+    } csr[MAX_LABELS + 1];
     // batched jobs (continuous batching): each job owns a vertex range
     uint32_t *row_job = nullptr;           // vertex -> job slot (EMPTY = free)
     uint32_t *job_cnt = nullptr;           // delta records per job slot in the last gather
@@ -1480,8 +1515,13 @@ Dev make_dev(const grg_ctx *c)
 
 void free_csr(grg_ctx *c)
 {
-    for (uint32_t *p : c->csr_bufs) cudaFree(p);
-    c->csr_bufs.clear();
+    for (auto &b : c->csr) {
+        cudaFree(b.ptr);
+        cudaFree(b.sums);
+        cudaFree(b.col);
+        cudaFree(b.row);
+        b = grg_ctx::CsrBuf();
+    }
 }
 
 void free_graph(grg_ctx *c)
@@ -1490,6 +1530,7 @@ void free_graph(grg_ctx *c)
     cudaFree(c->drs); c->drs = nullptr;
     cudaFree(c->drc); c->drc = nullptr;
     cudaFree(c->dvm); c->dvm = nullptr;
+    c->dvm_alloc = 0;
     cudaFree(c->row_job); c->row_job = nullptr;
     cudaFree(c->job_cnt); c->job_cnt = nullptr;
     c->max_jobs = 0;
@@ -1632,6 +1673,7 @@ int ensure_rbuf(grg_ctx *c, uint64_t n)
 int alloc_dindex(grg_ctx *c)
 {
     const uint64_t nt = (uint64_t)c->L * c->V, vw = (uint64_t)c->L * ((c->V + 31) / 32);
+    c->dvm_alloc = std::max<uint64_t>(vw, 1);
     GRG_CUDA(c, cudaMalloc(&c->drs, std::max<uint64_t>(nt, 1) * 4));
     GRG_CUDA(c, cudaMalloc(&c->drc, std::max<uint64_t>(nt, 1) * 4));
     GRG_CUDA(c, cudaMalloc(&c->dvm, std::max<uint64_t>(vw, 1) * 4));
@@ -1687,6 +1729,8 @@ int grg_create(grg_ctx **out, int device)
     c->stream = c->own_stream;
     const char *dr = getenv("GRG_DEVICE_ROUNDS");      // "0": every round driven from the host
     c->device_rounds = !(dr && dr[0] == '0');
+    const char *jw = getenv("GRG_JOIN_WINDOW");        // "narrow" / "wide"; otherwise chosen per closure
+    if (jw) c->join_window_mode = !strcmp(jw, "narrow") ? 0 : 1;
     *out = c;
     return GRG_OK;
 }
@@ -1726,6 +1770,13 @@ int grg_set_stream(grg_ctx *c, void *stream)
 {
     if (!c) return GRG_E_ARG;
     c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    return GRG_OK;
+}
+
+int grg_set_join_window(grg_ctx *c, int mode)
+{
+    if (!c || mode < 0 || mode > 1) return GRG_E_ARG;
+    c->join_window_mode = mode;
     return GRG_OK;
 }
 
@@ -1810,7 +1861,9 @@ int setup_tables(grg_ctx *c, uint32_t num_vars)
     c->V = num_vars;
     c->ntables = (uint64_t)c->L * num_vars;
     const uint64_t nt_all = c->ntables;
-    if (c->ntables_alloc != nt_all || c->batch) {
+    // table arrays are kept while a graph needs no more than they hold
+    if (c->ntables_alloc < nt_all || c->batch ||
+        c->dvm_alloc < (uint64_t)c->L * ((num_vars + 31) / 32)) {
         free_graph(c);
         GRG_CUDA(c, cudaMalloc(&c->desc, std::max<uint64_t>(nt_all, 1) * 8));
         GRG_CUDA(c, cudaMalloc(&c->cnt, std::max<uint64_t>(nt_all, 1) * 4));
@@ -2031,6 +2084,22 @@ int grg_load_elements(grg_ctx *c, uint32_t num_vars, uint64_t num_elems, const u
 // not fit after growing its tables. The pieces are separate so a round the
 // device-driven loop hands back can be finished where it stopped.
 
+// Window of this closure's joins. Measured on dataflow, alias, points-to and
+// small alias jobs, the 12-element window (with the registers its launch
+// bounds leave) was fastest or within 1.5% on every one, so it is the default;
+// the narrow window stays selectable.
+static void choose_window(grg_ctx *c) { c->join_wide = c->join_window_mode != 0; }
+
+// The join kernel in the window chosen for this closure (join_wide).
+static void launch_join(const grg_ctx *c, int grid, cudaStream_t s, const Dev &d, const uint4 *recs, uint64_t n,
+                        int n_ctr, uint4 *retry_out)
+{
+    if (c->join_wide)
+        k_join<WIN2, WIN2_LO><<<grid, JOIN_WARPS * 32, 0, s>>>(d, recs, n, n_ctr, retry_out);
+    else
+        k_join<WIN, WIN_LO><<<grid, JOIN_WARPS * 32, 0, s>>>(d, recs, n, n_ctr, retry_out);
+}
+
 // Round head: count and gather the dirty slots (rs: stamp for elements that
 // gained bits, 0 = none). *nd = delta records (0 = fixpoint).
 static int round_head(grg_ctx *c, uint32_t rs, grg_stats &S, uint64_t *nd_out)
@@ -2141,8 +2210,7 @@ static int round_retries(grg_ctx *c, uint64_t nr, uint64_t nf, grg_stats &S, dou
         GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_RETRY_N, 0, 16, s));
         if (c->timing) GRG_CUDA(c, cudaEventRecord(c->ev_c, s));
         if (nr) {
-            k_join<<<grid_for(c, (nr + RB - 1) / RB, JOIN_WARPS, 16), JOIN_WARPS * 32, 0, s>>>(d, c->rbuf[rb], nr, -1,
-                                                                                             c->rbuf[rb ^ 1]);
+            launch_join(c, grid_for(c, (nr + RB - 1) / RB, JOIN_WARPS, 16), s, d, c->rbuf[rb], nr, -1, c->rbuf[rb ^ 1]);
             c->launches++;
             joins++;
         }
@@ -2173,12 +2241,11 @@ static int round_joins(grg_ctx *c, uint64_t nd, uint64_t nv, grg_stats &S, doubl
     if (st) return st;
     Dev d = make_dev(c);
     if (c->timing) GRG_CUDA(c, cudaEventRecord(c->ev_c, s));
-    k_join<<<grid_for(c, (nd + RB - 1) / RB, JOIN_WARPS, 16), JOIN_WARPS * 32, 0, s>>>(d, c->gbuf, nd, -1, c->rbuf[0]);
+    launch_join(c, grid_for(c, (nd + RB - 1) / RB, JOIN_WARPS, 16), s, d, c->gbuf, nd, -1, c->rbuf[0]);
     c->launches++;
     joins++;
     if (nv) {
-        k_join<<<grid_for(c, (nv + RB - 1) / RB, JOIN_WARPS, 16), JOIN_WARPS * 32, 0, s>>>(d, c->vbuf, nv, -1,
-                                                                                         c->rbuf[0]);
+        launch_join(c, grid_for(c, (nv + RB - 1) / RB, JOIN_WARPS, 16), s, d, c->vbuf, nv, -1, c->rbuf[0]);
         c->launches++;
         joins++;
     }
@@ -2291,7 +2358,7 @@ static std::vector<uint64_t> round_graph_key(const grg_ctx *c, uint32_t rs, uint
                                (uint64_t)c->cand[1], c->cand_cap, (uint64_t)c->chunk, nchunks, (uint64_t)c->drs,
                                (uint64_t)c->drc, (uint64_t)c->dvm, c->pool_cap, c->V, rs, (uint64_t)c->timing,
                                (uint64_t)c->elem_loaded, (uint64_t)c->rt.nol, (uint64_t)c->row_job,
-                               (uint64_t)c->job_cnt, c->max_jobs};
+                               (uint64_t)c->job_cnt, c->max_jobs, (uint64_t)c->join_wide};
     for (int l = 1; l <= c->L; l++) k.push_back(c->rt.dindex[l]);
     return k;
 }
@@ -2356,10 +2423,10 @@ static int build_round_graph(grg_ctx *c, uint32_t rs)
         nk++;
     }
     const int jgrid = grid_for(c, ~0u, JOIN_WARPS, 16);
-    k_join<<<jgrid, JOIN_WARPS * 32, 0, s>>>(d, c->gbuf, 0, C_DIRTY_N, c->rbuf[0]);
+    launch_join(c, jgrid, s, d, c->gbuf, 0, C_DIRTY_N, c->rbuf[0]);
     nk++;
     if (c->rt.nol) {
-        k_join<<<jgrid, JOIN_WARPS * 32, 0, s>>>(d, c->vbuf, 0, C_VN, c->rbuf[0]);
+        launch_join(c, jgrid, s, d, c->vbuf, 0, C_VN, c->rbuf[0]);
         nk++;
     }
     if (c->cand_cap) {
@@ -2398,6 +2465,7 @@ static int run_rounds(grg_ctx *c, uint64_t max_rounds, grg_stats &S, double &joi
         if (max_rounds && done_rounds >= max_rounds) break;
         // elements that gain bits in this run get its stamp; round 1 gathers the load marks
         const uint32_t rs = (c->elem_loaded && done_rounds > 0) ? c->run_stamp : 0u;
+        choose_window(c);
         if (!graphs || done_rounds == 0) {
             uint64_t nd = 0, nv = 0;
             if ((st = round_head(c, rs, S, &nd))) return st;
@@ -2410,10 +2478,17 @@ static int run_rounds(grg_ctx *c, uint64_t max_rounds, grg_stats &S, double &joi
             if ((st = round_joins(c, nd, nv, S, join_ms, joins))) return st;
             continue;
         }
-        // device-driven rounds: buffers sized with room to grow, then the graph loop
+        // device-driven rounds: buffers sized with room to grow, then the graph loop. A round
+        // has at most one record per used slot (and one virtual record per old-left rule and
+        // element), so up to 16M records the buffers take what can never overflow and the
+        // recorded graph survives the whole closure.
         const uint64_t nd_last = std::max<uint64_t>(c->h_ctr[C_DIRTY_N], 1);
-        if ((st = ensure_buf(c, &c->gbuf, &c->gbuf_cap, 2 * nd_last))) return st;
-        if (c->rt.nol && (st = ensure_buf(c, &c->vbuf, &c->vbuf_cap, std::max<uint64_t>(c->h_ctr[C_VN], 1) * 4)))
+        const uint64_t top = c->h_ctr[C_POOL_TOP], floor_cap = 1ull << 24;
+        if ((st = ensure_buf(c, &c->gbuf, &c->gbuf_cap, std::max(4 * nd_last, std::min(top, floor_cap))))) return st;
+        if (c->rt.nol &&
+            (st = ensure_buf(c, &c->vbuf, &c->vbuf_cap,
+                             std::max<uint64_t>(4 * std::max<uint64_t>(c->h_ctr[C_VN], 1),
+                                                std::min<uint64_t>((uint64_t)c->rt.nol * top, floor_cap)))))
             return st;
         if ((st = ensure_cand(c, 2 * nd_last))) return st;    // a full candidate buffer falls back to direct inserts
         if ((st = ensure_rbuf(c, c->gbuf_cap + (c->rt.nol ? c->vbuf_cap : 0)))) return st;
@@ -2478,6 +2553,7 @@ int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *s
     if (!c || filter > 1) return GRG_E_ARG;
     if (!c->loaded) return fail(c, GRG_E_STATE, "grg_load_edges must come first");
     c->run_stamp = run_stamp;
+    choose_window(c);
     if (c->closed) return fail(c, GRG_E_STATE, "closure already computed; reload the graph");
     cudaSetDevice(c->device);
     RuleTable rt;
@@ -2502,23 +2578,29 @@ int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *s
             k_compact_static<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)l, 0, c->V);
             c->launches++;
         }
-    // CSR copies of static labels that are a binary rule's second symbol
-    free_csr(c);
+    // CSR copies of static labels that are a binary rule's second symbol (buffers kept per label)
     for (int l = 1; l <= c->L; l++) {
         bool rhs2 = false;
         for (int q = 0; q < c->R; q++)
             if (c->rules[3 * q + 1] && c->rules[3 * q + 2] == l) rhs2 = true;
         if (derivable[l] || !rhs2 || c->V == 0) continue;
-        uint32_t *ptr = nullptr, *sums = nullptr, *col = nullptr, *row = nullptr;
+        grg_ctx::CsrBuf &cb = c->csr[l];
         const uint64_t nb = (c->V + 1023) / 1024;
-        GRG_CUDA(c, cudaMalloc(&ptr, ((uint64_t)c->V + 1) * 4));
-        c->csr_bufs.push_back(ptr);
-        GRG_CUDA(c, cudaMalloc(&row, ((uint64_t)c->V + 1) * 8));
-        c->csr_bufs.push_back(row);
-        GRG_CUDA(c, cudaMalloc(&sums, (nb + 1) * 4));
-        c->csr_bufs.push_back(sums);
+        if (cb.vcap < (uint64_t)c->V + 1) {
+            cudaFree(cb.ptr); cudaFree(cb.row); cudaFree(cb.sums);
+            cb.ptr = cb.sums = nullptr;
+            cb.row = nullptr;
+            cb.vcap = 0;
+            const uint64_t vc = (uint64_t)c->V + 1 + c->V / 4;
+            GRG_CUDA(c, cudaMalloc(&cb.ptr, vc * 4));
+            GRG_CUDA(c, cudaMalloc(&cb.row, vc * 8));
+            GRG_CUDA(c, cudaMalloc(&cb.sums, ((vc + 1023) / 1024 + 1) * 4));
+            cb.vcap = vc;
+        }
+        uint32_t *ptr = cb.ptr, *sums = cb.sums;
+        uint2 *row = cb.row;
         GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_ERR, 0, 8, s));
-        k_csr_count<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)l, ptr, (uint2 *)row);
+        k_csr_count<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)l, ptr, row);
         k_scan_blocks<<<(unsigned)nb, 1024, 0, s>>>(ptr, ptr, sums, c->V, nullptr);
         k_scan_sums<<<1, 1024, 0, s>>>(sums, nb, nullptr);
         k_scan_add<<<(unsigned)nb, 1024, 0, s>>>(ptr, sums, c->V, nullptr);
@@ -2528,12 +2610,18 @@ int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *s
         uint32_t total = 0;
         GRG_CUDA(c, cudaMemcpyAsync(&total, sums + nb, 4, cudaMemcpyDeviceToHost, s));
         GRG_CUDA(c, cudaStreamSynchronize(s));
-        GRG_CUDA(c, cudaMalloc(&col, std::max<uint64_t>(total, 1) * 4));
-        c->csr_bufs.push_back(col);
-        k_csr_fill<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)l, ptr, (uint2 *)row, col);
+        if (cb.colcap < std::max<uint64_t>(total, 1)) {
+            cudaFree(cb.col);
+            cb.col = nullptr;
+            cb.colcap = 0;
+            const uint64_t cc = std::max<uint64_t>(total, 1) + total / 4;
+            GRG_CUDA(c, cudaMalloc(&cb.col, cc * 4));
+            cb.colcap = cc;
+        }
+        k_csr_fill<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)l, ptr, row, cb.col);
         c->launches += 6;
-        rt.csr_row[l] = (const uint2 *)row;
-        rt.csr_col[l] = col;
+        rt.csr_row[l] = row;
+        rt.csr_col[l] = cb.col;
     }
     c->rt = rt;
     GRG_CUDA(c, cudaMemcpyToSymbolAsync(c_rt, &rt, sizeof rt, 0, cudaMemcpyHostToDevice, s));
@@ -2560,6 +2648,8 @@ int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *s
     S.join_ms = join_ms;
     S.join_launches = joins;
     S.left_elems = c->h_ctr[C_LEFT];
+    S.window_out_elems = c->h_ctr[C_WOUT];
+    S.wide_window = c->join_wide ? 1 : 0;
     S.right_elems = c->h_ctr[C_RIGHT];
     S.out_elems = S.delta_elems;
     S.pool_elems_used = c->h_ctr[C_POOL_TOP];
@@ -3197,10 +3287,12 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
         for (int pass = 0;; pass++) {
             const int g = grid((n + RB - 1) / RB, JOIN_WARPS, 16);
             if (pass == 0) {
-                k_join<<<g, JOIN_WARPS * 32, 0, s>>>(d, gbuf, nd, -1, rbuf[0]);
-                if (nv) k_join<<<grid((nv + RB - 1) / RB, JOIN_WARPS, 16), JOIN_WARPS * 32, 0, s>>>(d, vbuf, nv, -1, rbuf[0]);
+                k_join<WIN, WIN_LO><<<g, JOIN_WARPS * 32, 0, s>>>(d, gbuf, nd, -1, rbuf[0]);
+                if (nv)
+                    k_join<WIN, WIN_LO><<<grid((nv + RB - 1) / RB, JOIN_WARPS, 16), JOIN_WARPS * 32, 0, s>>>(d, vbuf, nv,
+                                                                                                        -1, rbuf[0]);
             } else {
-                k_join<<<g, JOIN_WARPS * 32, 0, s>>>(d, rbuf[rb], n, -1, rbuf[rb ^ 1]);
+                k_join<WIN, WIN_LO><<<g, JOIN_WARPS * 32, 0, s>>>(d, rbuf[rb], n, -1, rbuf[rb ^ 1]);
             }
             NA_CUDA(cudaGetLastError());
             if ((st = na_read(h, d.ctr, s))) return st;

@@ -32,7 +32,7 @@ EXPORTS = (
     "grg_batch_step", "grg_batch_result", "grg_batch_release", "grg_get_rules", "grg_closure_ex",
     "grg_load_elements", "grg_export_elements", "grg_range_counts", "grg_set_pool_limit", "grg_part_create",
     "grg_part_destroy", "grg_part_load_edges", "grg_part_run", "grg_part_label_counts", "grg_part_bounds",
-    "grg_set_device_rounds", "grg_range_reach",
+    "grg_set_device_rounds", "grg_range_reach", "grg_set_join_window",
 )
 
 
@@ -49,7 +49,8 @@ class Stats(ctypes.Structure):
         ("retry_records", ctypes.c_uint64), ("grow_rows", ctypes.c_uint64), ("pool_elems_used", ctypes.c_uint64),
         ("pool_elems_cap", ctypes.c_uint64), ("closure_ms", ctypes.c_double), ("join_ms", ctypes.c_double),
         ("join_launches", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
-        ("join_phase_cycles", ctypes.c_uint64 * 5),
+        ("join_phase_cycles", ctypes.c_uint64 * 5), ("window_out_elems", ctypes.c_uint64),
+        ("wide_window", ctypes.c_uint64),
     ]
 
     def as_dict(self):
@@ -95,6 +96,7 @@ def load_library(path: str = LIB_PATH):
     L.grg_set_stream.argtypes = [P, P]
     L.grg_set_kernel_timing.argtypes = [P, I]
     L.grg_set_device_rounds.argtypes = [P, I]
+    L.grg_set_join_window.argtypes = [P, I]
     L.grg_transfer_rules.argtypes = [P, I, P, I]
     L.grg_allocate_pool.argtypes = [P, U64]
     L.grg_load_edges.argtypes = [P, U32, U64, P, P, P, I]
@@ -227,6 +229,10 @@ class Context:
 
     def set_kernel_timing(self, on: bool):
         self._check(self._L.grg_set_kernel_timing(self._h, int(bool(on))), "set_kernel_timing")
+
+    def set_join_window(self, mode: int):
+        """0 = narrow (8 elements), 1 = wide (12, the default)."""
+        self._check(self._L.grg_set_join_window(self._h, mode), "set_join_window")
 
     def set_device_rounds(self, on: bool):
         self._check(self._L.grg_set_device_rounds(self._h, int(bool(on))), "set_device_rounds")

@@ -63,6 +63,9 @@ typedef struct grg_stats {
     uint64_t join_phase_cycles[5]; /* join-kernel cycles per phase (record load, unary,
                                       binary join, flush, retry list) when built with
                                       -DGRG_PHASE_TIMERS; 0 otherwise */
+    uint64_t window_out_elems;     /* right elements beyond the narrow join window (the
+                                      statistic the window choice is keyed on) */
+    uint64_t wide_window;          /* 1 = the closure ended on the wide join window */
 } grg_stats;
 
 /* Error text of a status code, and the last detailed message of a context. */
@@ -88,6 +91,11 @@ int grg_set_kernel_timing(grg_ctx *ctx, int on);
  * host (table growth, buffer room), instead of launching and waiting per
  * round. The results are identical either way. */
 int grg_set_device_rounds(grg_ctx *ctx, int on);
+/* Join window: the join ORs right-hand elements into a dense per-record window
+ * of 12 elements (mode 1, the default) or 8 (mode 0); elements outside it go to
+ * a small shared-memory hash. Environment GRG_JOIN_WINDOW=narrow selects 8.
+ * Results are identical either way. */
+int grg_set_join_window(grg_ctx *ctx, int mode);
 
 /* Grammar: rules[3*i+{0,1,2}] = LHS, RHS1, RHS2 label ids (1-based, 0 = absent),
  * num_labels = number of distinct labels. Replaces transferRules

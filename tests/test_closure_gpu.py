@@ -218,3 +218,21 @@ def test_device_rounds_equal_host_rounds(grg_mod, oracle_mod, name):
         ctx.close()
     assert out[0] == out[1]
     assert out[1][0] == r.label_counts().tolist() and out[1][1] == r.set_hash
+
+
+@pytest.mark.parametrize("name", ["pointsto", "alias", "dataflow"])
+def test_join_windows_equal(grg_mod, oracle_mod, name):
+    """The narrow (8-element) and wide (12-element) join windows give the oracle's closure."""
+    w = {"pointsto": lambda: G.pointsto(seed=41, num_vars=900, num_edges=2200),
+         "alias": lambda: G.alias(seed=42, num_vars=4000, num_base_edges=9000, block=700),
+         "dataflow": lambda: G.dataflow_blocks(seed=43, num_blocks=20, block=500, num_edges=30000)}[name]()
+    r = oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, w.filter_flag, w.src, w.dst, w.lab)
+    for mode in (0, 1):
+        ctx = grg_mod.Context(0)
+        ctx.set_join_window(mode)
+        ctx.transfer_rules(w.rule_ids(), w.num_labels)
+        ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
+        st = ctx.closure(w.filter_flag)
+        assert st["wide_window"] == mode
+        assert ctx.label_counts().tolist() == r.label_counts().tolist() and ctx.set_hash() == r.set_hash
+        ctx.close()
