@@ -19,6 +19,14 @@ inside the timed region).
 in oracle/, all host threads) on a bounded sample of the same workload: every
 8th procedure block's source rows (rows are independent under filter 1).
 
+Beside the headline, the JSON line carries the other configurations, each
+measured on the device with results checked for consistency (skip them with
+--quick): `alias_c3` (1M-vertex alias closure), `alias_c4` (8M-vertex alias
+closure in-core, and out-of-core over 64 vertex-range partitions staged
+through host memory), `out_of_core_c2` (the dataflow closure under a pool
+limit of a quarter of what it needs in-core), and `serving` (the 512-job mix:
+continuous batching vs one graph at a time).
+
 Multi-GPU: the closure of one graph does not shard without an exchange step,
 so N GPUs run N independent replicas (one per rank, weak scaling).
 """
@@ -154,6 +162,82 @@ def run_reference(args, w, world, rank):
     print(json.dumps(out), flush=True)
 
 
+def _closure_once(grg, ctx, w, f):
+    ctx.transfer_rules(w.rule_ids(), w.num_labels)
+    ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
+    st = ctx.closure(f)
+    return st, [int(x) for x in ctx.label_counts()], ctx.set_hash()
+
+
+def _partitioned(grg, w, f, parts, pool_bytes=0):
+    ctx = grg.Context(0)
+    ctx.transfer_rules(w.rule_ids(), w.num_labels)
+    if pool_bytes:
+        ctx.set_pool_limit(pool_bytes)
+    p = grg.Partitioned(ctx, w.num_vars, parts)
+    t = time.perf_counter()
+    p.load_edges(w.src, w.dst, w.lab)
+    t_load = time.perf_counter() - t
+    st = p.run(f)
+    counts, h = p.label_counts()
+    p.close()
+    ctx.close()
+    return st, [int(x) for x in counts], h, t_load
+
+
+def extra_measurements(args, w2):
+    """C3 and C4 (alias, in-core; C4 also out-of-core over 64 partitions) and the
+    C2 dataflow closure out-of-core under a pool limit."""
+    import grg
+    import grg_gen as G
+    out = {}
+    # C3: 1M-vertex alias graph, block-confined locality
+    w = G.alias()
+    ctx = grg.Context(0)
+    ctx.allocate_pool(0)
+    _closure_once(grg, ctx, w, 0)                       # warm-up (pool and buffers sized)
+    st, c3_counts, c3_hash = _closure_once(grg, ctx, w, 0)
+    ctx.close()
+    out["alias_c3"] = {"workload": "alias grammar, 1M vertices, 4M base + 4M inverse edges, Zipf(1.8) cap 256, "
+                                   "1000-vertex blocks", "closure_edges": st["total_edges"],
+                       "time_to_fixpoint_ms": st["closure_ms"], "rounds": st["rounds"],
+                       "value": st["total_edges"] / (st["closure_ms"] * 1e-3), "unit": UNIT}
+    del w
+    # C4: 8M vertices, 40M base + 40M inverse edges; in-core, then 64 partitions through host memory
+    w = G.alias(seed=0x5EED0004, num_vars=8_000_000, num_base_edges=40_000_000, block=1000)
+    ctx = grg.Context(0)
+    ctx.allocate_pool(0)
+    st, c4_counts, c4_hash = _closure_once(grg, ctx, w, 0)
+    ctx.close()
+    pst, p_counts, p_hash, t_load = _partitioned(grg, w, 0, 64)
+    assert (p_counts, p_hash) == (c4_counts, c4_hash), "partitioned C4 differs from in-core"
+    out["alias_c4"] = {"workload": "alias grammar, 8M vertices, 40M base + 40M inverse edges, 1000-vertex blocks",
+                       "closure_edges": st["total_edges"], "in_core_ms": st["closure_ms"], "rounds": st["rounds"],
+                       "value": st["total_edges"] / (st["closure_ms"] * 1e-3), "unit": UNIT,
+                       "pool_elems_used": st["pool_elems_used"],
+                       "out_of_core": {"partitions": pst["num_parts"], "schedule": pst["schedule"],
+                                       "runs": pst["runs"], "pairs_skipped": pst["skipped"],
+                                       "supersteps": pst["supersteps"], "load_s": t_load, "run_ms": pst["ms"],
+                                       "h2d_bytes": pst["h2d_bytes"], "d2h_bytes": pst["d2h_bytes"],
+                                       "value": pst["total_edges"] / (pst["ms"] * 1e-3), "unit": UNIT,
+                                       "identical_to_in_core": True}}
+    del w
+    # C2 out-of-core: a pool limit of a quarter of what the in-core closure used
+    ctx = grg.Context(0)
+    ctx.allocate_pool(0)
+    st, c2_counts, c2_hash = _closure_once(grg, ctx, w2, w2.filter_flag)
+    ctx.close()
+    limit = st["pool_elems_used"] * 69 // 4
+    pst, p_counts, p_hash, t_load = _partitioned(grg, w2, w2.filter_flag, 4, limit)
+    assert (p_counts, p_hash) == (c2_counts, c2_hash), "partitioned C2 differs from in-core"
+    out["out_of_core_c2"] = {"workload": WORKLOAD, "pool_limit_bytes": limit, "partitions": pst["num_parts"],
+                             "splits": pst["splits"], "schedule": pst["schedule"], "runs": pst["runs"],
+                             "load_s": t_load, "run_ms": pst["ms"],
+                             "value": pst["total_edges"] / (pst["ms"] * 1e-3), "unit": UNIT,
+                             "identical_to_in_core": True}
+    return out
+
+
 def serving_measurement(args):
     """Config-5 style mix (half dataflow, half alias; Poisson arrivals at 200/s):
     the continuous-batching service vs the same jobs closed one at a time."""
@@ -187,9 +271,11 @@ def main():
     ap.add_argument("--blocks", type=int, default=2000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--pool-gb", type=float, default=0.0, help="initial element pool (0 = 1/8 of free memory)")
-    ap.add_argument("--serve-jobs", type=int, default=128,
-                    help="jobs of the served mix (config 5 is 512; 0 = skip the serving measurement)")
-    ap.add_argument("--serve-vmax", type=int, default=20000, help="largest job of the served mix (config 5: 200000)")
+    ap.add_argument("--serve-jobs", type=int, default=512,
+                    help="jobs of the served mix (0 = skip the serving measurement)")
+    ap.add_argument("--serve-vmax", type=int, default=200000, help="largest job of the served mix")
+    ap.add_argument("--quick", action="store_true",
+                    help="headline only: skip the other configurations and the serving mix")
     args = ap.parse_args()
     world, rank, local = dist_setup(args)
 
@@ -287,7 +373,8 @@ def main():
         if os.path.exists(tp):
             traffic = json.load(open(tp)).get("bytes_per_launch")
         cb = None if args.no_cpu_baseline else cpu_baseline(w)
-        serving = serving_measurement(args) if args.serve_jobs > 0 else None
+        serving = serving_measurement(args) if (args.serve_jobs > 0 and not args.quick) else None
+        extras = {} if args.quick else extra_measurements(args, w)
         out = {
             "metric": METRIC, "value": world * total / (ms_max * 1e-3), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True,
@@ -309,6 +396,7 @@ def main():
             "clocks": clk.summary(),
             "gpu_launches": int(sum(x["kernel_launches"] for x in stats)),
             "serving": serving,
+            **extras,
             "wall_s_timed": t_wall,
         }
         print(json.dumps(out), flush=True)

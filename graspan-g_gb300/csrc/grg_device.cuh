@@ -62,7 +62,10 @@ enum : int {
     C_JT0 = C_LABEL0 + MAX_SLOTS + 2,   // start time of the current join pass (device-driven rounds)
     C_MAXR = C_LABEL0 + MAX_SLOTS + 3,  // rounds a device-driven launch may run (0 = until the fixpoint)
     C_WOUT = C_LABEL0 + MAX_SLOTS + 4,  // right-hand items the join's dense window could not hold
-    NCTR = C_LABEL0 + MAX_SLOTS + 5
+    C_SPLIT_N = C_LABEL0 + MAX_SLOTS + 5,  // sub-records of a small round (k_split)
+    C_JN1 = C_LABEL0 + MAX_SLOTS + 6,   // records the join reads from the gathered buffer this round
+    C_JN2 = C_LABEL0 + MAX_SLOTS + 7,   // records the join reads from the virtual-record buffer this round
+    NCTR = C_LABEL0 + MAX_SLOTS + 8
 };
 enum : unsigned long long { ERR_POOL = 1, ERR_LOAD = 2, ERR_INTERNAL = 4 };
 
@@ -99,6 +102,7 @@ struct Dev {
     uint32_t *grow;           // grow list (table indices)
     uint4 *cand;              // candidate elements (32 B: bits[6], key, row) for k_apply; may be null
     uint64_t cand_cap;        // candidates
+    uint64_t retry_cap;       // records a join's retry list holds (more are counted, not written)
     // this round's delta index (labels with dindex): records [drs, drs+drc) of
     // the gathered delta buffer drec belong to table (label, row); dvm = vertex
     // bitmap per label of rows with deltas (vwords words per label)

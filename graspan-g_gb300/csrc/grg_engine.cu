@@ -689,6 +689,63 @@ __global__ void __launch_bounds__(256) k_apply(Dev d, const uint4 *__restrict__ 
     }
 }
 
+// Small rounds: a warp joins 32 records, so a round of few, dense records (alias
+// rows reach a whole block) leaves most SMs idle. Below SPLIT_MAX records the
+// round's gathered and virtual records are cut into sub-records of at most
+// SPLIT_BITS bits each (the union over a record's bits is the union over its
+// parts), which the join reads instead; above it the join reads the records
+// as they are. The choice is made here, on the device: the joins read their
+// counts from C_JN1 / C_JN2 / C_SPLIT_N.
+constexpr uint32_t SPLIT_MAX = 32768;
+constexpr uint32_t SPLIT_BITS = 8;
+constexpr uint32_t SPLIT_PARTS = (EIDS + SPLIT_BITS - 1) / SPLIT_BITS;
+
+__global__ void k_split(Dev d, const uint4 *__restrict__ grecs, const uint4 *__restrict__ vrecs, uint4 *out)
+{
+    if (d.ctr[C_HALT]) return;
+    const uint64_t nd = d.ctr[C_DIRTY_N], nv = d.ctr[C_VN];
+    const bool split = nd + nv < SPLIT_MAX;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        d.ctr[C_JN1] = split ? 0 : nd;
+        d.ctr[C_JN2] = split ? 0 : nv;
+    }
+    if (!split) return;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nd + nv;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint4 *r = i < nd ? grecs + 2 * i : vrecs + 2 * (i - nd);
+        const uint4 a = r[0], b = r[1];
+        const uint32_t w[EW] = {a.x, a.y, a.z, a.w, b.x, b.y};
+        uint32_t p = 0;
+#pragma unroll
+        for (int x = 0; x < EW; x++) p += __popc(w[x]);
+        const uint32_t parts = (p + SPLIT_BITS - 1) / SPLIT_BITS;
+        if (!parts) continue;
+        uint64_t pos = atomicAdd(&d.ctr[C_SPLIT_N], (unsigned long long)parts);
+        uint32_t cur[EW] = {0, 0, 0, 0, 0, 0}, c = 0;
+#pragma unroll
+        for (int x = 0; x < EW; x++) {
+            uint32_t m = w[x];
+            while (m) {
+                const uint32_t bit = m & (0u - m);
+                m ^= bit;
+                cur[x] |= bit;
+                if (++c == SPLIT_BITS) {
+                    out[2 * pos] = make_uint4(cur[0], cur[1], cur[2], cur[3]);
+                    out[2 * pos + 1] = make_uint4(cur[4], cur[5], b.z, b.w);
+                    pos++;
+                    c = 0;
+#pragma unroll
+                    for (int y = 0; y < EW; y++) cur[y] = 0;
+                }
+            }
+        }
+        if (c) {                      // the last, partial part
+            out[2 * pos] = make_uint4(cur[0], cur[1], cur[2], cur[3]);
+            out[2 * pos + 1] = make_uint4(cur[4], cur[5], b.z, b.w);
+        }
+    }
+}
+
 // One warp per batch of RB delta records (label B, row i, base, bits); lane r
 // owns record r for per-record work, and (record, k) tasks and their right-hand
 // items are flattened over the lanes so every phase keeps 32 independent memory
@@ -896,8 +953,8 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : 4))
             unsigned long long p = 0;
             if (lane == (uint32_t)(__ffs(fm) - 1)) p = atomicAdd(&d.ctr[C_RETRY_N], (unsigned long long)__popc(fm));
             p = __shfl_sync(0xffffffffu, p, __ffs(fm) - 1);
-            if (failed) {
-                const uint64_t o = p + __popc(fm & ((1u << lane) - 1u));
+            const uint64_t o = p + __popc(fm & ((1u << lane) - 1u));
+            if (failed && o < d.retry_cap) {
                 retry_out[2 * o] = make_uint4(rb.w[0], rb.w[1], rb.w[2], rb.w[3]);
                 retry_out[2 * o + 1] = make_uint4(rb.w[4], rb.w[5], key, row);
             }
@@ -1400,6 +1457,7 @@ struct grg_ctx {
     uint64_t gbuf_cap = 0;
     uint4 *vbuf = nullptr;                     // virtual records of old-left joins
     uint64_t vbuf_cap = 0;
+    uint4 *sbuf = nullptr;                     // sub-records of small rounds (k_split)
     uint32_t *drs = nullptr, *drc = nullptr, *dvm = nullptr;   // delta index (per label x row / vertex bitmap)
     uint4 *cand[2] = {nullptr, nullptr};       // join candidates for k_apply / failed candidates
     uint64_t cand_cap = 0;
@@ -1418,6 +1476,7 @@ struct grg_ctx {
     uint32_t *xst = nullptr;               // staged stamps
     uint64_t xcap = 0;
     uint64_t pool_limit = 0;               // maximum pool slots (0 = what the device holds)
+    uint64_t retry_min = 1ull << 20;       // smallest retry list (records; GRG_RETRY_ROOM)
     // join window: narrow (WIN) or wide (WIN2, the default)
     bool join_wide = true;
     int join_window_mode = 1;              // 0 = narrow, 1 = wide
@@ -1500,6 +1559,7 @@ Dev make_dev(const grg_ctx *c)
     d.want = c->want;
     d.cand = c->cand[c->cb];
     d.cand_cap = c->cand_cap;
+    d.retry_cap = c->rbuf_cap;
     d.drs = c->drs;
     d.drc = c->drc;
     d.dvm = c->dvm;
@@ -1623,9 +1683,10 @@ int grow_pool(grg_ctx *c, uint64_t min_elems)
 // Candidate buffers of a round (4 per delta record; a full buffer falls back to direct inserts).
 int ensure_cand(grg_ctx *c, uint64_t nd)
 {
-    const uint64_t want = std::max<uint64_t>(4 * nd, 1 << 20);
+    // capped at 2^26 candidates (2 GiB a buffer): past it, joins insert directly
+    const uint64_t want = std::min<uint64_t>(std::max<uint64_t>(4 * nd, 1 << 20), 1ull << 26);
     if (want <= c->cand_cap) return GRG_OK;
-    const uint64_t cap = want + want / 2;
+    const uint64_t cap = std::min<uint64_t>(want + want / 2, 1ull << 26);
     cudaFree(c->cand[0]);
     cudaFree(c->cand[1]);
     c->cand[0] = c->cand[1] = nullptr;
@@ -1729,6 +1790,8 @@ int grg_create(grg_ctx **out, int device)
     c->stream = c->own_stream;
     const char *dr = getenv("GRG_DEVICE_ROUNDS");      // "0": every round driven from the host
     c->device_rounds = !(dr && dr[0] == '0');
+    const char *rr = getenv("GRG_RETRY_ROOM");         // smallest retry list, in records
+    if (rr && atoll(rr) > 0) c->retry_min = (uint64_t)atoll(rr);
     const char *jw = getenv("GRG_JOIN_WINDOW");        // "narrow" / "wide"; otherwise chosen per closure
     if (jw) c->join_window_mode = !strcmp(jw, "narrow") ? 0 : 1;
     *out = c;
@@ -1745,6 +1808,7 @@ void grg_destroy(grg_ctx *c)
     for (int i = 0; i < 2; i++) cudaFree(c->rbuf[i]);
     cudaFree(c->gbuf);
     cudaFree(c->vbuf);
+    cudaFree(c->sbuf);
     cudaFree(c->xbuf);
     cudaFree(c->xst);
     cudaFree(c->cand[0]);
@@ -1884,7 +1948,7 @@ int setup_tables(grg_ctx *c, uint32_t num_vars)
 }
 
 // Labels on a rule's left-hand side get tables of DERIVED_MIN_CAP slots when
-// that fits in a quarter of the pool (fewer growths, rows stay in allocation order).
+// that fits in half of the pool (fewer growths, rows stay in allocation order).
 MinCap derived_min_cap(const grg_ctx *c)
 {
     MinCap mc;
@@ -1893,7 +1957,7 @@ MinCap derived_min_cap(const grg_ctx *c)
     bool lhs[MAX_LABELS + 1] = {false};
     for (int q = 0; q < c->R; q++) lhs[c->rules[3 * q]] = true;
     for (int l = 1; l <= c->L; l++) nder += lhs[l];
-    if ((uint64_t)nder * c->V * DERIVED_MIN_CAP <= c->pool_cap / 4)
+    if ((uint64_t)nder * c->V * DERIVED_MIN_CAP <= c->pool_cap / 2)
         for (int l = 1; l <= c->L; l++) mc.cap[l] = lhs[l] ? DERIVED_MIN_CAP : 0;
     return mc;
 }
@@ -1981,7 +2045,7 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
         bool lhs[MAX_LABELS + 1] = {false};
         for (int q = 0; q < c->R; q++) lhs[c->rules[3 * q]] = true;
         for (int l = 1; l <= c->L; l++) nder += lhs[l];
-        const uint64_t want = 4ull * nder * num_vars * DERIVED_MIN_CAP + 2 * num_edges;
+        const uint64_t want = 2ull * nder * num_vars * DERIVED_MIN_CAP + 2 * num_edges;
         if (want > c->pool_cap) {
             size_t fr = 0, tot = 0;
             cudaMemGetInfo(&fr, &tot);
@@ -2178,13 +2242,46 @@ static int round_oldleft(grg_ctx *c, uint64_t *nv_out)
 // Tables that overflowed grow (the pool too, when it is full); then the failed
 // records (rbuf[0]) and failed candidates (cand[cb ^ 1]) of the round's first
 // pass are re-run until nothing fails.
-static int round_retries(grg_ctx *c, uint64_t nr, uint64_t nf, grg_stats &S, double &join_ms, uint64_t &joins)
+// Retry list size for a round of n records: retries come only from tables at
+// their load limit, a small share; a round with more is re-run whole.
+static uint64_t retry_room(const grg_ctx *c, uint64_t n) { return std::max<uint64_t>(c->retry_min, n / 8); }
+
+// The first join pass of a round over its records: the parts of a small round
+// (sub-records in sbuf, count on the device) or the gathered and virtual records.
+static void first_pass_joins(grg_ctx *c, const Dev &d, uint64_t nd, uint64_t nv, bool split, uint64_t &joins)
+{
+    cudaStream_t s = c->stream;
+    if (split) {
+        launch_join(c, grid_for(c, ((nd + nv) * SPLIT_PARTS + RB - 1) / RB, JOIN_WARPS, 16), s, d, c->sbuf, 0,
+                    C_SPLIT_N, c->rbuf[0]);
+        c->launches++;
+        joins++;
+        return;
+    }
+    launch_join(c, grid_for(c, (nd + RB - 1) / RB, JOIN_WARPS, 16), s, d, c->gbuf, nd, -1, c->rbuf[0]);
+    c->launches++;
+    joins++;
+    if (nv) {
+        launch_join(c, grid_for(c, (nv + RB - 1) / RB, JOIN_WARPS, 16), s, d, c->vbuf, nv, -1, c->rbuf[0]);
+        c->launches++;
+        joins++;
+    }
+}
+
+// Tables that overflowed grow (the pool too, when it is full); then the failed
+// records (rbuf[0]) and failed candidates (cand[cb ^ 1]) of the round's first
+// pass are re-run until nothing fails. When more records failed than the retry
+// list holds, the round's whole first pass is re-run instead (joining a record
+// again adds nothing twice).
+static int round_retries(grg_ctx *c, uint64_t nr, uint64_t nf, grg_stats &S, double &join_ms, uint64_t &joins,
+                         uint64_t nd, uint64_t nv, bool split)
 {
     cudaStream_t s = c->stream;
     int rb = 0;    // the failed records of the last pass are in rbuf[rb]
     for (int pass = 1;; pass++) {
         if (nr == 0 && nf == 0) return GRG_OK;
         S.retry_records += nr + nf;
+        const bool rerun_all = nr > c->rbuf_cap;
         Dev d = make_dev(c);
         for (int gtry = 0;; gtry++) {
             const uint64_t ng = c->h_ctr[C_GROW_N];
@@ -2209,10 +2306,14 @@ static int round_retries(grg_ctx *c, uint64_t nr, uint64_t nf, grg_stats &S, dou
         GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_AFAIL, 0, 8, s));
         GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_RETRY_N, 0, 16, s));
         if (c->timing) GRG_CUDA(c, cudaEventRecord(c->ev_c, s));
-        if (nr) {
+        if (rerun_all) {
+            first_pass_joins(c, d, nd, nv, split, joins);
+            rb = 0;
+        } else if (nr) {
             launch_join(c, grid_for(c, (nr + RB - 1) / RB, JOIN_WARPS, 16), s, d, c->rbuf[rb], nr, -1, c->rbuf[rb ^ 1]);
             c->launches++;
             joins++;
+            rb ^= 1;
         }
         if (c->cand_cap) {
             k_apply<<<c->sms * 8, 256, 0, s>>>(d, c->cand[c->cb], c->cand[c->cb ^ 1]);
@@ -2227,28 +2328,35 @@ static int round_retries(grg_ctx *c, uint64_t nr, uint64_t nf, grg_stats &S, dou
             cudaEventElapsedTime(&ms, c->ev_c, c->ev_d);
             join_ms += ms;
         }
-        if (nr) rb ^= 1;
         nr = c->h_ctr[C_RETRY_N];
         nf = c->cand_cap ? c->h_ctr[C_AFAIL] : 0;
     }
 }
 
 // First join pass of a round over its nd gathered and nv virtual records, then retries.
+static int ensure_sbuf(grg_ctx *c)
+{
+    if (c->sbuf) return GRG_OK;
+    GRG_CUDA(c, cudaMalloc(&c->sbuf, (size_t)SPLIT_MAX * SPLIT_PARTS * 32));
+    return GRG_OK;
+}
+
 static int round_joins(grg_ctx *c, uint64_t nd, uint64_t nv, grg_stats &S, double &join_ms, uint64_t &joins)
 {
     cudaStream_t s = c->stream;
-    int st = ensure_rbuf(c, nd + nv);
+    const bool split = nd + nv < SPLIT_MAX;
+    int st = ensure_rbuf(c, retry_room(c, nd + nv));
     if (st) return st;
+    if (split && (st = ensure_sbuf(c))) return st;
     Dev d = make_dev(c);
     if (c->timing) GRG_CUDA(c, cudaEventRecord(c->ev_c, s));
-    launch_join(c, grid_for(c, (nd + RB - 1) / RB, JOIN_WARPS, 16), s, d, c->gbuf, nd, -1, c->rbuf[0]);
-    c->launches++;
-    joins++;
-    if (nv) {
-        launch_join(c, grid_for(c, (nv + RB - 1) / RB, JOIN_WARPS, 16), s, d, c->vbuf, nv, -1, c->rbuf[0]);
+    if (split) {
+        // few records: their parts spread the join over more warps
+        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_SPLIT_N, 0, 8, s));
+        k_split<<<grid_for(c, nd + nv, 256), 256, 0, s>>>(d, c->gbuf, c->vbuf, c->sbuf);
         c->launches++;
-        joins++;
     }
+    first_pass_joins(c, d, nd, nv, split, joins);
     // insert the candidates the joins wrote (count read on the device)
     if (c->cand_cap) {
         k_apply<<<c->sms * 8, 256, 0, s>>>(d, c->cand[c->cb], c->cand[c->cb ^ 1]);
@@ -2263,7 +2371,8 @@ static int round_joins(grg_ctx *c, uint64_t nd, uint64_t nv, grg_stats &S, doubl
         cudaEventElapsedTime(&ms, c->ev_c, c->ev_d);
         join_ms += ms;
     }
-    return round_retries(c, c->h_ctr[C_RETRY_N], c->cand_cap ? c->h_ctr[C_AFAIL] : 0, S, join_ms, joins);
+    return round_retries(c, c->h_ctr[C_RETRY_N], c->cand_cap ? c->h_ctr[C_AFAIL] : 0, S, join_ms, joins, nd, nv,
+                         split);
 }
 
 // ---------------------------------------------------------------- device-driven rounds
@@ -2281,7 +2390,7 @@ enum : unsigned long long {
 constexpr uint64_t GATE_MAX_ITERS = 1u << 20;   // iterations of one graph launch; past it the host takes over
 
 __global__ void k_gate_gather(unsigned long long *ctr, const uint32_t *csum, uint64_t max_chunks, uint64_t gbuf_cap,
-                              uint64_t rbuf_cap, uint64_t max_iters, cudaGraphConditionalHandle h)
+                              uint64_t max_iters, cudaGraphConditionalHandle h)
 {
     if (threadIdx.x != 0) return;
     const unsigned long long it = ++ctr[C_ITERS];
@@ -2293,7 +2402,7 @@ __global__ void k_gate_gather(unsigned long long *ctr, const uint32_t *csum, uin
     const uint64_t nb = (dyn_chunks(max_chunks, ctr) + 1023) / 1024;
     const uint64_t nd = csum[nb];
     ctr[C_DIRTY_N] = nd;
-    const unsigned long long halt = nd == 0 ? HALT_FIXPOINT : (nd > gbuf_cap || nd > rbuf_cap) ? HALT_CAPACITY : 0;
+    const unsigned long long halt = nd == 0 ? HALT_FIXPOINT : nd > gbuf_cap ? HALT_CAPACITY : 0;
     if (halt) {
         ctr[C_HALT] = halt;                  // later kernels of this iteration return at once
         cudaGraphSetConditional(h, 0);
@@ -2303,12 +2412,11 @@ __global__ void k_gate_gather(unsigned long long *ctr, const uint32_t *csum, uin
     ctr[C_GDSUM] += nd;
 }
 
-__global__ void k_gate_oldleft(unsigned long long *ctr, uint64_t vbuf_cap, uint64_t rbuf_cap,
-                               cudaGraphConditionalHandle h)
+__global__ void k_gate_oldleft(unsigned long long *ctr, uint64_t vbuf_cap, cudaGraphConditionalHandle h)
 {
     if (threadIdx.x != 0 || ctr[C_HALT]) return;
     const uint64_t nv = ctr[C_VN];
-    if (nv > vbuf_cap || ctr[C_DIRTY_N] + nv > rbuf_cap) {
+    if (nv > vbuf_cap) {
         ctr[C_HALT] = HALT_OLDLEFT;
         cudaGraphSetConditional(h, 0);
     }
@@ -2358,7 +2466,7 @@ static std::vector<uint64_t> round_graph_key(const grg_ctx *c, uint32_t rs, uint
                                (uint64_t)c->cand[1], c->cand_cap, (uint64_t)c->chunk, nchunks, (uint64_t)c->drs,
                                (uint64_t)c->drc, (uint64_t)c->dvm, c->pool_cap, c->V, rs, (uint64_t)c->timing,
                                (uint64_t)c->elem_loaded, (uint64_t)c->rt.nol, (uint64_t)c->row_job,
-                               (uint64_t)c->job_cnt, c->max_jobs, (uint64_t)c->join_wide};
+                               (uint64_t)c->job_cnt, c->max_jobs, (uint64_t)c->join_wide, (uint64_t)c->sbuf};
     for (int l = 1; l <= c->L; l++) k.push_back(c->rt.dindex[l]);
     return k;
 }
@@ -2399,7 +2507,7 @@ static int build_round_graph(grg_ctx *c, uint32_t rs)
     k_scan_blocks<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(ccnt, coff, csum, nchunks, ctr);
     k_scan_sums<<<1, 1024, 0, s>>>(csum, nb, ctr);
     k_scan_add<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(coff, csum, nchunks, ctr);
-    k_gate_gather<<<1, 32, 0, s>>>(ctr, csum, nchunks, c->gbuf_cap, c->rbuf_cap, GATE_MAX_ITERS, h);
+    k_gate_gather<<<1, 32, 0, s>>>(ctr, csum, nchunks, c->gbuf_cap, GATE_MAX_ITERS, h);
     nk += 5;
     for (int l = 1; l <= c->L; l++)
         if (c->rt.dindex[l]) {
@@ -2415,7 +2523,7 @@ static int build_round_graph(grg_ctx *c, uint32_t rs)
     if (c->rt.nol) {
         for (int q = 0; q < c->rt.nol; q++)
             k_oldleft<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)q, c->vbuf, c->vbuf_cap);
-        k_gate_oldleft<<<1, 32, 0, s>>>(ctr, c->vbuf_cap, c->rbuf_cap, h);
+        k_gate_oldleft<<<1, 32, 0, s>>>(ctr, c->vbuf_cap, h);
         nk += c->rt.nol + 1;
     }
     if (c->timing) {
@@ -2423,10 +2531,13 @@ static int build_round_graph(grg_ctx *c, uint32_t rs)
         nk++;
     }
     const int jgrid = grid_for(c, ~0u, JOIN_WARPS, 16);
-    launch_join(c, jgrid, s, d, c->gbuf, 0, C_DIRTY_N, c->rbuf[0]);
-    nk++;
+    cudaMemsetAsync(ctr + C_SPLIT_N, 0, 8, s);
+    k_split<<<grid_for(c, SPLIT_MAX, 256), 256, 0, s>>>(d, c->gbuf, c->vbuf, c->sbuf);
+    launch_join(c, jgrid, s, d, c->gbuf, 0, C_JN1, c->rbuf[0]);
+    launch_join(c, jgrid, s, d, c->sbuf, 0, C_SPLIT_N, c->rbuf[0]);
+    nk += 3;
     if (c->rt.nol) {
-        launch_join(c, jgrid, s, d, c->vbuf, 0, C_VN, c->rbuf[0]);
+        launch_join(c, jgrid, s, d, c->vbuf, 0, C_JN2, c->rbuf[0]);
         nk++;
     }
     if (c->cand_cap) {
@@ -2484,14 +2595,15 @@ static int run_rounds(grg_ctx *c, uint64_t max_rounds, grg_stats &S, double &joi
         // recorded graph survives the whole closure.
         const uint64_t nd_last = std::max<uint64_t>(c->h_ctr[C_DIRTY_N], 1);
         const uint64_t top = c->h_ctr[C_POOL_TOP], floor_cap = 1ull << 24;
-        if ((st = ensure_buf(c, &c->gbuf, &c->gbuf_cap, std::max(4 * nd_last, std::min(top, floor_cap))))) return st;
+        if ((st = ensure_buf(c, &c->gbuf, &c->gbuf_cap, std::max(2 * nd_last, std::min(top, floor_cap))))) return st;
         if (c->rt.nol &&
             (st = ensure_buf(c, &c->vbuf, &c->vbuf_cap,
-                             std::max<uint64_t>(4 * std::max<uint64_t>(c->h_ctr[C_VN], 1),
+                             std::max<uint64_t>(2 * std::max<uint64_t>(c->h_ctr[C_VN], 1),
                                                 std::min<uint64_t>((uint64_t)c->rt.nol * top, floor_cap)))))
             return st;
         if ((st = ensure_cand(c, 2 * nd_last))) return st;    // a full candidate buffer falls back to direct inserts
-        if ((st = ensure_rbuf(c, c->gbuf_cap + (c->rt.nol ? c->vbuf_cap : 0)))) return st;
+        if ((st = ensure_rbuf(c, retry_room(c, c->gbuf_cap + (c->rt.nol ? c->vbuf_cap : 0))))) return st;
+        if ((st = ensure_sbuf(c))) return st;
         if ((st = build_round_graph(c, rs))) return st;
         c->cb = 0;
         GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_HALT, 0, 8 * 5, s));   // halt, iterations, rounds, deltas, join ns
@@ -2531,7 +2643,9 @@ static int run_rounds(grg_ctx *c, uint64_t max_rounds, grg_stats &S, double &joi
             if ((st = round_oldleft(c, &nv))) return st;
             if ((st = round_joins(c, c->h_ctr[C_DIRTY_N], nv, S, join_ms, joins))) return st;
         } else if (halt == HALT_RETRY) {
-            if ((st = round_retries(c, c->h_ctr[C_RETRY_N], c->cand_cap ? c->h_ctr[C_AFAIL] : 0, S, join_ms, joins)))
+            const uint64_t nd = c->h_ctr[C_DIRTY_N], nv = c->h_ctr[C_VN];
+            if ((st = round_retries(c, c->h_ctr[C_RETRY_N], c->cand_cap ? c->h_ctr[C_AFAIL] : 0, S, join_ms, joins,
+                                    nd, nv, nd + nv < SPLIT_MAX)))
                 return st;
         } else if (halt == HALT_LIMIT) {
             // a launch that ran this long without a halt is not trusted: host-driven rounds from here
@@ -3203,6 +3317,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     d.pool_cap = (uint32_t)pool;
     d.cand = nullptr;          // no candidate buffer: joins insert directly
     d.cand_cap = 0;
+    d.retry_cap = pool;        // a round's records (and so its retries) never exceed the pool
     d.drs = (uint32_t *)(base + o_drs);
     d.drc = (uint32_t *)(base + o_drc);
     d.dvm = (uint32_t *)(base + o_dvm);

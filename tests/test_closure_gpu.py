@@ -236,3 +236,24 @@ def test_join_windows_equal(grg_mod, oracle_mod, name):
         assert st["wide_window"] == mode
         assert ctx.label_counts().tolist() == r.label_counts().tolist() and ctx.set_hash() == r.set_hash
         ctx.close()
+
+
+def test_small_rounds_split_and_retry_overflow(grg_mod, oracle_mod, monkeypatch):
+    """Small rounds are joined as sub-records; rows that outgrow their tables make
+    joins fail and retry, and with a 16-record retry list the failures overflow
+    it, so the round's whole first pass re-runs after the tables grow."""
+    monkeypatch.setenv("GRG_RETRY_ROOM", "16")
+    cases = [(G.dataflow_small(seed=46, num_vars=3000, num_edges=9000), 0),
+             (G.pointsto(seed=45, num_vars=700, num_edges=1800), 0)]
+    for w, f in cases:
+        r = oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, f, w.src, w.dst, w.lab)
+        for dev in (False, True):
+            ctx = grg_mod.Context(0)
+            ctx.set_device_rounds(dev)
+            ctx.transfer_rules(w.rule_ids(), w.num_labels)
+            ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
+            st = ctx.closure(f)
+            if w.name == "dataflow_small":           # rows of 3000 ids outgrow 16-slot tables
+                assert st["retry_records"] > 16 and st["grow_rows"] > 0
+            assert ctx.label_counts().tolist() == r.label_counts().tolist() and ctx.set_hash() == r.set_hash
+            ctx.close()
