@@ -344,10 +344,10 @@ __device__ __forceinline__ uint32_t select32(uint32_t w, uint32_t n)
 // chunk of 32 bitmap words; lanes take consecutive dirty slots of the chunk, so
 // the copies of a warp are independent and mostly coalesced.
 // Gather, pass 1: the dirty slots of the round, in slot order (a table's
-// records stay contiguous), each slot id written to word 7 of its record's
-// place in `out`; the dirty bits are cleared. Lanes walk their own bitmap word:
-// stores only, nothing to wait for.
-__global__ void k_gather_slots(Dev d, uint64_t nwords, const uint32_t *__restrict__ chunk_off, uint4 *out, int dyn)
+// records stay contiguous), as a dense array of slot ids; the dirty bits are
+// cleared. Lanes walk their own bitmap word: stores only, nothing to wait for.
+__global__ void k_gather_slots(Dev d, uint64_t nwords, const uint32_t *__restrict__ chunk_off, uint32_t *slots,
+                               int dyn)
 {
     if (d.ctr[C_HALT]) return;
     nwords = dyn_words(nwords, d.ctr, dyn);
@@ -365,11 +365,10 @@ __global__ void k_gather_slots(Dev d, uint64_t nwords, const uint32_t *__restric
             if (lane >= (uint32_t)o) incl += y;
         }
         if (m) d.dmap[wi] = 0;
-        uint32_t *w7 = reinterpret_cast<uint32_t *>(out) + (base_pos + incl - cnt) * 8 + 7;
+        uint32_t *sp = slots + base_pos + incl - cnt;
         while (m) {
-            *w7 = (uint32_t)(wi * 32 + (__ffs(m) - 1));
+            *sp++ = (uint32_t)(wi * 32 + (__ffs(m) - 1));
             m &= m - 1;
-            w7 += 8;
         }
     }
 }
@@ -378,13 +377,13 @@ __global__ void k_gather_slots(Dev d, uint64_t nwords, const uint32_t *__restric
 // bits new since the last gather; 6-7: the slot's key and row) becomes the
 // record and is cleared; the delta index and per-job counts are filled.
 // n_ctr >= 0: the record count is device counter n_ctr (round graphs).
-__global__ void k_gather_recs(Dev d, uint4 *out, uint64_t n, int n_ctr, const uint32_t *__restrict__ row_job,
-                              uint32_t *job_cnt, uint32_t run_stamp)
+__global__ void k_gather_recs(Dev d, const uint32_t *__restrict__ slots, uint4 *out, uint64_t n, int n_ctr,
+                              const uint32_t *__restrict__ row_job, uint32_t *job_cnt, uint32_t run_stamp)
 {
     if (d.ctr[C_HALT]) return;
     if (n_ctr >= 0) n = d.ctr[n_ctr];
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t s = reinterpret_cast<const uint32_t *>(out)[i * 8 + 7];
+        const uint64_t s = slots[i];
         uint4 *b = reinterpret_cast<uint4 *>(d.dbits + s * 8);
         const uint4 b0 = b[0], b1 = b[1];
         b[0] = make_uint4(0, 0, 0, 0);
@@ -1455,6 +1454,8 @@ struct grg_ctx {
     uint64_t rbuf_cap = 0;                     // records
     uint4 *gbuf = nullptr;                     // gathered delta records of the round
     uint64_t gbuf_cap = 0;
+    uint32_t *gslot = nullptr;                 // their slot ids (gather pass 1)
+    uint64_t gslot_cap = 0;
     uint4 *vbuf = nullptr;                     // virtual records of old-left joins
     uint64_t vbuf_cap = 0;
     uint4 *sbuf = nullptr;                     // sub-records of small rounds (k_split)
@@ -1715,6 +1716,20 @@ int ensure_buf(grg_ctx *c, uint4 **buf, uint64_t *cap, uint64_t n)
     return GRG_OK;
 }
 
+// Gathered records and their slot ids, room for n.
+int ensure_gather(grg_ctx *c, uint64_t n)
+{
+    int st = ensure_buf(c, &c->gbuf, &c->gbuf_cap, n);
+    if (st) return st;
+    if (c->gslot_cap >= c->gbuf_cap) return GRG_OK;
+    cudaFree(c->gslot);
+    c->gslot = nullptr;
+    c->gslot_cap = 0;
+    GRG_CUDA(c, cudaMalloc(&c->gslot, c->gbuf_cap * 4));
+    c->gslot_cap = c->gbuf_cap;
+    return GRG_OK;
+}
+
 // Retry buffers: every delta record of a pass may fail once, so n records each.
 int ensure_rbuf(grg_ctx *c, uint64_t n)
 {
@@ -1807,6 +1822,7 @@ void grg_destroy(grg_ctx *c)
     free_pool(c);
     for (int i = 0; i < 2; i++) cudaFree(c->rbuf[i]);
     cudaFree(c->gbuf);
+    cudaFree(c->gslot);
     cudaFree(c->vbuf);
     cudaFree(c->sbuf);
     cudaFree(c->xbuf);
@@ -2192,7 +2208,7 @@ static int round_head(grg_ctx *c, uint32_t rs, grg_stats &S, uint64_t *nd_out)
     const uint64_t nd = c->h_ctr[C_DIRTY_N];
     *nd_out = nd;
     if (nd == 0) return GRG_OK;
-    st = ensure_buf(c, &c->gbuf, &c->gbuf_cap, nd);
+    st = ensure_gather(c, nd);
     if (st) return st;
     st = ensure_cand(c, nd);
     if (st) return st;
@@ -2208,8 +2224,8 @@ static int round_head(grg_ctx *c, uint32_t rs, grg_stats &S, uint64_t *nd_out)
             GRG_CUDA(c, cudaMemsetAsync(c->drc + t0, 0, (size_t)c->V * 4, s));
             GRG_CUDA(c, cudaMemsetAsync(c->dvm + (size_t)(l - 1) * vw, 0, vw * 4, s));
         }
-    k_gather_slots<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->gbuf, 0);
-    k_gather_recs<<<grid_for(c, nd, 256), 256, 0, s>>>(d, c->gbuf, nd, -1, c->row_job, c->job_cnt, rs);
+    k_gather_slots<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->gslot, 0);
+    k_gather_recs<<<grid_for(c, nd, 256), 256, 0, s>>>(d, c->gslot, c->gbuf, nd, -1, c->row_job, c->job_cnt, rs);
     c->launches += 2;
     return GRG_OK;
 }
@@ -2461,7 +2477,7 @@ static std::vector<uint64_t> round_graph_key(const grg_ctx *c, uint32_t rs, uint
 {
     std::vector<uint64_t> k = {(uint64_t)c->elems, (uint64_t)c->dbits, (uint64_t)c->dmap, (uint64_t)c->stamp,
                                (uint64_t)c->desc, (uint64_t)c->cnt, (uint64_t)c->want, (uint64_t)c->grow,
-                               (uint64_t)c->gbuf, c->gbuf_cap, (uint64_t)c->vbuf, c->vbuf_cap,
+                               (uint64_t)c->gbuf, c->gbuf_cap, (uint64_t)c->gslot, (uint64_t)c->vbuf, c->vbuf_cap,
                                (uint64_t)c->rbuf[0], (uint64_t)c->rbuf[1], c->rbuf_cap, (uint64_t)c->cand[0],
                                (uint64_t)c->cand[1], c->cand_cap, (uint64_t)c->chunk, nchunks, (uint64_t)c->drs,
                                (uint64_t)c->drc, (uint64_t)c->dvm, c->pool_cap, c->V, rs, (uint64_t)c->timing,
@@ -2517,8 +2533,9 @@ static int build_round_graph(grg_ctx *c, uint32_t rs)
             cudaMemsetAsync(c->dvm + (size_t)(l - 1) * vw, 0, vw * 4, s);
         }
     cudaMemsetAsync(ctr + C_VN, 0, 8, s);
-    k_gather_slots<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->gbuf, 1);
-    k_gather_recs<<<grid_for(c, c->gbuf_cap, 256), 256, 0, s>>>(d, c->gbuf, 0, C_DIRTY_N, c->row_job, c->job_cnt, rs);
+    k_gather_slots<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->gslot, 1);
+    k_gather_recs<<<grid_for(c, c->gbuf_cap, 256), 256, 0, s>>>(d, c->gslot, c->gbuf, 0, C_DIRTY_N, c->row_job,
+                                                                c->job_cnt, rs);
     nk += 2;
     if (c->rt.nol) {
         for (int q = 0; q < c->rt.nol; q++)
@@ -2595,7 +2612,7 @@ static int run_rounds(grg_ctx *c, uint64_t max_rounds, grg_stats &S, double &joi
         // recorded graph survives the whole closure.
         const uint64_t nd_last = std::max<uint64_t>(c->h_ctr[C_DIRTY_N], 1);
         const uint64_t top = c->h_ctr[C_POOL_TOP], floor_cap = 1ull << 24;
-        if ((st = ensure_buf(c, &c->gbuf, &c->gbuf_cap, std::max(2 * nd_last, std::min(top, floor_cap))))) return st;
+        if ((st = ensure_gather(c, std::max(2 * nd_last, std::min(top, floor_cap))))) return st;
         if (c->rt.nol &&
             (st = ensure_buf(c, &c->vbuf, &c->vbuf_cap,
                              std::max<uint64_t>(2 * std::max<uint64_t>(c->h_ctr[C_VN], 1),
@@ -3255,7 +3272,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
             return GRG_E_ARG;
     }
     // scratch layout: counters | descriptors | cnt | want | grow | delta index | pool arrays
-    // (194 B per element slot: element, delta bitmap, dirty bit, four delta-record buffers) |
+    // (198 B per element slot: element, delta bitmap, dirty bit, slot id, four delta-record buffers) |
     // gather chunk counters. A round has at most one delta record per slot, old-left virtual
     // records at most one per (old-left rule, element), retries at most one per record.
     const uint64_t ntab = (uint64_t)num_labels * num_vars, vwords = (num_vars + 31) / 32;
@@ -3269,12 +3286,13 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     const size_t o_drc = off; off = align256(off + ntab * 4);
     const size_t o_dvm = off; off = align256(off + (uint64_t)num_labels * vwords * 4);
     if (off >= NOALLOC_SCRATCH_BYTES) return GRG_E_RANGE;            // tables alone exceed the scratch
-    uint64_t pool = (NOALLOC_SCRATCH_BYTES - off - 16 * 256) / 194;
+    uint64_t pool = (NOALLOC_SCRATCH_BYTES - off - 16 * 256) / 198;
     if (pool < 4096 || num_edges > pool / 2) return GRG_E_RANGE;    // graph too large for the scratch
     const uint64_t pwords = pool / 32 + 2, pchunks = (pwords + 31) / 32, pnb = (pchunks + 1023) / 1024;
     const size_t o_elems = off; off = align256(off + pool * 32);
     const size_t o_dbits = off; off = align256(off + pool * 32);
     const size_t o_dmap = off; off = align256(off + pwords * 4);
+    const size_t o_gslot = off; off = align256(off + pool * 4);
     const size_t o_gbuf = off; off = align256(off + pool * 32);
     const size_t o_vbuf = off; off = align256(off + pool * 32);
     const size_t o_rbuf0 = off; off = align256(off + pool * 32);
@@ -3324,6 +3342,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     d.vwords = (uint32_t)vwords;
     d.stamp = nullptr;
     uint4 *gbuf = (uint4 *)(base + o_gbuf), *vbuf = (uint4 *)(base + o_vbuf);
+    uint32_t *gslot = (uint32_t *)(base + o_gslot);
     d.drec = gbuf;
     uint4 *rbuf[2] = {(uint4 *)(base + o_rbuf0), (uint4 *)(base + o_rbuf1)};
     uint32_t *chunk = (uint32_t *)(base + o_chunk);
@@ -3385,8 +3404,8 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
                 NA_CUDA(cudaMemsetAsync(d.drc + (size_t)(l - 1) * num_vars, 0, (size_t)num_vars * 4, s));
                 NA_CUDA(cudaMemsetAsync(d.dvm + (size_t)(l - 1) * vwords, 0, vwords * 4, s));
             }
-        k_gather_slots<<<grid(nchunks * 32, 256, 8), 256, 0, s>>>(d, nwords, coff, gbuf, 0);
-        k_gather_recs<<<grid(nd, 256, 8), 256, 0, s>>>(d, gbuf, nd, -1, nullptr, nullptr, 0);
+        k_gather_slots<<<grid(nchunks * 32, 256, 8), 256, 0, s>>>(d, nwords, coff, gslot, 0);
+        k_gather_recs<<<grid(nd, 256, 8), 256, 0, s>>>(d, gslot, gbuf, nd, -1, nullptr, nullptr, 0);
         uint64_t nv = 0;
         if (rt.nol) {
             NA_CUDA(cudaMemsetAsync(d.ctr + C_VN, 0, 8, s));

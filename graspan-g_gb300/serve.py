@@ -108,12 +108,16 @@ class RangeAllocator:
 
 
 def serve(jobs, max_vars, max_jobs=256, budget_bytes=None, device=0, realtime=True, rounds_per_step=4,
-          drain_rounds=0):
+          drain_rounds=None):
     """Run the service over `jobs` (arrival_s relative to the start). With
     realtime=False every job is available at t=0 (a pure batch). A step runs
     rounds_per_step rounds while jobs wait for admission, else drain_rounds
-    (0 = until every admitted job has reached its fixpoint); the rounds of a
-    step run on the device without host round trips."""
+    (0 = until every admitted job has reached its fixpoint; default: 0 for a
+    pure batch, where only throughput counts, and 8 when serving, so that a job
+    is reported within a few rounds of its fixpoint). The rounds of a step run
+    on the device without host round trips."""
+    if drain_rounds is None:
+        drain_rounds = 8 if realtime else 0
     ctx = grg.Context(device)
     ctx.allocate_pool(0)
     batch = grg.Batch(ctx, max_vars, max_jobs, GRAMMARS, 0)

@@ -295,7 +295,7 @@ int grg_batch_release(grg_ctx *ctx, uint32_t job);
  * (the legacy default stream); the call returns after the stream is idle.
  *
  * Limits: the tables take 28 bytes per (label, vertex) and the rest of the
- * array holds 194 bytes per element slot; graphs whose tables leave fewer
+ * array holds 198 bytes per element slot; graphs whose tables leave fewer
  * than 4096 slots, or with more edges than half the slots, are rejected with
  * GRG_E_RANGE before any launch; a closure that outgrows the array returns
  * GRG_E_NOMEM.
