@@ -870,6 +870,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : 4))
                 // JOIN_UNROLL items per lane per iteration: their loads are issued together
                 for (uint32_t f0 = 0; f0 < nitems; f0 += 32 * JOIN_UNROLL) {
                     uint32_t it_r[JOIN_UNROLL], it_b2[JOIN_UNROLL];
+                    uint32_t it_ob[JOIN_UNROLL];      // CSR item: its id within the element (one bit); else EMPTY
                     Bits it_b[JOIN_UNROLL];
                     bool it_ok[JOIN_UNROLL];
 #pragma unroll
@@ -891,6 +892,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : 4))
                         it_r[u] = o_r;
                         it_ok[u] = false;
                         it_b2[u] = 0;
+                        it_ob[u] = EMPTY;
 #pragma unroll
                         for (int x = 0; x < EW; x++) it_b[u].w[x] = 0;
                         if (f < nitems) {
@@ -898,9 +900,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : 4))
                             if (o_csr == 1) {
                                 const uint32_t dst = __ldg(c_rt.csr_col[o_C] + item);
                                 it_b2[u] = dst / EIDS;
-                                const uint32_t ob = dst % EIDS;
-#pragma unroll
-                                for (int x = 0; x < EW; x++) it_b[u].w[x] = (uint32_t)x == (ob >> 5) ? 1u << (ob & 31) : 0u;
+                                it_ob[u] = dst % EIDS;
                                 it_ok[u] = true;
                             } else {
                                 const uint4 *ep = o_csr == 2 ? d.drec + 2 * (size_t)item
@@ -924,12 +924,22 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : 4))
                             // the statistic the window choice is keyed on: items beyond the narrow window
                             n_out += (unsigned)(dd - WIN_LO + grg::WIN_LO) >= (unsigned)grg::WIN;
                             if ((unsigned)dd < (unsigned)WIN) {
+                                if (it_ob[u] != EMPTY) {
+                                    // one destination id: one word of the window
+                                    atomicOr(&w.win[o_r][dd][it_ob[u] >> 5], 1u << (it_ob[u] & 31));
+                                } else {
 #pragma unroll
-                                for (int x = 0; x < EW; x++)
-                                    if (it_b[u].w[x]) atomicOr(&w.win[o_r][dd][x], it_b[u].w[x]);
+                                    for (int x = 0; x < EW; x++)
+                                        if (it_b[u].w[x]) atomicOr(&w.win[o_r][dd][x], it_b[u].w[x]);
+                                }
                             } else {
                                 pending = true;
                                 ckey = (o_r << KEY_SHIFT) | it_b2[u];
+                                if (it_ob[u] != EMPTY) {
+#pragma unroll
+                                    for (int x = 0; x < EW; x++)
+                                        it_b[u].w[x] = (uint32_t)x == (it_ob[u] >> 5) ? 1u << (it_ob[u] & 31) : 0u;
+                                }
                             }
                         }
                         while (__any_sync(0xffffffffu, pending)) {
