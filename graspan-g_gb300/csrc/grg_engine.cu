@@ -867,6 +867,9 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : 4))
                     if (lane >= (uint32_t)o) incl += y;
                 }
                 const uint32_t nitems = __shfl_sync(0xffffffffu, incl, 31);
+                // per task: item f sits at beg + f - (first f of the task); record, label and source packed
+                const uint32_t adj = beg - (incl - cnt);
+                const uint32_t pk = r | (C << 8) | (csr << 16);
                 // JOIN_UNROLL items per lane per iteration: their loads are issued together
                 for (uint32_t f0 = 0; f0 < nitems; f0 += 32 * JOIN_UNROLL) {
                     uint32_t it_r[JOIN_UNROLL], it_b2[JOIN_UNROLL];
@@ -883,12 +886,9 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : 4))
                             const uint32_t v = __shfl_sync(0xffffffffu, incl, lo + st - 1);
                             if (v <= f) lo += st;
                         }
-                        const uint32_t o_incl = __shfl_sync(0xffffffffu, incl, lo);
-                        const uint32_t o_cnt = __shfl_sync(0xffffffffu, cnt, lo);
-                        const uint32_t o_beg = __shfl_sync(0xffffffffu, beg, lo);
-                        const uint32_t o_r = __shfl_sync(0xffffffffu, r, lo);
-                        const uint32_t o_C = __shfl_sync(0xffffffffu, C, lo);
-                        const uint32_t o_csr = __shfl_sync(0xffffffffu, csr, lo);
+                        const uint32_t o_adj = __shfl_sync(0xffffffffu, adj, lo);
+                        const uint32_t o_pk = __shfl_sync(0xffffffffu, pk, lo);
+                        const uint32_t o_r = o_pk & 0xFFu, o_C = (o_pk >> 8) & 0xFFu, o_csr = o_pk >> 16;
                         it_r[u] = o_r;
                         it_ok[u] = false;
                         it_b2[u] = 0;
@@ -896,7 +896,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : 4))
 #pragma unroll
                         for (int x = 0; x < EW; x++) it_b[u].w[x] = 0;
                         if (f < nitems) {
-                            const uint32_t item = o_beg + (f - (o_incl - o_cnt));
+                            const uint32_t item = f + o_adj;
                             if (o_csr == 1) {
                                 const uint32_t dst = __ldg(c_rt.csr_col[o_C] + item);
                                 it_b2[u] = dst / EIDS;
