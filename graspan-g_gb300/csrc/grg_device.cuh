@@ -115,6 +115,10 @@ struct Dev {
     // the run in which the element last gained bits, carried through growth,
     // compaction and export; the out-of-core schedule marks deltas from them
     uint32_t *stamp;
+    // labels whose small tables (capacity <= PREFIX_CAP) are filled as a prefix
+    // (probing from slot 0), so a join reading the row as right-hand items reads
+    // only its occupied slots: bit l-1 = label l
+    unsigned long long prefix_mask;
     unsigned long long *ctr;  // counter block
     uint32_t V;
     uint32_t pool_cap;        // elements
@@ -125,6 +129,25 @@ __device__ __forceinline__ uint32_t hash_slot(uint32_t base, uint32_t lg)
     return lg ? (base * 0x9E3779B1u) >> (32 - lg) : 0u;
 }
 __device__ __forceinline__ uint32_t max_load(uint32_t cap) { return cap - (cap >> 2); }
+
+// Table layout: a hashed table (Fibonacci hash, linear probing, load <= 3/4),
+// or -- for labels in prefix_mask while their capacity is at most PREFIX_CAP --
+// a prefix-filled one: probing starts at slot 0 and a table may fill up, so its
+// occupied slots are always slots [0, count). Layout follows from the label and
+// capacity alone, so every kernel that places or finds an element agrees.
+constexpr uint32_t PREFIX_CAP = 16;
+__device__ __forceinline__ bool prefix_table(const Dev &d, uint32_t slot, uint32_t cap)
+{
+    return cap <= PREFIX_CAP && ((d.prefix_mask >> (slot - 1)) & 1ull);
+}
+__device__ __forceinline__ uint32_t table_start(const Dev &d, uint32_t slot, uint32_t base, uint32_t cap)
+{
+    return prefix_table(d, slot, cap) ? 0u : hash_slot(base, 31 - __clz(cap));
+}
+__device__ __forceinline__ uint32_t table_limit(const Dev &d, uint32_t slot, uint32_t cap)
+{
+    return prefix_table(d, slot, cap) ? cap : max_load(cap);
+}
 
 struct Bits { uint32_t w[EW]; };
 
@@ -153,15 +176,14 @@ __device__ __forceinline__ bool g_insert(const Dev &d, uint32_t slot, uint32_t r
     const uint32_t key = (slot << KEY_SHIFT) | base;
     uint32_t s = EMPTY;
     if (cap != 0 && (cap & (cap - 1)) == 0) {
-        const uint32_t lg = 31 - __clz(cap);
-        const uint32_t h = hash_slot(base, lg);
+        const uint32_t h = table_start(d, slot, base, cap), lim = table_limit(d, slot, cap);
         for (uint32_t p = 0; p < cap; p++) {
             const uint32_t q = off + ((h + p) & (cap - 1));
             uint32_t *kp = d.elems + (size_t)q * 8 + 6;
             const uint32_t k = __ldcg(kp);
             if (k == key) { s = q; break; }
             if (k != EMPTY) continue;
-            if (atomicAdd(&d.cnt[ti], 1u) >= max_load(cap)) { atomicSub(&d.cnt[ti], 1u); break; }
+            if (atomicAdd(&d.cnt[ti], 1u) >= lim) { atomicSub(&d.cnt[ti], 1u); break; }
             const uint32_t prev = atomicCAS(kp, EMPTY, key);
             if (prev == EMPTY) {
                 d.elems[(size_t)q * 8 + 7] = row;

@@ -422,7 +422,9 @@ __global__ void k_oldleft(Dev d, uint32_t q, uint4 *out, uint64_t cap)
     for (uint64_t b0 = blockIdx.x * (uint64_t)blockDim.x + (threadIdx.x & ~31u); b0 < d.V; b0 += stride) {
         const uint64_t v = b0 + lane_id();
         const uint64_t de = v < d.V ? d.desc[(size_t)(B - 1) * d.V + v] : 0ull;
-        const uint32_t off = (uint32_t)de, cap_v = (uint32_t)(de >> 32);
+        const uint32_t off = (uint32_t)de;
+        uint32_t cap_v = (uint32_t)(de >> 32);
+        if (v < d.V && prefix_table(d, B, cap_v)) cap_v = min(cap_v, d.cnt[(size_t)(B - 1) * d.V + v]);
         const uint32_t maxc = __reduce_max_sync(0xffffffffu, cap_v);
         for (uint32_t j = 0; j < maxc; j++) {
             Bits m;
@@ -855,9 +857,12 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : 4))
                         cnt = rw.y & 0xFFFFFFu;
                         n_right += rw.y >> 24;
                     } else {
-                        const uint64_t de = __ldg(d.desc + (size_t)(C - 1) * d.V + k);
+                        const size_t ti = (size_t)(C - 1) * d.V + k;
+                        const uint64_t de = __ldg(d.desc + ti);
                         beg = (uint32_t)de;
                         cnt = (uint32_t)(de >> 32);
+                        // a prefix-filled table: only slots [0, count) can be occupied
+                        if (prefix_table(d, C, cnt)) cnt = min(cnt, __ldcg(d.cnt + ti));
                     }
                 }
                 uint32_t incl = cnt;
@@ -1156,12 +1161,12 @@ __global__ void k_grow(Dev d, uint64_t n)
             if (d.stamp) d.stamp[nb + t] = 0;
         }
         __syncwarp();
-        const uint32_t lg = 31 - __clz(ncap);
+        const uint32_t lab = (uint32_t)(ti / d.V) + 1;
         for (uint32_t t = lane; t < cap; t += 32) {
             const uint4 *e = reinterpret_cast<const uint4 *>(d.elems + (size_t)(off + t) * 8);
             const uint4 e0 = e[0], e1 = e[1];
             if (e1.z == EMPTY) continue;
-            uint32_t h = hash_slot(e1.z & BASE_MASK, lg);
+            const uint32_t h = table_start(d, lab, e1.z & BASE_MASK, ncap);
             for (uint32_t p = 0; p < ncap; p++) {
                 const uint64_t q = nb + ((h + p) & (ncap - 1));
                 if (atomicCAS(d.elems + q * 8 + 6, EMPTY, e1.z) == EMPTY) {
@@ -1315,7 +1320,7 @@ __global__ void k_elem_insert(Dev d, const uint4 *recs, const uint32_t *stamps, 
         const uint32_t off = (uint32_t)de, cap = (uint32_t)(de >> 32);
         uint32_t q = EMPTY;
         if (cap && (cap & (cap - 1)) == 0) {
-            const uint32_t h = hash_slot(base, 31 - __clz(cap));
+            const uint32_t h = table_start(d, lab, base, cap);
             for (uint32_t p = 0; p < cap; p++) {
                 const uint32_t t = off + ((h + p) & (cap - 1));
                 const uint32_t prev = atomicCAS(d.elems + (size_t)t * 8 + 6, EMPTY, e1.z);
@@ -1488,6 +1493,7 @@ struct grg_ctx {
     uint64_t xcap = 0;
     uint64_t pool_limit = 0;               // maximum pool slots (0 = what the device holds)
     uint64_t retry_min = 1ull << 20;       // smallest retry list (records; GRG_RETRY_ROOM)
+    uint64_t prefix_mask = 0;              // labels with prefix-filled small tables (Dev::prefix_mask)
     // join window: narrow (WIN) or wide (WIN2, the default)
     bool join_wide = true;
     int join_window_mode = 1;              // 0 = narrow, 1 = wide
@@ -1581,6 +1587,7 @@ Dev make_dev(const grg_ctx *c)
     d.V = c->V;
     d.pool_cap = (uint32_t)c->pool_cap;
     d.stamp = c->elem_loaded ? c->stamp : nullptr;
+    d.prefix_mask = c->prefix_mask;
     return d;
 }
 
@@ -1899,6 +1906,18 @@ int grg_transfer_rules(grg_ctx *c, int num_rules, const int *rules, int num_labe
     c->L = num_labels;
     memset(c->rules, 0, sizeof c->rules);
     memcpy(c->rules, rules, sizeof(int) * 3 * (size_t)num_rules);
+    // prefix-filled small tables for the labels joins read as table rows: a binary
+    // rule's derivable second symbol (delta-left items) and that rule's first
+    // symbol (old-left virtual records scan its rows)
+    bool der[GRG_MAX_LABELS + 1] = {false};
+    for (int q = 0; q < num_rules; q++) der[rules[3 * q]] = true;
+    c->prefix_mask = 0;
+    for (int q = 0; q < num_rules; q++) {
+        const int *r = &rules[3 * q];
+        if (r[1] && r[2] && der[r[2]]) c->prefix_mask |= (1ull << (r[2] - 1)) | (1ull << (r[1] - 1));
+    }
+    const char *pt = getenv("GRG_PREFIX_TABLES");    // "0": every table hashed
+    if (pt && pt[0] == '0') c->prefix_mask = 0;
     c->have_rules = true;
     c->loaded = false;
     return GRG_OK;
@@ -3351,6 +3370,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     d.dvm = (uint32_t *)(base + o_dvm);
     d.vwords = (uint32_t)vwords;
     d.stamp = nullptr;
+    d.prefix_mask = 0;         // every table hashed
     uint4 *gbuf = (uint4 *)(base + o_gbuf), *vbuf = (uint4 *)(base + o_vbuf);
     uint32_t *gslot = (uint32_t *)(base + o_gslot);
     d.drec = gbuf;
