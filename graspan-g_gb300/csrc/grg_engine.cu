@@ -408,11 +408,30 @@ __global__ void k_gather_recs(Dev d, const uint32_t *__restrict__ slots, uint4 *
     }
 }
 
+// Device-driven rounds: clear the delta index entries the previous round's gather
+// set (its records are still in recs, n_ctr counts them), instead of clearing
+// every vertex.
+__global__ void k_dindex_clear(Dev d, const uint4 *__restrict__ recs, int n_ctr)
+{
+    if (d.ctr[C_HALT]) return;
+    const uint64_t n = d.ctr[n_ctr];
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint4 b1 = recs[2 * i + 1];
+        const uint32_t lab = b1.z >> KEY_SHIFT, row = b1.w;
+        if (lab > (uint32_t)MAX_LABELS || !c_rt.dindex[lab]) continue;
+        const size_t ti = (size_t)(lab - 1) * d.V + row;
+        d.drs[ti] = EMPTY;
+        d.drc[ti] = 0;
+        d.dvm[(size_t)(lab - 1) * d.vwords + (row >> 5)] = 0;
+    }
+}
+
 // Old-left join q (A ::= B C, C derivable): every element of every row of B,
 // masked to the vertices k whose row C[k] has deltas this round, becomes a
 // virtual delta record (label slot OL_SLOT0 + q). The 192 ids of an element are
 // exactly 6 words of the dirty-vertex bitmap. Records past cap are counted only.
-__global__ void k_oldleft(Dev d, uint32_t q, uint4 *out, uint64_t cap)
+__global__ void k_oldleft(Dev d, uint32_t q, uint4 *out, uint64_t cap, const uint32_t *__restrict__ row_job,
+                          const uint32_t *__restrict__ job_cnt)
 {
     if (d.ctr[C_HALT]) return;
     const uint32_t B = c_rt.ol_B[q], C = c_rt.ol_C[q];
@@ -425,6 +444,11 @@ __global__ void k_oldleft(Dev d, uint32_t q, uint4 *out, uint64_t cap)
         const uint32_t off = (uint32_t)de;
         uint32_t cap_v = (uint32_t)(de >> 32);
         if (v < d.V && prefix_table(d, B, cap_v)) cap_v = min(cap_v, d.cnt[(size_t)(B - 1) * d.V + v]);
+        // batched jobs: a job without delta records this round adds no virtual records
+        if (row_job && cap_v) {
+            const uint32_t job = row_job[v];
+            if (job == EMPTY || job_cnt[job] == 0) cap_v = 0;
+        }
         const uint32_t maxc = __reduce_max_sync(0xffffffffu, cap_v);
         for (uint32_t j = 0; j < maxc; j++) {
             Bits m;
@@ -2269,7 +2293,8 @@ static int round_oldleft(grg_ctx *c, uint64_t *nv_out)
             Dev d = make_dev(c);
             GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_VN, 0, 8, s));
             for (int q = 0; q < c->rt.nol; q++) {
-                k_oldleft<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)q, c->vbuf, c->vbuf_cap);
+                k_oldleft<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)q, c->vbuf, c->vbuf_cap, c->row_job,
+                                                                 c->job_cnt);
                 c->launches++;
             }
             int st = read_ctr(c);
@@ -2545,6 +2570,13 @@ static int build_round_graph(grg_ctx *c, uint32_t rs)
     uint32_t *ccnt = c->chunk, *coff = c->chunk + nchunks + 1, *csum = c->chunk + 2 * (nchunks + 1);
     unsigned long long *ctr = c->ctr;
     int nk = 0;
+    bool any_dindex = false;
+    for (int l = 1; l <= c->L; l++) any_dindex |= c->rt.dindex[l] != 0;
+    if (any_dindex) {
+        // first in the body: C_DIRTY_N still counts the previous round's records in gbuf
+        k_dindex_clear<<<grid_for(c, c->gbuf_cap, 256), 256, 0, s>>>(d, c->gbuf, C_DIRTY_N);
+        nk++;
+    }
     cudaMemsetAsync(ctr + C_RETRY_N, 0, 16, s);
     cudaMemsetAsync(ctr + C_CAND_N, 0, 16, s);
     if (c->job_cnt) cudaMemsetAsync(c->job_cnt, 0, (size_t)c->max_jobs * 4, s);
@@ -2554,13 +2586,6 @@ static int build_round_graph(grg_ctx *c, uint32_t rs)
     k_scan_add<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(coff, csum, nchunks, ctr);
     k_gate_gather<<<1, 32, 0, s>>>(ctr, csum, nchunks, c->gbuf_cap, GATE_MAX_ITERS, h);
     nk += 5;
-    for (int l = 1; l <= c->L; l++)
-        if (c->rt.dindex[l]) {
-            const size_t t0 = (size_t)(l - 1) * c->V, vw = (c->V + 31) / 32;
-            cudaMemsetAsync(c->drs + t0, 0xFF, (size_t)c->V * 4, s);
-            cudaMemsetAsync(c->drc + t0, 0, (size_t)c->V * 4, s);
-            cudaMemsetAsync(c->dvm + (size_t)(l - 1) * vw, 0, vw * 4, s);
-        }
     cudaMemsetAsync(ctr + C_VN, 0, 8, s);
     k_gather_slots<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->gslot, 1);
     k_gather_recs<<<grid_for(c, c->gbuf_cap, 256), 256, 0, s>>>(d, c->gslot, c->gbuf, 0, C_DIRTY_N, c->row_job,
@@ -2568,7 +2593,8 @@ static int build_round_graph(grg_ctx *c, uint32_t rs)
     nk += 2;
     if (c->rt.nol) {
         for (int q = 0; q < c->rt.nol; q++)
-            k_oldleft<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)q, c->vbuf, c->vbuf_cap);
+            k_oldleft<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)q, c->vbuf, c->vbuf_cap, c->row_job,
+                                                             c->job_cnt);
         k_gate_oldleft<<<1, 32, 0, s>>>(ctr, c->vbuf_cap, h);
         nk += c->rt.nol + 1;
     }
@@ -2652,6 +2678,16 @@ static int run_rounds(grg_ctx *c, uint64_t max_rounds, grg_stats &S, double &joi
         if ((st = ensure_sbuf(c))) return st;
         if ((st = build_round_graph(c, rs))) return st;
         c->cb = 0;
+        // the delta index starts clear: inside the graph each round clears what the previous
+        // round's records set, and those records may not have survived a buffer regrowth
+        for (int l = 1; l <= c->L; l++)
+            if (c->rt.dindex[l]) {
+                const size_t t0 = (size_t)(l - 1) * c->V, vw = (c->V + 31) / 32;
+                GRG_CUDA(c, cudaMemsetAsync(c->drs + t0, 0xFF, (size_t)c->V * 4, s));
+                GRG_CUDA(c, cudaMemsetAsync(c->drc + t0, 0, (size_t)c->V * 4, s));
+                GRG_CUDA(c, cudaMemsetAsync(c->dvm + (size_t)(l - 1) * vw, 0, vw * 4, s));
+            }
+        GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_DIRTY_N, 0, 8, s));
         GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_HALT, 0, 8 * 5, s));   // halt, iterations, rounds, deltas, join ns
         c->h_ctr[C_MAXR] = max_rounds ? max_rounds - done_rounds : 0;
         GRG_CUDA(c, cudaMemcpyAsync(c->ctr + C_MAXR, c->h_ctr + C_MAXR, 8, cudaMemcpyHostToDevice, s));
@@ -3440,7 +3476,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
         if (rt.nol) {
             NA_CUDA(cudaMemsetAsync(d.ctr + C_VN, 0, 8, s));
             for (int q = 0; q < rt.nol; q++)
-                k_oldleft<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)q, vbuf, pool);
+                k_oldleft<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)q, vbuf, pool, nullptr, nullptr);
             if ((st = na_read(h, d.ctr, s))) return st;
             nv = h[C_VN];
             if (nd + nv > pool) return GRG_E_NOMEM;                // records (and their retries) outgrew the scratch
