@@ -219,6 +219,8 @@ def extra_measurements(args, w2):
                                        "runs": pst["runs"], "pairs_skipped": pst["skipped"],
                                        "supersteps": pst["supersteps"], "load_s": t_load, "run_ms": pst["ms"],
                                        "h2d_bytes": pst["h2d_bytes"], "d2h_bytes": pst["d2h_bytes"],
+                                       "phase_ms": {k: pst[k] for k in ("stage_ms", "load_ms", "closure_ms",
+                                                                        "export_ms", "count_ms")},
                                        "value": pst["total_edges"] / (pst["ms"] * 1e-3), "unit": UNIT,
                                        "identical_to_in_core": True}}
     del w

@@ -33,6 +33,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <utility>
@@ -44,11 +45,81 @@ namespace {
 
 constexpr uint32_t KEY_SHIFT = 25;
 
+// Growable array in page-locked host memory (pageable if pinning fails): images
+// live here, so device<->host copies of them need no staging copy.
+struct HostVec {
+    uint32_t *p = nullptr;
+    uint64_t n = 0, cap = 0;
+    bool pinned = false;
+    HostVec() = default;
+    HostVec(const HostVec &) = delete;
+    HostVec &operator=(const HostVec &) = delete;
+    HostVec(HostVec &&o) noexcept : p(o.p), n(o.n), cap(o.cap), pinned(o.pinned) { o.p = nullptr; o.n = o.cap = 0; }
+    HostVec &operator=(HostVec &&o) noexcept
+    {
+        if (this != &o) {
+            release();
+            p = o.p; n = o.n; cap = o.cap; pinned = o.pinned;
+            o.p = nullptr; o.n = o.cap = 0;
+        }
+        return *this;
+    }
+    ~HostVec() { release(); }
+    void release()
+    {
+        if (p) {
+            if (pinned) cudaFreeHost(p); else free(p);
+        }
+        p = nullptr;
+        n = cap = 0;
+    }
+    bool reserve(uint64_t c)       // keeps the contents
+    {
+        if (c <= cap) return true;
+        const uint64_t nc = std::max<uint64_t>(c + c / 4, 256);
+        uint32_t *q = nullptr;
+        bool pin = true;
+        if (cudaHostAlloc((void **)&q, nc * 4, cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            pin = false;
+            q = (uint32_t *)malloc(nc * 4);
+            if (!q) return false;
+        }
+        if (n) memcpy(q, p, n * 4);
+        const uint64_t keep = n;
+        release();
+        p = q; n = keep; cap = nc; pinned = pin;
+        return true;
+    }
+    bool resize(uint64_t m)
+    {
+        if (!reserve(m)) return false;
+        n = m;
+        return true;
+    }
+    bool append(const uint32_t *src, uint64_t m)
+    {
+        if (!reserve(n + m)) return false;
+        memcpy(p + n, src, m * 4);
+        n += m;
+        return true;
+    }
+    uint32_t *data() { return p; }
+    const uint32_t *data() const { return p; }
+    uint64_t size() const { return n; }
+    uint32_t &operator[](uint64_t i) { return p[i]; }
+    uint32_t operator[](uint64_t i) const { return p[i]; }
+    uint32_t *begin() { return p; }
+    uint32_t *end() { return p + n; }
+    const uint32_t *begin() const { return p; }
+    const uint32_t *end() const { return p + n; }
+};
+
 struct Image {
     uint32_t id = 0;                 // unique per partition (splits make new ids)
     uint32_t lo = 0, hi = 0;         // source vertices [lo, hi)
-    std::vector<uint32_t> rec;       // 8 words per element
-    std::vector<uint32_t> st;        // stamp per element
+    HostVec rec;                     // 8 words per element
+    HostVec st;                      // stamp per element
     uint32_t max_stamp = 0;
     uint32_t last_run = 0;           // last run that held this partition
     bool counted = false;            // counts/hash are those of the current image
@@ -106,7 +177,7 @@ struct grg_part {
     uint32_t run_id = 1;                                       // stamps of loaded edges are 1
     bool loaded = false;
     bool closed = false;
-    Pinned in, out;
+    Pinned in;                       // run inputs assembled for the device
     grg_part_stats S{};
     uint64_t bmask = 0;              // labels that are a binary rule's first symbol
 };
@@ -114,6 +185,14 @@ struct grg_part {
 namespace {
 
 std::pair<uint32_t, uint32_t> pkey(uint32_t a, uint32_t b) { return a < b ? std::make_pair(a, b) : std::make_pair(b, a); }
+
+// Adds the wall time of its scope to a stats field.
+struct Timer {
+    double &acc;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    explicit Timer(double &a) : acc(a) {}
+    ~Timer() { acc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(); }
+};
 
 // Labels any rule can add edges to under the filter (epsilon rules count: they
 // add edges at the load), as the engine classifies them.
@@ -130,23 +209,26 @@ void derivable_labels(const grg_part *p, uint32_t filter, bool *der)
 // Export rows [lo, hi) of the loaded graph into img (records + device stamps).
 int export_image(grg_part *p, Image &img)
 {
-    int st = p->out.ensure(1024);
-    if (st) return st;
-    uint64_t n2 = 0;
-    st = grg_export_elements(p->ctx, img.lo, img.hi, p->out.cap, p->out.rec, p->out.st, &n2);
-    if (st == GRG_E_RANGE && n2 > p->out.cap) {
-        if ((st = p->out.ensure(n2))) return st;
-        st = grg_export_elements(p->ctx, img.lo, img.hi, p->out.cap, p->out.rec, p->out.st, &n2);
+    Timer tm(p->S.export_ms);
+    // straight into the image's own (pinned) arrays; regrown once when they are too small
+    uint64_t cap = std::min(img.rec.cap / 8, img.st.cap), n2 = 0;
+    img.rec.n = img.st.n = 0;
+    int st = grg_export_elements(p->ctx, img.lo, img.hi, cap, img.rec.data(), img.st.data(), &n2);
+    if (st == GRG_E_RANGE && n2 > cap) {
+        if (!img.rec.reserve(n2 * 8) || !img.st.reserve(n2)) return GRG_E_NOMEM;
+        cap = std::min(img.rec.cap / 8, img.st.cap);
+        st = grg_export_elements(p->ctx, img.lo, img.hi, cap, img.rec.data(), img.st.data(), &n2);
     }
     if (st) return st;
-    img.rec.assign(p->out.rec, p->out.rec + n2 * 8);
-    img.st.assign(p->out.st, p->out.st + n2);
+    img.rec.n = n2 * 8;
+    img.st.n = n2;
     p->S.d2h_bytes += n2 * 36;
     return GRG_OK;
 }
 
 int count_image(grg_part *p, Image &img)
 {
+    Timer tm(p->S.count_ms);
     img.counts.assign(p->L, 0);
     int st = grg_range_counts(p->ctx, img.lo, img.hi, img.counts.data(), &img.hash);
     if (st) return st;
@@ -157,6 +239,7 @@ int count_image(grg_part *p, Image &img)
 // Reach set of parts[i] over the current partition bounds (graph loaded on the device).
 int reach_image(grg_part *p, size_t i)
 {
+    Timer tm(p->S.count_ms);
     const size_t m = p->parts.size();
     std::vector<uint32_t> bounds(m + 1);
     for (size_t q = 0; q < m; q++) bounds[q] = p->parts[q].lo;
@@ -195,8 +278,8 @@ bool split(grg_part *p, size_t i)
     b.lo = mid; b.hi = x.hi;
     for (uint64_t e = 0; e < x.size(); e++) {
         Image &t = x.rec[8 * e + 7] < mid ? a : b;
-        t.rec.insert(t.rec.end(), x.rec.begin() + 8 * e, x.rec.begin() + 8 * e + 8);
-        t.st.push_back(x.st[e]);
+        t.rec.append(x.rec.data() + 8 * e, 8);
+        t.st.append(&x.st[e], 1);
     }
     a.refresh();
     b.refresh();
@@ -252,30 +335,50 @@ int run_once(grg_part *p, uint32_t filter, const std::vector<size_t> &idx, const
              const bool *keep_label, uint32_t mark_after, uint32_t run_stamp)
 {
     uint64_t n = extra ? extra->size() : 0;
-    for (size_t i : idx)
-        for (uint64_t e = 0; e < p->parts[i].size(); e++)
-            if (!keep_label || keep_label[p->parts[i].rec[8 * e + 6] >> KEY_SHIFT]) n++;
-    int st = p->in.ensure(n);
-    if (st) return st;
-    uint64_t k = 0;
-    if (extra && extra->size()) {
-        memcpy(p->in.rec, extra->rec.data(), extra->size() * 32);
-        memcpy(p->in.st, extra->st.data(), extra->size() * 4);
-        k = extra->size();
-    }
-    for (size_t i : idx) {
-        const Image &x = p->parts[i];
-        for (uint64_t e = 0; e < x.size(); e++) {
-            if (keep_label && !keep_label[x.rec[8 * e + 6] >> KEY_SHIFT]) continue;
-            memcpy(p->in.rec + 8 * k, x.rec.data() + 8 * e, 32);
-            p->in.st[k] = x.st[e];
-            k++;
+    int st;
+    {
+        Timer tm(p->S.stage_ms);
+        for (size_t i : idx) {
+            if (!keep_label) {
+                n += p->parts[i].size();
+                continue;
+            }
+            for (uint64_t e = 0; e < p->parts[i].size(); e++)
+                if (keep_label[p->parts[i].rec[8 * e + 6] >> KEY_SHIFT]) n++;
+        }
+        if ((st = p->in.ensure(n))) return st;
+        uint64_t k = 0;
+        if (extra && extra->size()) {
+            memcpy(p->in.rec, extra->rec.data(), extra->size() * 32);
+            memcpy(p->in.st, extra->st.data(), extra->size() * 4);
+            k = extra->size();
+        }
+        for (size_t i : idx) {
+            const Image &x = p->parts[i];
+            if (!keep_label) {               // whole images: one copy each
+                memcpy(p->in.rec + 8 * k, x.rec.data(), x.size() * 32);
+                memcpy(p->in.st + k, x.st.data(), x.size() * 4);
+                k += x.size();
+                continue;
+            }
+            for (uint64_t e = 0; e < x.size(); e++) {
+                if (!keep_label[x.rec[8 * e + 6] >> KEY_SHIFT]) continue;
+                memcpy(p->in.rec + 8 * k, x.rec.data() + 8 * e, 32);
+                p->in.st[k] = x.st[e];
+                k++;
+            }
         }
     }
     p->S.h2d_bytes += n * 36;
-    if ((st = grg_load_elements(p->ctx, p->V, n, p->in.rec, p->in.st, mark_after, 0))) return st;
+    {
+        Timer tm(p->S.load_ms);
+        if ((st = grg_load_elements(p->ctx, p->V, n, p->in.rec, p->in.st, mark_after, 0))) return st;
+    }
     grg_stats cs;
-    if ((st = grg_closure_ex(p->ctx, filter, run_stamp, &cs))) return st;
+    {
+        Timer tm(p->S.closure_ms);
+        if ((st = grg_closure_ex(p->ctx, filter, run_stamp, &cs))) return st;
+    }
     p->S.runs++;
     p->S.rounds += cs.rounds;
     return GRG_OK;
@@ -292,8 +395,9 @@ int run_stream(grg_part *p, uint32_t filter, const bool *der)
             const Image &x = p->parts[j];
             for (uint64_t e = 0; e < x.size(); e++) {
                 if (derived[x.rec[8 * e + 6] >> KEY_SHIFT]) continue;
-                stat.rec.insert(stat.rec.end(), x.rec.begin() + 8 * e, x.rec.begin() + 8 * e + 8);
-                stat.st.push_back(j == i ? 1u : 0u);
+                const uint32_t mark = j == i ? 1u : 0u;
+                stat.rec.append(x.rec.data() + 8 * e, 8);
+                stat.st.append(&mark, 1);
             }
         }
         Image &x = p->parts[i];

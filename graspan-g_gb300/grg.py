@@ -64,7 +64,9 @@ class PartStats(ctypes.Structure):
         ("total_edges", ctypes.c_uint64), ("num_parts", ctypes.c_uint32), ("schedule", ctypes.c_uint32),
         ("supersteps", ctypes.c_uint64), ("runs", ctypes.c_uint64), ("skipped", ctypes.c_uint64),
         ("splits", ctypes.c_uint64), ("rounds", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64),
-        ("d2h_bytes", ctypes.c_uint64), ("ms", ctypes.c_double),
+        ("d2h_bytes", ctypes.c_uint64), ("ms", ctypes.c_double), ("stage_ms", ctypes.c_double),
+        ("load_ms", ctypes.c_double), ("closure_ms", ctypes.c_double), ("export_ms", ctypes.c_double),
+        ("count_ms", ctypes.c_double),
     ]
 
     def as_dict(self):

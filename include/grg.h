@@ -213,6 +213,11 @@ typedef struct {
     uint64_t h2d_bytes;       /* image bytes loaded to the device */
     uint64_t d2h_bytes;       /* image bytes read back */
     double ms;                /* wall time of grg_part_run */
+    double stage_ms;          /* of which: assembling run inputs in host memory */
+    double load_ms;           /*           loading them on the device (grg_load_elements) */
+    double closure_ms;        /*           closures (grg_closure_ex) */
+    double export_ms;         /*           reading images back (grg_export_elements) */
+    double count_ms;          /*           per-partition counts and reach sets */
 } grg_part_stats;
 
 /* A partitioned graph over [0, num_vars) on context ctx (which holds the
