@@ -276,6 +276,12 @@ bool split(grg_part *p, size_t i)
     b.id = p->next_id++;
     a.lo = x.lo; a.hi = mid;
     b.lo = mid; b.hi = x.hi;
+    uint64_t na = 0;
+    for (uint64_t e = 0; e < x.size(); e++) na += x.rec[8 * e + 7] < mid;
+    a.rec.reserve(na * 8);
+    a.st.reserve(na);
+    b.rec.reserve((x.size() - na) * 8);
+    b.st.reserve(x.size() - na);
     for (uint64_t e = 0; e < x.size(); e++) {
         Image &t = x.rec[8 * e + 7] < mid ? a : b;
         t.rec.append(x.rec.data() + 8 * e, 8);
@@ -388,23 +394,39 @@ int run_stream(grg_part *p, uint32_t filter, const bool *der)
 {
     bool derived[GRG_MAX_LABELS + 1];
     for (int l = 0; l <= GRG_MAX_LABELS; l++) derived[l] = der[l];
+    // static records of every partition (never inserted into, so built once; again after
+    // a split), in partition order; seg[j] = where partition j's begin. A run marks only
+    // its own partition's segment.
+    Image stat;
+    std::vector<uint64_t> seg;
+    bool stale = true;
     for (size_t i = 0; i < p->parts.size();) {
-        // static records of every partition, marked only for partition i's rows
-        Image stat;
-        for (size_t j = 0; j < p->parts.size(); j++) {
-            const Image &x = p->parts[j];
-            for (uint64_t e = 0; e < x.size(); e++) {
-                if (derived[x.rec[8 * e + 6] >> KEY_SHIFT]) continue;
-                const uint32_t mark = j == i ? 1u : 0u;
-                stat.rec.append(x.rec.data() + 8 * e, 8);
-                stat.st.append(&mark, 1);
+        if (stale) {
+            uint64_t ns = 0;
+            for (const Image &x : p->parts)
+                for (uint64_t e = 0; e < x.size(); e++) ns += !derived[x.rec[8 * e + 6] >> KEY_SHIFT];
+            stat.rec.n = stat.st.n = 0;
+            if (!stat.rec.reserve(ns * 8) || !stat.st.reserve(ns)) return GRG_E_NOMEM;
+            seg.assign(1, 0);
+            const uint32_t zero = 0;
+            for (const Image &x : p->parts) {
+                for (uint64_t e = 0; e < x.size(); e++) {
+                    if (derived[x.rec[8 * e + 6] >> KEY_SHIFT]) continue;
+                    stat.rec.append(x.rec.data() + 8 * e, 8);
+                    stat.st.append(&zero, 1);
+                }
+                seg.push_back(stat.size());
             }
+            stale = false;
         }
+        for (uint64_t e = seg[i]; e < seg[i + 1]; e++) stat.st[e] = 1;
         Image &x = p->parts[i];
         for (uint32_t &s : x.st) s = 1;
         const int st = run_once(p, filter, {i}, &stat, derived, 0, 0);
+        for (uint64_t e = seg[i]; e < seg[i + 1]; e++) stat.st[e] = 0;
         if (st == GRG_E_NOMEM) {
             if (!split(p, i)) return GRG_E_NOMEM;
+            stale = true;
             continue;
         }
         if (st) return st;
