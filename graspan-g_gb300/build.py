@@ -22,7 +22,7 @@ COMP = os.path.join(OUT, "comp")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC, "-I", CSRC]
-# tuning overrides of the join kernel, e.g. GRG_NVCC_DEFS="-DGRG_WIN=4 -DGRG_JOIN_UNROLL=2"
+# tuning overrides of the join kernel, e.g. GRG_NVCC_DEFS="-DGRG_WIN2=16 -DGRG_WIN2_LO=8"
 NVCC_FLAGS += os.environ.get("GRG_NVCC_DEFS", "").split()
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I", INC]
 CUDA_INC = ["-I", os.path.join(os.path.dirname(os.path.dirname(shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")), "include")]

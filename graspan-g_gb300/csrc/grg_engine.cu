@@ -102,9 +102,6 @@ static int make_rule_table(const int *rules, int R, int L, uint32_t filter, Rule
 #ifndef GRG_JOIN_MINB
 #define GRG_JOIN_MINB 6
 #endif
-#ifndef GRG_JOIN_UNROLL
-#define GRG_JOIN_UNROLL 1
-#endif
 #ifdef GRG_PHASE_TIMERS
 #define PH_MARK(i)                                   \
     do {                                             \
@@ -127,7 +124,6 @@ constexpr int WIN_LO = GRG_WIN_LO;
 #endif
 constexpr int WIN2 = GRG_WIN2;    // wide window: rows whose destinations spread over many elements
 constexpr int WIN2_LO = GRG_WIN2_LO;
-constexpr int JOIN_UNROLL = GRG_JOIN_UNROLL;
 constexpr int ACC_LG = GRG_ACC_LG;
 constexpr int ACC = 1 << ACC_LG;  // per-warp hash accumulator entries (candidates outside the window)
 constexpr int ACC_MAX = ACC * 3 / 4;
@@ -889,93 +885,85 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : 4))
                         if (prefix_table(d, C, cnt)) cnt = min(cnt, __ldcg(d.cnt + ti));
                     }
                 }
-                uint32_t incl = cnt;
+                // one right-hand item: a CSR destination id (csr 1), a table element (0) or a
+                // delta record of row C[k] (2), ORed into its record's window or, outside it,
+                // the shared hash. Every lane calls this together (the hash needs the warp).
+                auto do_item = [&](bool valid, uint32_t o_r, uint32_t o_C, uint32_t o_csr, uint32_t item) {
+                    bool ok_i = false, pending = false;
+                    uint32_t b2 = 0, ob = EMPTY, ckey = 0;
+                    Bits ib;
+#pragma unroll
+                    for (int x = 0; x < EW; x++) ib.w[x] = 0;
+                    if (valid) {
+                        if (o_csr == 1) {
+                            const uint32_t dst = __ldg(c_rt.csr_col[o_C] + item);
+                            b2 = dst / EIDS;
+                            ob = dst % EIDS;
+                            ok_i = true;
+                        } else {
+                            const uint4 *ep = o_csr == 2 ? d.drec + 2 * (size_t)item
+                                                         : reinterpret_cast<const uint4 *>(d.elems + (size_t)item * 8);
+                            const uint4 e0 = ep[0], e1 = ep[1];
+                            ok_i = e1.z != EMPTY;
+                            b2 = e1.z & BASE_MASK;
+                            ib.w[0] = e0.x; ib.w[1] = e0.y; ib.w[2] = e0.z; ib.w[3] = e0.w;
+                            ib.w[4] = e1.x; ib.w[5] = e1.y;
+                            n_right += ok_i ? 1 : 0;
+                        }
+                    }
+                    if (ok_i) {
+                        const int dd = (int)b2 - (int)w.rbase[o_r] + WIN_LO;
+                        // the statistic the window choice is keyed on: items beyond the narrow window
+                        n_out += (unsigned)(dd - WIN_LO + grg::WIN_LO) >= (unsigned)grg::WIN;
+                        if ((unsigned)dd < (unsigned)WIN) {
+                            if (ob != EMPTY) {
+                                // one destination id: one word of the window
+                                atomicOr(&w.win[o_r][dd][ob >> 5], 1u << (ob & 31));
+                            } else {
+#pragma unroll
+                                for (int x = 0; x < EW; x++)
+                                    if (ib.w[x]) atomicOr(&w.win[o_r][dd][x], ib.w[x]);
+                            }
+                        } else {
+                            pending = true;
+                            ckey = (o_r << KEY_SHIFT) | b2;
+                            if (ob != EMPTY) {
+#pragma unroll
+                                for (int x = 0; x < EW; x++) ib.w[x] = (uint32_t)x == (ob >> 5) ? 1u << (ob & 31) : 0u;
+                            }
+                        }
+                    }
+                    while (__any_sync(0xffffffffu, pending)) {
+                        if (pending) pending = !acc_insert(w, ckey, ib);
+                        if (__any_sync(0xffffffffu, pending)) acc_flush(d, w, inserts);
+                    }
+                };
+                // first item of every task in the task's own lane: no search, no broadcast
+                do_item(cnt > 0, r, C, csr, beg);
+                // the rest, flattened over the lanes
+                const uint32_t cnt1 = cnt ? cnt - 1 : 0;
+                uint32_t incl = cnt1;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
                     const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
                     if (lane >= (uint32_t)o) incl += y;
                 }
                 const uint32_t nitems = __shfl_sync(0xffffffffu, incl, 31);
-                // per task: item f sits at beg + f - (first f of the task); record, label and source packed
-                const uint32_t adj = beg - (incl - cnt);
+                // per task: item f sits at beg + 1 + f - (first f of the task); record, label and source packed
+                const uint32_t adj = beg + 1 - (incl - cnt1);
                 const uint32_t pk = r | (C << 8) | (csr << 16);
-                // JOIN_UNROLL items per lane per iteration: their loads are issued together
-                for (uint32_t f0 = 0; f0 < nitems; f0 += 32 * JOIN_UNROLL) {
-                    uint32_t it_r[JOIN_UNROLL], it_b2[JOIN_UNROLL];
-                    uint32_t it_ob[JOIN_UNROLL];      // CSR item: its id within the element (one bit); else EMPTY
-                    Bits it_b[JOIN_UNROLL];
-                    bool it_ok[JOIN_UNROLL];
+                for (uint32_t f0 = 0; f0 < nitems; f0 += 32) {
+                    const uint32_t f = f0 + lane;
+                    // owner lane: smallest o with incl(o) > f
+                    uint32_t lo = 0;
 #pragma unroll
-                    for (int u = 0; u < JOIN_UNROLL; u++) {
-                        const uint32_t f = f0 + u * 32 + lane;
-                        // owner lane: smallest o with incl(o) > f
-                        uint32_t lo = 0;
-#pragma unroll
-                        for (int st = 16; st; st >>= 1) {
-                            const uint32_t v = __shfl_sync(0xffffffffu, incl, lo + st - 1);
-                            if (v <= f) lo += st;
-                        }
-                        const uint32_t o_adj = __shfl_sync(0xffffffffu, adj, lo);
-                        const uint32_t o_pk = __shfl_sync(0xffffffffu, pk, lo);
-                        const uint32_t o_r = o_pk & 0xFFu, o_C = (o_pk >> 8) & 0xFFu, o_csr = o_pk >> 16;
-                        it_r[u] = o_r;
-                        it_ok[u] = false;
-                        it_b2[u] = 0;
-                        it_ob[u] = EMPTY;
-#pragma unroll
-                        for (int x = 0; x < EW; x++) it_b[u].w[x] = 0;
-                        if (f < nitems) {
-                            const uint32_t item = f + o_adj;
-                            if (o_csr == 1) {
-                                const uint32_t dst = __ldg(c_rt.csr_col[o_C] + item);
-                                it_b2[u] = dst / EIDS;
-                                it_ob[u] = dst % EIDS;
-                                it_ok[u] = true;
-                            } else {
-                                const uint4 *ep = o_csr == 2 ? d.drec + 2 * (size_t)item
-                                                             : reinterpret_cast<const uint4 *>(d.elems + (size_t)item * 8);
-                                const uint4 e0 = ep[0], e1 = ep[1];
-                                it_ok[u] = e1.z != EMPTY;
-                                it_b2[u] = e1.z & BASE_MASK;
-                                it_b[u].w[0] = e0.x; it_b[u].w[1] = e0.y; it_b[u].w[2] = e0.z; it_b[u].w[3] = e0.w;
-                                it_b[u].w[4] = e1.x; it_b[u].w[5] = e1.y;
-                                n_right += it_ok[u] ? 1 : 0;
-                            }
-                        }
+                    for (int st = 16; st; st >>= 1) {
+                        const uint32_t v = __shfl_sync(0xffffffffu, incl, lo + st - 1);
+                        if (v <= f) lo += st;
                     }
-#pragma unroll
-                    for (int u = 0; u < JOIN_UNROLL; u++) {
-                        bool pending = false;
-                        uint32_t ckey = 0;
-                        if (it_ok[u]) {
-                            const uint32_t o_r = it_r[u];
-                            const int dd = (int)it_b2[u] - (int)w.rbase[o_r] + WIN_LO;
-                            // the statistic the window choice is keyed on: items beyond the narrow window
-                            n_out += (unsigned)(dd - WIN_LO + grg::WIN_LO) >= (unsigned)grg::WIN;
-                            if ((unsigned)dd < (unsigned)WIN) {
-                                if (it_ob[u] != EMPTY) {
-                                    // one destination id: one word of the window
-                                    atomicOr(&w.win[o_r][dd][it_ob[u] >> 5], 1u << (it_ob[u] & 31));
-                                } else {
-#pragma unroll
-                                    for (int x = 0; x < EW; x++)
-                                        if (it_b[u].w[x]) atomicOr(&w.win[o_r][dd][x], it_b[u].w[x]);
-                                }
-                            } else {
-                                pending = true;
-                                ckey = (o_r << KEY_SHIFT) | it_b2[u];
-                                if (it_ob[u] != EMPTY) {
-#pragma unroll
-                                    for (int x = 0; x < EW; x++)
-                                        it_b[u].w[x] = (uint32_t)x == (it_ob[u] >> 5) ? 1u << (it_ob[u] & 31) : 0u;
-                                }
-                            }
-                        }
-                        while (__any_sync(0xffffffffu, pending)) {
-                            if (pending) pending = !acc_insert(w, ckey, it_b[u]);
-                            if (__any_sync(0xffffffffu, pending)) acc_flush(d, w, inserts);
-                        }
-                    }
+                    const uint32_t o_adj = __shfl_sync(0xffffffffu, adj, lo);
+                    const uint32_t o_pk = __shfl_sync(0xffffffffu, pk, lo);
+                    do_item(f < nitems, o_pk & 0xFFu, (o_pk >> 8) & 0xFFu, o_pk >> 16, f + o_adj);
                 }
             }
             PH_MARK(2);
