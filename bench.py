@@ -393,6 +393,7 @@ def main():
                        "closure_edges": total, "rounds": s["rounds"], "parallelism": f"replicas{world}",
                        "l2_flush": "512 MiB write before every timed step", "time_to_fixpoint_ms": ms_max,
                        "closure_ms": statistics.mean(x["closure_ms"] for x in stats),
+                       "gather_ms": statistics.mean(x["gather_ms"] for x in stats),
                        "join_launches": s["join_launches"], "retry_records": s["retry_records"],
                        "grow_rows": s["grow_rows"], "delta_elems": s["delta_elems"],
                        "pool_elems_used": s["pool_elems_used"]},

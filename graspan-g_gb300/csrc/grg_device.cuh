@@ -65,7 +65,9 @@ enum : int {
     C_SPLIT_N = C_LABEL0 + MAX_SLOTS + 5,  // sub-records of a small round (k_split)
     C_JN1 = C_LABEL0 + MAX_SLOTS + 6,   // records the join reads from the gathered buffer this round
     C_JN2 = C_LABEL0 + MAX_SLOTS + 7,   // records the join reads from the virtual-record buffer this round
-    NCTR = C_LABEL0 + MAX_SLOTS + 8
+    C_GT0 = C_LABEL0 + MAX_SLOTS + 8,   // start time of the current gather (kernel timing)
+    C_GNS = C_LABEL0 + MAX_SLOTS + 9,   // gather nanoseconds (kernel timing)
+    NCTR = C_LABEL0 + MAX_SLOTS + 10
 };
 enum : unsigned long long { ERR_POOL = 1, ERR_LOAD = 2, ERR_INTERNAL = 4 };
 

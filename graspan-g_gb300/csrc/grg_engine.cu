@@ -378,28 +378,51 @@ __global__ void k_gather_recs(Dev d, const uint32_t *__restrict__ slots, uint4 *
 {
     if (d.ctr[C_HALT]) return;
     if (n_ctr >= 0) n = d.ctr[n_ctr];
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t s = slots[i];
-        uint4 *b = reinterpret_cast<uint4 *>(d.dbits + s * 8);
-        const uint4 b0 = b[0], b1 = b[1];
-        b[0] = make_uint4(0, 0, 0, 0);
-        reinterpret_cast<uint2 *>(b + 1)[0] = make_uint2(0, 0);
-        if (run_stamp) d.stamp[s] = run_stamp;         // gained bits during this run
-        out[2 * i] = b0;
-        out[2 * i + 1] = b1;
-        const uint32_t lab = b1.z >> KEY_SHIFT, row = b1.w;
-        if (lab <= (uint32_t)MAX_LABELS && c_rt.dindex[lab]) {
-            const size_t ti = (size_t)(lab - 1) * d.V + row;
-            atomicMin(&d.drs[ti], (uint32_t)i);
-            atomicAdd(&d.drc[ti], 1u);
-            atomicOr(&d.dvm[(size_t)(lab - 1) * d.vwords + (row >> 5)], 1u << (row & 31));
+    // GR records per thread per step, their random delta reads issued together
+    constexpr int GR = 4;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i0 < n; i0 += stride * GR) {
+        uint64_t sl[GR];
+        uint4 b0[GR], b1[GR];
+#pragma unroll
+        for (int u = 0; u < GR; u++) {
+            const uint64_t i = i0 + u * stride;
+            sl[u] = i < n ? slots[i] : 0;
         }
-        if (row_job) {
-            // batched jobs: records per job (a job with none has reached its fixpoint)
-            const uint32_t job = row_job[row];
-            const unsigned act = __activemask();
-            const unsigned g = __match_any_sync(act, job);
-            if (job != EMPTY && lane_id() == (uint32_t)(__ffs(g) - 1)) atomicAdd(&job_cnt[job], (uint32_t)__popc(g));
+#pragma unroll
+        for (int u = 0; u < GR; u++) {
+            if (i0 + u * stride < n) {
+                const uint4 *b = reinterpret_cast<const uint4 *>(d.dbits + sl[u] * 8);
+                b0[u] = b[0];
+                b1[u] = b[1];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < GR; u++) {
+            const uint64_t i = i0 + u * stride;
+            if (i >= n) continue;
+            const uint64_t s = sl[u];
+            uint4 *b = reinterpret_cast<uint4 *>(d.dbits + s * 8);
+            // words 0-5 cleared; 6-7 keep the slot's key and row
+            b[0] = make_uint4(0, 0, 0, 0);
+            b[1] = make_uint4(0, 0, b1[u].z, b1[u].w);
+            if (run_stamp) d.stamp[s] = run_stamp;     // gained bits during this run
+            out[2 * i] = b0[u];
+            out[2 * i + 1] = b1[u];
+            const uint32_t lab = b1[u].z >> KEY_SHIFT, row = b1[u].w;
+            if (lab <= (uint32_t)MAX_LABELS && c_rt.dindex[lab]) {
+                const size_t ti = (size_t)(lab - 1) * d.V + row;
+                atomicMin(&d.drs[ti], (uint32_t)i);
+                atomicAdd(&d.drc[ti], 1u);
+                atomicOr(&d.dvm[(size_t)(lab - 1) * d.vwords + (row >> 5)], 1u << (row & 31));
+            }
+            if (row_job) {
+                // batched jobs: records per job (a job with none has reached its fixpoint)
+                const uint32_t job = row_job[row];
+                const unsigned act = __activemask();
+                const unsigned g = __match_any_sync(act, job);
+                if (job != EMPTY && lane_id() == (uint32_t)(__ffs(g) - 1)) atomicAdd(&job_cnt[job], (uint32_t)__popc(g));
+            }
         }
     }
 }
@@ -2200,6 +2223,19 @@ int grg_load_elements(grg_ctx *c, uint32_t num_vars, uint64_t num_elems, const u
 
 }  // extern "C"
 
+// Kernel timing of a phase (join pass, gather): the global nanosecond timer at its start
+// (t0_slot) and the elapsed time added at its end (acc_slot).
+__global__ void k_tmark(unsigned long long *ctr, int t0_slot, int acc_slot, int end)
+{
+    if (threadIdx.x != 0 || ctr[C_HALT]) return;
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (!end)
+        ctr[t0_slot] = t;
+    else
+        ctr[acc_slot] += t - ctr[t0_slot];
+}
+
 // Semi-naive rounds on the host's side: gather the dirty slots of the last
 // round into delta records, join them, insert the candidates, re-run what did
 // not fit after growing its tables. The pieces are separate so a round the
@@ -2235,6 +2271,7 @@ static int round_head(grg_ctx *c, uint32_t rs, grg_stats &S, uint64_t *nd_out)
     uint32_t *ccnt = c->chunk, *coff = c->chunk + nchunks + 1, *csum = c->chunk + 2 * (nchunks + 1);
     const uint64_t nb = (nchunks + 1023) / 1024;
     Dev d = make_dev(c);
+    if (c->timing) k_tmark<<<1, 32, 0, s>>>(c->ctr, C_GT0, C_GNS, 0);
     k_dcount<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, ccnt, 0);
     k_scan_blocks<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(ccnt, coff, csum, nchunks, nullptr);
     k_scan_sums<<<1, 1024, 0, s>>>(csum, nb, nullptr);
@@ -2268,6 +2305,7 @@ static int round_head(grg_ctx *c, uint32_t rs, grg_stats &S, uint64_t *nd_out)
     k_gather_slots<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, coff, c->gslot, 0);
     k_gather_recs<<<grid_for(c, nd, 256), 256, 0, s>>>(d, c->gslot, c->gbuf, nd, -1, c->row_job, c->job_cnt, rs);
     c->launches += 2;
+    if (c->timing) k_tmark<<<1, 32, 0, s>>>(c->ctr, C_GT0, C_GNS, 1);
     return GRG_OK;
 }
 
@@ -2493,17 +2531,6 @@ __global__ void k_gate_end(unsigned long long *ctr, cudaGraphConditionalHandle h
     }
 }
 
-// Join-pass time of device-driven rounds (kernel timing on): global nanosecond timer.
-__global__ void k_tmark(unsigned long long *ctr, int end)
-{
-    if (threadIdx.x != 0 || ctr[C_HALT]) return;
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    if (!end)
-        ctr[C_JT0] = t;
-    else
-        ctr[C_JNS] += t - ctr[C_JT0];
-}
 
 static void free_round_graph(grg_ctx *c)
 {
@@ -2568,6 +2595,10 @@ static int build_round_graph(grg_ctx *c, uint32_t rs)
     cudaMemsetAsync(ctr + C_RETRY_N, 0, 16, s);
     cudaMemsetAsync(ctr + C_CAND_N, 0, 16, s);
     if (c->job_cnt) cudaMemsetAsync(c->job_cnt, 0, (size_t)c->max_jobs * 4, s);
+    if (c->timing) {
+        k_tmark<<<1, 32, 0, s>>>(ctr, C_GT0, C_GNS, 0);
+        nk++;
+    }
     k_dcount<<<grid_for(c, nchunks * 32, 256), 256, 0, s>>>(d, nwords, ccnt, 1);
     k_scan_blocks<<<(unsigned)std::max<uint64_t>(nb, 1), 1024, 0, s>>>(ccnt, coff, csum, nchunks, ctr);
     k_scan_sums<<<1, 1024, 0, s>>>(csum, nb, ctr);
@@ -2579,6 +2610,10 @@ static int build_round_graph(grg_ctx *c, uint32_t rs)
     k_gather_recs<<<grid_for(c, c->gbuf_cap, 256), 256, 0, s>>>(d, c->gslot, c->gbuf, 0, C_DIRTY_N, c->row_job,
                                                                 c->job_cnt, rs);
     nk += 2;
+    if (c->timing) {
+        k_tmark<<<1, 32, 0, s>>>(ctr, C_GT0, C_GNS, 1);
+        nk++;
+    }
     if (c->rt.nol) {
         for (int q = 0; q < c->rt.nol; q++)
             k_oldleft<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)q, c->vbuf, c->vbuf_cap, c->row_job,
@@ -2587,7 +2622,7 @@ static int build_round_graph(grg_ctx *c, uint32_t rs)
         nk += c->rt.nol + 1;
     }
     if (c->timing) {
-        k_tmark<<<1, 32, 0, s>>>(ctr, 0);
+        k_tmark<<<1, 32, 0, s>>>(ctr, C_JT0, C_JNS, 0);
         nk++;
     }
     const int jgrid = grid_for(c, ~0u, JOIN_WARPS, 16);
@@ -2605,7 +2640,7 @@ static int build_round_graph(grg_ctx *c, uint32_t rs)
         nk++;
     }
     if (c->timing) {
-        k_tmark<<<1, 32, 0, s>>>(ctr, 1);
+        k_tmark<<<1, 32, 0, s>>>(ctr, C_JT0, C_JNS, 1);
         nk++;
     }
     k_gate_end<<<1, 32, 0, s>>>(ctr, h);
@@ -2833,6 +2868,7 @@ int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *s
     S.join_launches = joins;
     S.left_elems = c->h_ctr[C_LEFT];
     S.window_out_elems = c->h_ctr[C_WOUT];
+    S.gather_ms = c->h_ctr[C_GNS] * 1e-6;
     S.wide_window = c->join_wide ? 1 : 0;
     S.right_elems = c->h_ctr[C_RIGHT];
     S.out_elems = S.delta_elems;

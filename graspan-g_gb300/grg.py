@@ -50,7 +50,7 @@ class Stats(ctypes.Structure):
         ("pool_elems_cap", ctypes.c_uint64), ("closure_ms", ctypes.c_double), ("join_ms", ctypes.c_double),
         ("join_launches", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
         ("join_phase_cycles", ctypes.c_uint64 * 5), ("window_out_elems", ctypes.c_uint64),
-        ("wide_window", ctypes.c_uint64),
+        ("wide_window", ctypes.c_uint64), ("gather_ms", ctypes.c_double),
     ]
 
     def as_dict(self):

@@ -66,6 +66,7 @@ typedef struct grg_stats {
     uint64_t window_out_elems;     /* right elements beyond the narrow join window (the
                                       statistic the window choice is keyed on) */
     uint64_t wide_window;          /* 1 = the closure ended on the wide join window */
+    double gather_ms;              /* time of the rounds' gathers (when kernel timing is on) */
 } grg_stats;
 
 /* Error text of a status code, and the last detailed message of a context. */
