@@ -27,7 +27,7 @@ NVCC_FLAGS += os.environ.get("GRG_NVCC_DEFS", "").split()
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I", INC]
 CUDA_INC = ["-I", os.path.join(os.path.dirname(os.path.dirname(shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")), "include")]
 
-CU_SOURCES = ["grg_engine.cu"]
+CU_SOURCES = ["grg_engine.cu", "grg_format.cu"]
 CXX_SOURCES = ["grg_parse.cpp", "grg_part.cpp"]
 
 

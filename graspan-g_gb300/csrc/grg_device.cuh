@@ -67,9 +67,12 @@ enum : int {
     C_JN2 = C_LABEL0 + MAX_SLOTS + 7,   // records the join reads from the virtual-record buffer this round
     C_GT0 = C_LABEL0 + MAX_SLOTS + 8,   // start time of the current gather (kernel timing)
     C_GNS = C_LABEL0 + MAX_SLOTS + 9,   // gather nanoseconds (kernel timing)
-    NCTR = C_LABEL0 + MAX_SLOTS + 10
+    C_BADIN = C_LABEL0 + MAX_SLOTS + 10, // input edges refused: ERR_IN_LABEL / ERR_IN_RANGE bits
+    NCTR = C_LABEL0 + MAX_SLOTS + 11
 };
-enum : unsigned long long { ERR_POOL = 1, ERR_LOAD = 2, ERR_INTERNAL = 4 };
+// error bits of C_ERR; ERR_IN_* (in C_BADIN) flag input edges that were refused
+// (label outside 1..L, vertex id outside the graph) and never touched a table
+enum : unsigned long long { ERR_POOL = 1, ERR_LOAD = 2, ERR_INTERNAL = 4, ERR_IN_LABEL = 8, ERR_IN_RANGE = 16 };
 
 struct RuleTable {
     int L;                                   // labels
@@ -165,6 +168,37 @@ __device__ __forceinline__ uint64_t edge_hash(uint32_t l, uint32_t s, uint32_t d
     return splitmix64(splitmix64(((uint64_t)s << 32) | d) ^ ((uint64_t)l * 0x9E3779B97F4A7C15ull));
 }
 
+// OR `b` into the element in pool slot s. With `track`, the bits that were new
+// go to its delta bitmap and its dirty bit is set (both without waiting).
+__device__ __forceinline__ bool g_or_into(const Dev &d, uint32_t s, const Bits b, bool track)
+{
+    uint32_t *e = d.elems + (size_t)s * 8;
+    // words whose candidate bits are all present already need no atomic: bits are
+    // only ever set during a round, so a stale read can only show fewer of them
+    const uint4 c0 = __ldcg(reinterpret_cast<const uint4 *>(e));
+    const uint2 c1 = __ldcg(reinterpret_cast<const uint2 *>(e + 4));
+    const uint32_t cur[EW] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y};
+    Bits nb;
+    uint32_t any = 0;
+#pragma unroll
+    for (int w = 0; w < EW; w++) {
+        nb.w[w] = 0;
+        if (b.w[w] & ~cur[w]) {
+            const uint32_t old = atomicOr(&e[w], b.w[w]);
+            nb.w[w] = b.w[w] & ~old;
+            any |= nb.w[w];
+        }
+    }
+    if (track && any) {
+        uint32_t *db = d.dbits + (size_t)s * 8;
+#pragma unroll
+        for (int w = 0; w < EW; w++)
+            if (nb.w[w]) atomicOr(&db[w], nb.w[w]);
+        atomicOr(&d.dmap[s >> 5], 1u << (s & 31));
+    }
+    return true;
+}
+
 // OR `b` into element (slot, row, base). Returns false when the table is full
 // or absent; the failure is recorded so the table grows before a retry. With
 // `track`, the bits that were new are ORed into the element's delta bitmap and
@@ -205,31 +239,7 @@ __device__ __forceinline__ bool g_insert(const Dev &d, uint32_t slot, uint32_t r
         }
         return false;
     }
-    uint32_t *e = d.elems + (size_t)s * 8;
-    // words whose candidate bits are all present already need no atomic: bits are
-    // only ever set during a round, so a stale read can only show fewer of them
-    const uint4 c0 = __ldcg(reinterpret_cast<const uint4 *>(e));
-    const uint2 c1 = __ldcg(reinterpret_cast<const uint2 *>(e + 4));
-    const uint32_t cur[EW] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y};
-    Bits nb;
-    uint32_t any = 0;
-#pragma unroll
-    for (int w = 0; w < EW; w++) {
-        nb.w[w] = 0;
-        if (b.w[w] & ~cur[w]) {
-            const uint32_t old = atomicOr(&e[w], b.w[w]);
-            nb.w[w] = b.w[w] & ~old;
-            any |= nb.w[w];
-        }
-    }
-    if (track && any) {
-        uint32_t *db = d.dbits + (size_t)s * 8;
-#pragma unroll
-        for (int w = 0; w < EW; w++)
-            if (nb.w[w]) atomicOr(&db[w], nb.w[w]);
-        atomicOr(&d.dmap[s >> 5], 1u << (s & 31));
-    }
-    return true;
+    return g_or_into(d, s, b, track);
 }
 
 }  // namespace grg

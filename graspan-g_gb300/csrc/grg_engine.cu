@@ -25,6 +25,7 @@
 
 #include "grg.h"
 #include "grg_device.cuh"
+#include "grg_format.h"
 
 namespace grg {
 
@@ -153,10 +154,29 @@ __global__ void k_fill_u32(uint32_t *p, uint64_t n, uint32_t v)
         p[i] = v;
 }
 
-__global__ void k_load_hist(Dev d, const uint32_t *src, const uint8_t *lab, uint64_t n, uint32_t base)
+// Input edges are checked where they are first read: a label outside 1..L or a
+// vertex id outside [0, nv) is flagged and skipped here and in k_load_insert.
+__device__ __forceinline__ bool edge_ok(Dev d, uint32_t s, uint32_t t, uint32_t l, uint32_t nv, uint32_t L, bool flag)
 {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        atomicAdd(&d.cnt[(size_t)(lab[i] - 1) * d.V + base + src[i]], 1u);
+    if (l - 1u >= L) {
+        if (flag) atomicOr(&d.ctr[C_BADIN], (unsigned long long)ERR_IN_LABEL);
+        return false;
+    }
+    if (s >= nv || t >= nv) {
+        if (flag) atomicOr(&d.ctr[C_BADIN], (unsigned long long)ERR_IN_RANGE);
+        return false;
+    }
+    return true;
+}
+
+__global__ void k_load_hist(Dev d, const uint32_t *src, const uint32_t *dst, const uint8_t *lab, uint64_t n,
+                            uint32_t base, uint32_t nv, uint32_t L)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t s = src[i], l = lab[i];
+        if (!edge_ok(d, s, dst[i], l, nv, L, true)) continue;
+        atomicAdd(&d.cnt[(size_t)(l - 1) * d.V + base + s], 1u);
+    }
 }
 
 __global__ void k_eps_hist(Dev d, uint32_t slot, uint32_t first, uint32_t nv)
@@ -208,9 +228,10 @@ __global__ void k_load_alloc(Dev d, uint32_t first, uint32_t nv, uint32_t L, Min
 }
 
 __global__ void k_load_insert(Dev d, const uint32_t *src, const uint32_t *dst, const uint8_t *lab, uint64_t n,
-                              uint32_t vbase)
+                              uint32_t vbase, uint32_t nv, uint32_t L)
 {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (!edge_ok(d, src[i], dst[i], lab[i], nv, L, false)) continue;
         const uint32_t v = vbase + dst[i];
         Bits b;
         const uint32_t o = v % EIDS;
@@ -1672,6 +1693,28 @@ int read_ctr(grg_ctx *c)
     return GRG_OK;
 }
 
+// Device staging of num_edges input edges (src and dst in d_in32, labels in d_in8).
+static int ensure_input(grg_ctx *c, uint64_t num_edges)
+{
+    if (c->in_cap >= num_edges) return GRG_OK;
+    cudaFree(c->d_in32); cudaFree(c->d_in8);
+    c->d_in32 = nullptr; c->d_in8 = nullptr;
+    c->in_cap = 0;
+    GRG_CUDA(c, cudaMalloc(&c->d_in32, num_edges * 8));
+    GRG_CUDA(c, cudaMalloc(&c->d_in8, num_edges));
+    c->in_cap = num_edges;
+    return GRG_OK;
+}
+
+// Status for input edges the load kernels refused (counters already read).
+int input_status(grg_ctx *c)
+{
+    const unsigned long long b = c->h_ctr[C_BADIN];
+    if (b & ERR_IN_LABEL) return fail(c, GRG_E_LABEL, "edge label outside 1..numLabels");
+    if (b & ERR_IN_RANGE) return fail(c, GRG_E_RANGE, "edge vertex id >= numVars");
+    return GRG_OK;
+}
+
 
 constexpr uint64_t POOL_BYTES_PER_SLOT = 32 + 32 + 1;
 constexpr uint32_t DERIVED_MIN_CAP = 16;   // element, delta bitmap, dirty bit (rounded up)
@@ -2092,14 +2135,8 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
     const uint32_t *dsrc = src, *ddst = dst;
     const uint8_t *dlab = label;
     if (!on_device && num_edges) {
-        if (c->in_cap < num_edges) {
-            cudaFree(c->d_in32); cudaFree(c->d_in8);
-            c->d_in32 = nullptr; c->d_in8 = nullptr;
-            c->in_cap = 0;
-            GRG_CUDA(c, cudaMalloc(&c->d_in32, num_edges * 8));
-            GRG_CUDA(c, cudaMalloc(&c->d_in8, num_edges));
-            c->in_cap = num_edges;
-        }
+        st = ensure_input(c, num_edges);
+        if (st) return st;
         GRG_CUDA(c, cudaMemcpyAsync(c->d_in32, src, num_edges * 4, cudaMemcpyHostToDevice, s));
         GRG_CUDA(c, cudaMemcpyAsync(c->d_in32 + num_edges, dst, num_edges * 4, cudaMemcpyHostToDevice, s));
         GRG_CUDA(c, cudaMemcpyAsync(c->d_in8, label, num_edges, cudaMemcpyHostToDevice, s));
@@ -2110,7 +2147,7 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
     c->launches = 0;
     auto hist = [&](Dev d) {
         if (num_edges) {
-            k_load_hist<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, dlab, num_edges, 0);
+            k_load_hist<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges, 0, num_vars, (uint32_t)c->L);
             c->launches++;
         }
         for (int q = 0; q < c->R; q++)
@@ -2139,9 +2176,10 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
     uint64_t top = 0;
     st = alloc_tables(c, derived_min_cap(c), hist, &top);
     if (st) return st;
+    if ((st = input_status(c))) return st;
     Dev d = make_dev(c);
     if (num_edges) {
-        k_load_insert<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges, 0);
+        k_load_insert<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges, 0, num_vars, (uint32_t)c->L);
         c->launches++;
     }
     for (int q = 0; q < c->R; q++)
@@ -2971,6 +3009,8 @@ int grg_export_edges(grg_ctx *c, uint64_t cap, uint32_t *src, uint32_t *dst, uin
     return GRG_OK;
 }
 
+static int stage_elements(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t *n_out);
+
 int grg_export_elements(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t cap, uint32_t *elems,
                         uint32_t *stamps, uint64_t *num_out)
 {
@@ -2981,14 +3021,36 @@ int grg_export_elements(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t c
     cudaStream_t s = c->stream;
     Dev d = make_dev(c);
     const uint64_t ntab = (uint64_t)c->L * (v_end - v_begin);
-    // count, then write into a staging buffer of exactly that size
+    // count first: nothing is staged when the caller's buffer is too small
+    GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_EXPORT, 0, 8, s));
+    if (ntab) k_export_elems<<<grid_for(c, ntab * 32, 256), 256, 0, s>>>(d, v_begin, v_end, (uint32_t)c->L, nullptr, nullptr, 0);
+    int st = read_ctr(c);
+    if (st) return st;
+    uint64_t n = c->h_ctr[C_EXPORT];
+    if (num_out) *num_out = n;
+    if (n > cap) return fail(c, GRG_E_RANGE, "export buffer too small");
+    if (!n) return GRG_OK;
+    if ((st = stage_elements(c, v_begin, v_end, &n))) return st;
+    GRG_CUDA(c, cudaMemcpyAsync(elems, c->xbuf, n * 32, cudaMemcpyDeviceToHost, s));
+    GRG_CUDA(c, cudaMemcpyAsync(stamps, c->xst, n * 4, cudaMemcpyDeviceToHost, s));
+    GRG_CUDA(c, cudaStreamSynchronize(s));
+    GRG_CUDA(c, cudaGetLastError());
+    return GRG_OK;
+}
+
+// Records of rows [v_begin, v_end) into the staging buffer xbuf (8 words each,
+// any order; stamps into xst). *n = their number.
+static int stage_elements(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t *n_out)
+{
+    cudaStream_t s = c->stream;
+    Dev d = make_dev(c);
+    const uint64_t ntab = (uint64_t)c->L * (v_end - v_begin);
     GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_EXPORT, 0, 8, s));
     if (ntab) k_export_elems<<<grid_for(c, ntab * 32, 256), 256, 0, s>>>(d, v_begin, v_end, (uint32_t)c->L, nullptr, nullptr, 0);
     int st = read_ctr(c);
     if (st) return st;
     const uint64_t n = c->h_ctr[C_EXPORT];
-    if (num_out) *num_out = n;
-    if (n > cap) return fail(c, GRG_E_RANGE, "export buffer too small");
+    *n_out = n;
     if (!n) return GRG_OK;
     if (c->xcap < n) {
         cudaFree(c->xbuf); cudaFree(c->xst);
@@ -3001,11 +3063,84 @@ int grg_export_elements(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t c
     }
     GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_EXPORT, 0, 8, s));
     k_export_elems<<<grid_for(c, ntab * 32, 256), 256, 0, s>>>(d, v_begin, v_end, (uint32_t)c->L, c->xbuf, c->xst, n);
-    GRG_CUDA(c, cudaMemcpyAsync(elems, c->xbuf, n * 32, cudaMemcpyDeviceToHost, s));
-    GRG_CUDA(c, cudaMemcpyAsync(stamps, c->xst, n * 4, cudaMemcpyDeviceToHost, s));
-    GRG_CUDA(c, cudaStreamSynchronize(s));
     GRG_CUDA(c, cudaGetLastError());
     return GRG_OK;
+}
+
+
+int grg_export_csr5(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t cap, uint8_t *edges, uint32_t *degree,
+                    uint64_t *num_edges)
+{
+    if (!c || v_begin > v_end || !num_edges || (cap && (!edges || !degree))) return GRG_E_ARG;
+    if (!c->loaded) return fail(c, GRG_E_STATE, "no graph loaded");
+    if (v_end > c->V) return fail(c, GRG_E_RANGE, "vertex range beyond the graph");
+    cudaSetDevice(c->device);
+    // the stream's length is the range's popcount
+    std::vector<uint64_t> counts(c->L + 1, 0);
+    uint64_t h = 0, total = 0;
+    int st = grg_range_counts(c, v_begin, v_end, counts.data(), &h);
+    if (st) return st;
+    for (int l = 0; l < c->L; l++) total += counts[l];
+    *num_edges = total;
+    if (total > cap) return total ? fail(c, GRG_E_RANGE, "stream buffer too small") : GRG_OK;
+    const uint32_t nrows = v_end - v_begin;
+    if (!nrows) return GRG_OK;
+    uint64_t n = 0;
+    if ((st = stage_elements(c, v_begin, v_end, &n))) return st;
+    uint8_t *dbytes = nullptr;
+    uint32_t *ddeg = nullptr;
+    cudaError_t e = cudaMalloc(&ddeg, (size_t)nrows * 4);
+    if (e == cudaSuccess && total) e = cudaMalloc(&dbytes, total * 5);
+    if (e == cudaSuccess) e = grg_fmt_records_to_csr5(c->xbuf, n, v_begin, nrows, total, dbytes, ddeg, c->stream);
+    if (e == cudaSuccess && total) e = cudaMemcpy(edges, dbytes, total * 5, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(degree, ddeg, (size_t)nrows * 4, cudaMemcpyDeviceToHost);
+    cudaFree(dbytes);
+    cudaFree(ddeg);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, e == cudaErrorMemoryAllocation ? GRG_E_NOMEM : GRG_E_CUDA,
+                    std::string("compressed export: ") + cudaGetErrorString(e));
+    }
+    return GRG_OK;
+}
+
+int grg_load_csr5(grg_ctx *c, uint32_t num_vars, uint32_t v_begin, uint32_t v_end, const uint32_t *degree,
+                  uint64_t num_edges, const uint8_t *edges, int on_device)
+{
+    if (!c || v_begin > v_end || (v_end > v_begin && !degree) || (num_edges && !edges)) return GRG_E_ARG;
+    if (!c->have_rules) return fail(c, GRG_E_STATE, "grg_transfer_rules must come first");
+    if (v_end > num_vars) return fail(c, GRG_E_RANGE, "vertex range beyond numVars");
+    cudaSetDevice(c->device);
+    const uint32_t nrows = v_end - v_begin;
+    if (num_edges && !nrows) return fail(c, GRG_E_ARG, "edges without rows");
+    int st = ensure_input(c, num_edges);
+    if (st) return st;
+    const uint8_t *dbytes = edges;
+    const uint32_t *ddeg = degree;
+    uint8_t *sbytes = nullptr;
+    uint32_t *sdeg = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (!on_device) {
+        if (num_edges) e = cudaMalloc(&sbytes, num_edges * 5);
+        if (e == cudaSuccess && nrows) e = cudaMalloc(&sdeg, (size_t)nrows * 4);
+        if (e == cudaSuccess && num_edges) e = cudaMemcpyAsync(sbytes, edges, num_edges * 5, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess && nrows) e = cudaMemcpyAsync(sdeg, degree, (size_t)nrows * 4, cudaMemcpyHostToDevice, c->stream);
+        dbytes = sbytes;
+        ddeg = sdeg;
+    }
+    uint64_t sum = 0;
+    if (e == cudaSuccess)
+        e = grg_fmt_csr5_to_edges(dbytes, num_edges, ddeg, v_begin, nrows, c->d_in32, c->d_in32 + num_edges, c->d_in8,
+                                  &sum, c->stream);
+    cudaFree(sbytes);
+    cudaFree(sdeg);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, e == cudaErrorMemoryAllocation ? GRG_E_NOMEM : GRG_E_CUDA,
+                    std::string("compressed load: ") + cudaGetErrorString(e));
+    }
+    if (sum != num_edges) return fail(c, GRG_E_ARG, "row lengths do not add up to num_edges");
+    return grg_load_edges(c, num_vars, num_edges, c->d_in32, c->d_in32 + num_edges, c->d_in8, 1);
 }
 
 int grg_range_counts(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t *counts, uint64_t *hash)
@@ -3141,13 +3276,8 @@ int grg_batch_admit(grg_ctx *c, uint32_t job, uint32_t base, uint32_t num_vars, 
     const uint32_t *dsrc = src, *ddst = dst;
     const uint8_t *dlab = label;
     if (!on_device && num_edges) {
-        if (c->in_cap < num_edges) {
-            cudaFree(c->d_in32); cudaFree(c->d_in8);
-            c->d_in32 = nullptr; c->d_in8 = nullptr;
-            GRG_CUDA(c, cudaMalloc(&c->d_in32, num_edges * 8));
-            GRG_CUDA(c, cudaMalloc(&c->d_in8, num_edges));
-            c->in_cap = num_edges;
-        }
+        const int se = ensure_input(c, num_edges);
+        if (se) return se;
         GRG_CUDA(c, cudaMemcpyAsync(c->d_in32, src, num_edges * 4, cudaMemcpyHostToDevice, s));
         GRG_CUDA(c, cudaMemcpyAsync(c->d_in32 + num_edges, dst, num_edges * 4, cudaMemcpyHostToDevice, s));
         GRG_CUDA(c, cudaMemcpyAsync(c->d_in8, label, num_edges, cudaMemcpyHostToDevice, s));
@@ -3194,17 +3324,30 @@ int grg_batch_admit(grg_ctx *c, uint32_t job, uint32_t base, uint32_t num_vars, 
     c->h_ctr[C_POOL_TOP] = top0;
     GRG_CUDA(c, cudaMemcpyAsync(c->ctr + C_POOL_TOP, c->h_ctr + C_POOL_TOP, 8, cudaMemcpyHostToDevice, s));
     GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_ERR, 0, 8, s));
+    GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_BADIN, 0, 8, s));
     Dev d = make_dev(c);
-    if (num_edges) k_load_hist<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, dlab, num_edges, base);
+    if (num_edges) k_load_hist<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges, base, num_vars, (uint32_t)c->L);
     for (int l = 1; l <= c->L; l++)
         if ((eps_mask >> (l - 1)) & 1ull) k_eps_hist<<<grid_for(c, num_vars, 256), 256, 0, s>>>(d, (uint32_t)l, base, num_vars);
     k_load_alloc<<<grid_for(c, (uint64_t)c->L * num_vars, 256), 256, 0, s>>>(d, base, num_vars, (uint32_t)c->L, mc);
     st = read_ctr(c);
     if (st) return st;
+    if (c->h_ctr[C_BADIN]) {
+        // refused input: the job's tables are given back (rows cleared as a release clears them)
+        for (int slot = 1; slot <= c->L; slot++) {
+            const size_t t0 = (size_t)(slot - 1) * c->V + base;
+            GRG_CUDA(c, cudaMemsetAsync(c->desc + t0, 0, (size_t)num_vars * 8, s));
+            GRG_CUDA(c, cudaMemsetAsync(c->cnt + t0, 0, (size_t)num_vars * 4, s));
+        }
+        c->h_ctr[C_POOL_TOP] = top0;
+        GRG_CUDA(c, cudaMemcpyAsync(c->ctr + C_POOL_TOP, c->h_ctr + C_POOL_TOP, 8, cudaMemcpyHostToDevice, s));
+        GRG_CUDA(c, cudaStreamSynchronize(s));
+        return input_status(c);
+    }
     if (c->h_ctr[C_ERR] & ERR_POOL) return fail(c, GRG_E_NOMEM, "element pool too small for the job");
     const uint64_t top1 = c->h_ctr[C_POOL_TOP];
     if (top1 > top0) k_init_region<<<grid_for(c, top1 - top0, 256), 256, 0, s>>>(c->elems, c->dbits, nullptr, top0, top1);
-    if (num_edges) k_load_insert<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges, base);
+    if (num_edges) k_load_insert<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges, base, num_vars, (uint32_t)c->L);
     for (int l = 1; l <= c->L; l++)
         if ((eps_mask >> (l - 1)) & 1ull) k_eps_insert<<<grid_for(c, num_vars, 256), 256, 0, s>>>(d, (uint32_t)l, base, num_vars);
     // rows of labels that no active rule derives are packed (as grg_closure does)
@@ -3451,17 +3594,19 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
 
     // load (grg_load_edges)
     const uint64_t nlab = (uint64_t)num_labels * num_vars;
-    if (num_edges) k_load_hist<<<grid(num_edges, 256, 8), 256, 0, s>>>(d, d_src, d_label, num_edges, 0);
+    if (num_edges) k_load_hist<<<grid(num_edges, 256, 8), 256, 0, s>>>(d, d_src, d_dst, d_label, num_edges, 0, num_vars, (uint32_t)num_labels);
     for (int q = 0; q < num_rules; q++)
         if (rules[3 * q + 1] == 0) k_eps_hist<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)rules[3 * q], 0, num_vars);
     MinCap mc;
     memset(&mc, 0, sizeof mc);
     k_load_alloc<<<grid(nlab, 256, 8), 256, 0, s>>>(d, 0, num_vars, (uint32_t)num_labels, mc);
     if ((st = na_read(h, d.ctr, s))) return st;
+    if (h[C_BADIN] & ERR_IN_LABEL) return GRG_E_LABEL;
+    if (h[C_BADIN] & ERR_IN_RANGE) return GRG_E_RANGE;
     if (h[C_ERR] & ERR_POOL) return GRG_E_NOMEM;
     const uint64_t top0 = h[C_POOL_TOP];
     if (top0) k_init_region<<<grid(top0, 256, 8), 256, 0, s>>>(d.elems, d.dbits, nullptr, 0, top0);
-    if (num_edges) k_load_insert<<<grid(num_edges, 256, 8), 256, 0, s>>>(d, d_src, d_dst, d_label, num_edges, 0);
+    if (num_edges) k_load_insert<<<grid(num_edges, 256, 8), 256, 0, s>>>(d, d_src, d_dst, d_label, num_edges, 0, num_vars, (uint32_t)num_labels);
     for (int q = 0; q < num_rules; q++)
         if (rules[3 * q + 1] == 0) k_eps_insert<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)rules[3 * q], 0, num_vars);
     for (int l = 1; l <= num_labels; l++)

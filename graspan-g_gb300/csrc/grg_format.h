@@ -1,0 +1,27 @@
+// grg_format.h -- device conversions between element records and the
+// reference's compressed edge stream (5 bytes per edge: little-endian uint32
+// destination, then the uint8 label id; rows back to back, each row's edges by
+// label, then destination). Internal to libgrg: the C ABI entry points are
+// grg_export_csr5 / grg_load_csr5 in grg_engine.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+// Stream of the n element records rec (8 words each: bitmap words 0-5, word 6 =
+// label << 25 | base, word 7 = source row; any order) whose rows lie in
+// [v_begin, v_begin + nrows). Writes the stream (total_edges x 5 bytes) to
+// out_bytes and each row's edge count to degree (nrows entries, device memory).
+// total_edges must be the records' popcount (cudaErrorInvalidValue, nothing
+// written, otherwise). Temporary device memory is
+// allocated and freed here; the call returns when the stream is complete.
+cudaError_t grg_fmt_records_to_csr5(const uint4 *rec, uint64_t n, uint32_t v_begin, uint32_t nrows,
+                                    uint64_t total_edges, uint8_t *out_bytes, uint32_t *degree, cudaStream_t s);
+
+// Expands a stream of num_edges edges for rows [v_begin, v_begin + nrows) with
+// row lengths degree (device) into edge arrays src/dst/label (device, num_edges
+// each). Sets *sum to the sum of degree, so the caller can refuse a stream whose
+// lengths do not add up (nothing is expanded then). Returns after the expansion.
+cudaError_t grg_fmt_csr5_to_edges(const uint8_t *bytes, uint64_t num_edges, const uint32_t *degree, uint32_t v_begin,
+                                  uint32_t nrows, uint32_t *src, uint32_t *dst, uint8_t *label, uint64_t *sum,
+                                  cudaStream_t s);

@@ -32,7 +32,7 @@ EXPORTS = (
     "grg_batch_step", "grg_batch_result", "grg_batch_release", "grg_get_rules", "grg_closure_ex",
     "grg_load_elements", "grg_export_elements", "grg_range_counts", "grg_set_pool_limit", "grg_part_create",
     "grg_part_destroy", "grg_part_load_edges", "grg_part_run", "grg_part_label_counts", "grg_part_bounds",
-    "grg_set_device_rounds", "grg_range_reach", "grg_set_join_window",
+    "grg_set_device_rounds", "grg_range_reach", "grg_set_join_window", "grg_export_csr5", "grg_load_csr5",
 )
 
 
@@ -123,6 +123,8 @@ def load_library(path: str = LIB_PATH):
     L.grg_range_counts.argtypes = [P, U32, U32, P, ctypes.POINTER(U64)]
     L.grg_set_pool_limit.argtypes = [P, U64]
     L.grg_range_reach.argtypes = [P, U32, U32, U64, U32, P, P]
+    L.grg_export_csr5.argtypes = [P, U32, U32, U64, P, P, ctypes.POINTER(U64)]
+    L.grg_load_csr5.argtypes = [P, U32, U32, U32, P, U64, P, ctypes.c_int]
     L.grg_part_create.argtypes = [ctypes.POINTER(P), P, U32, U32]
     L.grg_part_destroy.argtypes = [P]
     L.grg_part_destroy.restype = None
@@ -327,6 +329,31 @@ class Context:
         self._check(self._L.grg_export_elements(self._h, v_begin, v_end, n.value, _ptr(recs), _ptr(stamps),
                                                 ctypes.byref(n)), "export_elements")
         return recs, stamps
+
+    def export_csr5(self, v_begin=0, v_end=None):
+        """Rows [v_begin, v_end) as the compressed edge stream: (uint8 array of
+        5 bytes per edge, uint32 edges per source vertex)."""
+        if v_end is None:
+            v_end = self.num_vars
+        n = ctypes.c_uint64()
+        st = self._L.grg_export_csr5(self._h, v_begin, v_end, 0, None, None, ctypes.byref(n))
+        if st not in (OK, E_RANGE):
+            self._check(st, "export_csr5")
+        out = np.zeros(n.value * 5, np.uint8)
+        deg = np.zeros(v_end - v_begin, np.uint32)
+        self._check(self._L.grg_export_csr5(self._h, v_begin, v_end, n.value, _ptr(out), _ptr(deg),
+                                            ctypes.byref(n)), "export_csr5")
+        return out, deg
+
+    def load_csr5(self, num_vars, stream, degree, v_begin=0):
+        """Load a graph from a compressed edge stream whose rows start at v_begin."""
+        stream = np.ascontiguousarray(stream, dtype=np.uint8)
+        degree = np.ascontiguousarray(degree, dtype=np.uint32)
+        if stream.size % 5:
+            raise ValueError("stream length is not a multiple of 5 bytes")
+        self._check(self._L.grg_load_csr5(self._h, num_vars, v_begin, v_begin + len(degree), _ptr(degree),
+                                          stream.size // 5, _ptr(stream), 0), "load_csr5")
+        self.num_vars = num_vars
 
     def range_reach(self, v_begin, v_end, label_mask, bounds):
         bounds = np.ascontiguousarray(bounds, dtype=np.uint32)

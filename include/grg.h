@@ -191,6 +191,31 @@ int grg_range_reach(grg_ctx *ctx, uint32_t v_begin, uint32_t v_end, uint64_t lab
  * A pool already larger is freed (the loaded graph is dropped). */
 int grg_set_pool_limit(grg_ctx *ctx, uint64_t pool_bytes);
 
+/* ---- The reference's compressed edge stream: its CSR spill format
+ * (COMPRESSED=1), written by storeElements_c / elements2Edges
+ * (src/main.cpp:510-596) and read by readElements_c / edges2Elements
+ * (src/main.cpp:335-445, 364-445). For each source vertex in order, for each
+ * label 1..L, the vertex's destinations ascending, 5 bytes per edge: the
+ * destination as a little-endian uint32, then the label id (uint8). The row
+ * lengths (edges per source vertex) travel beside it, as the reference keeps
+ * them in degree[] (src/main.cpp:541-548). */
+
+/* Rows [v_begin, v_end) of the loaded graph into HOST buffers: edges (cap x 5
+ * bytes) and degree (v_end - v_begin values). *num_edges = the stream's length
+ * in edges; GRG_E_RANGE (nothing written) when that exceeds cap, so cap = 0
+ * asks for the size. Converted on the device (records sorted by row, label,
+ * base). */
+int grg_export_csr5(grg_ctx *ctx, uint32_t v_begin, uint32_t v_end, uint64_t cap, uint8_t *edges,
+                    uint32_t *degree, uint64_t *num_edges);
+/* Load a graph over [0, num_vars) from a stream of num_edges edges whose source
+ * rows are [v_begin, v_end) with row lengths degree (v_end - v_begin values);
+ * expanded on the device, then loaded as grg_load_edges loads edges (epsilon
+ * rules applied, duplicates collapse). Lengths that do not add up to num_edges
+ * fail with GRG_E_ARG, labels outside 1..L with GRG_E_LABEL, destinations >=
+ * num_vars with GRG_E_RANGE. on_device as for grg_load_edges (both arrays). */
+int grg_load_csr5(grg_ctx *ctx, uint32_t num_vars, uint32_t v_begin, uint32_t v_end, const uint32_t *degree,
+                  uint64_t num_edges, const uint8_t *edges, int on_device);
+
 /* ---- Out-of-core closure over vertex-range partitions (host scheduler on
  * the calls above). Replaces the reference's partitioned driver: partition
  * set-up (src/main.cpp:141-175), precomputation / run_computation supersteps

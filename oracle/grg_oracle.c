@@ -679,3 +679,49 @@ uint64_t oracle_export(const oracle_result *r, uint32_t *src, uint32_t *dst, uin
 }
 
 uint64_t oracle_edge_hash(uint32_t l, uint32_t s, uint32_t d) { return edge_hash(l, s, d); }
+
+/*
+ * Closure edges of source rows [v_begin, v_end) in the reference's compressed
+ * spill format: elements2Edges (src/main.cpp:510-539) as storeElements_c
+ * (src/main.cpp:541-596) lays it out. For each source vertex in order, for
+ * each label 1..L, the row's elements in base order and each element's ids
+ * ascending: 5 bytes per edge, the destination as a little-endian uint32, then
+ * the label id. degree[v - v_begin] = the vertex's edge count, the row lengths
+ * readElements_c (src/main.cpp:364-372) reads the stream back with. Returns the
+ * number of edges; writes at most cap of them (degree always in full).
+ */
+uint64_t oracle_export_csr5(const oracle_result *r, uint32_t v_begin, uint32_t v_end, uint8_t *out,
+                            uint32_t *degree, uint64_t cap)
+{
+    uint64_t n = 0;
+    for (uint32_t i = v_begin; i < v_end && i < r->V; i++) {
+        uint32_t deg = 0;
+        for (int A = 1; A <= r->L; A++) {
+            const orow *o = &r->O[(size_t)(A - 1) * r->V + i];
+            for (uint32_t x = 0; x < o->n; x++) {
+                const oelem *el = &o->e[x];
+                for (int w = 0; w < EW; w++) {
+                    uint32_t b = el->bits[w];
+                    while (b) {
+                        const int bit = __builtin_ctz(b);
+                        b &= b - 1;
+                        if (n < cap && out) {
+                            const uint32_t dst = el->base * EIDS + (uint32_t)w * 32 + (uint32_t)bit;
+                            uint8_t *q = out + n * 5;
+                            q[0] = (uint8_t)dst;
+                            q[1] = (uint8_t)(dst >> 8);
+                            q[2] = (uint8_t)(dst >> 16);
+                            q[3] = (uint8_t)(dst >> 24);
+                            q[4] = (uint8_t)A;
+                        }
+                        n++;
+                        deg++;
+                    }
+                }
+            }
+        }
+        if (degree) degree[i - v_begin] = deg;
+    }
+    return n;
+}
+

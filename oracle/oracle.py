@@ -74,6 +74,8 @@ def lib():
         L.oracle_degree.argtypes = [P, P, P]
         L.oracle_export.restype = ctypes.c_uint64
         L.oracle_export.argtypes = [P, P, P, P, ctypes.c_uint64]
+        L.oracle_export_csr5.restype = ctypes.c_uint64
+        L.oracle_export_csr5.argtypes = [P, ctypes.c_uint32, ctypes.c_uint32, P, P, ctypes.c_uint64]
         L.oracle_free.argtypes = [P]
         L.oracle_edge_hash.restype = ctypes.c_uint64
         L.oracle_edge_hash.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32]
@@ -178,6 +180,17 @@ class ClosureResult:
         lab = np.zeros(n, dtype=np.uint8)
         lib().oracle_export(self._h, _ptr(src), _ptr(dst), _ptr(lab), n)
         return src, dst, lab
+
+    def csr5(self, v_begin: int = 0, v_end: int | None = None):
+        """Rows [v_begin, v_end) in the compressed spill format: (uint8 stream of
+        5 bytes per edge, uint32 edge count per vertex)."""
+        if v_end is None:
+            v_end = self.num_vars
+        deg = np.zeros(max(v_end - v_begin, 0), dtype=np.uint32)
+        n = int(lib().oracle_export_csr5(self._h, v_begin, v_end, None, _ptr(deg), 0))
+        out = np.zeros(n * 5, dtype=np.uint8)
+        lib().oracle_export_csr5(self._h, v_begin, v_end, _ptr(out), _ptr(deg), n)
+        return out, deg
 
 
 class OracleError(RuntimeError):

@@ -83,3 +83,35 @@ def test_plain_and_served_agree(grg_mod):
     assert [r[1] for r in p["results"]] == [j.counts for j in jobs]
     assert [r[2] for r in p["results"]] == [j.hash for j in jobs]
     assert res["total_edges"] == p["total_edges"]
+
+
+def test_refused_admission_leaves_the_batch_usable(grg_mod, oracle_mod):
+    # a job with an edge label outside the union grammar, or a vertex id beyond its
+    # range, is refused; its slot and range are admitted again with valid edges
+    jobs = small_jobs(n=2, seed=29)
+    ctx = grg_mod.Context(0)
+    ctx.allocate_pool(0)
+    b = grg_mod.Batch(ctx, sum(j.num_vars for j in jobs) + 10, 4, serve.GRAMMARS, 0)
+    j = jobs[0]
+    lab = np.asarray(j.lab, np.int64).copy()
+    lab[3] = 200 - b.offsets[j.grammar]          # label id 200 > every union label
+    with pytest.raises(grg_mod.GrgError) as ei:
+        b.admit(0, 0, j.grammar, j.num_vars, j.src, j.dst, lab)
+    assert ei.value.status == grg_mod.E_LABEL
+    dst = np.asarray(j.dst, np.uint32).copy()
+    dst[4] = j.num_vars
+    with pytest.raises(grg_mod.GrgError) as ei:
+        b.admit(0, 0, j.grammar, j.num_vars, j.src, dst, j.lab)
+    assert ei.value.status == grg_mod.E_RANGE
+    base = 0
+    for k, jj in enumerate(jobs):
+        b.admit(k, base, jj.grammar, jj.num_vars, jj.src, jj.dst, jj.lab)
+        base += jj.num_vars
+    for _ in range(10000):
+        rec, n = b.step(8)
+        if n == 0 and not rec.any():
+            break
+    for k, jj in enumerate(jobs):
+        counts, h = b.result(k, jj.grammar)
+        assert ([int(x) for x in counts], h) == alone(oracle_mod, jj)
+    ctx.close()

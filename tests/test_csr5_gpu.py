@@ -1,0 +1,154 @@
+"""GPU tests of the compressed edge stream (grg_export_csr5 / grg_load_csr5)
+and of the refusal of invalid input edges by every load path. Byte work, so
+every comparison is bit-exact against the oracle's writer."""
+import numpy as np
+import pytest
+
+import grg_gen as G
+from test_csr5 import pack_csr5, unpack_csr5
+
+pytestmark = pytest.mark.gpu
+
+WORKLOADS = [
+    ("pointsto", lambda: G.pointsto(seed=41, num_vars=900, num_edges=2500), 0),
+    ("dataflow", lambda: G.dataflow_blocks(seed=42, num_blocks=4, block=500, num_edges=6000), 1),
+    ("alias", lambda: G.alias(seed=43, num_vars=3000, num_base_edges=7000, block=500), 0),
+]
+
+
+def closed_context(grg, w, f):
+    ctx = grg.Context(0)
+    ctx.transfer_rules(w.rule_ids(), w.num_labels)
+    ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
+    ctx.closure(f)
+    return ctx
+
+
+@pytest.mark.parametrize("name,make,f", WORKLOADS, ids=[x[0] for x in WORKLOADS])
+def test_export_matches_oracle_stream(grg_mod, oracle_mod, name, make, f):
+    w = make()
+    r = oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, f, w.src, w.dst, w.lab)
+    ctx = closed_context(grg_mod, w, f)
+    V = w.num_vars
+    for lo, hi in [(0, V), (0, 1), (V // 4, V // 2), (V - 1, V), (7, 7)]:
+        got, deg = ctx.export_csr5(lo, hi)
+        want, wdeg = r.csr5(lo, hi)
+        assert len(got) == len(want), (lo, hi)
+        assert np.array_equal(got, want), (lo, hi)
+        assert np.array_equal(deg, wdeg), (lo, hi)
+    ctx.close()
+
+
+def test_random_grammars_export(grg_mod, oracle_mod):
+    for seed in range(6):
+        w = G.random_grammar_graph(500 + seed, num_vars=200 + 37 * seed, num_edges=500 + 60 * seed,
+                                   num_labels=3 + seed % 4, num_rules=3 + seed % 5)
+        r = oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, 0, w.src, w.dst, w.lab)
+        ctx = closed_context(grg_mod, w, 0)
+        got, deg = ctx.export_csr5()
+        want, wdeg = r.csr5()
+        assert np.array_equal(got, want) and np.array_equal(deg, wdeg), seed
+        ctx.close()
+
+
+def test_load_of_input_stream_equals_load_of_edges(grg_mod, oracle_mod):
+    w = G.pointsto(seed=44, num_vars=800, num_edges=2200)
+    want = oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, 0, w.src, w.dst, w.lab)
+    stream, deg = pack_csr5(w.src, w.dst, w.lab, 0, w.num_vars)
+    ctx = grg_mod.Context(0)
+    ctx.transfer_rules(w.rule_ids(), w.num_labels)
+    ctx.load_csr5(w.num_vars, stream, deg)
+    ctx.closure(0)
+    assert [int(x) for x in ctx.label_counts()] == [int(x) for x in want.label_counts()]
+    assert ctx.set_hash() == want.set_hash
+    got, gdeg = ctx.export_csr5()
+    ws, wd = want.csr5()
+    assert np.array_equal(got, ws) and np.array_equal(gdeg, wd)
+    ctx.close()
+
+
+def test_closed_stream_reloads_to_the_same_fixpoint(grg_mod, oracle_mod):
+    w = G.alias(seed=45, num_vars=2000, num_base_edges=5000, block=500)
+    want = oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, 0, w.src, w.dst, w.lab)
+    ctx = closed_context(grg_mod, w, 0)
+    stream, deg = ctx.export_csr5()
+    ctx2 = grg_mod.Context(0)
+    ctx2.transfer_rules(w.rule_ids(), w.num_labels)
+    ctx2.load_csr5(w.num_vars, stream, deg)
+    ctx2.closure(0)
+    assert [int(x) for x in ctx2.label_counts()] == [int(x) for x in want.label_counts()]
+    assert ctx2.set_hash() == want.set_hash
+    ctx.close()
+    ctx2.close()
+
+
+def test_partial_range_stream(grg_mod):
+    # the stream of rows [a, b) holds exactly the input edges leaving those rows
+    w = G.dataflow_small(seed=46, num_vars=1200, num_edges=3600)
+    a, b = 300, 700
+    stream, deg = pack_csr5(w.src, w.dst, w.lab, a, b)
+    ctx = grg_mod.Context(0)
+    ctx.transfer_rules(w.rule_ids(), w.num_labels)
+    ctx.load_csr5(w.num_vars, stream, deg, v_begin=a)
+    got, gdeg = ctx.export_csr5(0, w.num_vars)
+    assert np.array_equal(gdeg[:a], np.zeros(a, np.uint32)) and np.all(gdeg[b:] == 0)
+    assert np.array_equal(got, stream) and np.array_equal(gdeg[a:b], deg)
+    ctx.close()
+
+
+def test_invalid_streams_are_refused(grg_mod):
+    w = G.pointsto(seed=47, num_vars=400, num_edges=1000)
+    stream, deg = pack_csr5(w.src, w.dst, w.lab, 0, w.num_vars)
+    ctx = grg_mod.Context(0)
+    ctx.transfer_rules(w.rule_ids(), w.num_labels)
+    # lengths that do not add up
+    bad = deg.copy()
+    bad[3] += 1
+    with pytest.raises(grg_mod.GrgError) as ei:
+        ctx.load_csr5(w.num_vars, stream, bad)
+    assert ei.value.status == grg_mod.E_ARG
+    # a label outside 1..L
+    s2 = stream.copy().reshape(-1, 5)
+    s2[10, 4] = w.num_labels + 1
+    with pytest.raises(grg_mod.GrgError) as ei:
+        ctx.load_csr5(w.num_vars, s2.reshape(-1), deg)
+    assert ei.value.status == grg_mod.E_LABEL
+    s2[10, 4] = 0
+    with pytest.raises(grg_mod.GrgError) as ei:
+        ctx.load_csr5(w.num_vars, s2.reshape(-1), deg)
+    assert ei.value.status == grg_mod.E_LABEL
+    # a destination beyond the graph
+    s3 = stream.copy().reshape(-1, 5)
+    s3[20, :4] = np.frombuffer(np.uint32(w.num_vars).tobytes(), np.uint8)
+    with pytest.raises(grg_mod.GrgError) as ei:
+        ctx.load_csr5(w.num_vars, s3.reshape(-1), deg)
+    assert ei.value.status == grg_mod.E_RANGE
+    # the context still loads and closes a valid stream
+    ctx.load_csr5(w.num_vars, stream, deg)
+    ctx.closure(0)
+    assert sum(int(x) for x in ctx.label_counts()) >= len(w.src)
+    ctx.close()
+
+
+def test_invalid_edges_are_refused_by_every_load_path(grg_mod, oracle_mod):
+    w = G.pointsto(seed=48, num_vars=300, num_edges=800)
+    want = oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, 0, w.src, w.dst, w.lab)
+    cases = []
+    lab = w.lab.copy(); lab[5] = w.num_labels + 1
+    cases.append((w.src, w.dst, lab, grg_mod.E_LABEL))
+    lab = w.lab.copy(); lab[6] = 0
+    cases.append((w.src, w.dst, lab, grg_mod.E_LABEL))
+    src = w.src.copy(); src[7] = w.num_vars
+    cases.append((src, w.dst, w.lab, grg_mod.E_RANGE))
+    dst = w.dst.copy(); dst[8] = 0xFFFFFFFF
+    cases.append((w.src, dst, w.lab, grg_mod.E_RANGE))
+    ctx = grg_mod.Context(0)
+    ctx.transfer_rules(w.rule_ids(), w.num_labels)
+    for s, d, l, code in cases:
+        with pytest.raises(grg_mod.GrgError) as ei:
+            ctx.load_edges(w.num_vars, s, d, l)
+        assert ei.value.status == code
+    ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
+    ctx.closure(0)
+    assert ctx.set_hash() == want.set_hash
+    ctx.close()

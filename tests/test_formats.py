@@ -13,7 +13,7 @@ from conftest import REFERENCE_SAMPLE, ROOT
 def test_library_exports_every_declared_symbol(grg_mod):
     lib = grg_mod.load_library()
     header = open(os.path.join(ROOT, "include", "grg.h")).read()
-    declared = set(re.findall(r"\b(grg_[a-z_]+)\s*\(", header))
+    declared = set(re.findall(r"\b(grg_[a-z0-9_]+)\s*\(", header))
     assert declared == set(grg_mod.EXPORTS)
     for name in declared:
         assert hasattr(lib, name), name

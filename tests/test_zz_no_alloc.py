@@ -79,3 +79,23 @@ def test_noalloc_rejects_oversized_graphs(grg_mod):
     w.lab = np.ones(w.num_edges, np.uint8)
     st, _, _, _ = _noalloc(lib, torch, w, 1)
     assert st == grg_mod.E_FILTER
+
+
+def test_noalloc_refuses_invalid_edges(grg_mod):
+    torch = pytest.importorskip("torch")
+    lib = grg_mod.load_library()
+    w = G.pointsto(seed=49, num_vars=300, num_edges=800)
+    good = w.lab.copy()
+    w.lab = good.copy()
+    w.lab[2] = w.num_labels + 1
+    st, counts, _, _ = _noalloc(lib, torch, w, 0)
+    assert st == grg_mod.E_LABEL
+    w.lab = good
+    src = w.src
+    w.src = src.copy()
+    w.src[9] = w.num_vars
+    st, _, _, _ = _noalloc(lib, torch, w, 0)
+    assert st == grg_mod.E_RANGE
+    w.src = src
+    st, counts, h, _ = _noalloc(lib, torch, w, 0)
+    assert st == grg_mod.OK and (counts, h) == tuple(_allocating(grg_mod, w, 0)[:2])
