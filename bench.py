@@ -23,9 +23,11 @@ Beside the headline, the JSON line carries the other configurations, each
 measured on the device with results checked for consistency (skip them with
 --quick): `alias_c3` (1M-vertex alias closure), `alias_c4` (8M-vertex alias
 closure in-core, and out-of-core over 64 vertex-range partitions staged
-through host memory), `out_of_core_c2` (the dataflow closure under a pool
-limit of a quarter of what it needs in-core), and `serving` (the 512-job mix:
-continuous batching vs one graph at a time).
+through host memory), `stream_c2` (the dataflow closure exported as the
+compressed 5-byte-per-edge stream into page-locked host memory and loaded
+back), `out_of_core_c2` (the dataflow closure under a pool limit of a quarter
+of what it needs in-core), and `serving` (the 512-job mix: continuous
+batching vs one graph at a time).
 
 Multi-GPU: the closure of one graph does not shard without an exchange step,
 so N GPUs run N independent replicas (one per rank, weak scaling).
@@ -194,9 +196,48 @@ def _partitioned(grg, w, f, parts, pool_bytes=0):
     return st, [int(x) for x in counts], h, t_load
 
 
+def _stream_measurement(grg, w, f, counts, h):
+    """The closed graph as the compressed edge stream (5 bytes per edge) through
+    the C ABI into page-locked host memory, and loaded back into a new context;
+    the reloaded graph must close to the same counts and hash."""
+    import ctypes
+    import torch
+    ctx = grg.Context(0)
+    ctx.allocate_pool(0)
+    _closure_once(grg, ctx, w, f)
+    L, V = ctx._L, w.num_vars
+    n = ctypes.c_uint64()
+    st = L.grg_export_csr5(ctx._h, 0, V, 0, None, None, ctypes.byref(n))
+    assert st in (grg.OK, grg.E_RANGE)
+    m = n.value
+    stream = torch.empty(m * 5, dtype=torch.uint8, pin_memory=True)
+    deg = torch.empty(V, dtype=torch.int32, pin_memory=True)
+    t0 = time.perf_counter()
+    ctx._check(L.grg_export_csr5(ctx._h, 0, V, m, ctypes.c_void_p(stream.data_ptr()), ctypes.c_void_p(deg.data_ptr()),
+                                 ctypes.byref(n)), "export_csr5")
+    t_export = time.perf_counter() - t0
+    ctx.close()
+    ctx = grg.Context(0)
+    ctx.allocate_pool(0)
+    ctx.transfer_rules(w.rule_ids(), w.num_labels)
+    t0 = time.perf_counter()
+    ctx._check(L.grg_load_csr5(ctx._h, V, 0, V, ctypes.c_void_p(deg.data_ptr()), m,
+                               ctypes.c_void_p(stream.data_ptr()), 0), "load_csr5")
+    t_load = time.perf_counter() - t0
+    ctx.closure(f)
+    same = ([int(x) for x in ctx.label_counts()], ctx.set_hash()) == (counts, h)
+    ctx.close()
+    assert same, "reloaded stream closes to a different result"
+    return {"edges": m, "stream_bytes": m * 5, "export_s": t_export, "load_s": t_load,
+            "export_edges_per_s": m / t_export, "load_edges_per_s": m / t_load,
+            "export_stream_gbs": m * 5 / t_export / 1e9, "load_stream_gbs": m * 5 / t_load / 1e9,
+            "host_memory": "page-locked", "reload_closes_to_same_result": True}
+
+
 def extra_measurements(args, w2):
-    """C3 and C4 (alias, in-core; C4 also out-of-core over 64 partitions) and the
-    C2 dataflow closure out-of-core under a pool limit."""
+    """C3 and C4 (alias, in-core; C4 also out-of-core over 64 partitions), the
+    C2 closure as the compressed edge stream (export and reload), and the C2
+    dataflow closure out-of-core under a pool limit."""
     import grg
     import grg_gen as G
     out = {}
@@ -238,6 +279,7 @@ def extra_measurements(args, w2):
     ctx.allocate_pool(0)
     st, c2_counts, c2_hash = _closure_once(grg, ctx, w2, w2.filter_flag)
     ctx.close()
+    out["stream_c2"] = dict(workload=WORKLOAD, **_stream_measurement(grg, w2, w2.filter_flag, c2_counts, c2_hash))
     limit = st["pool_elems_used"] * 69 // 4
     pst, p_counts, p_hash, t_load = _partitioned(grg, w2, w2.filter_flag, 4, limit)
     assert (p_counts, p_hash) == (c2_counts, c2_hash), "partitioned C2 differs from in-core"

@@ -1588,6 +1588,7 @@ const char *status_text(int s)
     switch (s) {
     case GRG_OK: return "ok";
     case GRG_NEED_REPARTITION: return "partition needs repartitioning";
+    case GRG_PAUSED: return "paused at the run budget";
     case GRG_E_ARG: return "invalid argument";
     case GRG_E_CUDA: return "CUDA error";
     case GRG_E_NOMEM: return "out of memory";
@@ -3113,8 +3114,6 @@ int grg_load_csr5(grg_ctx *c, uint32_t num_vars, uint32_t v_begin, uint32_t v_en
     cudaSetDevice(c->device);
     const uint32_t nrows = v_end - v_begin;
     if (num_edges && !nrows) return fail(c, GRG_E_ARG, "edges without rows");
-    int st = ensure_input(c, num_edges);
-    if (st) return st;
     const uint8_t *dbytes = edges;
     const uint32_t *ddeg = degree;
     uint8_t *sbytes = nullptr;
@@ -3128,19 +3127,34 @@ int grg_load_csr5(grg_ctx *c, uint32_t num_vars, uint32_t v_begin, uint32_t v_en
         dbytes = sbytes;
         ddeg = sdeg;
     }
-    uint64_t sum = 0;
+    uint64_t sum = 0, n = 0;
+    unsigned bad = 0;
+    uint4 *recs = nullptr;
+    uint32_t *stamps = nullptr;
     if (e == cudaSuccess)
-        e = grg_fmt_csr5_to_edges(dbytes, num_edges, ddeg, v_begin, nrows, c->d_in32, c->d_in32 + num_edges, c->d_in8,
-                                  &sum, c->stream);
+        e = grg_fmt_csr5_to_records(dbytes, num_edges, ddeg, v_begin, nrows, num_vars, (uint32_t)c->L, &recs, &stamps,
+                                    &n, &sum, &bad, c->stream);
     cudaFree(sbytes);
     cudaFree(sdeg);
+    int st = GRG_OK;
     if (e != cudaSuccess) {
         cudaGetLastError();
-        return fail(c, e == cudaErrorMemoryAllocation ? GRG_E_NOMEM : GRG_E_CUDA,
-                    std::string("compressed load: ") + cudaGetErrorString(e));
+        st = fail(c, e == cudaErrorMemoryAllocation ? GRG_E_NOMEM : GRG_E_CUDA,
+                  std::string("compressed load: ") + cudaGetErrorString(e));
+    } else if (sum != num_edges) {
+        st = fail(c, GRG_E_ARG, "row lengths do not add up to num_edges");
+    } else if (bad & 1u) {
+        st = fail(c, GRG_E_LABEL, "edge label outside 1..numLabels");
+    } else if (bad & 2u) {
+        st = fail(c, GRG_E_RANGE, "edge vertex id >= numVars");
+    } else {
+        // a stream is a spilled image: it already holds its epsilon edges, and every
+        // element is a delta of round 1 of the next closure
+        st = grg_load_elements(c, num_vars, n, reinterpret_cast<const uint32_t *>(recs), stamps, 0, 1);
     }
-    if (sum != num_edges) return fail(c, GRG_E_ARG, "row lengths do not add up to num_edges");
-    return grg_load_edges(c, num_vars, num_edges, c->d_in32, c->d_in32 + num_edges, c->d_in8, 1);
+    cudaFree(recs);
+    cudaFree(stamps);
+    return st;
 }
 
 int grg_range_counts(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t *counts, uint64_t *hash)

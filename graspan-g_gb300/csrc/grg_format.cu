@@ -96,29 +96,105 @@ __global__ void k_fmt_widen(const uint32_t *__restrict__ degree, uint32_t nrows,
         roff[r] = r < nrows ? degree[r] : 0;
 }
 
-// Each thread expands EXPAND_RUN consecutive edges; its first row is the last r
-// with start[r] <= e (rows of length 0 share their start with the next row).
-__global__ void k_fmt_expand(const uint8_t *__restrict__ bytes, const uint64_t *__restrict__ start, uint32_t nrows,
-                             uint64_t m, uint32_t v_begin, uint32_t *src, uint32_t *dst, uint8_t *lab)
+// Walks the EXPAND_RUN consecutive edges of run u: f(row, label, dst, starts)
+// per edge, where `starts` says the edge begins a new element -- the first edge
+// of a row, or one whose label or 192-id base differs from the edge before it
+// (the stream is sorted by label, then destination, within a row). The run's
+// first row is the last r with start[r] <= e0 (rows of length 0 share their
+// start with the next row).
+template <class F>
+__device__ __forceinline__ void walk_run(const uint8_t *__restrict__ bytes, const uint64_t *__restrict__ start,
+                                         uint32_t nrows, uint64_t m, uint64_t u, F f)
+{
+    const uint64_t e0 = u * EXPAND_RUN;
+    uint32_t lo = 0, hi = nrows;                 // start[lo] <= e0 < start[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        if (start[mid] <= e0) lo = mid; else hi = mid;
+    }
+    uint32_t r = lo, plab = 0, pbase = 0;
+    bool have_prev = false;
+    if (e0 > start[r]) {                         // the edge before e0 is in the same row
+        const uint8_t *q = bytes + (e0 - 1) * 5;
+        plab = q[4];
+        pbase = ((uint32_t)q[0] | ((uint32_t)q[1] << 8) | ((uint32_t)q[2] << 16) | ((uint32_t)q[3] << 24)) / EIDS;
+        have_prev = true;
+    }
+    const uint64_t e1 = e0 + EXPAND_RUN < m ? e0 + EXPAND_RUN : m;
+    for (uint64_t e = e0; e < e1; e++) {
+        while (r + 1 < nrows && start[r + 1] <= e) {
+            r++;
+            have_prev = false;
+        }
+        const uint8_t *q = bytes + e * 5;
+        const uint32_t dst = (uint32_t)q[0] | ((uint32_t)q[1] << 8) | ((uint32_t)q[2] << 16) | ((uint32_t)q[3] << 24);
+        const uint32_t lab = q[4], base = dst / EIDS;
+        f(r, lab, dst, !have_prev || lab != plab || base != pbase);
+        have_prev = true;
+        plab = lab;
+        pbase = base;
+    }
+}
+
+// Pass 1: elements starting in each run; labels outside 1..L and destinations
+// >= num_vars set bits 1 and 2 of *bad.
+__global__ void k_fmt_starts(const uint8_t *__restrict__ bytes, const uint64_t *__restrict__ start, uint32_t nrows,
+                             uint64_t m, uint32_t num_vars, uint32_t L, uint64_t *run_cnt, unsigned *bad)
 {
     const uint64_t runs = (m + EXPAND_RUN - 1) / EXPAND_RUN;
     for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < runs; u += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t e0 = u * EXPAND_RUN;
-        uint32_t lo = 0, hi = nrows;                 // start[lo] <= e0 < start[hi]
-        while (hi - lo > 1) {
-            const uint32_t mid = lo + (hi - lo) / 2;
-            if (start[mid] <= e0) lo = mid; else hi = mid;
-        }
-        uint32_t r = lo;
-        const uint64_t e1 = e0 + EXPAND_RUN < m ? e0 + EXPAND_RUN : m;
-        for (uint64_t e = e0; e < e1; e++) {
-            while (r + 1 < nrows && start[r + 1] <= e) r++;
-            const uint8_t *q = bytes + e * 5;
-            src[e] = v_begin + r;
-            dst[e] = (uint32_t)q[0] | ((uint32_t)q[1] << 8) | ((uint32_t)q[2] << 16) | ((uint32_t)q[3] << 24);
-            lab[e] = q[4];
-        }
+        uint32_t c = 0;
+        unsigned b = 0;
+        walk_run(bytes, start, nrows, m, u, [&](uint32_t, uint32_t lab, uint32_t dst, bool starts) {
+            if (lab - 1u >= L) b |= 1u;
+            if (dst >= num_vars) b |= 2u;
+            c += starts;
+        });
+        run_cnt[u] = c;
+        if (b) atomicOr(bad, b);
     }
+}
+
+// Pass 2: ORs each edge's bit into its element (id = elements started before
+// it); the element's first edge writes its key and row. Bits gather in
+// registers while consecutive edges share an element.
+__global__ void k_fmt_build(const uint8_t *__restrict__ bytes, const uint64_t *__restrict__ start, uint32_t nrows,
+                            uint64_t m, uint32_t v_begin, const uint64_t *__restrict__ run_off, uint32_t *rec)
+{
+    const uint64_t runs = (m + EXPAND_RUN - 1) / EXPAND_RUN;
+    for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < runs; u += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t id = run_off[u] - 1;            // the element the run's first edge continues, if it does
+        uint32_t acc[6] = {0, 0, 0, 0, 0, 0};
+        bool open = false;
+        auto flush = [&]() {
+            if (!open) return;
+#pragma unroll
+            for (int w = 0; w < 6; w++)
+                if (acc[w]) atomicOr(&rec[id * 8 + w], acc[w]);
+#pragma unroll
+            for (int w = 0; w < 6; w++) acc[w] = 0;
+        };
+        walk_run(bytes, start, nrows, m, u, [&](uint32_t r, uint32_t lab, uint32_t dst, bool starts) {
+            if (starts) {
+                flush();
+                id++;
+                rec[id * 8 + 6] = (lab << 25) | (dst / EIDS);
+                rec[id * 8 + 7] = v_begin + r;
+            }
+            open = true;
+            const uint32_t o = dst % EIDS;
+#pragma unroll
+            for (int w = 0; w < 6; w++)
+                if ((o >> 5) == (uint32_t)w) acc[w] |= 1u << (o & 31);
+        });
+        flush();
+    }
+}
+
+__global__ void k_fmt_fill(uint32_t *p, uint64_t n, uint32_t v)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        p[i] = v;
 }
 
 int bit_width(uint64_t x)
@@ -183,32 +259,62 @@ done:
     return err;
 }
 
-cudaError_t grg_fmt_csr5_to_edges(const uint8_t *bytes, uint64_t num_edges, const uint32_t *degree, uint32_t v_begin,
-                                  uint32_t nrows, uint32_t *src, uint32_t *dst, uint8_t *label, uint64_t *sum,
-                                  cudaStream_t s)
+cudaError_t grg_fmt_csr5_to_records(const uint8_t *bytes, uint64_t num_edges, const uint32_t *degree,
+                                    uint32_t v_begin, uint32_t nrows, uint32_t num_vars, uint32_t L, uint4 **recs,
+                                    uint32_t **stamps, uint64_t *n_elems, uint64_t *sum, unsigned *bad,
+                                    cudaStream_t s)
 {
     cudaError_t err = cudaSuccess;
-    uint64_t *roff = nullptr, *start = nullptr;
+    uint64_t *roff = nullptr, *start = nullptr, *rcnt = nullptr, *roffs = nullptr;
+    unsigned *dbad = nullptr;
     void *tmp = nullptr;
-    size_t tscan = 0;
+    size_t tscan = 0, tscan2 = 0;
+    const uint64_t runs = (num_edges + EXPAND_RUN - 1) / EXPAND_RUN;
+    uint32_t *rec = nullptr, *st = nullptr;
+    *recs = nullptr;
+    *stamps = nullptr;
+    *n_elems = 0;
     *sum = 0;
+    *bad = 0;
     if (!nrows) return cudaSuccess;
     FMT_CHECK(cudaMalloc(&roff, ((uint64_t)nrows + 1) * 16));
     start = roff + nrows + 1;
+    FMT_CHECK(cudaMalloc(&rcnt, (runs + 1) * 16 + 16));
+    roffs = rcnt + runs + 1;
+    dbad = (unsigned *)(roffs + runs + 1);
     FMT_CHECK(cub::DeviceScan::ExclusiveSum(nullptr, tscan, roff, start, (uint64_t)nrows + 1, s));
-    FMT_CHECK(cudaMalloc(&tmp, tscan));
+    FMT_CHECK(cub::DeviceScan::ExclusiveSum(nullptr, tscan2, rcnt, roffs, runs + 1, s));
+    FMT_CHECK(cudaMalloc(&tmp, tscan > tscan2 ? tscan : tscan2));
     k_fmt_widen<<<grid_of((uint64_t)nrows + 1, 256), 256, 0, s>>>(degree, nrows, roff);
     FMT_CHECK(cub::DeviceScan::ExclusiveSum(tmp, tscan, roff, start, (uint64_t)nrows + 1, s));
     FMT_CHECK(cudaMemcpyAsync(sum, start + nrows, 8, cudaMemcpyDeviceToHost, s));
     FMT_CHECK(cudaStreamSynchronize(s));
-    if (*sum == num_edges && num_edges) {
-        k_fmt_expand<<<grid_of((num_edges + EXPAND_RUN - 1) / EXPAND_RUN, 256), 256, 0, s>>>(
-            bytes, start, nrows, num_edges, v_begin, src, dst, label);
-        FMT_CHECK(cudaGetLastError());
-        FMT_CHECK(cudaStreamSynchronize(s));
-    }
+    if (*sum != num_edges || !num_edges) goto done;
+    FMT_CHECK(cudaMemsetAsync(rcnt, 0, (runs + 1) * 8, s));
+    FMT_CHECK(cudaMemsetAsync(dbad, 0, 4, s));
+    k_fmt_starts<<<grid_of(runs, 256), 256, 0, s>>>(bytes, start, nrows, num_edges, num_vars, L, rcnt, dbad);
+    FMT_CHECK(cub::DeviceScan::ExclusiveSum(tmp, tscan2, rcnt, roffs, runs + 1, s));
+    FMT_CHECK(cudaMemcpyAsync(bad, dbad, 4, cudaMemcpyDeviceToHost, s));
+    FMT_CHECK(cudaMemcpyAsync(n_elems, roffs + runs, 8, cudaMemcpyDeviceToHost, s));
+    FMT_CHECK(cudaStreamSynchronize(s));
+    if (*bad || !*n_elems) goto done;
+    FMT_CHECK(cudaMalloc(&rec, *n_elems * 32));
+    FMT_CHECK(cudaMalloc(&st, *n_elems * 4));
+    FMT_CHECK(cudaMemsetAsync(rec, 0, *n_elems * 32, s));
+    k_fmt_fill<<<grid_of(*n_elems, 256), 256, 0, s>>>(st, *n_elems, 1u);
+    // run u's edges belong to elements run_off[u] - 1 (continued) and run_off[u] .. run_off[u+1] - 1
+    k_fmt_build<<<grid_of(runs, 256), 256, 0, s>>>(bytes, start, nrows, num_edges, v_begin, roffs, rec);
+    FMT_CHECK(cudaGetLastError());
+    FMT_CHECK(cudaStreamSynchronize(s));
+    *recs = reinterpret_cast<uint4 *>(rec);
+    *stamps = st;
+    rec = nullptr;
+    st = nullptr;
 done:
+    cudaFree(rec);
+    cudaFree(st);
     cudaFree(tmp);
+    cudaFree(rcnt);
     cudaFree(roff);
     return err;
 }

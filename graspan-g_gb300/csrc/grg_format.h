@@ -18,10 +18,15 @@
 cudaError_t grg_fmt_records_to_csr5(const uint4 *rec, uint64_t n, uint32_t v_begin, uint32_t nrows,
                                     uint64_t total_edges, uint8_t *out_bytes, uint32_t *degree, cudaStream_t s);
 
-// Expands a stream of num_edges edges for rows [v_begin, v_begin + nrows) with
-// row lengths degree (device) into edge arrays src/dst/label (device, num_edges
-// each). Sets *sum to the sum of degree, so the caller can refuse a stream whose
-// lengths do not add up (nothing is expanded then). Returns after the expansion.
-cudaError_t grg_fmt_csr5_to_edges(const uint8_t *bytes, uint64_t num_edges, const uint32_t *degree, uint32_t v_begin,
-                                  uint32_t nrows, uint32_t *src, uint32_t *dst, uint8_t *label, uint64_t *sum,
-                                  cudaStream_t s);
+// Element records of a stream of num_edges edges for rows [v_begin, v_begin +
+// nrows) with row lengths degree (device memory): consecutive edges of a row
+// with the same label and 192-id base form one record (8 words: bitmap words
+// 0-5, label << 25 | base, source row), each with stamp 1. *sum = the sum of
+// degree; nothing else is done unless it equals num_edges. *bad = 1 (a label
+// outside 1..L) | 2 (a destination >= num_vars); nothing is built then.
+// Otherwise *recs / *stamps are device arrays of *n_elems entries that the
+// caller frees with cudaFree. Returns after the records are complete.
+cudaError_t grg_fmt_csr5_to_records(const uint8_t *bytes, uint64_t num_edges, const uint32_t *degree,
+                                    uint32_t v_begin, uint32_t nrows, uint32_t num_vars, uint32_t L, uint4 **recs,
+                                    uint32_t **stamps, uint64_t *n_elems, uint64_t *sum, unsigned *bad,
+                                    cudaStream_t s);

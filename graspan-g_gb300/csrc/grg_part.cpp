@@ -34,8 +34,10 @@
 #include <chrono>
 #include <cstdint>
 #include <cstdlib>
+#include <cstdio>
 #include <cstring>
 #include <map>
+#include <string>
 #include <utility>
 #include <vector>
 
@@ -123,6 +125,7 @@ struct Image {
     uint32_t max_stamp = 0;
     uint32_t last_run = 0;           // last run that held this partition
     bool counted = false;            // counts/hash are those of the current image
+    bool done = false;               // stream schedule: this partition's rows are closed
     std::vector<uint32_t> reach;     // ids of partitions this one's B-edges may end in (sorted)
     std::vector<uint64_t> counts;
     uint64_t hash = 0;
@@ -180,6 +183,14 @@ struct grg_part {
     Pinned in;                       // run inputs assembled for the device
     grg_part_stats S{};
     uint64_t bmask = 0;              // labels that are a binary rule's first symbol
+    // checkpoint / run budget
+    std::string ckpt_path;           // empty = no automatic checkpoints
+    uint32_t ckpt_every = 0;         // save after every this many runs of a call
+    uint64_t run_budget = 0;         // runs per grg_part_run call (0 = unbounded)
+    uint64_t runs_call = 0;          // runs made by the current call
+    int run_filter = -1;             // filter of a paused run (-1 = none)
+    uint64_t cursor = 0;             // pairs schedule: position in the paused superstep's pair order
+    bool cursor_ran = false;         // a run happened in that superstep before the pause
 };
 
 namespace {
@@ -322,6 +333,202 @@ bool split(grg_part *p, size_t i)
     return true;
 }
 
+// ---- checkpoint file: the partition set's whole state, with a checksum over
+// every byte before it (64-bit words, FNV-1a style). Native byte order.
+
+constexpr char CKPT_MAGIC[8] = {'G', 'R', 'G', 'P', 'A', 'R', 'T', '1'};
+constexpr uint32_t CKPT_VERSION = 1;
+
+struct Hasher {
+    uint64_t h = 1469598103934665603ull, pend = 0;
+    int npend = 0;
+    void byte(uint8_t b)
+    {
+        pend |= (uint64_t)b << (8 * npend);
+        if (++npend == 8) word();
+    }
+    void word()
+    {
+        h = (h ^ pend) * 1099511628211ull;
+        pend = 0;
+        npend = 0;
+    }
+    void mix(const void *p, size_t n)
+    {
+        const uint8_t *b = (const uint8_t *)p;
+        while (n && npend) { byte(*b++); n--; }
+        for (; n >= 8; n -= 8, b += 8) {
+            memcpy(&pend, b, 8);
+            word();
+        }
+        while (n) { byte(*b++); n--; }
+    }
+    uint64_t final_value()
+    {
+        if (npend) word();
+        return h;
+    }
+};
+
+struct Writer {
+    FILE *f = nullptr;
+    Hasher hs;
+    bool ok = true;
+    void put(const void *p, size_t n)
+    {
+        if (!ok || !n) return;
+        if (fwrite(p, 1, n, f) != n) ok = false;
+        hs.mix(p, n);
+    }
+    template <class T> void val(T v) { put(&v, sizeof v); }
+};
+
+struct Reader {
+    FILE *f = nullptr;
+    Hasher hs;
+    uint64_t left = 0;               // bytes of the file not read yet
+    bool ok = true;
+    bool get(void *p, size_t n)
+    {
+        if (!ok) return false;
+        if (n > left || (n && fread(p, 1, n, f) != n)) return ok = false;
+        left -= n;
+        hs.mix(p, n);
+        return true;
+    }
+    template <class T> bool val(T &v) { return get(&v, sizeof v); }
+};
+
+int save_state(grg_part *p, const char *path)
+{
+    const std::string tmp = std::string(path) + ".tmp";
+    Writer w;
+    w.f = fopen(tmp.c_str(), "wb");
+    if (!w.f) return GRG_E_IO;
+    w.put(CKPT_MAGIC, 8);
+    w.val(CKPT_VERSION);
+    w.val(p->V);
+    w.val(p->R);
+    w.val(p->L);
+    w.put(p->rules, sizeof(int) * 3 * p->R);
+    w.val(p->run_id);
+    w.val(p->next_id);
+    w.val(p->run_filter);
+    w.val((uint8_t)p->loaded);
+    w.val((uint8_t)p->closed);
+    w.val((uint64_t)p->S.splits);
+    w.val(p->cursor);
+    w.val((uint8_t)p->cursor_ran);
+    w.val((uint64_t)p->parts.size());
+    for (const Image &x : p->parts) {
+        w.val(x.id); w.val(x.lo); w.val(x.hi); w.val(x.max_stamp); w.val(x.last_run);
+        w.val((uint8_t)x.counted);
+        w.val((uint8_t)x.done);
+        w.val((uint64_t)x.reach.size());
+        w.put(x.reach.data(), 4 * x.reach.size());
+        w.val((uint64_t)x.counts.size());
+        w.put(x.counts.data(), 8 * x.counts.size());
+        w.val(x.hash);
+        w.val((uint64_t)x.size());
+        w.put(x.rec.data(), 32 * x.size());
+        w.put(x.st.data(), 4 * x.size());
+    }
+    w.val((uint64_t)p->seen.size());
+    for (const auto &kv : p->seen) {
+        w.val(kv.first.first);
+        w.val(kv.first.second);
+        w.val(kv.second);
+    }
+    const uint64_t sum = w.hs.final_value();
+    if (w.ok && fwrite(&sum, 8, 1, w.f) != 1) w.ok = false;
+    if (fflush(w.f) != 0) w.ok = false;
+    if (fclose(w.f) != 0) w.ok = false;
+    if (!w.ok || rename(tmp.c_str(), path) != 0) {
+        remove(tmp.c_str());
+        return GRG_E_IO;
+    }
+    return GRG_OK;
+}
+
+// Reads a checkpoint into p (created on the right context, without partitions).
+int read_state(grg_part *p, FILE *f, uint64_t size)
+{
+    Reader r;
+    r.f = f;
+    if (size < 8) return GRG_E_IO;
+    r.left = size - 8;               // the checksum is not part of the hashed bytes
+    char magic[8];
+    uint32_t ver = 0, V = 0;
+    int R = 0, L = 0;
+    if (!r.get(magic, 8) || memcmp(magic, CKPT_MAGIC, 8) != 0) return GRG_E_IO;
+    if (!r.val(ver) || ver != CKPT_VERSION) return GRG_E_IO;
+    if (!r.val(V) || !r.val(R) || !r.val(L)) return GRG_E_IO;
+    if (V != p->V || R != p->R || L != p->L) return GRG_E_IO;
+    int rules[3 * GRG_MAX_RULES];
+    if (!r.get(rules, sizeof(int) * 3 * R) || memcmp(rules, p->rules, sizeof(int) * 3 * R) != 0) return GRG_E_IO;
+    uint8_t loaded = 0, closed = 0, cran = 0;
+    uint64_t splits = 0, nparts = 0;
+    if (!r.val(p->run_id) || !r.val(p->next_id) || !r.val(p->run_filter) || !r.val(loaded) || !r.val(closed) ||
+        !r.val(splits) || !r.val(p->cursor) || !r.val(cran) || !r.val(nparts))
+        return GRG_E_IO;
+    p->cursor_ran = cran != 0;
+    if (nparts == 0 || nparts > (uint64_t)V + 1 || p->run_filter < -1 || p->run_filter > 1) return GRG_E_IO;
+    p->parts.clear();
+    uint32_t expect_lo = 0;
+    for (uint64_t q = 0; q < nparts; q++) {
+        Image x;
+        uint8_t counted = 0, done = 0;
+        uint64_t nreach = 0, ncounts = 0, n = 0;
+        if (!r.val(x.id) || !r.val(x.lo) || !r.val(x.hi) || !r.val(x.max_stamp) || !r.val(x.last_run) ||
+            !r.val(counted) || !r.val(done) || !r.val(nreach))
+            return GRG_E_IO;
+        if (x.lo != expect_lo || x.hi <= x.lo || x.hi > V || x.id >= p->next_id) return GRG_E_IO;
+        expect_lo = x.hi;
+        if (nreach > r.left / 4) return GRG_E_IO;
+        x.reach.resize(nreach);
+        if (!r.get(x.reach.data(), 4 * nreach) || !r.val(ncounts)) return GRG_E_IO;
+        if (ncounts != 0 && ncounts != (uint64_t)L) return GRG_E_IO;
+        x.counts.resize(ncounts);
+        if (!r.get(x.counts.data(), 8 * ncounts) || !r.val(x.hash) || !r.val(n)) return GRG_E_IO;
+        if (n > r.left / 36) return GRG_E_IO;
+        if (!x.rec.resize(8 * n) || !x.st.resize(n)) return GRG_E_NOMEM;
+        if (!r.get(x.rec.data(), 32 * n) || !r.get(x.st.data(), 4 * n)) return GRG_E_IO;
+        for (uint64_t e = 0; e < n; e++) {
+            const uint32_t row = x.rec[8 * e + 7], lab = x.rec[8 * e + 6] >> KEY_SHIFT;
+            if (row < x.lo || row >= x.hi || lab < 1 || lab > (uint32_t)L) return GRG_E_IO;
+        }
+        x.counted = counted != 0;
+        x.done = done != 0;
+        if (x.counted && ncounts != (uint64_t)L) return GRG_E_IO;
+        p->parts.push_back(std::move(x));
+    }
+    if (expect_lo != V) return GRG_E_IO;
+    uint64_t nseen = 0;
+    if (!r.val(nseen) || nseen > r.left / 12) return GRG_E_IO;
+    p->seen.clear();
+    for (uint64_t q = 0; q < nseen; q++) {
+        uint32_t a = 0, b = 0, t = 0;
+        if (!r.val(a) || !r.val(b) || !r.val(t)) return GRG_E_IO;
+        p->seen[std::make_pair(a, b)] = t;
+    }
+    uint64_t want = 0;
+    if (r.left != 0 || fread(&want, 8, 1, f) != 1 || want != r.hs.final_value()) return GRG_E_IO;
+    p->loaded = loaded != 0;
+    p->closed = closed != 0;
+    p->S = grg_part_stats{};
+    p->S.splits = splits;
+    return GRG_OK;
+}
+
+// Bookkeeping after each completed device run: count it, checkpoint when due.
+int after_run(grg_part *p)
+{
+    p->runs_call++;
+    if (p->ckpt_every && !p->ckpt_path.empty() && p->runs_call % p->ckpt_every == 0)
+        return save_state(p, p->ckpt_path.c_str());
+    return GRG_OK;
+}
+
 // Load one partition's image (nothing marked) and count its rows.
 int recount(grg_part *p, Image &x)
 {
@@ -401,6 +608,11 @@ int run_stream(grg_part *p, uint32_t filter, const bool *der)
     std::vector<uint64_t> seg;
     bool stale = true;
     for (size_t i = 0; i < p->parts.size();) {
+        if (p->parts[i].done) {          // closed before a pause
+            i++;
+            continue;
+        }
+        if (p->run_budget && p->runs_call >= p->run_budget) return GRG_PAUSED;
         if (stale) {
             uint64_t ns = 0;
             for (const Image &x : p->parts)
@@ -433,6 +645,8 @@ int run_stream(grg_part *p, uint32_t filter, const bool *der)
         int s2 = export_image(p, p->parts[i]);
         if (s2) return s2;
         if ((s2 = count_image(p, p->parts[i]))) return s2;
+        p->parts[i].done = true;
+        if ((s2 = after_run(p))) return s2;
         i++;
     }
     return GRG_OK;
@@ -460,8 +674,16 @@ int run_pairs(grg_part *p, uint32_t filter)
         for (size_t i = 0; i < m; i++)
             for (size_t j = i + 1; j < m; j++) order.emplace_back(i, j);
         for (size_t i = 0; i < m; i++) order.emplace_back(i, i);
-        for (const auto &ij : order) {
-            const size_t i = ij.first, j = ij.second;
+        // a paused superstep continues where it stopped (later pairs are not starved by a restart)
+        size_t k0 = 0;
+        if (p->cursor && p->cursor < order.size()) {
+            k0 = (size_t)p->cursor;
+            ran = p->cursor_ran;
+        }
+        p->cursor = 0;
+        p->cursor_ran = false;
+        for (size_t k = k0; k < order.size(); k++) {
+            const size_t i = order[k].first, j = order[k].second;
             Image &a = p->parts[i], &b = p->parts[j];
             const uint32_t t = seen_of(p, a.id, b.id);
             bool need;
@@ -472,6 +694,11 @@ int run_pairs(grg_part *p, uint32_t filter)
             if (!need) {
                 p->S.skipped++;
                 continue;
+            }
+            if (p->run_budget && p->runs_call >= p->run_budget) {
+                p->cursor = k;
+                p->cursor_ran = ran;
+                return GRG_PAUSED;
             }
             const uint32_t r = ++p->run_id;
             std::vector<size_t> idx = {i};
@@ -496,6 +723,8 @@ int run_pairs(grg_part *p, uint32_t filter)
             }
             p->seen[pkey(a.id, b.id)] = r;
             ran = true;
+            const int s3 = after_run(p);
+            if (s3) return s3;
         }
         if (restart) continue;
         p->S.supersteps++;
@@ -603,10 +832,12 @@ int grg_part_run(grg_part *p, uint32_t filter, grg_part_stats *stats)
     if (!p || filter > 1) return GRG_E_ARG;
     if (!p->loaded) return GRG_E_STATE;
     if (p->closed) return GRG_E_STATE;
+    if (p->run_filter >= 0 && (uint32_t)p->run_filter != filter) return GRG_E_ARG;   // a paused run's filter
     const auto t0 = std::chrono::steady_clock::now();
     const uint64_t splits0 = p->S.splits;
     p->S = grg_part_stats{};
     p->S.splits = splits0;
+    p->runs_call = 0;
     bool der[GRG_MAX_LABELS + 1];
     derivable_labels(p, filter, der);
     bool coupled = false;
@@ -616,6 +847,14 @@ int grg_part_run(grg_part *p, uint32_t filter, grg_part_stats *stats)
     }
     p->S.schedule = coupled ? 1 : 0;
     int st = coupled ? run_pairs(p, filter) : run_stream(p, filter, der);
+    if (st == GRG_PAUSED) {
+        p->run_filter = (int)filter;
+        p->S.num_parts = (uint32_t)p->parts.size();
+        if (!p->ckpt_path.empty() && (st = save_state(p, p->ckpt_path.c_str()))) return st;
+        p->S.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (stats) *stats = p->S;
+        return GRG_PAUSED;
+    }
     if (st) return st;
     // partitions whose counts predate a split are counted from their images
     for (size_t i = 0; i < p->parts.size(); i++) {
@@ -626,8 +865,10 @@ int grg_part_run(grg_part *p, uint32_t filter, grg_part_stats *stats)
     for (const Image &x : p->parts)
         for (int l = 0; l < p->L; l++) p->S.total_edges += x.counts[l];
     p->S.num_parts = (uint32_t)p->parts.size();
-    p->S.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     p->closed = true;
+    p->run_filter = -1;
+    if (!p->ckpt_path.empty() && (st = save_state(p, p->ckpt_path.c_str()))) return st;
+    p->S.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (stats) *stats = p->S;
     return GRG_OK;
 }
@@ -653,6 +894,83 @@ int grg_part_bounds(grg_part *p, uint32_t cap, uint32_t *bounds, uint32_t *num_p
     if (cap < p->parts.size() + 1 || !bounds) return cap ? GRG_E_RANGE : GRG_OK;
     for (size_t i = 0; i < p->parts.size(); i++) bounds[i] = p->parts[i].lo;
     bounds[p->parts.size()] = p->parts.empty() ? 0 : p->parts.back().hi;
+    return GRG_OK;
+}
+
+int grg_part_export_csr5(grg_part *p, uint32_t index, uint64_t cap, uint8_t *edges, uint32_t *degree,
+                         uint64_t *num_edges)
+{
+    if (!p || !num_edges) return GRG_E_ARG;
+    if (!p->closed) return GRG_E_STATE;
+    if (index >= p->parts.size()) return GRG_E_RANGE;
+    Image &x = p->parts[index];
+    uint64_t total = 0;
+    for (uint64_t c : x.counts) total += c;
+    *num_edges = total;
+    if (total > cap) return total ? GRG_E_RANGE : GRG_OK;
+    int st = p->in.ensure(x.size());
+    if (st) return st;
+    memcpy(p->in.rec, x.rec.data(), x.size() * 32);
+    memcpy(p->in.st, x.st.data(), x.size() * 4);
+    if ((st = grg_load_elements(p->ctx, p->V, x.size(), p->in.rec, p->in.st, ~0u, 0))) return st;
+    return grg_export_csr5(p->ctx, x.lo, x.hi, cap, edges, degree, num_edges);
+}
+
+int grg_part_save(grg_part *p, const char *path)
+{
+    if (!p || !path) return GRG_E_ARG;
+    if (!p->loaded) return GRG_E_STATE;
+    return save_state(p, path);
+}
+
+int grg_part_restore(grg_part **out, grg_ctx *ctx, const char *path)
+{
+    if (!out || !ctx || !path) return GRG_E_ARG;
+    *out = nullptr;
+    FILE *f = fopen(path, "rb");
+    if (!f) return GRG_E_IO;
+    uint64_t size = 0;
+    if (fseek(f, 0, SEEK_END) == 0) {
+        const long e = ftell(f);
+        size = e > 0 ? (uint64_t)e : 0;
+    }
+    fseek(f, 0, SEEK_SET);
+    grg_part *p = new grg_part;
+    p->ctx = ctx;
+    int st = grg_get_rules(ctx, &p->R, p->rules, &p->L);
+    if (!st) {
+        for (int q = 0; q < p->R; q++)
+            if (p->rules[3 * q + 1] && p->rules[3 * q + 2]) p->bmask |= 1ull << (p->rules[3 * q + 1] - 1);
+        // the vertex count is the file's; read it first so read_state can compare the rest
+        uint32_t V = 0;
+        char magic[8];
+        uint32_t ver = 0;
+        if (fread(magic, 1, 8, f) != 8 || fread(&ver, 4, 1, f) != 1 || fread(&V, 4, 1, f) != 1) st = GRG_E_IO;
+        fseek(f, 0, SEEK_SET);
+        p->V = V;
+        if (!st) st = read_state(p, f, size);
+    }
+    fclose(f);
+    if (st) {
+        delete p;
+        return st;
+    }
+    *out = p;
+    return GRG_OK;
+}
+
+int grg_part_set_checkpoint(grg_part *p, const char *path, uint32_t every_runs)
+{
+    if (!p) return GRG_E_ARG;
+    p->ckpt_path = path ? path : "";
+    p->ckpt_every = path ? every_runs : 0;
+    return GRG_OK;
+}
+
+int grg_part_set_run_budget(grg_part *p, uint64_t max_runs)
+{
+    if (!p) return GRG_E_ARG;
+    p->run_budget = max_runs;
     return GRG_OK;
 }
 

@@ -18,6 +18,7 @@ COMP_PATH = os.path.join(HERE, "_build", "comp")
 
 OK = 0
 NEED_REPARTITION = 1
+PAUSED = 2
 E_ARG, E_CUDA, E_NOMEM, E_FILTER, E_IO, E_LABEL, E_RANGE, E_STATE, E_NODEV = -1, -2, -3, -4, -5, -6, -7, -8, -9
 MAX_RULES = 64
 MAX_LABELS = 63
@@ -33,6 +34,7 @@ EXPORTS = (
     "grg_load_elements", "grg_export_elements", "grg_range_counts", "grg_set_pool_limit", "grg_part_create",
     "grg_part_destroy", "grg_part_load_edges", "grg_part_run", "grg_part_label_counts", "grg_part_bounds",
     "grg_set_device_rounds", "grg_range_reach", "grg_set_join_window", "grg_export_csr5", "grg_load_csr5",
+    "grg_part_export_csr5", "grg_part_save", "grg_part_restore", "grg_part_set_checkpoint", "grg_part_set_run_budget",
 )
 
 
@@ -132,6 +134,11 @@ def load_library(path: str = LIB_PATH):
     L.grg_part_run.argtypes = [P, U32, ctypes.POINTER(PartStats)]
     L.grg_part_label_counts.argtypes = [P, P, ctypes.POINTER(U64)]
     L.grg_part_bounds.argtypes = [P, U32, P, ctypes.POINTER(U32)]
+    L.grg_part_export_csr5.argtypes = [P, U32, U64, P, P, ctypes.POINTER(U64)]
+    L.grg_part_save.argtypes = [P, ctypes.c_char_p]
+    L.grg_part_restore.argtypes = [ctypes.POINTER(P), P, ctypes.c_char_p]
+    L.grg_part_set_checkpoint.argtypes = [P, ctypes.c_char_p, U32]
+    L.grg_part_set_run_budget.argtypes = [P, U64]
     _lib = L
     return L
 
@@ -384,12 +391,18 @@ class Partitioned:
     """Out-of-core closure over vertex-range partitions (grg_part_*) on a
     context that holds the grammar (and, optionally, a pool limit)."""
 
-    def __init__(self, ctx: Context, num_vars: int, num_parts: int):
+    def __init__(self, ctx: Context, num_vars: int, num_parts: int, restore_from: str | None = None):
+        """num_parts equal vertex ranges; or, with restore_from, the partition set
+        saved in that checkpoint file (num_vars and num_parts are then ignored)."""
         self.ctx = ctx
         self.num_vars = num_vars
         h = ctypes.c_void_p()
-        ctx._check(ctx._L.grg_part_create(ctypes.byref(h), ctx._h, num_vars, num_parts), "part_create")
+        if restore_from is not None:
+            ctx._check(ctx._L.grg_part_restore(ctypes.byref(h), ctx._h, os.fsencode(restore_from)), "part_restore")
+        else:
+            ctx._check(ctx._L.grg_part_create(ctypes.byref(h), ctx._h, num_vars, num_parts), "part_create")
         self._h = h
+        self.paused = False
 
     def close(self):
         if getattr(self, "_h", None):
@@ -407,9 +420,36 @@ class Partitioned:
                         "part_load_edges")
 
     def run(self, filter_flag: int) -> dict:
+        """This call's statistics; self.paused tells whether the run budget stopped it."""
         s = PartStats()
-        self.ctx._check(self.ctx._L.grg_part_run(self._h, filter_flag, ctypes.byref(s)), "part_run")
+        st = self.ctx._L.grg_part_run(self._h, filter_flag, ctypes.byref(s))
+        if st != PAUSED:
+            self.ctx._check(st, "part_run")
+        self.paused = st == PAUSED
         return s.as_dict()
+
+    def save(self, path: str):
+        self.ctx._check(self.ctx._L.grg_part_save(self._h, os.fsencode(path)), "part_save")
+
+    def set_checkpoint(self, path: str | None, every_runs: int = 1):
+        self.ctx._check(self.ctx._L.grg_part_set_checkpoint(self._h, os.fsencode(path) if path else None,
+                                                            every_runs), "part_set_checkpoint")
+
+    def set_run_budget(self, max_runs: int):
+        self.ctx._check(self.ctx._L.grg_part_set_run_budget(self._h, max_runs), "part_set_run_budget")
+
+    def export_csr5(self, index: int):
+        """Partition index's rows as the compressed edge stream (closed sets)."""
+        n = ctypes.c_uint64()
+        st = self.ctx._L.grg_part_export_csr5(self._h, index, 0, None, None, ctypes.byref(n))
+        if st not in (OK, E_RANGE):
+            self.ctx._check(st, "part_export_csr5")
+        b = self.bounds()
+        out = np.zeros(n.value * 5, np.uint8)
+        deg = np.zeros(int(b[index + 1] - b[index]), np.uint32)
+        self.ctx._check(self.ctx._L.grg_part_export_csr5(self._h, index, n.value, _ptr(out), _ptr(deg),
+                                                         ctypes.byref(n)), "part_export_csr5")
+        return out, deg
 
     def label_counts(self):
         counts = np.zeros(self.ctx.num_labels, dtype=np.uint64)

@@ -26,6 +26,7 @@ extern "C" {
 /* status codes */
 #define GRG_OK 0
 #define GRG_NEED_REPARTITION 1   /* partition does not fit its budget (the reference's r=true, src/kernel.cu:65-76) */
+#define GRG_PAUSED 2             /* grg_part_run stopped at its run budget; call it again to continue */
 #define GRG_E_ARG (-1)           /* invalid argument */
 #define GRG_E_CUDA (-2)          /* CUDA runtime error (see grg_last_error) */
 #define GRG_E_NOMEM (-3)         /* device or host memory exhausted */
@@ -208,11 +209,16 @@ int grg_set_pool_limit(grg_ctx *ctx, uint64_t pool_bytes);
 int grg_export_csr5(grg_ctx *ctx, uint32_t v_begin, uint32_t v_end, uint64_t cap, uint8_t *edges,
                     uint32_t *degree, uint64_t *num_edges);
 /* Load a graph over [0, num_vars) from a stream of num_edges edges whose source
- * rows are [v_begin, v_end) with row lengths degree (v_end - v_begin values);
- * expanded on the device, then loaded as grg_load_edges loads edges (epsilon
- * rules applied, duplicates collapse). Lengths that do not add up to num_edges
- * fail with GRG_E_ARG, labels outside 1..L with GRG_E_LABEL, destinations >=
- * num_vars with GRG_E_RANGE. on_device as for grg_load_edges (both arrays). */
+ * rows are [v_begin, v_end) with row lengths degree (v_end - v_begin values),
+ * as readElements_c reloads a spilled partition: the stream becomes element
+ * records on the device (consecutive edges of a row with one label and 192-id
+ * base share a record), loaded as grg_load_elements loads them with every
+ * record a delta of round 1; epsilon rules are not applied (a spilled image
+ * holds its epsilon edges). Each row's edges must be in the stream's order
+ * (label, then destination): a record that repeats fails with GRG_E_ARG, as do
+ * lengths that do not add up to num_edges; labels outside 1..L fail with
+ * GRG_E_LABEL, destinations >= num_vars with GRG_E_RANGE. on_device as for
+ * grg_load_edges (both arrays). */
 int grg_load_csr5(grg_ctx *ctx, uint32_t num_vars, uint32_t v_begin, uint32_t v_end, const uint32_t *degree,
                   uint64_t num_edges, const uint8_t *edges, int on_device);
 
@@ -255,13 +261,42 @@ void grg_part_destroy(grg_part *part);
  * partition images on the device one partition at a time. */
 int grg_part_load_edges(grg_part *part, uint64_t num_edges, const uint32_t *src, const uint32_t *dst,
                         const uint8_t *label);
-/* Close the graph (filter as for grg_closure). stats may be NULL. */
+/* Close the graph (filter as for grg_closure). stats may be NULL; they count
+ * this call's work. GRG_PAUSED when the run budget stopped it. */
 int grg_part_run(grg_part *part, uint32_t filter, grg_part_stats *stats);
 /* Per-label closure edge counts (num_labels values) and the edge-set hash
  * (may be NULL), equal to grg_label_counts / grg_set_hash of the in-core closure. */
 int grg_part_label_counts(grg_part *part, uint64_t *counts, uint64_t *hash);
 /* Current partition bounds: bounds[0..num_parts] (cap entries at most). */
 int grg_part_bounds(grg_part *part, uint32_t cap, uint32_t *bounds, uint32_t *num_parts);
+/* Rows of partition index (0-based, in bound order) of a closed set as the
+ * compressed edge stream (grg_export_csr5 conventions, rows [bounds[index],
+ * bounds[index+1])): the reference's per-partition spill file of
+ * storeElements_c (src/main.cpp:541-596). The image is loaded on the device. */
+int grg_part_export_csr5(grg_part *part, uint32_t index, uint64_t cap, uint8_t *edges, uint32_t *degree,
+                         uint64_t *num_edges);
+
+/* Checkpoint / resume. The reference keeps no superstep state (its spill files
+ * hold pools only, src/main.cpp:447-456), so an interrupted run starts over.
+ * Here the whole partition set -- bounds, images with stamps, the pairs each
+ * run closed, run counters -- is written to one file, and a new process
+ * continues from it. */
+
+/* Write the state to path (written to path + ".tmp", then renamed over path). */
+int grg_part_save(grg_part *part, const char *path);
+/* A partition set rebuilt from a file written by grg_part_save, on a context
+ * with the same grammar. An open set continues on grg_part_run (with the
+ * filter of the interrupted run), a closed one answers grg_part_label_counts.
+ * A file that is short, corrupt (checksum) or of another grammar or vertex
+ * count fails with GRG_E_IO. */
+int grg_part_restore(grg_part **part, grg_ctx *ctx, const char *path);
+/* During grg_part_run, save to path after every `every_runs` device runs (0 =
+ * never) and when the run budget stops it. */
+int grg_part_set_checkpoint(grg_part *part, const char *path, uint32_t every_runs);
+/* Stop grg_part_run with GRG_PAUSED once it has made max_runs device runs in
+ * that call (0 = no budget): a time slice for a shared device, or a stop
+ * between runs with nothing in flight. */
+int grg_part_set_run_budget(grg_part *part, uint64_t max_runs);
 
 /* Text formats (host). Grammar: readAndTransferRules (src/main.cpp:60-97);
  * names must hold GRG_MAX_LABELS*GRG_NAME_LEN bytes, label l at

@@ -52,7 +52,8 @@ def test_random_grammars_export(grg_mod, oracle_mod):
 
 
 def test_load_of_input_stream_equals_load_of_edges(grg_mod, oracle_mod):
-    w = G.pointsto(seed=44, num_vars=800, num_edges=2200)
+    # a grammar without epsilon rules: the stream load applies none (a spilled image holds its own)
+    w = G.alias(seed=44, num_vars=1600, num_base_edges=4000, block=400)
     want = oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, 0, w.src, w.dst, w.lab)
     stream, deg = pack_csr5(w.src, w.dst, w.lab, 0, w.num_vars)
     ctx = grg_mod.Context(0)
@@ -68,7 +69,8 @@ def test_load_of_input_stream_equals_load_of_edges(grg_mod, oracle_mod):
 
 
 def test_closed_stream_reloads_to_the_same_fixpoint(grg_mod, oracle_mod):
-    w = G.alias(seed=45, num_vars=2000, num_base_edges=5000, block=500)
+    # the points-to grammar has epsilon rules: the closed stream carries their edges
+    w = G.pointsto(seed=45, num_vars=900, num_edges=2400)
     want = oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, 0, w.src, w.dst, w.lab)
     ctx = closed_context(grg_mod, w, 0)
     stream, deg = ctx.export_csr5()
@@ -84,7 +86,7 @@ def test_closed_stream_reloads_to_the_same_fixpoint(grg_mod, oracle_mod):
 
 def test_partial_range_stream(grg_mod):
     # the stream of rows [a, b) holds exactly the input edges leaving those rows
-    w = G.dataflow_small(seed=46, num_vars=1200, num_edges=3600)
+    w = G.alias(seed=46, num_vars=1200, num_base_edges=3600, block=400)
     a, b = 300, 700
     stream, deg = pack_csr5(w.src, w.dst, w.lab, a, b)
     ctx = grg_mod.Context(0)
@@ -123,6 +125,13 @@ def test_invalid_streams_are_refused(grg_mod):
     with pytest.raises(grg_mod.GrgError) as ei:
         ctx.load_csr5(w.num_vars, s3.reshape(-1), deg)
     assert ei.value.status == grg_mod.E_RANGE
+    # a row whose edges are out of order splits a record in two: refused as a repeat
+    def rec(dst, lab):
+        return list(np.frombuffer(np.uint32(dst).tobytes(), np.uint8)) + [lab]
+    s4 = np.array(rec(1, 1) + rec(3, 2) + rec(2, 1), np.uint8)
+    with pytest.raises(grg_mod.GrgError) as ei:
+        ctx.load_csr5(w.num_vars, s4, np.array([3], np.uint32))
+    assert ei.value.status == grg_mod.E_ARG
     # the context still loads and closes a valid stream
     ctx.load_csr5(w.num_vars, stream, deg)
     ctx.closure(0)
