@@ -539,6 +539,7 @@ struct __align__(16) WarpSmemT {
     uint32_t rC[RB];              // per record: right operand label
     uint32_t rOff[RB];            // per record: 1 = virtual old-left record
     uint32_t kpre[RB + 1];        // exclusive prefix of per-record task counts
+    uint8_t own[32];              // per chunk of 32 tasks (items): lane whose record (task) starts there
     uint32_t acc_n;
     uint32_t fail;                // records with a failed insert (retry after growth)
 };
@@ -584,16 +585,25 @@ __device__ __forceinline__ uint32_t warp_tasks(WS &w, uint32_t cnt)
     return total;
 }
 
-// Record owning flattened task t: largest r with kpre[r] <= t.
+// Owner of position `lane` of a chunk of 32 flattened tasks (or items): every
+// lane whose run of positions starts in the chunk (starts, at offset pos) marks
+// it; a position belongs to the highest mark at or below it, or to `carry`
+// (the owner running into the chunk) when there is none. carry is updated to
+// the owner of the chunk's last position. Warp-uniform; one OR-reduction and
+// one shared-memory read instead of a 5-step dependent search.
 template <class WS>
-__device__ __forceinline__ uint32_t task_record(const WS &w, uint32_t t)
+__device__ __forceinline__ uint32_t chunk_owner(WS &w, bool starts, uint32_t pos, uint32_t &carry)
 {
-    uint32_t lo = 0, hi = RB - 1;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi + 1) >> 1;
-        if (w.kpre[mid] <= t) lo = mid; else hi = mid - 1;
-    }
-    return lo;
+    const uint32_t lane = lane_id();
+    if (starts) w.own[pos] = (uint8_t)lane;
+    const uint32_t m = __reduce_or_sync(0xffffffffu, starts ? 1u << pos : 0u);
+    __syncwarp();
+    const uint32_t below = m & (0xFFFFFFFFu >> (31 - lane));
+    const uint32_t o = below ? w.own[31 - __clz(below)] : carry;
+    const uint32_t last = m ? w.own[31 - __clz(m)] : carry;
+    __syncwarp();
+    carry = last;
+    return o;
 }
 
 // OR (key, b) into the warp's hash accumulator; false when it is full.
@@ -898,15 +908,22 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : 4))
             w.rA[lane] = !hr ? 0 : virt ? c_rt.ol_A[q] : c_rt.bin_A[q];
             w.rC[lane] = !hr ? 0 : virt ? c_rt.ol_C[q] : c_rt.bin_C[q];
             n_left += hr;
-            const uint32_t total = warp_tasks(w, hr ? nbits : 0);
+            const uint32_t my_cnt = hr ? nbits : 0;
+            const uint32_t total = warp_tasks(w, my_cnt);
+            const uint32_t my_st = w.kpre[lane];
+            uint32_t carry_r = 0;
             for (uint32_t t0 = 0; t0 < total; t0 += 32) {
-                // task (record r, intermediate k) -> items of row C[k]
+                // task (record r, intermediate k) -> items of row C[k]. The record of task t
+                // is the last record that starts at or before t: records starting in this
+                // chunk mark their start position, a lane takes the highest mark at or below it
                 const uint32_t t = t0 + lane;
+                const uint32_t rr = chunk_owner(w, my_cnt != 0 && my_st - t0 < 32u, my_st - t0, carry_r);
+                const uint32_t r_st = __shfl_sync(0xffffffffu, my_st, rr);
                 uint32_t r = 0, C = 0, beg = 0, cnt = 0, csr = 0;   // csr: item source 0 table, 1 CSR, 2 delta records
                 if (t < total) {
-                    r = task_record(w, t);
+                    r = rr;
                     C = w.rC[r];
-                    const uint32_t k = w.rbase[r] * EIDS + select_bit(w.rbits[r], t - w.kpre[r]);
+                    const uint32_t k = w.rbase[r] * EIDS + select_bit(w.rbits[r], t - r_st);
                     const uint2 *cr = c_rt.csr_row[C];
                     if (w.rOff[r]) {
                         const size_t ti = (size_t)(C - 1) * d.V + k;
@@ -996,15 +1013,12 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : 4))
                 // per task: item f sits at beg + 1 + f - (first f of the task); record, label and source packed
                 const uint32_t adj = beg + 1 - (incl - cnt1);
                 const uint32_t pk = r | (C << 8) | (csr << 16);
+                const uint32_t s1 = incl - cnt1;             // the task's first flattened item
+                uint32_t carry_o = 0;
                 for (uint32_t f0 = 0; f0 < nitems; f0 += 32) {
                     const uint32_t f = f0 + lane;
-                    // owner lane: smallest o with incl(o) > f
-                    uint32_t lo = 0;
-#pragma unroll
-                    for (int st = 16; st; st >>= 1) {
-                        const uint32_t v = __shfl_sync(0xffffffffu, incl, lo + st - 1);
-                        if (v <= f) lo += st;
-                    }
+                    // owner lane: the last task whose items start at or before f
+                    const uint32_t lo = chunk_owner(w, cnt1 != 0 && s1 - f0 < 32u, s1 - f0, carry_o);
                     const uint32_t o_adj = __shfl_sync(0xffffffffu, adj, lo);
                     const uint32_t o_pk = __shfl_sync(0xffffffffu, pk, lo);
                     do_item(f < nitems, o_pk & 0xFFu, (o_pk >> 8) & 0xFFu, o_pk >> 16, f + o_adj);
