@@ -103,6 +103,9 @@ static int make_rule_table(const int *rules, int R, int L, uint32_t filter, Rule
 #ifndef GRG_JOIN_MINB
 #define GRG_JOIN_MINB 6
 #endif
+#ifndef GRG_JOIN_MINB_WIDE
+#define GRG_JOIN_MINB_WIDE 5
+#endif
 #ifdef GRG_PHASE_TIMERS
 #define PH_MARK(i)                                   \
     do {                                             \
@@ -118,10 +121,10 @@ constexpr int RB = 32;            // delta records per warp batch (one per lane)
 constexpr int WIN = GRG_WIN;      // dense accumulator window: elements base-WIN_LO .. base+WIN-1-WIN_LO
 constexpr int WIN_LO = GRG_WIN_LO;
 #ifndef GRG_WIN2
-#define GRG_WIN2 12
+#define GRG_WIN2 10
 #endif
 #ifndef GRG_WIN2_LO
-#define GRG_WIN2_LO 6
+#define GRG_WIN2_LO 4
 #endif
 constexpr int WIN2 = GRG_WIN2;    // wide window: rows whose destinations spread over many elements
 constexpr int WIN2_LO = GRG_WIN2_LO;
@@ -828,7 +831,7 @@ __global__ void k_split(Dev d, const uint4 *__restrict__ grecs, const uint4 *__r
 // n_ctr >= 0: the record count is device counter n_ctr (round graphs).
 // W, LO: the dense window (instantiated for narrow and wide rows; see join_wide).
 template <int W, int LO>
-__global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : 4))
+__global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG_JOIN_MINB_WIDE))
     k_join(Dev d, const uint4 *__restrict__ recs, uint64_t n, int n_ctr, uint4 *retry_out)
 {
     constexpr int WIN = W, WIN_LO = LO;
@@ -2295,9 +2298,11 @@ __global__ void k_tmark(unsigned long long *ctr, int t0_slot, int acc_slot, int 
 // device-driven loop hands back can be finished where it stopped.
 
 // Window of this closure's joins. Measured on dataflow, alias, points-to and
-// small alias jobs, the 12-element window (with the registers its launch
-// bounds leave) was fastest or within 1.5% on every one, so it is the default;
-// the narrow window stays selectable.
+// small alias jobs, the wide window was fastest or within 1.5% on every one, so
+// it is the default; the narrow window stays selectable. Wide is 10 elements
+// (4 below the record's base) at 5 blocks per SM: 44 KB of shared memory per
+// block; 12 elements fit only 4 blocks and were 1.5% slower on the dataflow
+// and alias closures, 8 elements (6 blocks) 11% slower.
 static void choose_window(grg_ctx *c) { c->join_wide = c->join_window_mode != 0; }
 
 // The join kernel in the window chosen for this closure (join_wide).

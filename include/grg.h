@@ -94,7 +94,7 @@ int grg_set_kernel_timing(grg_ctx *ctx, int on);
  * round. The results are identical either way. */
 int grg_set_device_rounds(grg_ctx *ctx, int on);
 /* Join window: the join ORs right-hand elements into a dense per-record window
- * of 12 elements (mode 1, the default) or 8 (mode 0); elements outside it go to
+ * of 10 elements (mode 1, the default) or 8 (mode 0); elements outside it go to
  * a small shared-memory hash. Environment GRG_JOIN_WINDOW=narrow selects 8.
  * Results are identical either way. */
 int grg_set_join_window(grg_ctx *ctx, int mode);
