@@ -170,13 +170,14 @@ __device__ __forceinline__ uint64_t edge_hash(uint32_t l, uint32_t s, uint32_t d
 
 // OR `b` into the element in pool slot s. With `track`, the bits that were new
 // go to its delta bitmap and its dirty bit is set (both without waiting).
-__device__ __forceinline__ bool g_or_into(const Dev &d, uint32_t s, const Bits b, bool track)
+// OR `b` into slot s whose bitmap words were read as c0 (words 0-3) and c1.x/.y
+// (words 4-5). Words whose candidate bits are all present already need no
+// atomic: bits are only ever set during a round, so a stale read can only show
+// fewer of them.
+__device__ __forceinline__ bool g_or_cur(const Dev &d, uint32_t s, const Bits b, bool track, const uint4 c0,
+                                         const uint4 c1)
 {
     uint32_t *e = d.elems + (size_t)s * 8;
-    // words whose candidate bits are all present already need no atomic: bits are
-    // only ever set during a round, so a stale read can only show fewer of them
-    const uint4 c0 = __ldcg(reinterpret_cast<const uint4 *>(e));
-    const uint2 c1 = __ldcg(reinterpret_cast<const uint2 *>(e + 4));
     const uint32_t cur[EW] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y};
     Bits nb;
     uint32_t any = 0;
@@ -199,37 +200,62 @@ __device__ __forceinline__ bool g_or_into(const Dev &d, uint32_t s, const Bits b
     return true;
 }
 
+__device__ __forceinline__ bool g_or_into(const Dev &d, uint32_t s, const Bits b, bool track)
+{
+    const uint32_t *e = d.elems + (size_t)s * 8;
+    return g_or_cur(d, s, b, track, __ldcg(reinterpret_cast<const uint4 *>(e)),
+                    __ldcg(reinterpret_cast<const uint4 *>(e + 4)));
+}
+
 // OR `b` into element (slot, row, base). Returns false when the table is full
 // or absent; the failure is recorded so the table grows before a retry. With
 // `track`, the bits that were new are ORed into the element's delta bitmap and
-// its dirty bit is set (both without waiting for a reply).
-__device__ __forceinline__ bool g_insert(const Dev &d, uint32_t slot, uint32_t row, uint32_t base, const Bits b,
-                                         bool track)
+// its dirty bit is set (both without waiting for a reply). WHOLE: a probe of a
+// hashed table reads the whole 32-byte element (one sector), so a key found at
+// its probe brings the bitmap words for the pre-check without a second round
+// trip (prefix-filled tables, scanned from slot 0, read keys only).
+template <bool WHOLE>
+__device__ __forceinline__ bool g_insert_t(const Dev &d, uint32_t slot, uint32_t row, uint32_t base, const Bits b,
+                                           bool track)
 {
     const size_t ti = (size_t)(slot - 1) * d.V + row;
     const uint64_t de = d.desc[ti];
     const uint32_t off = (uint32_t)de, cap = (uint32_t)(de >> 32);
     const uint32_t key = (slot << KEY_SHIFT) | base;
     uint32_t s = EMPTY;
+    bool have = false;                        // c0 / c1 hold slot s's bitmap words (or zeros)
+    uint4 c0 = make_uint4(0, 0, 0, 0), c1 = make_uint4(0, 0, 0, 0);
     if (cap != 0 && (cap & (cap - 1)) == 0) {
         const uint32_t h = table_start(d, slot, base, cap), lim = table_limit(d, slot, cap);
+        const bool whole = WHOLE && !prefix_table(d, slot, cap);
         for (uint32_t p = 0; p < cap; p++) {
             const uint32_t q = off + ((h + p) & (cap - 1));
             uint32_t *kp = d.elems + (size_t)q * 8 + 6;
-            const uint32_t k = __ldcg(kp);
-            if (k == key) { s = q; break; }
+            uint32_t k;
+            if (whole) {
+                c0 = __ldcg(reinterpret_cast<const uint4 *>(d.elems + (size_t)q * 8));
+                c1 = __ldcg(reinterpret_cast<const uint4 *>(d.elems + (size_t)q * 8 + 4));
+                k = c1.z;
+            } else {
+                k = __ldcg(kp);
+            }
+            if (k == key) { s = q; have = whole; break; }
             if (k != EMPTY) continue;
             if (atomicAdd(&d.cnt[ti], 1u) >= lim) { atomicSub(&d.cnt[ti], 1u); break; }
             const uint32_t prev = atomicCAS(kp, EMPTY, key);
+            // a slot claimed here, or by a concurrent insert of the same key, is ORed
+            // into without a pre-check (its words read as zero)
+            c0 = c1 = make_uint4(0, 0, 0, 0);
             if (prev == EMPTY) {
                 d.elems[(size_t)q * 8 + 7] = row;
                 // the delta bitmap's spare words carry the slot's key and row for the gather
                 reinterpret_cast<uint2 *>(d.dbits + (size_t)q * 8)[3] = make_uint2(key, row);
                 s = q;
+                have = true;
                 break;
             }
             atomicSub(&d.cnt[ti], 1u);
-            if (prev == key) { s = q; break; }
+            if (prev == key) { s = q; have = true; break; }
         }
     }
     if (s == EMPTY) {
@@ -239,7 +265,13 @@ __device__ __forceinline__ bool g_insert(const Dev &d, uint32_t slot, uint32_t r
         }
         return false;
     }
-    return g_or_into(d, s, b, track);
+    return have ? g_or_cur(d, s, b, track, c0, c1) : g_or_into(d, s, b, track);
+}
+
+__device__ __forceinline__ bool g_insert(const Dev &d, uint32_t slot, uint32_t row, uint32_t base, const Bits b,
+                                         bool track)
+{
+    return g_insert_t<false>(d, slot, row, base, b, track);
 }
 
 }  // namespace grg

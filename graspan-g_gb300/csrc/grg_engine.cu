@@ -748,7 +748,7 @@ __device__ __forceinline__ void win_flush(const Dev &d, WS &w, uint32_t &inserts
 // Insert candidate elements (label, row, base, bits) written by k_join. One
 // thread per candidate: thousands of independent insert chains per SM.
 // Candidates whose table is full go to fail_out (C_AFAIL) for a retry after growth.
-__global__ void __launch_bounds__(256) k_apply(Dev d, const uint4 *__restrict__ cand, uint4 *fail_out)
+__global__ void __launch_bounds__(256, 8) k_apply(Dev d, const uint4 *__restrict__ cand, uint4 *fail_out)
 {
     if (d.ctr[C_HALT]) return;
     // the candidate count is read on the device, so the host need not wait for the join
@@ -759,7 +759,7 @@ __global__ void __launch_bounds__(256) k_apply(Dev d, const uint4 *__restrict__ 
         Bits bits;
         bits.w[0] = a.x; bits.w[1] = a.y; bits.w[2] = a.z; bits.w[3] = a.w; bits.w[4] = b.x; bits.w[5] = b.y;
         const uint32_t A = b.z >> KEY_SHIFT;
-        if (!g_insert(d, A, b.w, b.z & BASE_MASK, bits, c_rt.track[A])) {
+        if (!g_insert_t<true>(d, A, b.w, b.z & BASE_MASK, bits, c_rt.track[A])) {
             const unsigned long long f = atomicAdd(&d.ctr[C_AFAIL], 1ull);
             fail_out[2 * f] = a;
             fail_out[2 * f + 1] = b;
