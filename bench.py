@@ -26,8 +26,8 @@ closure in-core, and out-of-core over 64 vertex-range partitions staged
 through host memory), `stream_c2` (the dataflow closure exported as the
 compressed 5-byte-per-edge stream into page-locked host memory and loaded
 back), `out_of_core_c2` (the dataflow closure under a pool limit of a quarter
-of what it needs in-core), and `serving` (the 512-job mix: continuous
-batching vs one graph at a time).
+of what it needs in-core, and its checkpoint saved and restored), and
+`serving` (the 512-job mix: continuous batching vs one graph at a time).
 
 Multi-GPU: the closure of one graph does not shard without an exchange step,
 so N GPUs run N independent replicas (one per rank, weak scaling).
@@ -180,7 +180,10 @@ def _closure_once(grg, ctx, w, f):
     return st, [int(x) for x in ctx.label_counts()], ctx.set_hash()
 
 
-def _partitioned(grg, w, f, parts, pool_bytes=0):
+def _partitioned(grg, w, f, parts, pool_bytes=0, checkpoint=None):
+    """Out-of-core closure; with `checkpoint` (a dict), the closed set is also
+    saved to a file and restored into a new context, timed, and the restored
+    counts checked."""
     ctx = grg.Context(0)
     ctx.transfer_rules(w.rule_ids(), w.num_labels)
     if pool_bytes:
@@ -191,6 +194,29 @@ def _partitioned(grg, w, f, parts, pool_bytes=0):
     t_load = time.perf_counter() - t
     st = p.run(f)
     counts, h = p.label_counts()
+    if checkpoint is not None:
+        import tempfile
+        fd, path = tempfile.mkstemp(suffix=".grgpart")
+        os.close(fd)
+        try:
+            t = time.perf_counter()
+            p.save(path)
+            t_save = time.perf_counter() - t
+            size = os.path.getsize(path)
+            ctx2 = grg.Context(0)
+            ctx2.transfer_rules(w.rule_ids(), w.num_labels)
+            t = time.perf_counter()
+            p2 = grg.Partitioned(ctx2, 0, 0, restore_from=path)
+            t_restore = time.perf_counter() - t
+            c2, h2 = p2.label_counts()
+            p2.close()
+            ctx2.close()
+        finally:
+            os.remove(path)
+        assert ([int(x) for x in c2], h2) == ([int(x) for x in counts], h), "restored set differs"
+        checkpoint.update({"file_bytes": size, "save_s": t_save, "restore_s": t_restore,
+                           "save_gbs": size / t_save / 1e9, "restore_gbs": size / t_restore / 1e9,
+                           "restored_counts_identical": True})
     p.close()
     ctx.close()
     return st, [int(x) for x in counts], h, t_load
@@ -281,13 +307,14 @@ def extra_measurements(args, w2):
     ctx.close()
     out["stream_c2"] = dict(workload=WORKLOAD, **_stream_measurement(grg, w2, w2.filter_flag, c2_counts, c2_hash))
     limit = st["pool_elems_used"] * 69 // 4
-    pst, p_counts, p_hash, t_load = _partitioned(grg, w2, w2.filter_flag, 4, limit)
+    ck = {}
+    pst, p_counts, p_hash, t_load = _partitioned(grg, w2, w2.filter_flag, 4, limit, checkpoint=ck)
     assert (p_counts, p_hash) == (c2_counts, c2_hash), "partitioned C2 differs from in-core"
     out["out_of_core_c2"] = {"workload": WORKLOAD, "pool_limit_bytes": limit, "partitions": pst["num_parts"],
                              "splits": pst["splits"], "schedule": pst["schedule"], "runs": pst["runs"],
                              "load_s": t_load, "run_ms": pst["ms"],
                              "value": pst["total_edges"] / (pst["ms"] * 1e-3), "unit": UNIT,
-                             "identical_to_in_core": True}
+                             "identical_to_in_core": True, "checkpoint": ck}
     return out
 
 
