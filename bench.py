@@ -465,7 +465,10 @@ def main():
                        "gather_ms": statistics.mean(x["gather_ms"] for x in stats),
                        "join_launches": s["join_launches"], "retry_records": s["retry_records"],
                        "grow_rows": s["grow_rows"], "delta_elems": s["delta_elems"],
-                       "pool_elems_used": s["pool_elems_used"]},
+                       "pool_elems_used": s["pool_elems_used"],
+                       "join_window": ("wide (10 elements)" if s["wide_window"] else "narrow (8 elements)") +
+                       {0: ", fixed", 1: ", measured in this step", 2: ", tuned (degree-key cache)"}[
+                           int(s["window_tuned"])]},
             "e2e": {"value": world * total / (e2e_max * 1e-3), "unit": UNIT,
                     "h2d_bytes_per_step": int(w.num_edges * 9), "d2h_bytes_per_step": int(w.num_labels * 8)},
             "roofline": {"bound": "hbm", "kernel": "join pass (k_join + k_apply)", "achieved": achieved, "peak": hbm,

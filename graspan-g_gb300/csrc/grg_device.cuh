@@ -68,7 +68,8 @@ enum : int {
     C_GT0 = C_LABEL0 + MAX_SLOTS + 8,   // start time of the current gather (kernel timing)
     C_GNS = C_LABEL0 + MAX_SLOTS + 9,   // gather nanoseconds (kernel timing)
     C_BADIN = C_LABEL0 + MAX_SLOTS + 10, // input edges refused: ERR_IN_LABEL / ERR_IN_RANGE bits
-    NCTR = C_LABEL0 + MAX_SLOTS + 11
+    C_DH0 = C_LABEL0 + MAX_SLOTS + 11,   // 8 counters: tables by log2 of their elements (tuning key)
+    NCTR = C_LABEL0 + MAX_SLOTS + 19
 };
 // error bits of C_ERR; ERR_IN_* (in C_BADIN) flag input edges that were refused
 // (label outside 1..L, vertex id outside the graph) and never touched a table

@@ -20,6 +20,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1069,6 +1071,23 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
     }
 }
 
+// Tables of labels 1..L by log2 of their occupied elements (buckets 0..7, the
+// last open-ended) into C_DH0..C_DH0+7: the degree distribution that keys the
+// join-window tuning.
+__global__ void k_degree_hist(Dev d, uint32_t L)
+{
+    __shared__ unsigned long long h[8];
+    if (threadIdx.x < 8) h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint64_t nt = (uint64_t)L * d.V;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < nt; t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = d.cnt[t];
+        if (c) atomicAdd(&h[min(31 - __clz(c), 7)], 1ull);
+    }
+    __syncthreads();
+    if (threadIdx.x < 8 && h[threadIdx.x]) atomicAdd(&d.ctr[C_DH0 + threadIdx.x], h[threadIdx.x]);
+}
+
 // ------------------------------------------------------------ CSR of static rows
 
 // Edges per row of a packed (static) label: deg[v], and row[v].y = deg | min(elements,255) << 24.
@@ -1569,7 +1588,13 @@ struct grg_ctx {
     uint64_t prefix_mask = 0;              // labels with prefix-filled small tables (Dev::prefix_mask)
     // join window: narrow (WIN) or wide (WIN2, the default)
     bool join_wide = true;
-    int join_window_mode = 1;              // 0 = narrow, 1 = wide
+    int join_window_mode = 2;              // 0 narrow, 1 wide, 2 tuned per degree key, 3 re-measured
+    bool tuned_wide = true;                // the tuned choice for the current closure
+    bool tune_pending = false;             // measure both windows in the first large round
+    uint64_t tune_key = 0;
+    int tune_source = 0;                   // grg_stats.window_tuned
+    float tune_ms[2] = {0, 0};
+    cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
     // device-driven rounds: a CUDA graph whose WHILE node repeats one closure round
     bool device_rounds = true;
     cudaStream_t cap_stream = nullptr;     // stream the round graph is recorded on
@@ -1921,7 +1946,7 @@ int grg_create(grg_ctx **out, int device)
     const char *rr = getenv("GRG_RETRY_ROOM");         // smallest retry list, in records
     if (rr && atoll(rr) > 0) c->retry_min = (uint64_t)atoll(rr);
     const char *jw = getenv("GRG_JOIN_WINDOW");        // "narrow" / "wide"; otherwise chosen per closure
-    if (jw) c->join_window_mode = !strcmp(jw, "narrow") ? 0 : 1;
+    if (jw) c->join_window_mode = !strcmp(jw, "narrow") ? 0 : !strcmp(jw, "wide") ? 1 : 2;
     *out = c;
     return GRG_OK;
 }
@@ -1951,6 +1976,8 @@ void grg_destroy(grg_ctx *c)
     if (c->ev_b) cudaEventDestroy(c->ev_b);
     if (c->ev_c) cudaEventDestroy(c->ev_c);
     if (c->ev_d) cudaEventDestroy(c->ev_d);
+    if (c->ev_t0) cudaEventDestroy(c->ev_t0);
+    if (c->ev_t1) cudaEventDestroy(c->ev_t1);
     free_round_graph(c);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -1968,7 +1995,7 @@ int grg_set_stream(grg_ctx *c, void *stream)
 
 int grg_set_join_window(grg_ctx *c, int mode)
 {
-    if (!c || mode < 0 || mode > 1) return GRG_E_ARG;
+    if (!c || mode < 0 || mode > 3) return GRG_E_ARG;
     c->join_window_mode = mode;
     return GRG_OK;
 }
@@ -2303,7 +2330,10 @@ __global__ void k_tmark(unsigned long long *ctr, int t0_slot, int acc_slot, int 
 // (4 below the record's base) at 5 blocks per SM: 44 KB of shared memory per
 // block; 12 elements fit only 4 blocks and were 1.5% slower on the dataflow
 // and alias closures, 8 elements (6 blocks) 11% slower.
-static void choose_window(grg_ctx *c) { c->join_wide = c->join_window_mode != 0; }
+static void choose_window(grg_ctx *c)
+{
+    c->join_wide = c->join_window_mode >= 2 ? c->tuned_wide : c->join_window_mode != 0;
+}
 
 // The join kernel in the window chosen for this closure (join_wide).
 static void launch_join(const grg_ctx *c, int grid, cudaStream_t s, const Dev &d, const uint4 *recs, uint64_t n,
@@ -2313,6 +2343,101 @@ static void launch_join(const grg_ctx *c, int grid, cudaStream_t s, const Dev &d
         k_join<WIN2, WIN2_LO><<<grid, JOIN_WARPS * 32, 0, s>>>(d, recs, n, n_ctr, retry_out);
     else
         k_join<WIN, WIN_LO><<<grid, JOIN_WARPS * 32, 0, s>>>(d, recs, n, n_ctr, retry_out);
+}
+
+// ---------------------------------------------------------------- join-window tuning
+//
+// A closure's input is keyed by grammar, filter, vertex count and the share of
+// its tables in each log2 size bucket (eighths). The first closure of a key
+// whose first round is large enough to time runs that round's join pass three
+// times -- wide (the pass that counts), then narrow and wide again, both timed
+// on the same records with warm caches -- and keeps the faster window for the
+// rest of the closure and for later closures with the key. Running a pass again
+// is harmless: a join pass only appends candidates and retry records, and
+// applying a candidate or re-running a record twice adds nothing.
+
+static std::mutex g_tune_mu;
+static std::map<uint64_t, bool> g_tune_cache;          // degree key -> wide window faster
+constexpr uint64_t TUNE_MIN_RECORDS = 1u << 16;        // smaller first rounds are not timed
+
+static int degree_key(grg_ctx *c, uint32_t filter, uint64_t *key)
+{
+    cudaStream_t s = c->stream;
+    GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_DH0, 0, 8 * 8, s));
+    if (c->V) k_degree_hist<<<grid_for(c, (uint64_t)c->L * c->V, 256), 256, 0, s>>>(make_dev(c), (uint32_t)c->L);
+    c->launches++;
+    int st = read_ctr(c);
+    if (st) return st;
+    uint64_t h = 1469598103934665603ull, tot = 0;
+    auto mix = [&](uint64_t v) { h = (h ^ v) * 1099511628211ull; };
+    mix((uint64_t)c->L);
+    mix(filter);
+    for (int q = 0; q < 3 * c->R; q++) mix((uint64_t)c->rules[q]);
+    uint32_t vb = 0;
+    while ((1ull << vb) < c->V) vb++;
+    mix(vb);
+    for (int b = 0; b < 8; b++) tot += c->h_ctr[C_DH0 + b];
+    for (int b = 0; b < 8; b++) mix(tot ? c->h_ctr[C_DH0 + b] * 8 / tot : 0);
+    *key = h;
+    return GRG_OK;
+}
+
+// Sets the closure's window from the cache, or marks it for measurement.
+static int tune_begin(grg_ctx *c, uint32_t filter)
+{
+    c->tune_pending = false;
+    c->tune_source = 0;
+    c->tune_ms[0] = c->tune_ms[1] = 0;
+    if (c->join_window_mode < 2) return GRG_OK;
+    int st = degree_key(c, filter, &c->tune_key);
+    if (st) return st;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(c->tune_key);
+    if (it != g_tune_cache.end() && c->join_window_mode == 2) {
+        c->tuned_wide = it->second;
+        c->tune_source = 2;
+    } else {
+        c->tuned_wide = true;
+        c->tune_pending = true;
+    }
+    return GRG_OK;
+}
+
+static void first_pass_joins(grg_ctx *c, const Dev &d, uint64_t nd, uint64_t nv, bool split, uint64_t &joins);
+
+// The first pass of a round with its window measured (see above).
+static int tune_first_pass(grg_ctx *c, const Dev &d, uint64_t nd, uint64_t nv, uint64_t &joins)
+{
+    cudaStream_t s = c->stream;
+    if (!c->ev_t0) GRG_CUDA(c, cudaEventCreate(&c->ev_t0));
+    if (!c->ev_t1) GRG_CUDA(c, cudaEventCreate(&c->ev_t1));
+    c->join_wide = true;
+    first_pass_joins(c, d, nd, nv, false, joins);
+    int st = read_ctr(c);
+    if (st) return st;
+    const int kept[4] = {C_LEFT, C_RIGHT, C_WOUT, C_INSERTS};
+    unsigned long long keep[4];
+    for (int i = 0; i < 4; i++) keep[i] = c->h_ctr[kept[i]];
+    for (int k = 0; k < 2; k++) {              // 0 narrow, 1 wide
+        c->join_wide = k == 1;
+        GRG_CUDA(c, cudaEventRecord(c->ev_t0, s));
+        first_pass_joins(c, d, nd, nv, false, joins);
+        GRG_CUDA(c, cudaEventRecord(c->ev_t1, s));
+        GRG_CUDA(c, cudaEventSynchronize(c->ev_t1));
+        GRG_CUDA(c, cudaEventElapsedTime(&c->tune_ms[k], c->ev_t0, c->ev_t1));
+    }
+    // the statistics count the pass that counts only
+    for (int i = 0; i < 4; i++) {
+        c->h_ctr[kept[i]] = keep[i];
+        GRG_CUDA(c, cudaMemcpyAsync(c->ctr + kept[i], c->h_ctr + kept[i], 8, cudaMemcpyHostToDevice, s));
+    }
+    const bool wide = c->tune_ms[1] <= c->tune_ms[0];
+    c->tuned_wide = c->join_wide = wide;
+    c->tune_pending = false;
+    c->tune_source = 1;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[c->tune_key] = wide;
+    return GRG_OK;
 }
 
 // Round head: count and gather the dirty slots (rs: stamp for elements that
@@ -2510,7 +2635,11 @@ static int round_joins(grg_ctx *c, uint64_t nd, uint64_t nv, grg_stats &S, doubl
         k_split<<<grid_for(c, nd + nv, 256), 256, 0, s>>>(d, c->gbuf, c->vbuf, c->sbuf);
         c->launches++;
     }
-    first_pass_joins(c, d, nd, nv, split, joins);
+    if (c->tune_pending && !split && nd + nv >= TUNE_MIN_RECORDS) {
+        if ((st = tune_first_pass(c, d, nd, nv, joins))) return st;
+    } else {
+        first_pass_joins(c, d, nd, nv, split, joins);
+    }
     // insert the candidates the joins wrote (count read on the device)
     if (c->cand_cap) {
         k_apply<<<c->sms * 8, 256, 0, s>>>(d, c->cand[c->cb], c->cand[c->cb ^ 1]);
@@ -2842,6 +2971,8 @@ int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *s
     grg_stats S;
     memset(&S, 0, sizeof S);
     GRG_CUDA(c, cudaEventRecord(c->ev_a, s));
+    if ((st = tune_begin(c, filter))) return st;
+    choose_window(c);
     Dev d = make_dev(c);
     // labels never inserted into after the load are packed
     bool derivable[MAX_LABELS + 1] = {false};
@@ -2928,6 +3059,10 @@ int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *s
     S.window_out_elems = c->h_ctr[C_WOUT];
     S.gather_ms = c->h_ctr[C_GNS] * 1e-6;
     S.wide_window = c->join_wide ? 1 : 0;
+    S.window_tuned = (uint64_t)c->tune_source;
+    S.window_trial_ms[0] = c->tune_ms[0];
+    S.window_trial_ms[1] = c->tune_ms[1];
+    c->tune_pending = false;              // an untimed closure leaves its key for the next one
     S.right_elems = c->h_ctr[C_RIGHT];
     S.out_elems = S.delta_elems;
     S.pool_elems_used = c->h_ctr[C_POOL_TOP];

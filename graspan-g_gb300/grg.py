@@ -53,11 +53,13 @@ class Stats(ctypes.Structure):
         ("join_launches", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
         ("join_phase_cycles", ctypes.c_uint64 * 5), ("window_out_elems", ctypes.c_uint64),
         ("wide_window", ctypes.c_uint64), ("gather_ms", ctypes.c_double),
+        ("window_tuned", ctypes.c_uint64), ("window_trial_ms", ctypes.c_double * 2),
     ]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
         d["join_phase_cycles"] = list(d["join_phase_cycles"])
+        d["window_trial_ms"] = list(d["window_trial_ms"])
         return d
 
 
@@ -242,7 +244,8 @@ class Context:
         self._check(self._L.grg_set_kernel_timing(self._h, int(bool(on))), "set_kernel_timing")
 
     def set_join_window(self, mode: int):
-        """0 = narrow (8 elements), 1 = wide (12, the default)."""
+        """0 = narrow (8 elements), 1 = wide (10), 2 = tuned per degree key (the
+        default), 3 = tuned and measured again even when the key is cached."""
         self._check(self._L.grg_set_join_window(self._h, mode), "set_join_window")
 
     def set_device_rounds(self, on: bool):

@@ -68,6 +68,9 @@ typedef struct grg_stats {
                                       statistic the window choice is keyed on) */
     uint64_t wide_window;          /* 1 = the closure ended on the wide join window */
     double gather_ms;              /* time of the rounds' gathers (when kernel timing is on) */
+    uint64_t window_tuned;         /* how the join window was chosen: 0 fixed by grg_set_join_window,
+                                      1 measured in this closure, 2 taken from the tuning cache */
+    double window_trial_ms[2];     /* the measured trial passes (narrow, wide) when window_tuned = 1 */
 } grg_stats;
 
 /* Error text of a status code, and the last detailed message of a context. */
@@ -94,9 +97,15 @@ int grg_set_kernel_timing(grg_ctx *ctx, int on);
  * round. The results are identical either way. */
 int grg_set_device_rounds(grg_ctx *ctx, int on);
 /* Join window: the join ORs right-hand elements into a dense per-record window
- * of 10 elements (mode 1, the default) or 8 (mode 0); elements outside it go to
- * a small shared-memory hash. Environment GRG_JOIN_WINDOW=narrow selects 8.
- * Results are identical either way. */
+ * of 10 elements (mode 1) or 8 (mode 0); elements outside it go to a small
+ * shared-memory hash. Mode 2 (the default) tunes the choice: the closure's input
+ * is keyed by its grammar, filter, vertex count and the distribution of its
+ * table sizes (elements per label and row, log2 buckets); the first closure of
+ * a key whose first round is large times one join pass of that round in each
+ * window and keeps the faster, and later closures with the key reuse the
+ * choice (a process-wide cache). Mode 3 measures again even when the key is
+ * cached, and updates the cache. Environment GRG_JOIN_WINDOW=narrow / wide /
+ * tuned selects the default. Results are identical in every mode. */
 int grg_set_join_window(grg_ctx *ctx, int mode);
 
 /* Grammar: rules[3*i+{0,1,2}] = LHS, RHS1, RHS2 label ids (1-based, 0 = absent),

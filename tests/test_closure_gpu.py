@@ -222,7 +222,7 @@ def test_device_rounds_equal_host_rounds(grg_mod, oracle_mod, name):
 
 @pytest.mark.parametrize("name", ["pointsto", "alias", "dataflow"])
 def test_join_windows_equal(grg_mod, oracle_mod, name):
-    """The narrow (8-element) and wide (12-element) join windows give the oracle's closure."""
+    """The narrow (8-element) and wide (10-element) join windows give the oracle's closure."""
     w = {"pointsto": lambda: G.pointsto(seed=41, num_vars=900, num_edges=2200),
          "alias": lambda: G.alias(seed=42, num_vars=4000, num_base_edges=9000, block=700),
          "dataflow": lambda: G.dataflow_blocks(seed=43, num_blocks=20, block=500, num_edges=30000)}[name]()
@@ -236,6 +236,38 @@ def test_join_windows_equal(grg_mod, oracle_mod, name):
         assert st["wide_window"] == mode
         assert ctx.label_counts().tolist() == r.label_counts().tolist() and ctx.set_hash() == r.set_hash
         ctx.close()
+
+
+@pytest.mark.parametrize("device_rounds", [True, False])
+def test_tuned_window_measures_then_reuses(grg_mod, oracle_mod, device_rounds):
+    """A closure whose degree key must be measured (mode 3 measures even when
+    another closure of the process cached the key) times its large first
+    round's join pass in both windows (window_tuned 1), and the closure is the
+    oracle's despite the extra passes; a mode-2 closure of the same input then
+    takes the choice from the cache (window_tuned 2). Fixed modes report 0."""
+    w = G.dataflow_blocks(seed=44 + device_rounds, num_blocks=97 + 2 * device_rounds, block=1000,
+                          num_edges=291_000 + 6000 * device_rounds)
+    r = oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, w.filter_flag, w.src, w.dst, w.lab)
+    want = (r.label_counts().tolist(), r.set_hash)
+    seen = []
+    for k in range(2):
+        ctx = grg_mod.Context(0)
+        ctx.set_join_window(3 if k == 0 else 2)
+        ctx.set_device_rounds(device_rounds)
+        ctx.transfer_rules(w.rule_ids(), w.num_labels)
+        ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
+        st = ctx.closure(w.filter_flag)
+        assert (ctx.label_counts().tolist(), ctx.set_hash()) == want
+        seen.append((st["window_tuned"], st["wide_window"], st["window_trial_ms"]))
+        ctx.close()
+    assert seen[0][0] == 1 and min(seen[0][2]) > 0
+    assert seen[1][0] == 2 and seen[1][1] == seen[0][1] and seen[1][2] == [0.0, 0.0]
+    ctx = grg_mod.Context(0)
+    ctx.set_join_window(1)
+    ctx.transfer_rules(w.rule_ids(), w.num_labels)
+    ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
+    assert ctx.closure(w.filter_flag)["window_tuned"] == 0
+    ctx.close()
 
 
 def test_small_rounds_split_and_retry_overflow(grg_mod, oracle_mod, monkeypatch):
