@@ -2349,10 +2349,9 @@ static void launch_join(const grg_ctx *c, int grid, cudaStream_t s, const Dev &d
 //
 // A closure's input is keyed by grammar, filter, vertex count and the share of
 // its tables in each log2 size bucket (eighths). The first closure of a key
-// whose first round is large enough to time runs that round's join pass three
-// times -- wide (the pass that counts), then narrow and wide again, both timed
-// on the same records with warm caches -- and keeps the faster window for the
-// rest of the closure and for later closures with the key. Running a pass again
+// whose first round is large enough to time joins a slice of that round's
+// records in each window, keeps the faster window for the round, the rest of
+// the closure and later closures with the key. Joining a record more than once
 // is harmless: a join pass only appends candidates and retry records, and
 // applying a candidate or re-running a record twice adds nothing.
 
@@ -2405,38 +2404,56 @@ static int tune_begin(grg_ctx *c, uint32_t filter)
 
 static void first_pass_joins(grg_ctx *c, const Dev &d, uint64_t nd, uint64_t nv, bool split, uint64_t &joins);
 
-// The first pass of a round with its window measured (see above).
+// The first pass of a round with its window measured (see above): both windows
+// are timed twice, interleaved, on a slice of the round's records (an eighth, at
+// least TUNE_MIN_RECORDS), after an untimed pass over the slice that warms the
+// caches; narrow is taken only when its best time beats wide's by 10% (slices
+// of one round differ by a few percent between runs). Then the whole round
+// runs in the chosen window.
 static int tune_first_pass(grg_ctx *c, const Dev &d, uint64_t nd, uint64_t nv, uint64_t &joins)
 {
     cudaStream_t s = c->stream;
     if (!c->ev_t0) GRG_CUDA(c, cudaEventCreate(&c->ev_t0));
     if (!c->ev_t1) GRG_CUDA(c, cudaEventCreate(&c->ev_t1));
-    c->join_wide = true;
-    first_pass_joins(c, d, nd, nv, false, joins);
     int st = read_ctr(c);
     if (st) return st;
     const int kept[4] = {C_LEFT, C_RIGHT, C_WOUT, C_INSERTS};
     unsigned long long keep[4];
     for (int i = 0; i < 4; i++) keep[i] = c->h_ctr[kept[i]];
-    for (int k = 0; k < 2; k++) {              // 0 narrow, 1 wide
+    const uint64_t nt = std::min(nd, std::max<uint64_t>(TUNE_MIN_RECORDS, nd / 8));
+    const int grid = grid_for(c, (nt + RB - 1) / RB, JOIN_WARPS, 16);
+    // an untimed wide pass, then narrow / wide twice, interleaved; each window's best time
+    c->tune_ms[0] = c->tune_ms[1] = 1e30f;
+    for (int it = -1; it < 4; it++) {
+        const int k = it < 0 ? 1 : it & 1;     // 0 narrow, 1 wide
         c->join_wide = k == 1;
-        GRG_CUDA(c, cudaEventRecord(c->ev_t0, s));
-        first_pass_joins(c, d, nd, nv, false, joins);
+        if (it >= 0) GRG_CUDA(c, cudaEventRecord(c->ev_t0, s));
+        launch_join(c, grid, s, d, c->gbuf, nt, -1, c->rbuf[0]);
+        c->launches++;
+        joins++;
+        if (it < 0) continue;
+        float ms = 0;
         GRG_CUDA(c, cudaEventRecord(c->ev_t1, s));
         GRG_CUDA(c, cudaEventSynchronize(c->ev_t1));
-        GRG_CUDA(c, cudaEventElapsedTime(&c->tune_ms[k], c->ev_t0, c->ev_t1));
+        GRG_CUDA(c, cudaEventElapsedTime(&ms, c->ev_t0, c->ev_t1));
+        c->tune_ms[k] = std::min(c->tune_ms[k], ms);
     }
-    // the statistics count the pass that counts only
+    // the statistics count the round's own pass only
     for (int i = 0; i < 4; i++) {
         c->h_ctr[kept[i]] = keep[i];
         GRG_CUDA(c, cudaMemcpyAsync(c->ctr + kept[i], c->h_ctr + kept[i], 8, cudaMemcpyHostToDevice, s));
     }
-    const bool wide = c->tune_ms[1] <= c->tune_ms[0];
+    // the wide window is the measured default (faster on every workload swept): narrow must
+    // win by a margin the trial's noise cannot produce
+    const bool wide = !(c->tune_ms[0] < 0.9f * c->tune_ms[1]);
     c->tuned_wide = c->join_wide = wide;
     c->tune_pending = false;
     c->tune_source = 1;
-    std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune_cache[c->tune_key] = wide;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[c->tune_key] = wide;
+    }
+    first_pass_joins(c, d, nd, nv, false, joins);
     return GRG_OK;
 }
 
@@ -2635,7 +2652,7 @@ static int round_joins(grg_ctx *c, uint64_t nd, uint64_t nv, grg_stats &S, doubl
         k_split<<<grid_for(c, nd + nv, 256), 256, 0, s>>>(d, c->gbuf, c->vbuf, c->sbuf);
         c->launches++;
     }
-    if (c->tune_pending && !split && nd + nv >= TUNE_MIN_RECORDS) {
+    if (c->tune_pending && !split && nd >= TUNE_MIN_RECORDS) {
         if ((st = tune_first_pass(c, d, nd, nv, joins))) return st;
     } else {
         first_pass_joins(c, d, nd, nv, split, joins);

@@ -189,6 +189,7 @@ struct grg_part {
     uint64_t run_budget = 0;         // runs per grg_part_run call (0 = unbounded)
     uint64_t runs_call = 0;          // runs made by the current call
     int run_filter = -1;             // filter of a paused run (-1 = none)
+    bool window_pinned = false;      // the first tuned run's join window holds for the other runs
     uint64_t cursor = 0;             // pairs schedule: position in the paused superstep's pair order
     bool cursor_ran = false;         // a run happened in that superstep before the pause
 };
@@ -592,6 +593,12 @@ int run_once(grg_part *p, uint32_t filter, const std::vector<size_t> &idx, const
         Timer tm(p->S.closure_ms);
         if ((st = grg_closure_ex(p->ctx, filter, run_stamp, &cs))) return st;
     }
+    // partitions of one graph share its degree distribution: the window the first tuned
+    // run chose holds for the rest (no trial per partition)
+    if (cs.window_tuned && !p->window_pinned) {
+        grg_set_join_window(p->ctx, cs.wide_window ? 1 : 0);
+        p->window_pinned = true;
+    }
     p->S.runs++;
     p->S.rounds += cs.rounds;
     return GRG_OK;
@@ -847,6 +854,10 @@ int grg_part_run(grg_part *p, uint32_t filter, grg_part_stats *stats)
     }
     p->S.schedule = coupled ? 1 : 0;
     int st = coupled ? run_pairs(p, filter) : run_stream(p, filter, der);
+    if (p->window_pinned) {                // the context tunes again after this run
+        grg_set_join_window(p->ctx, 2);
+        p->window_pinned = false;
+    }
     if (st == GRG_PAUSED) {
         p->run_filter = (int)filter;
         p->S.num_parts = (uint32_t)p->parts.size();

@@ -101,8 +101,9 @@ int grg_set_device_rounds(grg_ctx *ctx, int on);
  * shared-memory hash. Mode 2 (the default) tunes the choice: the closure's input
  * is keyed by its grammar, filter, vertex count and the distribution of its
  * table sizes (elements per label and row, log2 buckets); the first closure of
- * a key whose first round is large times one join pass of that round in each
- * window and keeps the faster, and later closures with the key reuse the
+ * a key whose first round is large times a slice of that round's join in each
+ * window and keeps the faster (the wide window unless narrow wins by 10%), and
+ * later closures with the key reuse the
  * choice (a process-wide cache). Mode 3 measures again even when the key is
  * cached, and updates the cache. Environment GRG_JOIN_WINDOW=narrow / wide /
  * tuned selects the default. Results are identical in every mode. */
