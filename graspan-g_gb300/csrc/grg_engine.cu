@@ -3240,25 +3240,30 @@ static int stage_elements(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t
 }
 
 
-int grg_export_csr5(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t cap, uint8_t *edges, uint32_t *degree,
-                    uint64_t *num_edges)
+// Elements of rows [a, b) (a count-only pass of the element export).
+static int count_elements(grg_ctx *c, uint32_t a, uint32_t b, uint64_t *n)
 {
-    if (!c || v_begin > v_end || !num_edges || (cap && (!edges || !degree))) return GRG_E_ARG;
-    if (!c->loaded) return fail(c, GRG_E_STATE, "no graph loaded");
-    if (v_end > c->V) return fail(c, GRG_E_RANGE, "vertex range beyond the graph");
-    cudaSetDevice(c->device);
-    // the stream's length is the range's popcount
-    std::vector<uint64_t> counts(c->L + 1, 0);
-    uint64_t h = 0, total = 0;
-    int st = grg_range_counts(c, v_begin, v_end, counts.data(), &h);
+    cudaStream_t s = c->stream;
+    const uint64_t ntab = (uint64_t)c->L * (b - a);
+    GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_EXPORT, 0, 8, s));
+    if (ntab) k_export_elems<<<grid_for(c, ntab * 32, 256), 256, 0, s>>>(make_dev(c), a, b, (uint32_t)c->L, nullptr,
+                                                                          nullptr, 0);
+    int st = read_ctr(c);
     if (st) return st;
-    for (int l = 0; l < c->L; l++) total += counts[l];
-    *num_edges = total;
-    if (total > cap) return total ? fail(c, GRG_E_RANGE, "stream buffer too small") : GRG_OK;
+    *n = c->h_ctr[C_EXPORT];
+    return GRG_OK;
+}
+
+// One piece of a stream export: rows [v_begin, v_end), `total` edges, into host
+// buffers edges / degree.
+static int export_csr5_piece(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t total, uint8_t *edges,
+                             uint32_t *degree)
+{
     const uint32_t nrows = v_end - v_begin;
     if (!nrows) return GRG_OK;
     uint64_t n = 0;
-    if ((st = stage_elements(c, v_begin, v_end, &n))) return st;
+    int st = stage_elements(c, v_begin, v_end, &n);
+    if (st) return st;
     uint8_t *dbytes = nullptr;
     uint32_t *ddeg = nullptr;
     cudaError_t e = cudaMalloc(&ddeg, (size_t)nrows * 4);
@@ -3274,6 +3279,55 @@ int grg_export_csr5(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t cap, 
                     std::string("compressed export: ") + cudaGetErrorString(e));
     }
     return GRG_OK;
+}
+
+// Device bytes one piece needs: its stream (5 B per edge) and, per element, the
+// staged record and stamp (36 B), sort keys and indices in and out (24 B), the
+// counts and offsets (16 B) and the sort's own room (~12 B).
+static uint64_t csr5_footprint(uint64_t edges, uint64_t elems) { return 5 * edges + 88 * elems; }
+
+// Rows [a, b) with `total` edges: halved by rows until a piece fits `budget`
+// bytes of device memory; pieces go out in row order, so their streams and row
+// lengths concatenate into the range's.
+static int export_csr5_split(grg_ctx *c, uint32_t a, uint32_t b, uint64_t total, uint64_t budget, uint8_t *edges,
+                             uint32_t *degree)
+{
+    uint64_t n = 0;
+    int st = count_elements(c, a, b, &n);
+    if (st) return st;
+    if (csr5_footprint(total, n) <= budget || b - a <= 1) return export_csr5_piece(c, a, b, total, edges, degree);
+    const uint32_t mid = a + (b - a) / 2;
+    std::vector<uint64_t> counts(c->L + 1, 0);
+    uint64_t h = 0, t1 = 0;
+    if ((st = grg_range_counts(c, a, mid, counts.data(), &h))) return st;
+    for (int l = 0; l < c->L; l++) t1 += counts[l];
+    if ((st = export_csr5_split(c, a, mid, t1, budget, edges, degree))) return st;
+    return export_csr5_split(c, mid, b, total - t1, budget, edges + t1 * 5, degree + (mid - a));
+}
+
+int grg_export_csr5(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t cap, uint8_t *edges, uint32_t *degree,
+                    uint64_t *num_edges)
+{
+    if (!c || v_begin > v_end || !num_edges || (cap && (!edges || !degree))) return GRG_E_ARG;
+    if (!c->loaded) return fail(c, GRG_E_STATE, "no graph loaded");
+    if (v_end > c->V) return fail(c, GRG_E_RANGE, "vertex range beyond the graph");
+    cudaSetDevice(c->device);
+    // the stream's length is the range's popcount
+    std::vector<uint64_t> counts(c->L + 1, 0);
+    uint64_t h = 0, total = 0;
+    int st = grg_range_counts(c, v_begin, v_end, counts.data(), &h);
+    if (st) return st;
+    for (int l = 0; l < c->L; l++) total += counts[l];
+    *num_edges = total;
+    if (total > cap) return total ? fail(c, GRG_E_RANGE, "stream buffer too small") : GRG_OK;
+    if (v_end == v_begin) return GRG_OK;
+    // pieces take at most half of the free device memory (at least 256 MiB)
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    uint64_t budget = std::max<uint64_t>(fr / 2, 256ull << 20);
+    const char *eb = getenv("GRG_CSR5_BUDGET");         // bytes; smaller budgets split (tests)
+    if (eb && atoll(eb) > 0) budget = (uint64_t)atoll(eb);
+    return export_csr5_split(c, v_begin, v_end, total, budget, edges, degree);
 }
 
 int grg_load_csr5(grg_ctx *c, uint32_t num_vars, uint32_t v_begin, uint32_t v_end, const uint32_t *degree,

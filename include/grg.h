@@ -215,7 +215,7 @@ int grg_set_pool_limit(grg_ctx *ctx, uint64_t pool_bytes);
  * bytes) and degree (v_end - v_begin values). *num_edges = the stream's length
  * in edges; GRG_E_RANGE (nothing written) when that exceeds cap, so cap = 0
  * asks for the size. Converted on the device (records sorted by row, label,
- * base). */
+ * base), in row pieces that fit half of the free device memory. */
 int grg_export_csr5(grg_ctx *ctx, uint32_t v_begin, uint32_t v_end, uint64_t cap, uint8_t *edges,
                     uint32_t *degree, uint64_t *num_edges);
 /* Load a graph over [0, num_vars) from a stream of num_edges edges whose source

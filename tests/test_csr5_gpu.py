@@ -161,3 +161,17 @@ def test_invalid_edges_are_refused_by_every_load_path(grg_mod, oracle_mod):
     ctx.closure(0)
     assert ctx.set_hash() == want.set_hash
     ctx.close()
+
+
+def test_export_in_pieces_under_a_small_budget(grg_mod, oracle_mod, monkeypatch):
+    # a device budget of a few tens of KB splits the range into many row pieces; their
+    # streams and row lengths concatenate to the oracle's
+    w = G.alias(seed=49, num_vars=3000, num_base_edges=7000, block=500)
+    r = oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, 0, w.src, w.dst, w.lab)
+    ctx = closed_context(grg_mod, w, 0)
+    monkeypatch.setenv("GRG_CSR5_BUDGET", "40000")
+    for lo, hi in [(0, w.num_vars), (123, 2500)]:
+        got, deg = ctx.export_csr5(lo, hi)
+        want, wdeg = r.csr5(lo, hi)
+        assert np.array_equal(got, want) and np.array_equal(deg, wdeg), (lo, hi)
+    ctx.close()
