@@ -3339,28 +3339,56 @@ int grg_load_csr5(grg_ctx *c, uint32_t num_vars, uint32_t v_begin, uint32_t v_en
     cudaSetDevice(c->device);
     const uint32_t nrows = v_end - v_begin;
     if (num_edges && !nrows) return fail(c, GRG_E_ARG, "edges without rows");
-    const uint8_t *dbytes = edges;
-    const uint32_t *ddeg = degree;
-    uint8_t *sbytes = nullptr;
-    uint32_t *sdeg = nullptr;
+    struct Part { uint4 *recs; uint32_t *stamps; uint64_t n; };
+    std::vector<Part> parts;
+    auto free_parts = [&]() {
+        for (Part &q : parts) { cudaFree(q.recs); cudaFree(q.stamps); }
+        parts.clear();
+    };
     cudaError_t e = cudaSuccess;
-    if (!on_device) {
-        if (num_edges) e = cudaMalloc(&sbytes, num_edges * 5);
-        if (e == cudaSuccess && nrows) e = cudaMalloc(&sdeg, (size_t)nrows * 4);
-        if (e == cudaSuccess && num_edges) e = cudaMemcpyAsync(sbytes, edges, num_edges * 5, cudaMemcpyHostToDevice, c->stream);
-        if (e == cudaSuccess && nrows) e = cudaMemcpyAsync(sdeg, degree, (size_t)nrows * 4, cudaMemcpyHostToDevice, c->stream);
-        dbytes = sbytes;
-        ddeg = sdeg;
-    }
-    uint64_t sum = 0, n = 0;
+    uint64_t sum = 0;
     unsigned bad = 0;
-    uint4 *recs = nullptr;
-    uint32_t *stamps = nullptr;
-    if (e == cudaSuccess)
-        e = grg_fmt_csr5_to_records(dbytes, num_edges, ddeg, v_begin, nrows, num_vars, (uint32_t)c->L, &recs, &stamps,
-                                    &n, &sum, &bad, c->stream);
-    cudaFree(sbytes);
-    cudaFree(sdeg);
+    if (on_device) {
+        Part q{nullptr, nullptr, 0};
+        e = grg_fmt_csr5_to_records(edges, num_edges, degree, v_begin, nrows, num_vars, (uint32_t)c->L, &q.recs,
+                                    &q.stamps, &q.n, &sum, &bad, c->stream);
+        parts.push_back(q);
+    } else {
+        // host stream: its lengths are checked here, then it goes to the device in row
+        // pieces of at most a quarter of the free device memory (records are far smaller
+        // than the stream, so the whole graph's records meet on the device)
+        for (uint32_t r = 0; r < nrows; r++) sum += degree[r];
+        if (sum != num_edges) return fail(c, GRG_E_ARG, "row lengths do not add up to num_edges");
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        uint64_t budget = std::max<uint64_t>(fr / 4, 64ull << 20);
+        const char *eb = getenv("GRG_CSR5_BUDGET");     // bytes; smaller budgets split (tests)
+        if (eb && atoll(eb) > 0) budget = (uint64_t)atoll(eb);
+        uint64_t e0 = 0;
+        for (uint32_t r0 = 0; r0 < nrows && e == cudaSuccess && !bad;) {
+            uint32_t r1 = r0;
+            uint64_t pe = 0;
+            while (r1 < nrows && (r1 == r0 || (pe + degree[r1]) * 5 <= budget)) pe += degree[r1++];
+            uint8_t *sbytes = nullptr;
+            uint32_t *sdeg = nullptr;
+            Part q{nullptr, nullptr, 0};
+            uint64_t psum = 0;
+            if (pe) e = cudaMalloc(&sbytes, pe * 5);
+            if (e == cudaSuccess) e = cudaMalloc(&sdeg, (size_t)(r1 - r0) * 4);
+            if (e == cudaSuccess && pe)
+                e = cudaMemcpyAsync(sbytes, edges + e0 * 5, pe * 5, cudaMemcpyHostToDevice, c->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(sdeg, degree + r0, (size_t)(r1 - r0) * 4, cudaMemcpyHostToDevice, c->stream);
+            if (e == cudaSuccess)
+                e = grg_fmt_csr5_to_records(sbytes, pe, sdeg, v_begin + r0, r1 - r0, num_vars, (uint32_t)c->L, &q.recs,
+                                            &q.stamps, &q.n, &psum, &bad, c->stream);
+            cudaFree(sbytes);
+            cudaFree(sdeg);
+            parts.push_back(q);
+            e0 += pe;
+            r0 = r1;
+        }
+    }
     int st = GRG_OK;
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -3372,13 +3400,47 @@ int grg_load_csr5(grg_ctx *c, uint32_t num_vars, uint32_t v_begin, uint32_t v_en
         st = fail(c, GRG_E_LABEL, "edge label outside 1..numLabels");
     } else if (bad & 2u) {
         st = fail(c, GRG_E_RANGE, "edge vertex id >= numVars");
+    }
+    if (st) {
+        free_parts();
+        return st;
+    }
+    // the pieces' records side by side (a row is never split, so no record repeats)
+    uint64_t n = 0;
+    for (const Part &q : parts) n += q.n;
+    uint4 *recs = nullptr;
+    uint32_t *stamps = nullptr;
+    bool own = false;
+    if (parts.size() == 1) {
+        recs = parts[0].recs;
+        stamps = parts[0].stamps;
+    } else if (n) {
+        own = true;
+        e = cudaMalloc(&recs, n * 32);
+        if (e == cudaSuccess) e = cudaMalloc(&stamps, n * 4);
+        uint64_t o = 0;
+        for (const Part &q : parts) {
+            if (e != cudaSuccess || !q.n) continue;
+            e = cudaMemcpyAsync(recs + 2 * o, q.recs, q.n * 32, cudaMemcpyDeviceToDevice, c->stream);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(stamps + o, q.stamps, q.n * 4, cudaMemcpyDeviceToDevice, c->stream);
+            o += q.n;
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        st = fail(c, e == cudaErrorMemoryAllocation ? GRG_E_NOMEM : GRG_E_CUDA,
+                  std::string("compressed load: ") + cudaGetErrorString(e));
     } else {
         // a stream is a spilled image: it already holds its epsilon edges, and every
         // element is a delta of round 1 of the next closure
         st = grg_load_elements(c, num_vars, n, reinterpret_cast<const uint32_t *>(recs), stamps, 0, 1);
     }
-    cudaFree(recs);
-    cudaFree(stamps);
+    if (own) {
+        cudaFree(recs);
+        cudaFree(stamps);
+    }
+    free_parts();
     return st;
 }
 

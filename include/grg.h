@@ -228,7 +228,8 @@ int grg_export_csr5(grg_ctx *ctx, uint32_t v_begin, uint32_t v_end, uint64_t cap
  * (label, then destination): a record that repeats fails with GRG_E_ARG, as do
  * lengths that do not add up to num_edges; labels outside 1..L fail with
  * GRG_E_LABEL, destinations >= num_vars with GRG_E_RANGE. on_device as for
- * grg_load_edges (both arrays). */
+ * grg_load_edges (both arrays); a host stream goes to the device in row pieces
+ * of at most a quarter of the free device memory. */
 int grg_load_csr5(grg_ctx *ctx, uint32_t num_vars, uint32_t v_begin, uint32_t v_end, const uint32_t *degree,
                   uint64_t num_edges, const uint8_t *edges, int on_device);
 

@@ -175,3 +175,29 @@ def test_export_in_pieces_under_a_small_budget(grg_mod, oracle_mod, monkeypatch)
         want, wdeg = r.csr5(lo, hi)
         assert np.array_equal(got, want) and np.array_equal(deg, wdeg), (lo, hi)
     ctx.close()
+
+
+def test_load_in_pieces_under_a_small_budget(grg_mod, oracle_mod, monkeypatch):
+    # a host stream larger than the budget goes to the device in row pieces whose records
+    # are joined before the load; the closure is the oracle's
+    w = G.pointsto(seed=50, num_vars=900, num_edges=2400)
+    want = oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, 0, w.src, w.dst, w.lab)
+    ctx = closed_context(grg_mod, w, 0)
+    stream, deg = ctx.export_csr5()
+    ctx.close()
+    monkeypatch.setenv("GRG_CSR5_BUDGET", "20000")
+    ctx2 = grg_mod.Context(0)
+    ctx2.transfer_rules(w.rule_ids(), w.num_labels)
+    ctx2.load_csr5(w.num_vars, stream, deg)
+    got, gdeg = ctx2.export_csr5()
+    assert np.array_equal(got, stream) and np.array_equal(gdeg, deg)
+    ctx2.closure(0)
+    assert [int(x) for x in ctx2.label_counts()] == [int(x) for x in want.label_counts()]
+    assert ctx2.set_hash() == want.set_hash
+    # a bad label in a late piece is still refused
+    s2 = stream.copy().reshape(-1, 5)
+    s2[-3, 4] = w.num_labels + 1
+    with pytest.raises(grg_mod.GrgError) as ei:
+        ctx2.load_csr5(w.num_vars, s2.reshape(-1), deg)
+    assert ei.value.status == grg_mod.E_LABEL
+    ctx2.close()
