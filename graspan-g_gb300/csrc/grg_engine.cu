@@ -105,6 +105,9 @@ static int make_rule_table(const int *rules, int R, int L, uint32_t filter, Rule
 #ifndef GRG_JOIN_MINB
 #define GRG_JOIN_MINB 6
 #endif
+#ifndef GRG_GATHER_GR
+#define GRG_GATHER_GR 4           // delta records per thread per step of the gather's record pass
+#endif
 #ifndef GRG_JOIN_MINB_WIDE
 #define GRG_JOIN_MINB_WIDE 5
 #endif
@@ -405,7 +408,7 @@ __global__ void k_gather_recs(Dev d, const uint32_t *__restrict__ slots, uint4 *
     if (d.ctr[C_HALT]) return;
     if (n_ctr >= 0) n = d.ctr[n_ctr];
     // GR records per thread per step, their random delta reads issued together
-    constexpr int GR = 4;
+    constexpr int GR = GRG_GATHER_GR;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i0 < n; i0 += stride * GR) {
         uint64_t sl[GR];
