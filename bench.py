@@ -356,12 +356,24 @@ def main():
     ap.add_argument("--serve-vmax", type=int, default=200000, help="largest job of the served mix")
     ap.add_argument("--quick", action="store_true",
                     help="headline only: skip the other configurations and the serving mix")
+    ap.add_argument("--workload", default="dataflow", choices=["dataflow", "alias"],
+                    help="dataflow: the headline; alias: the 1M-vertex alias closure alone (for profiling; "
+                         "implies --quick and --no-cpu-baseline)")
     args = ap.parse_args()
     world, rank, local = dist_setup(args)
 
     import grg_gen as G
-    edges = 6_000_000 * args.blocks // 2000
-    w = G.dataflow_blocks(num_blocks=args.blocks, num_edges=edges)
+    global WORKLOAD
+    if args.workload == "alias" and args.impl == "reference":
+        ap.error("--workload alias is a GPU profiling case; the reference arm runs the headline workload")
+    if args.workload == "alias":
+        WORKLOAD = ("alias grammar, 1M vertices, 4M base + 4M inverse edges, Zipf(1.8) cap 256, "
+                    "1000-vertex blocks, filter_flag 0")
+        w = G.alias()
+        args.quick = args.no_cpu_baseline = True
+    else:
+        edges = 6_000_000 * args.blocks // 2000
+        w = G.dataflow_blocks(num_blocks=args.blocks, num_edges=edges)
     if args.impl == "reference":
         run_reference(args, w, world, rank)
         return
@@ -447,7 +459,7 @@ def main():
         achieved = alg_bytes / (join_ms * 1e-3) / 1e9 if join_ms > 0 else None
         traffic = None
         tp = os.path.join(ROOT, "profiles", "join_pass_traffic.json")
-        if os.path.exists(tp):
+        if os.path.exists(tp) and args.workload == "dataflow":
             traffic = json.load(open(tp)).get("bytes_per_launch")
         cb = None if args.no_cpu_baseline else cpu_baseline(w)
         # the other configurations run once, on a single GPU (replica runs hold every GPU meanwhile)
