@@ -128,6 +128,11 @@ struct Dev {
     unsigned long long *ctr;  // counter block
     uint32_t V;
     uint32_t pool_cap;        // elements
+    // the context's grammar under this closure's filter. It travels with every
+    // launch (kernel parameters live in the constant bank, so reads cost what a
+    // __constant__ table costs), so contexts with different grammars can run
+    // on one device, on one stream or several, without sharing any table
+    RuleTable rt;
 };
 
 __device__ __forceinline__ uint32_t hash_slot(uint32_t base, uint32_t lg)

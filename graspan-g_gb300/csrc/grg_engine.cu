@@ -31,8 +31,6 @@
 
 namespace grg {
 
-__constant__ RuleTable c_rt;
-
 // Rule table of a grammar under a filter (filter semantics: src/kernel.cu:490-494,
 // 499-503): binary rules by first symbol, unary rules (filter 0 only), old-left
 // joins for binary rules whose second symbol is derivable (filter 0; refused
@@ -314,7 +312,7 @@ __global__ void k_mark_all(Dev d, uint64_t begin, uint64_t end)   // begin: mult
         if (s < end) {
             const uint4 *e = reinterpret_cast<const uint4 *>(d.elems + s * 8);
             const uint4 e1 = e[1];
-            if (e1.z != EMPTY && c_rt.track[e1.z >> KEY_SHIFT]) {
+            if (e1.z != EMPTY && d.rt.track[e1.z >> KEY_SHIFT]) {
                 const uint4 e0 = e[0];
                 uint4 *b = reinterpret_cast<uint4 *>(d.dbits + s * 8);
                 b[0] = e0;
@@ -439,7 +437,7 @@ __global__ void k_gather_recs(Dev d, const uint32_t *__restrict__ slots, uint4 *
             out[2 * i] = b0[u];
             out[2 * i + 1] = b1[u];
             const uint32_t lab = b1[u].z >> KEY_SHIFT, row = b1[u].w;
-            if (lab <= (uint32_t)MAX_LABELS && c_rt.dindex[lab]) {
+            if (lab <= (uint32_t)MAX_LABELS && d.rt.dindex[lab]) {
                 const size_t ti = (size_t)(lab - 1) * d.V + row;
                 atomicMin(&d.drs[ti], (uint32_t)i);
                 atomicAdd(&d.drc[ti], 1u);
@@ -466,7 +464,7 @@ __global__ void k_dindex_clear(Dev d, const uint4 *__restrict__ recs, int n_ctr)
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint4 b1 = recs[2 * i + 1];
         const uint32_t lab = b1.z >> KEY_SHIFT, row = b1.w;
-        if (lab > (uint32_t)MAX_LABELS || !c_rt.dindex[lab]) continue;
+        if (lab > (uint32_t)MAX_LABELS || !d.rt.dindex[lab]) continue;
         const size_t ti = (size_t)(lab - 1) * d.V + row;
         d.drs[ti] = EMPTY;
         d.drc[ti] = 0;
@@ -482,7 +480,7 @@ __global__ void k_oldleft(Dev d, uint32_t q, uint4 *out, uint64_t cap, const uin
                           const uint32_t *__restrict__ job_cnt)
 {
     if (d.ctr[C_HALT]) return;
-    const uint32_t B = c_rt.ol_B[q], C = c_rt.ol_C[q];
+    const uint32_t B = d.rt.ol_B[q], C = d.rt.ol_C[q];
     const uint32_t *dv = d.dvm + (size_t)(C - 1) * d.vwords;
     const uint32_t vkey = (OL_SLOT0 + q) << KEY_SHIFT;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -703,7 +701,7 @@ __device__ __forceinline__ void acc_flush(const Dev &d, WS &w, uint32_t &inserts
             if (ci != ~0ull) {
                 cand_write(d, ci++, b, (A << KEY_SHIFT) | (k & BASE_MASK), w.rrow[r]);
             } else {
-                if (!g_insert(d, A, w.rrow[r], k & BASE_MASK, b, c_rt.track[A])) atomicOr(&w.fail, 1u << r);
+                if (!g_insert(d, A, w.rrow[r], k & BASE_MASK, b, d.rt.track[A])) atomicOr(&w.fail, 1u << r);
                 inserts++;
             }
         }
@@ -742,7 +740,7 @@ __device__ __forceinline__ void win_flush(const Dev &d, WS &w, uint32_t &inserts
             if (ci != ~0ull) {
                 cand_write(d, ci++, b, (A << KEY_SHIFT) | base, w.rrow[r]);
             } else {
-                if (!g_insert(d, A, w.rrow[r], base, b, c_rt.track[A])) atomicOr(&w.fail, 1u << r);
+                if (!g_insert(d, A, w.rrow[r], base, b, d.rt.track[A])) atomicOr(&w.fail, 1u << r);
                 inserts++;
             }
         }
@@ -764,7 +762,7 @@ __global__ void __launch_bounds__(256, 8) k_apply(Dev d, const uint4 *__restrict
         Bits bits;
         bits.w[0] = a.x; bits.w[1] = a.y; bits.w[2] = a.z; bits.w[3] = a.w; bits.w[4] = b.x; bits.w[5] = b.y;
         const uint32_t A = b.z >> KEY_SHIFT;
-        if (!g_insert_t<true>(d, A, b.w, b.z & BASE_MASK, bits, c_rt.track[A])) {
+        if (!g_insert_t<true>(d, A, b.w, b.z & BASE_MASK, bits, d.rt.track[A])) {
             const unsigned long long f = atomicAdd(&d.ctr[C_AFAIL], 1ull);
             fail_out[2 * f] = a;
             fail_out[2 * f + 1] = b;
@@ -889,14 +887,14 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
         PH_MARK(0);
         // unary rules A ::= B (compute10): the delta itself joins row (A, row)
         // a record names a label 1..L or an old-left rule; anything else joins nothing
-        const bool virt = have && B >= OL_SLOT0 && B < OL_SLOT0 + (uint32_t)c_rt.nol;
-        const bool real = have && B >= 1 && B <= (uint32_t)c_rt.L;
-        const uint32_t nu = real ? c_rt.un_start[B + 1] - c_rt.un_start[B] : 0;
+        const bool virt = have && B >= OL_SLOT0 && B < OL_SLOT0 + (uint32_t)d.rt.nol;
+        const bool real = have && B >= 1 && B <= (uint32_t)d.rt.L;
+        const uint32_t nu = real ? d.rt.un_start[B + 1] - d.rt.un_start[B] : 0;
         const uint32_t maxu = __reduce_max_sync(0xffffffffu, nu);
         for (uint32_t u = 0; u < maxu; u++) {
             if (u < nu) {
-                const uint32_t A = c_rt.un_A[c_rt.un_start[B] + u];
-                ok &= g_insert(d, A, row, base, rb, c_rt.track[A]);
+                const uint32_t A = d.rt.un_A[d.rt.un_start[B] + u];
+                ok &= g_insert(d, A, row, base, rb, d.rt.track[A]);
                 inserts++;
             }
         }
@@ -907,14 +905,14 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
         // (O_B o D_C, virtual record of rule q): right rows are this round's delta
         // records of C[k], found through the delta index.
         const uint32_t qv = virt ? B - OL_SLOT0 : 0;
-        const uint32_t nbr = virt ? 1 : real ? c_rt.bin_start[B + 1] - c_rt.bin_start[B] : 0;
+        const uint32_t nbr = virt ? 1 : real ? d.rt.bin_start[B + 1] - d.rt.bin_start[B] : 0;
         const uint32_t maxb = __reduce_max_sync(0xffffffffu, nbr);
         w.rOff[lane] = virt;
         for (uint32_t rho = 0; rho < maxb; rho++) {
             const bool hr = rho < nbr;
-            const uint32_t q = virt ? qv : c_rt.bin_start[B] + rho;
-            w.rA[lane] = !hr ? 0 : virt ? c_rt.ol_A[q] : c_rt.bin_A[q];
-            w.rC[lane] = !hr ? 0 : virt ? c_rt.ol_C[q] : c_rt.bin_C[q];
+            const uint32_t q = virt ? qv : d.rt.bin_start[B] + rho;
+            w.rA[lane] = !hr ? 0 : virt ? d.rt.ol_A[q] : d.rt.bin_A[q];
+            w.rC[lane] = !hr ? 0 : virt ? d.rt.ol_C[q] : d.rt.bin_C[q];
             n_left += hr;
             const uint32_t my_cnt = hr ? nbits : 0;
             const uint32_t total = warp_tasks(w, my_cnt);
@@ -932,7 +930,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                     r = rr;
                     C = w.rC[r];
                     const uint32_t k = w.rbase[r] * EIDS + select_bit(w.rbits[r], t - r_st);
-                    const uint2 *cr = c_rt.csr_row[C];
+                    const uint2 *cr = d.rt.csr_row[C];
                     if (w.rOff[r]) {
                         const size_t ti = (size_t)(C - 1) * d.V + k;
                         const uint32_t s0 = __ldg(d.drs + ti);
@@ -965,7 +963,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                     for (int x = 0; x < EW; x++) ib.w[x] = 0;
                     if (valid) {
                         if (o_csr == 1) {
-                            const uint32_t dst = __ldg(c_rt.csr_col[o_C] + item);
+                            const uint32_t dst = __ldg(d.rt.csr_col[o_C] + item);
                             b2 = dst / EIDS;
                             ob = dst % EIDS;
                             ok_i = true;
@@ -1643,6 +1641,7 @@ const char *status_text(int s)
     case GRG_E_RANGE: return "value out of range";
     case GRG_E_STATE: return "call out of order";
     case GRG_E_NODEV: return "no CUDA device";
+    case GRG_E_INTERNAL: return "internal limit or consistency check failed";
     default: return "unknown status";
     }
 }
@@ -1690,6 +1689,7 @@ Dev make_dev(const grg_ctx *c)
     d.pool_cap = (uint32_t)c->pool_cap;
     d.stamp = c->elem_loaded ? c->stamp : nullptr;
     d.prefix_mask = c->prefix_mask;
+    d.rt = c->rt;
     return d;
 }
 
@@ -2238,7 +2238,7 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
     GRG_CUDA(c, cudaGetLastError());
     st = read_ctr(c);
     if (st) return st;
-    if (c->h_ctr[C_ERR]) return fail(c, GRG_E_CUDA, "internal error while loading edges");
+    if (c->h_ctr[C_ERR]) return fail(c, GRG_E_INTERNAL, "internal error while loading edges");
     c->loaded = true;
     c->closed = false;
     return GRG_OK;
@@ -2446,6 +2446,11 @@ static int tune_first_pass(grg_ctx *c, const Dev &d, uint64_t nd, uint64_t nv, u
         c->h_ctr[kept[i]] = keep[i];
         GRG_CUDA(c, cudaMemcpyAsync(c->ctr + kept[i], c->h_ctr + kept[i], 8, cudaMemcpyHostToDevice, s));
     }
+    // the trial passes' retry records and candidates are dropped: the round's own pass
+    // below joins every record again. Tables they queued for growth stay queued (their
+    // want counters are set, so the real pass would not queue them a second time).
+    GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_RETRY_N, 0, 8, s));
+    GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_CAND_N, 0, 16, s));    // candidates + failed candidates
     // the wide window is the measured default (faster on every workload swept): narrow must
     // win by a margin the trial's noise cannot produce
     const bool wide = !(c->tune_ms[0] < 0.9f * c->tune_ms[1]);
@@ -2596,7 +2601,7 @@ static int round_retries(grg_ctx *c, uint64_t nr, uint64_t nf, grg_stats &S, dou
             if (st) return st;
             d = make_dev(c);
         }
-        if (pass > 64) return fail(c, GRG_E_CUDA, "table growth did not converge");
+        if (pass > 64) return fail(c, GRG_E_INTERNAL, "table growth did not converge in 64 passes");
         // failed candidates (in cand[cb^1]) become the candidate list; join retries append to it
         c->cb ^= 1;
         d = make_dev(c);
@@ -2760,6 +2765,10 @@ static std::vector<uint64_t> round_graph_key(const grg_ctx *c, uint32_t rs, uint
                                (uint64_t)c->elem_loaded, (uint64_t)c->rt.nol, (uint64_t)c->row_job,
                                (uint64_t)c->job_cnt, c->max_jobs, (uint64_t)c->join_wide, (uint64_t)c->sbuf};
     for (int l = 1; l <= c->L; l++) k.push_back(c->rt.dindex[l]);
+    // the rule table is a parameter of every recorded launch
+    uint64_t w[(sizeof(RuleTable) + 7) / 8] = {0};
+    memcpy(w, &c->rt, sizeof(RuleTable));
+    k.insert(k.end(), w, w + (sizeof(RuleTable) + 7) / 8);
     return k;
 }
 
@@ -2964,7 +2973,7 @@ static int run_rounds(grg_ctx *c, uint64_t max_rounds, grg_stats &S, double &joi
             c->device_rounds = false;
             graphs = false;
         } else {
-            return fail(c, GRG_E_CUDA, "device-driven rounds stopped without a reason");
+            return fail(c, GRG_E_INTERNAL, "device-driven rounds stopped without a reason");
         }
     }
     return GRG_OK;
@@ -2987,7 +2996,6 @@ int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *s
     if (st) return st;
     c->rt = rt;
     cudaStream_t s = c->stream;
-    GRG_CUDA(c, cudaMemcpyToSymbolAsync(c_rt, &rt, sizeof rt, 0, cudaMemcpyHostToDevice, s));
     grg_stats S;
     memset(&S, 0, sizeof S);
     GRG_CUDA(c, cudaEventRecord(c->ev_a, s));
@@ -3052,7 +3060,6 @@ int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *s
         rt.csr_col[l] = cb.col;
     }
     c->rt = rt;
-    GRG_CUDA(c, cudaMemcpyToSymbolAsync(c_rt, &rt, sizeof rt, 0, cudaMemcpyHostToDevice, s));
     st = read_ctr(c);
     if (st) return st;
     const uint64_t top = c->h_ctr[C_POOL_TOP];
@@ -3342,24 +3349,21 @@ int grg_load_csr5(grg_ctx *c, uint32_t num_vars, uint32_t v_begin, uint32_t v_en
     cudaSetDevice(c->device);
     const uint32_t nrows = v_end - v_begin;
     if (num_edges && !nrows) return fail(c, GRG_E_ARG, "edges without rows");
-    struct Part { uint4 *recs; uint32_t *stamps; uint64_t n; };
-    std::vector<Part> parts;
-    auto free_parts = [&]() {
-        for (Part &q : parts) { cudaFree(q.recs); cudaFree(q.stamps); }
-        parts.clear();
-    };
     cudaError_t e = cudaSuccess;
-    uint64_t sum = 0;
+    uint64_t sum = 0, n = 0;
     unsigned bad = 0;
+    uint4 *recs = nullptr;
+    uint32_t *stamps = nullptr;
     if (on_device) {
-        Part q{nullptr, nullptr, 0};
-        e = grg_fmt_csr5_to_records(edges, num_edges, degree, v_begin, nrows, num_vars, (uint32_t)c->L, &q.recs,
-                                    &q.stamps, &q.n, &sum, &bad, c->stream);
-        parts.push_back(q);
+        e = grg_fmt_csr5_to_records(edges, num_edges, degree, v_begin, nrows, num_vars, (uint32_t)c->L, nullptr,
+                                    nullptr, 0, &recs, &stamps, &n, &sum, &bad, c->stream);
     } else {
         // host stream: its lengths are checked here, then it goes to the device in row
-        // pieces of at most a quarter of the free device memory (records are far smaller
-        // than the stream, so the whole graph's records meet on the device)
+        // pieces. A piece's stream bytes (5 per edge) and its records (at most one
+        // 32-byte record and a 4-byte stamp per edge) fit a quarter of the free device
+        // memory. With more than one piece, a first pass counts each piece's records,
+        // the joined record buffer is allocated once, and a second pass builds every
+        // piece's records at its own offset, so no second copy is ever held.
         for (uint32_t r = 0; r < nrows; r++) sum += degree[r];
         if (sum != num_edges) return fail(c, GRG_E_ARG, "row lengths do not add up to num_edges");
         size_t fr = 0, tot = 0;
@@ -3367,30 +3371,67 @@ int grg_load_csr5(grg_ctx *c, uint32_t num_vars, uint32_t v_begin, uint32_t v_en
         uint64_t budget = std::max<uint64_t>(fr / 4, 64ull << 20);
         const char *eb = getenv("GRG_CSR5_BUDGET");     // bytes; smaller budgets split (tests)
         if (eb && atoll(eb) > 0) budget = (uint64_t)atoll(eb);
+        constexpr uint64_t PIECE_BYTES_PER_EDGE = 5 + 32 + 4;
+        struct Piece { uint32_t r0, r1; uint64_t e0, ne, n; };
+        std::vector<Piece> pieces;
+        uint64_t max_ne = 0;
         uint64_t e0 = 0;
-        for (uint32_t r0 = 0; r0 < nrows && e == cudaSuccess && !bad;) {
+        for (uint32_t r0 = 0; r0 < nrows;) {
             uint32_t r1 = r0;
             uint64_t pe = 0;
-            while (r1 < nrows && (r1 == r0 || (pe + degree[r1]) * 5 <= budget)) pe += degree[r1++];
-            uint8_t *sbytes = nullptr;
-            uint32_t *sdeg = nullptr;
-            Part q{nullptr, nullptr, 0};
-            uint64_t psum = 0;
-            if (pe) e = cudaMalloc(&sbytes, pe * 5);
-            if (e == cudaSuccess) e = cudaMalloc(&sdeg, (size_t)(r1 - r0) * 4);
-            if (e == cudaSuccess && pe)
-                e = cudaMemcpyAsync(sbytes, edges + e0 * 5, pe * 5, cudaMemcpyHostToDevice, c->stream);
-            if (e == cudaSuccess)
-                e = cudaMemcpyAsync(sdeg, degree + r0, (size_t)(r1 - r0) * 4, cudaMemcpyHostToDevice, c->stream);
-            if (e == cudaSuccess)
-                e = grg_fmt_csr5_to_records(sbytes, pe, sdeg, v_begin + r0, r1 - r0, num_vars, (uint32_t)c->L, &q.recs,
-                                            &q.stamps, &q.n, &psum, &bad, c->stream);
-            cudaFree(sbytes);
-            cudaFree(sdeg);
-            parts.push_back(q);
+            while (r1 < nrows && (r1 == r0 || (pe + degree[r1]) * PIECE_BYTES_PER_EDGE <= budget)) pe += degree[r1++];
+            pieces.push_back({r0, r1, e0, pe, 0});
+            max_ne = std::max(max_ne, pe);
             e0 += pe;
             r0 = r1;
         }
+        uint8_t *sbytes = nullptr;
+        uint32_t *sdeg = nullptr;
+        uint32_t max_rows = 0;
+        for (const Piece &q : pieces) max_rows = std::max(max_rows, q.r1 - q.r0);
+        if (max_ne) e = cudaMalloc(&sbytes, max_ne * 5);
+        if (e == cudaSuccess) e = cudaMalloc(&sdeg, (size_t)std::max<uint32_t>(max_rows, 1) * 4);
+        auto upload = [&](const Piece &q) {
+            cudaError_t r = cudaSuccess;
+            if (q.ne) r = cudaMemcpyAsync(sbytes, edges + q.e0 * 5, q.ne * 5, cudaMemcpyHostToDevice, c->stream);
+            if (r == cudaSuccess)
+                r = cudaMemcpyAsync(sdeg, degree + q.r0, (size_t)(q.r1 - q.r0) * 4, cudaMemcpyHostToDevice, c->stream);
+            return r;
+        };
+        uint64_t psum = 0;
+        if (pieces.size() == 1) {
+            if (e == cudaSuccess) e = upload(pieces[0]);
+            if (e == cudaSuccess)
+                e = grg_fmt_csr5_to_records(sbytes, pieces[0].ne, sdeg, v_begin, nrows, num_vars, (uint32_t)c->L,
+                                            nullptr, nullptr, 0, &recs, &stamps, &n, &psum, &bad, c->stream);
+        } else {
+            for (Piece &q : pieces) {                 // pass 1: records per piece
+                if (e != cudaSuccess || bad) break;
+                e = upload(q);
+                if (e == cudaSuccess)
+                    e = grg_fmt_csr5_to_records(sbytes, q.ne, sdeg, v_begin + q.r0, q.r1 - q.r0, num_vars,
+                                                (uint32_t)c->L, nullptr, nullptr, 0, nullptr, nullptr, &q.n, &psum,
+                                                &bad, c->stream);
+                n += q.n;
+            }
+            if (e == cudaSuccess && !bad && n) {
+                e = cudaMalloc(&recs, n * 32);
+                if (e == cudaSuccess) e = cudaMalloc(&stamps, n * 4);
+            }
+            uint64_t o = 0;
+            for (const Piece &q : pieces) {           // pass 2: each piece at its offset
+                if (e != cudaSuccess || bad || !n) break;
+                uint64_t qn = 0;
+                e = upload(q);
+                if (e == cudaSuccess && q.n)
+                    e = grg_fmt_csr5_to_records(sbytes, q.ne, sdeg, v_begin + q.r0, q.r1 - q.r0, num_vars,
+                                                (uint32_t)c->L, recs + 2 * o, stamps + o, q.n, nullptr, nullptr,
+                                                &qn, &psum, &bad, c->stream);
+                o += q.n;
+            }
+        }
+        cudaFree(sbytes);
+        cudaFree(sdeg);
     }
     int st = GRG_OK;
     if (e != cudaSuccess) {
@@ -3405,45 +3446,15 @@ int grg_load_csr5(grg_ctx *c, uint32_t num_vars, uint32_t v_begin, uint32_t v_en
         st = fail(c, GRG_E_RANGE, "edge vertex id >= numVars");
     }
     if (st) {
-        free_parts();
-        return st;
-    }
-    // the pieces' records side by side (a row is never split, so no record repeats)
-    uint64_t n = 0;
-    for (const Part &q : parts) n += q.n;
-    uint4 *recs = nullptr;
-    uint32_t *stamps = nullptr;
-    bool own = false;
-    if (parts.size() == 1) {
-        recs = parts[0].recs;
-        stamps = parts[0].stamps;
-    } else if (n) {
-        own = true;
-        e = cudaMalloc(&recs, n * 32);
-        if (e == cudaSuccess) e = cudaMalloc(&stamps, n * 4);
-        uint64_t o = 0;
-        for (const Part &q : parts) {
-            if (e != cudaSuccess || !q.n) continue;
-            e = cudaMemcpyAsync(recs + 2 * o, q.recs, q.n * 32, cudaMemcpyDeviceToDevice, c->stream);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(stamps + o, q.stamps, q.n * 4, cudaMemcpyDeviceToDevice, c->stream);
-            o += q.n;
-        }
-        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    }
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        st = fail(c, e == cudaErrorMemoryAllocation ? GRG_E_NOMEM : GRG_E_CUDA,
-                  std::string("compressed load: ") + cudaGetErrorString(e));
-    } else {
-        // a stream is a spilled image: it already holds its epsilon edges, and every
-        // element is a delta of round 1 of the next closure
-        st = grg_load_elements(c, num_vars, n, reinterpret_cast<const uint32_t *>(recs), stamps, 0, 1);
-    }
-    if (own) {
         cudaFree(recs);
         cudaFree(stamps);
+        return st;
     }
-    free_parts();
+    // a stream is a spilled image: it already holds its epsilon edges, and every
+    // element is a delta of round 1 of the next closure
+    st = grg_load_elements(c, num_vars, n, reinterpret_cast<const uint32_t *>(recs), stamps, 0, 1);
+    cudaFree(recs);
+    cudaFree(stamps);
     return st;
 }
 
@@ -3557,7 +3568,6 @@ int grg_batch_begin(grg_ctx *c, uint32_t max_vars, uint32_t max_jobs, int num_ru
     GRG_CUDA(c, cudaMemsetAsync(c->ctr, 0, sizeof(unsigned long long) * NCTR, s));
     GRG_CUDA(c, cudaMemsetAsync(c->dmap, 0, (c->pool_cap / 32 + 2) * 4, s));
     c->rt = rt;   // batch mode keeps every label in hash tables (no CSR copies)
-    GRG_CUDA(c, cudaMemcpyToSymbolAsync(c_rt, &rt, sizeof rt, 0, cudaMemcpyHostToDevice, s));
     c->batch = true;
     c->filter = filter;
     c->loaded = true;
@@ -3668,7 +3678,7 @@ int grg_batch_admit(grg_ctx *c, uint32_t job, uint32_t base, uint32_t num_vars, 
     GRG_CUDA(c, cudaGetLastError());
     st = read_ctr(c);
     if (st) return st;
-    if (c->h_ctr[C_ERR]) return fail(c, GRG_E_CUDA, "internal error while admitting a job");
+    if (c->h_ctr[C_ERR]) return fail(c, GRG_E_INTERNAL, "internal error while admitting a job");
     c->jobs[job].base = base;
     c->jobs[job].nv = num_vars;
     c->jobs[job].active = true;
@@ -3878,6 +3888,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     d.vwords = (uint32_t)vwords;
     d.stamp = nullptr;
     d.prefix_mask = 0;         // every table hashed
+    d.rt = rt;                 // the grammar travels with every launch (no shared table)
     uint4 *gbuf = (uint4 *)(base + o_gbuf), *vbuf = (uint4 *)(base + o_vbuf);
     uint32_t *gslot = (uint32_t *)(base + o_gslot);
     d.drec = gbuf;
@@ -3894,7 +3905,6 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     NA_CUDA(cudaMemsetAsync(d.drs, 0xFF, ntab * 4, s));
     NA_CUDA(cudaMemsetAsync(d.drc, 0, ntab * 4, s));
     NA_CUDA(cudaMemsetAsync(d.dvm, 0, (uint64_t)num_labels * vwords * 4, s));
-    NA_CUDA(cudaMemcpyToSymbolAsync(c_rt, &rt, sizeof rt, 0, cudaMemcpyHostToDevice, s));
 
     // load (grg_load_edges)
     const uint64_t nlab = (uint64_t)num_labels * num_vars;
@@ -3918,7 +3928,8 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     if (top0) k_mark_all<<<grid(top0, 256, 8), 256, 0, s>>>(d, 0, top0);
     NA_CUDA(cudaGetLastError());
     if ((st = na_read(h, d.ctr, s))) return st;
-    if (h[C_ERR]) return GRG_E_CUDA;
+    if (h[C_ERR] & ERR_POOL) return GRG_E_NOMEM;
+    if (h[C_ERR]) return GRG_E_INTERNAL;
 
     // semi-naive rounds (grg_closure); the pool cannot grow here
     uint64_t rounds = 0;
@@ -3975,7 +3986,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
             k_grow<<<grid(h[C_GROW_N] * 32, 256, 8), 256, 0, s>>>(d, h[C_GROW_N]);
             if ((st = na_read(h, d.ctr, s))) return st;
             if (h[C_ERR] & ERR_POOL) return GRG_E_NOMEM;          // closure outgrew the scratch
-            if (pass > 64) return GRG_E_CUDA;
+            if (pass > 64) return GRG_E_INTERNAL;             // table growth did not converge
             rb = pass == 0 ? 0 : rb ^ 1;
             n = nr;
             NA_CUDA(cudaMemsetAsync(d.ctr + C_RETRY_N, 0, 16, s));

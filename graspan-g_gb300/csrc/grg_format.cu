@@ -260,9 +260,9 @@ done:
 }
 
 cudaError_t grg_fmt_csr5_to_records(const uint8_t *bytes, uint64_t num_edges, const uint32_t *degree,
-                                    uint32_t v_begin, uint32_t nrows, uint32_t num_vars, uint32_t L, uint4 **recs,
-                                    uint32_t **stamps, uint64_t *n_elems, uint64_t *sum, unsigned *bad,
-                                    cudaStream_t s)
+                                    uint32_t v_begin, uint32_t nrows, uint32_t num_vars, uint32_t L, uint4 *into,
+                                    uint32_t *into_st, uint64_t into_cap, uint4 **recs, uint32_t **stamps,
+                                    uint64_t *n_elems, uint64_t *sum, unsigned *bad, cudaStream_t s)
 {
     cudaError_t err = cudaSuccess;
     uint64_t *roff = nullptr, *start = nullptr, *rcnt = nullptr, *roffs = nullptr;
@@ -271,8 +271,8 @@ cudaError_t grg_fmt_csr5_to_records(const uint8_t *bytes, uint64_t num_edges, co
     size_t tscan = 0, tscan2 = 0;
     const uint64_t runs = (num_edges + EXPAND_RUN - 1) / EXPAND_RUN;
     uint32_t *rec = nullptr, *st = nullptr;
-    *recs = nullptr;
-    *stamps = nullptr;
+    if (recs) *recs = nullptr;
+    if (stamps) *stamps = nullptr;
     *n_elems = 0;
     *sum = 0;
     *bad = 0;
@@ -297,22 +297,35 @@ cudaError_t grg_fmt_csr5_to_records(const uint8_t *bytes, uint64_t num_edges, co
     FMT_CHECK(cudaMemcpyAsync(bad, dbad, 4, cudaMemcpyDeviceToHost, s));
     FMT_CHECK(cudaMemcpyAsync(n_elems, roffs + runs, 8, cudaMemcpyDeviceToHost, s));
     FMT_CHECK(cudaStreamSynchronize(s));
-    if (*bad || !*n_elems) goto done;
-    FMT_CHECK(cudaMalloc(&rec, *n_elems * 32));
-    FMT_CHECK(cudaMalloc(&st, *n_elems * 4));
+    if (*bad || !*n_elems || (!into && !recs)) goto done;
+    if (into) {
+        if (*n_elems > into_cap) {
+            err = cudaErrorInvalidValue;
+            goto done;
+        }
+        rec = reinterpret_cast<uint32_t *>(into);
+        st = into_st;
+    } else {
+        FMT_CHECK(cudaMalloc(&rec, *n_elems * 32));
+        FMT_CHECK(cudaMalloc(&st, *n_elems * 4));
+    }
     FMT_CHECK(cudaMemsetAsync(rec, 0, *n_elems * 32, s));
     k_fmt_fill<<<grid_of(*n_elems, 256), 256, 0, s>>>(st, *n_elems, 1u);
     // run u's edges belong to elements run_off[u] - 1 (continued) and run_off[u] .. run_off[u+1] - 1
     k_fmt_build<<<grid_of(runs, 256), 256, 0, s>>>(bytes, start, nrows, num_edges, v_begin, roffs, rec);
     FMT_CHECK(cudaGetLastError());
     FMT_CHECK(cudaStreamSynchronize(s));
-    *recs = reinterpret_cast<uint4 *>(rec);
-    *stamps = st;
+    if (!into) {
+        *recs = reinterpret_cast<uint4 *>(rec);
+        *stamps = st;
+    }
     rec = nullptr;
     st = nullptr;
 done:
-    cudaFree(rec);
-    cudaFree(st);
+    if (!into) {
+        cudaFree(rec);
+        cudaFree(st);
+    }
     cudaFree(tmp);
     cudaFree(rcnt);
     cudaFree(roff);

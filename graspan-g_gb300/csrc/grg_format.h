@@ -24,9 +24,15 @@ cudaError_t grg_fmt_records_to_csr5(const uint4 *rec, uint64_t n, uint32_t v_beg
 // 0-5, label << 25 | base, source row), each with stamp 1. *sum = the sum of
 // degree; nothing else is done unless it equals num_edges. *bad = 1 (a label
 // outside 1..L) | 2 (a destination >= num_vars); nothing is built then.
-// Otherwise *recs / *stamps are device arrays of *n_elems entries that the
-// caller frees with cudaFree. Returns after the records are complete.
+// Otherwise *n_elems = the number of records, and where they go depends on the
+// outputs given:
+//   into != null: written to into / into_st (room for into_cap records;
+//                 cudaErrorInvalidValue, nothing written, when they do not fit);
+//   recs != null: *recs / *stamps = new device arrays of *n_elems entries that
+//                 the caller frees with cudaFree;
+//   neither:      only counted.
+// Returns after the records are complete.
 cudaError_t grg_fmt_csr5_to_records(const uint8_t *bytes, uint64_t num_edges, const uint32_t *degree,
-                                    uint32_t v_begin, uint32_t nrows, uint32_t num_vars, uint32_t L, uint4 **recs,
-                                    uint32_t **stamps, uint64_t *n_elems, uint64_t *sum, unsigned *bad,
-                                    cudaStream_t s);
+                                    uint32_t v_begin, uint32_t nrows, uint32_t num_vars, uint32_t L, uint4 *into,
+                                    uint32_t *into_st, uint64_t into_cap, uint4 **recs, uint32_t **stamps,
+                                    uint64_t *n_elems, uint64_t *sum, unsigned *bad, cudaStream_t s);

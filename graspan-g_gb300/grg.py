@@ -19,7 +19,7 @@ COMP_PATH = os.path.join(HERE, "_build", "comp")
 OK = 0
 NEED_REPARTITION = 1
 PAUSED = 2
-E_ARG, E_CUDA, E_NOMEM, E_FILTER, E_IO, E_LABEL, E_RANGE, E_STATE, E_NODEV = -1, -2, -3, -4, -5, -6, -7, -8, -9
+E_ARG, E_CUDA, E_NOMEM, E_FILTER, E_IO, E_LABEL, E_RANGE, E_STATE, E_NODEV, E_INTERNAL = -1, -2, -3, -4, -5, -6, -7, -8, -9, -10
 MAX_RULES = 64
 MAX_LABELS = 63
 NAME_LEN = 64

@@ -11,7 +11,10 @@
  * takes plain pointers and sizes only.
  *
  * Threading: a context is used by one host thread at a time. All device work
- * of a context is issued on its stream (grg_set_stream).
+ * of a context is issued on its stream (grg_set_stream). Contexts share no
+ * device state: each passes its own grammar to every kernel it launches, so
+ * different contexts (with different grammars) can be used from different
+ * threads and streams at the same time.
  */
 #ifndef GRG_H
 #define GRG_H
@@ -36,6 +39,8 @@ extern "C" {
 #define GRG_E_RANGE (-7)         /* vertex id >= numVars, too many rules or labels */
 #define GRG_E_STATE (-8)         /* call made out of order */
 #define GRG_E_NODEV (-9)         /* no CUDA device */
+#define GRG_E_INTERNAL (-10)     /* a bounded internal loop ran out (table growth that did not
+                                    converge) or a consistency check failed; not a CUDA error */
 
 #define GRG_MAX_RULES 64
 #define GRG_MAX_LABELS 63        /* label ids 1..63; each may also get a reverse-index slot */
@@ -374,15 +379,19 @@ int grg_batch_release(grg_ctx *ctx, uint32_t job);
  * Limits: the tables take 28 bytes per (label, vertex) and the rest of the
  * array holds 198 bytes per element slot; graphs whose tables leave fewer
  * than 4096 slots, or with more edges than half the slots, are rejected with
- * GRG_E_RANGE before any launch; a closure that outgrows the array returns
- * GRG_E_NOMEM.
+ * GRG_E_RANGE before any launch. A graph whose loaded tables (at least 4
+ * slots per non-empty row) do not fit, or whose closure outgrows the array,
+ * returns GRG_E_NOMEM; the outputs are then left untouched and the next call
+ * starts from a cleared array as usual.
  *
  * The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture. Every call reuses the same array and clears it
- * itself, so calls that overlap on the GPU race, with each other and with a
- * grg_closure running on the same device (they share the rule table in
- * constant memory). */
+ * before any stream capture. The per-device address cache is written without
+ * a lock: two threads making their first calls on one device at once both
+ * store the same address, which is harmless. Every call reuses the same array
+ * and clears it itself, so calls that overlap on the GPU race with each other.
+ * The grammar travels with each launch, so a grg_closure of another context
+ * running at the same time is not affected. */
 #define GRG_NOALLOC_SCRATCH_BYTES (64ull << 20)
 int grg_closure_noalloc(int device, void *stream, int num_rules, const int *rules, int num_labels,
                         uint32_t filter, uint32_t num_vars, uint64_t num_edges, const uint32_t *d_src,

@@ -9,7 +9,8 @@ for p in (ROOT, PKG, os.path.join(ROOT, "tests")):
     if p not in sys.path:
         sys.path.insert(0, p)
 
-REFERENCE_SAMPLE = "/root/reference/src/inputFiles"
+# the reference's own sample inputs (src/inputFiles), copied unchanged
+REFERENCE_SAMPLE = os.path.join(ROOT, "tests", "fixtures")
 
 
 def pytest_configure(config):

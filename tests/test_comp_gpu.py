@@ -74,3 +74,67 @@ def test_partitioned_checkpoint_and_resume(grg_mod, oracle_mod, tmp_path):
     want, wdeg = r.csr5()
     assert np.array_equal(np.fromfile(out, np.uint8), want)
     assert np.array_equal(np.fromfile(out + ".degree", np.uint32), wdeg)
+
+
+# The reference's own sample (src/inputFiles, run by src/run.sh), copied to tests/fixtures.
+SAMPLE_COUNTS = {"M": 0, "DV": 0, "d": 352, "-d": 0, "V": 591, "MAM": 530, "AMs": 591, "MAs": 530,
+                 "Mq": 530, "MA": 0, "-a": 0, "AM": 61, "a": 61}
+
+
+def _sample_paths():
+    from conftest import REFERENCE_SAMPLE
+    return (os.path.join(REFERENCE_SAMPLE, "rules_pointsto.txt"),
+            os.path.join(REFERENCE_SAMPLE, "programGraph_sample_pointsto.txt"))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("parts", [0, 3])
+def test_reference_sample_inputs(grg_mod, oracle_mod, tmp_path, parts):
+    """`comp` on the reference's sample grammar and graph, argument order as in
+    src/run.sh, filter 0: the reference's stdout lines, 3246 closure edges with
+    the per-label counts, and the compressed stream byte for byte against the
+    oracle's writer (in core and over partitions)."""
+    gp, fp = _sample_paths()
+    out = str(tmp_path / "closure.bin")
+    extra = ["--partitions", parts] if parts else []
+    rc, so, se = run_comp(grg_mod, fp, gp, 0, "--out", out, *extra)
+    assert rc == 0, se
+    assert "NUM RULES: 12" in so and "NUM LABELS: 13" in so
+    assert "NUM VERTICES: 530" in so and "INITIAL NUM EDGES: 2000" in so
+    assert final_edges(so) == 3246
+    got = {m.group(1): int(m.group(2)) for m in re.finditer(r"^LABEL (\S+) EDGES: (\d+)$", so, re.M)}
+    assert got == SAMPLE_COUNTS
+    g = oracle_mod.parse_grammar(gp)
+    nv, s, d, l = oracle_mod.parse_graph(fp, g)
+    r = oracle_mod.closure(nv, g.rules, g.num_labels, 0, s, d, l)
+    assert r.total == 3246
+    want, wdeg = r.csr5()
+    assert np.array_equal(np.fromfile(out, np.uint8), want)
+    assert np.array_equal(np.fromfile(out + ".degree", np.uint32), wdeg)
+
+
+@pytest.mark.gpu
+def test_reference_sample_edges_through_library(grg_mod, oracle_mod):
+    """The same sample through the C ABI: identical sorted edge list and edge-set hash."""
+    gp, fp = _sample_paths()
+    g = grg_mod.parse_grammar(gp)
+    nv, s, d, l = grg_mod.parse_graph(fp, g)
+    ctx, st = grg_mod.run_closure(nv, g.rules, g.num_labels, 0, s, d, l, device=0)
+    go = oracle_mod.parse_grammar(gp)
+    r = oracle_mod.closure(nv, go.rules, go.num_labels, 0, *oracle_mod.parse_graph(fp, go)[1:])
+    assert st["total_edges"] == r.total == 3246
+    assert ctx.set_hash() == r.set_hash
+    for a, b in zip(ctx.export_edges(), r.edges()):
+        assert np.array_equal(a, b)
+    ctx.close()
+
+
+@pytest.mark.gpu
+def test_reference_sample_filter1_refused(grg_mod):
+    """filter 1 on the sample grammar: its binary rules have derivable second
+    symbols (AMs ::= AMs AM with AM derived), where the reference's answer
+    depends on its partition schedule; comp exits with the filter status."""
+    gp, fp = _sample_paths()
+    rc, so, se = run_comp(grg_mod, fp, gp, 1)
+    assert rc == 1
+    assert "filter_flag=1" in se

@@ -58,7 +58,6 @@ def test_parsers_match_oracle_and_generator(tmp_path, grg_mod, oracle_mod, make)
     assert np.array_equal(s, w.src[order]) and np.array_equal(d, w.dst[order]) and np.array_equal(l, w.lab[order])
 
 
-@pytest.mark.skipif(not os.path.isdir(REFERENCE_SAMPLE), reason="reference checkout not present")
 def test_parsers_on_reference_sample(grg_mod, oracle_mod):
     gp = os.path.join(REFERENCE_SAMPLE, "rules_pointsto.txt")
     fp = os.path.join(REFERENCE_SAMPLE, "programGraph_sample_pointsto.txt")

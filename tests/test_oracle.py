@@ -20,7 +20,6 @@ def _oracle_set(O, w, filter_flag=None):
     return r, set(zip(s.tolist(), d.tolist(), l.tolist()))
 
 
-@pytest.mark.skipif(not os.path.isdir(REFERENCE_SAMPLE), reason="reference checkout not present")
 def test_reference_sample_figure(oracle_mod):
     O = oracle_mod
     g = O.parse_grammar(os.path.join(REFERENCE_SAMPLE, "rules_pointsto.txt"))

@@ -99,3 +99,22 @@ def test_noalloc_refuses_invalid_edges(grg_mod):
     w.src = src
     st, counts, h, _ = _noalloc(lib, torch, w, 0)
     assert st == grg_mod.OK and (counts, h) == tuple(_allocating(grg_mod, w, 0)[:2])
+
+
+def test_noalloc_nomem_then_normal_call(grg_mod):
+    """A graph that passes the size check but whose closure outgrows the static
+    array (a 20k-vertex dataflow graph whose closure is ~V^2 edges) returns
+    GRG_E_NOMEM with the outputs untouched; the next call on a small graph
+    starts from a cleared array and matches the allocating path bit for bit."""
+    torch = pytest.importorskip("torch")
+    lib = grg_mod.load_library()
+    big = G.dataflow_small(seed=31, num_vars=20_000, num_edges=60_000)
+    st, counts, _, _ = _noalloc(lib, torch, big, 0)
+    assert st == grg_mod.E_NOMEM, grg_mod.error_string(st)
+    assert counts == [2**64 - 1] * big.num_labels       # outputs untouched
+    small = G.pointsto(seed=32, num_vars=500, num_edges=1500)
+    want = _allocating(grg_mod, small, 0)
+    for _ in range(2):
+        st, counts, h, rounds = _noalloc(lib, torch, small, 0)
+        assert st == grg_mod.OK
+        assert (counts, h, rounds) == want
