@@ -91,6 +91,14 @@ struct RuleTable {
     uint8_t ol_A[MAX_RULES], ol_B[MAX_RULES], ol_C[MAX_RULES];
     uint8_t dindex[MAX_LABELS + 1];          // label C: index this round's deltas per row
     uint8_t track[MAX_SLOTS + 2];            // slot: new bits become deltas
+    // labels stored by destination: the table of (label, row j) holds the sources
+    // i of edges (i, j), as 192-id elements over i. A binary rule A ::= B C whose
+    // B and A are stored so and whose C is never derived is then joined by pushing
+    // each delta element of B at column k, whole, into A's column j for every
+    // edge (k, j) of C -- bit-parallel over the sources, where the join by source
+    // rows visits every source-intermediate pair. Chosen per label when the
+    // grammar allows it (see plan_columns); C stays stored by source.
+    uint8_t tpose[MAX_LABELS + 1];
     // labels never inserted into after the load that are a rule's second
     // symbol also get a CSR copy (row pointers + destination ids): joins read
     // 4 bytes per edge instead of a 32-byte element per 192-id block

@@ -86,6 +86,51 @@ static int make_rule_table(const int *rules, int R, int L, uint32_t filter, Rule
     return GRG_OK;
 }
 
+// Labels that can be stored by destination (bit l-1 = label l; see RuleTable::tpose).
+// Decided from the grammar alone, so the layout chosen at the load holds under
+// either filter. Start from every label a rule derives and drop labels until:
+//  - a binary rule A ::= B C whose C is derived needs old-left joins, which read
+//    rows of B and C by source: A, B and C stay by source;
+//  - a binary rule A ::= B C with a C that is never derived joins by pushing B's
+//    columns along C's source rows: A and B are stored alike (both or neither);
+//  - a unary rule A ::= B keeps the orientation (A and B alike), except that A may
+//    be stored by destination when B is never derived: B's loaded edges are then
+//    turned around once, in round 1;
+//  - a label read as a rule's second symbol is never derived here, so it stays by
+//    source (its rows, or their CSR copy, are what a push walks).
+// Labels no rule derives stay by source (they are inputs: read as second symbols
+// or unary sources by source rows).
+static uint64_t plan_columns(const int *rules, int R, int L)
+{
+    bool der[MAX_LABELS + 1] = {false};
+    for (int q = 0; q < R; q++) der[rules[3 * q]] = true;
+    uint64_t t = 0;
+    for (int l = 1; l <= L; l++)
+        if (der[l]) t |= 1ull << (l - 1);
+    auto in = [&](int l) { return l >= 1 && ((t >> (l - 1)) & 1ull); };
+    auto drop = [&](int l) { if (l >= 1) t &= ~(1ull << (l - 1)); };
+    for (bool changed = true; changed;) {
+        const uint64_t before = t;
+        for (int q = 0; q < R; q++) {
+            const int A = rules[3 * q], B = rules[3 * q + 1], C = rules[3 * q + 2];
+            if (B && C) {
+                if (der[C]) { drop(A); drop(B); drop(C); }
+                else if (in(A) != in(B)) { drop(A); drop(B); }
+            } else if (B) {
+                if (in(B) && !in(A)) drop(B);
+                if (in(A) && !in(B) && der[B]) drop(A);
+            }
+        }
+        changed = t != before;
+    }
+    return t;
+}
+
+static void set_columns(RuleTable &rt, uint64_t tmask, int L)
+{
+    for (int l = 1; l <= L; l++) rt.tpose[l] = (uint8_t)((tmask >> (l - 1)) & 1ull);
+}
+
 
 // Join tuning (compile-time; -DGRG_... overrides for sweeps)
 #ifndef GRG_JOIN_WARPS
@@ -175,13 +220,16 @@ __device__ __forceinline__ bool edge_ok(Dev d, uint32_t s, uint32_t t, uint32_t 
     return true;
 }
 
+// tmask: labels stored by destination (bit l-1): their edges go to the table of
+// the destination, as the source's bit.
 __global__ void k_load_hist(Dev d, const uint32_t *src, const uint32_t *dst, const uint8_t *lab, uint64_t n,
-                            uint32_t base, uint32_t nv, uint32_t L)
+                            uint32_t base, uint32_t nv, uint32_t L, unsigned long long tmask)
 {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t s = src[i], l = lab[i];
-        if (!edge_ok(d, s, dst[i], l, nv, L, true)) continue;
-        atomicAdd(&d.cnt[(size_t)(l - 1) * d.V + base + s], 1u);
+        const uint32_t s = src[i], t = dst[i], l = lab[i];
+        if (!edge_ok(d, s, t, l, nv, L, true)) continue;
+        const uint32_t row = ((tmask >> (l - 1)) & 1ull) ? t : s;
+        atomicAdd(&d.cnt[(size_t)(l - 1) * d.V + base + row], 1u);
     }
 }
 
@@ -234,16 +282,19 @@ __global__ void k_load_alloc(Dev d, uint32_t first, uint32_t nv, uint32_t L, Min
 }
 
 __global__ void k_load_insert(Dev d, const uint32_t *src, const uint32_t *dst, const uint8_t *lab, uint64_t n,
-                              uint32_t vbase, uint32_t nv, uint32_t L)
+                              uint32_t vbase, uint32_t nv, uint32_t L, unsigned long long tmask)
 {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        if (!edge_ok(d, src[i], dst[i], lab[i], nv, L, false)) continue;
-        const uint32_t v = vbase + dst[i];
+        const uint32_t l = lab[i];
+        if (!edge_ok(d, src[i], dst[i], l, nv, L, false)) continue;
+        const bool by_dst = (tmask >> (l - 1)) & 1ull;
+        const uint32_t row = vbase + (by_dst ? dst[i] : src[i]);
+        const uint32_t v = vbase + (by_dst ? src[i] : dst[i]);
         Bits b;
         const uint32_t o = v % EIDS;
 #pragma unroll
         for (int w = 0; w < EW; w++) b.w[w] = (uint32_t)w == (o >> 5) ? 1u << (o & 31) : 0u;
-        if (!g_insert(d, lab[i], vbase + src[i], v / EIDS, b, false)) atomicOr(&d.ctr[C_ERR], (unsigned long long)ERR_LOAD);
+        if (!g_insert(d, l, row, v / EIDS, b, false)) atomicOr(&d.ctr[C_ERR], (unsigned long long)ERR_LOAD);
     }
 }
 
@@ -770,6 +821,122 @@ __global__ void __launch_bounds__(256, 8) k_apply(Dev d, const uint4 *__restrict
     }
 }
 
+// Delta records of labels stored by destination (RuleTable::tpose). A record
+// (label B, column k, base, bits = sources i of new edges (i, k)) is pushed
+// whole: a unary rule A ::= B puts it into A's column k, a binary rule A ::= B C
+// into A's column j for every edge (k, j) of C (C's CSR copy, or its table
+// elements by source) -- one element insert per edge of C, for up to 192
+// sources at once. The kernel also turns around the records of a label stored
+// by source that a unary rule A ::= B copies into a destination-stored A (B's
+// loaded edges, in round 1): one single-bit insert per edge. One thread per
+// record; a record with an insert into a full table goes to the retry list,
+// as in k_join (pushing a record again adds nothing twice).
+// n_ctr >= 0: the record count is device counter n_ctr (round graphs).
+__global__ void __launch_bounds__(256, 4) k_push(Dev d, const uint4 *__restrict__ recs, uint64_t n, int n_ctr,
+                                                  uint4 *retry_out)
+{
+    if (d.ctr[C_HALT]) return;
+    if (n_ctr >= 0) n = d.ctr[n_ctr];
+    unsigned long long n_left = 0, n_right = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    // i0 is the same for every thread of a block, so each warp runs the ballot together
+    for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x; i0 < n; i0 += stride) {
+        const uint64_t i = i0 + threadIdx.x;
+        bool failed = false;
+        uint4 a = make_uint4(0, 0, 0, 0), b = make_uint4(0, 0, EMPTY, 0);
+        if (i < n) {
+            a = recs[2 * i];
+            b = recs[2 * i + 1];
+        }
+        const uint32_t B = b.z >> KEY_SHIFT, base = b.z & BASE_MASK, row = b.w;
+        if (i < n && B >= 1 && B <= (uint32_t)d.rt.L) {
+            Bits bits;
+            bits.w[0] = a.x; bits.w[1] = a.y; bits.w[2] = a.z; bits.w[3] = a.w; bits.w[4] = b.x; bits.w[5] = b.y;
+            bool ok = true;
+            if (d.rt.tpose[B]) {
+                for (uint32_t u = d.rt.un_start[B]; u < d.rt.un_start[B + 1]; u++) {
+                    const uint32_t A = d.rt.un_A[u];
+                    ok &= g_insert_t<true>(d, A, row, base, bits, d.rt.track[A]);
+                }
+                for (uint32_t q = d.rt.bin_start[B]; q < d.rt.bin_start[B + 1]; q++) {
+                    const uint32_t A = d.rt.bin_A[q], C = d.rt.bin_C[q];
+                    const bool tr = d.rt.track[A];
+                    n_left++;
+                    const uint2 *cr = d.rt.csr_row[C];
+                    if (cr) {
+                        const uint2 rw = __ldg(cr + row);
+                        const uint32_t *col = d.rt.csr_col[C] + rw.x;
+                        const uint32_t cnt = rw.y & 0xFFFFFFu;
+                        n_right += cnt;
+                        for (uint32_t t = 0; t < cnt; t++) ok &= g_insert_t<true>(d, A, __ldg(col + t), base, bits, tr);
+                    } else {
+                        const size_t ti = (size_t)(C - 1) * d.V + row;
+                        const uint64_t de = __ldg(d.desc + ti);
+                        const uint32_t off = (uint32_t)de;
+                        uint32_t cap = (uint32_t)(de >> 32);
+                        if (prefix_table(d, C, cap)) cap = min(cap, __ldcg(d.cnt + ti));
+                        for (uint32_t t = 0; t < cap; t++) {
+                            const uint32_t *e = d.elems + (size_t)(off + t) * 8;
+                            const uint32_t ek = __ldcg(e + 6);
+                            if (ek == EMPTY) continue;
+                            const uint32_t eb = (ek & BASE_MASK) * EIDS;
+#pragma unroll 1
+                            for (int x = 0; x < EW; x++) {
+                                uint32_t w = __ldcg(e + x);
+                                while (w) {
+                                    const uint32_t j = eb + x * 32 + (__ffs(w) - 1);
+                                    w &= w - 1;
+                                    n_right++;
+                                    ok &= g_insert_t<true>(d, A, j, base, bits, tr);
+                                }
+                            }
+                        }
+                    }
+                }
+            } else {
+                for (uint32_t u = d.rt.un_start[B]; u < d.rt.un_start[B + 1]; u++) {
+                    const uint32_t A = d.rt.un_A[u];
+                    if (!d.rt.tpose[A]) continue;
+                    Bits one;
+                    const uint32_t o = row % EIDS;
+#pragma unroll
+                    for (int x = 0; x < EW; x++) one.w[x] = (uint32_t)x == (o >> 5) ? 1u << (o & 31) : 0u;
+#pragma unroll 1
+                    for (int x = 0; x < EW; x++) {
+                        uint32_t w = bits.w[x];
+                        while (w) {
+                            const uint32_t j = base * EIDS + x * 32 + (__ffs(w) - 1);
+                            w &= w - 1;
+                            ok &= g_insert(d, A, j, row / EIDS, one, d.rt.track[A]);
+                        }
+                    }
+                }
+            }
+            failed = !ok;
+        }
+        const unsigned fm = __ballot_sync(0xffffffffu, failed);
+        if (fm) {
+            const uint32_t lane = lane_id();
+            unsigned long long p = 0;
+            if (lane == (uint32_t)(__ffs(fm) - 1)) p = atomicAdd(&d.ctr[C_RETRY_N], (unsigned long long)__popc(fm));
+            p = __shfl_sync(0xffffffffu, p, __ffs(fm) - 1);
+            const uint64_t o = p + __popc(fm & ((1u << lane) - 1u));
+            if (failed && o < d.retry_cap) {
+                retry_out[2 * o] = a;
+                retry_out[2 * o + 1] = b;
+            }
+        }
+    }
+    for (int o = 16; o; o >>= 1) {
+        n_left += __shfl_xor_sync(0xffffffffu, n_left, o);
+        n_right += __shfl_xor_sync(0xffffffffu, n_right, o);
+    }
+    if (lane_id() == 0) {
+        if (n_left) atomicAdd(&d.ctr[C_LEFT], n_left);
+        if (n_right) atomicAdd(&d.ctr[C_RIGHT], n_right);
+    }
+}
+
 // Small rounds: a warp joins 32 records, so a round of few, dense records (alias
 // rows reach a whole block) leaves most SMs idle. Below SPLIT_MAX records the
 // round's gathered and virtual records are cut into sub-records of at most
@@ -799,6 +966,14 @@ __global__ void k_split(Dev d, const uint4 *__restrict__ grecs, const uint4 *__r
         uint32_t p = 0;
 #pragma unroll
         for (int x = 0; x < EW; x++) p += __popc(w[x]);
+        const uint32_t lab = b.z >> KEY_SHIFT;
+        if (p && lab <= (uint32_t)MAX_LABELS && d.rt.tpose[lab]) {
+            // a column's record is pushed whole (its bits cost nothing extra): never split
+            const uint64_t pos = atomicAdd(&d.ctr[C_SPLIT_N], 1ull);
+            out[2 * pos] = a;
+            out[2 * pos + 1] = b;
+            continue;
+        }
         const uint32_t parts = (p + SPLIT_BITS - 1) / SPLIT_BITS;
         if (!parts) continue;
         uint64_t pos = atomicAdd(&d.ctr[C_SPLIT_N], (unsigned long long)parts);
@@ -874,7 +1049,10 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
 #pragma unroll
             for (int x = 0; x < EW; x++) rb.w[x] = 0;
         }
-        const uint32_t B = have ? key >> KEY_SHIFT : 0, base = key & BASE_MASK;
+        // records of labels stored by destination are pushed by k_push, not joined here
+        const uint32_t B = (have && !((key >> KEY_SHIFT) <= (uint32_t)MAX_LABELS && d.rt.tpose[key >> KEY_SHIFT]))
+                               ? key >> KEY_SHIFT : 0,
+                       base = key & BASE_MASK;
 #pragma unroll
         for (int x = 0; x < EW; x++) w.rbits[lane][x] = rb.w[x];
         w.rrow[lane] = row;
@@ -894,8 +1072,10 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
         for (uint32_t u = 0; u < maxu; u++) {
             if (u < nu) {
                 const uint32_t A = d.rt.un_A[d.rt.un_start[B] + u];
-                ok &= g_insert(d, A, row, base, rb, d.rt.track[A]);
-                inserts++;
+                if (!d.rt.tpose[A]) {          // into a label stored by destination: k_push turns it around
+                    ok &= g_insert(d, A, row, base, rb, d.rt.track[A]);
+                    inserts++;
+                }
             }
         }
 
@@ -1296,8 +1476,11 @@ __global__ void k_grow(Dev d, uint64_t n)
 // ---------------------------------------------------------------- results
 
 // One warp per table of a label slot: edge/element counts, optional degree and hash.
+// by_dst: the label is stored by destination (rows are destinations), which only
+// turns the hash terms around; degrees need tables by source.
 __global__ void k_count(Dev d, uint32_t slot, uint32_t *deg_edges, uint32_t *deg_elems, uint32_t first,
-                        uint32_t last, int do_hash, uint32_t r0, uint32_t r1, uint32_t hash_base, uint32_t id0)
+                        uint32_t last, int do_hash, uint32_t r0, uint32_t r1, uint32_t hash_base, uint32_t id0,
+                        int by_dst)
 {
     const uint32_t lane = lane_id();
     const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
@@ -1319,7 +1502,10 @@ __global__ void k_count(Dev d, uint32_t slot, uint32_t *deg_edges, uint32_t *deg
                     while (bw) {
                         const int bit = __ffs(bw) - 1;
                         bw &= bw - 1;
-                        my_hash += edge_hash(slot - hash_base, (uint32_t)v - id0, hb * EIDS + x * 32 + bit - id0);
+                    {
+                        const uint32_t a = (uint32_t)v - id0, b = hb * EIDS + x * 32 + bit - id0;
+                        my_hash += by_dst ? edge_hash(slot - hash_base, b, a) : edge_hash(slot - hash_base, a, b);
+                    }
                     }
             }
         }
@@ -1338,7 +1524,7 @@ __global__ void k_count(Dev d, uint32_t slot, uint32_t *deg_edges, uint32_t *deg
     if (lane == 0 && my_hash) atomicAdd(&d.ctr[C_HASH], my_hash);
 }
 
-__global__ void k_export(Dev d, uint32_t slot, uint32_t *src, uint32_t *dst, uint8_t *lab, uint64_t cap_out)
+__global__ void k_export(Dev d, uint32_t slot, uint32_t *src, uint32_t *dst, uint8_t *lab, uint64_t cap_out, int by_dst)
 {
     const uint64_t n = (uint64_t)d.V;
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
@@ -1358,8 +1544,9 @@ __global__ void k_export(Dev d, uint32_t slot, uint32_t *src, uint32_t *dst, uin
                     const int bit = __ffs(bw) - 1;
                     bw &= bw - 1;
                     if (pos < cap_out) {
-                        src[pos] = (uint32_t)v;
-                        dst[pos] = hb * EIDS + x * 32 + bit;
+                        const uint32_t o = hb * EIDS + x * 32 + bit;
+                        src[pos] = by_dst ? o : (uint32_t)v;
+                        dst[pos] = by_dst ? (uint32_t)v : o;
                         lab[pos] = (uint8_t)slot;
                     }
                     pos++;
@@ -1604,6 +1791,13 @@ struct grg_ctx {
     std::vector<uint64_t> rg_key;          // pointers and sizes the recorded launches hold
     int rg_kernels = 0;                    // kernels per recorded round
     RuleTable rt{};
+    // labels stored by destination in the loaded graph (bit l-1), and whether loads
+    // may choose that layout (grg_set_layout)
+    uint64_t tmask = 0;
+    int layout_mode = 1;
+    // kernels a join pass needs under the current rule table: k_join for records
+    // joined by source rows, k_push for records of destination-stored labels
+    bool need_join = true, need_push = false;
     uint64_t launches = 0;
     // CSR copies of static labels, per label; reused by later closures while they fit
     struct CsrBuf {
@@ -1906,6 +2100,7 @@ int build_rules(grg_ctx *c, uint32_t filter, RuleTable &rt)
     bool derivable[MAX_LABELS + 1];
     const int st = make_rule_table(c->rules, c->R, c->L, filter, rt, derivable);
     if (st) return fail(c, st, status_text(st));
+    set_columns(rt, c->tmask, c->L);
     return GRG_OK;
 }
 
@@ -1950,6 +2145,8 @@ int grg_create(grg_ctx **out, int device)
     if (rr && atoll(rr) > 0) c->retry_min = (uint64_t)atoll(rr);
     const char *jw = getenv("GRG_JOIN_WINDOW");        // "narrow" / "wide"; otherwise chosen per closure
     if (jw) c->join_window_mode = !strcmp(jw, "narrow") ? 0 : !strcmp(jw, "wide") ? 1 : 2;
+    const char *ly = getenv("GRG_LAYOUT");             // "rows": every label stored by source
+    if (ly && !strcmp(ly, "rows")) c->layout_mode = 0;
     *out = c;
     return GRG_OK;
 }
@@ -2007,6 +2204,13 @@ int grg_set_device_rounds(grg_ctx *c, int on)
 {
     if (!c) return GRG_E_ARG;
     c->device_rounds = on != 0;
+    return GRG_OK;
+}
+
+int grg_set_layout(grg_ctx *c, int mode)
+{
+    if (!c || mode < 0 || mode > 1) return GRG_E_ARG;
+    c->layout_mode = mode;
     return GRG_OK;
 }
 
@@ -2179,6 +2383,7 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
     c->elem_loaded = false;
     int st = setup_tables(c, num_vars);
     if (st) return st;
+    c->tmask = c->layout_mode ? plan_columns(c->rules, c->R, c->L) : 0;
     cudaStream_t s = c->stream;
     const uint32_t *dsrc = src, *ddst = dst;
     const uint8_t *dlab = label;
@@ -2195,7 +2400,8 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
     c->launches = 0;
     auto hist = [&](Dev d) {
         if (num_edges) {
-            k_load_hist<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges, 0, num_vars, (uint32_t)c->L);
+            k_load_hist<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges, 0, num_vars, (uint32_t)c->L,
+                                                                    c->tmask);
             c->launches++;
         }
         for (int q = 0; q < c->R; q++)
@@ -2227,7 +2433,8 @@ int grg_load_edges(grg_ctx *c, uint32_t num_vars, uint64_t num_edges, const uint
     if ((st = input_status(c))) return st;
     Dev d = make_dev(c);
     if (num_edges) {
-        k_load_insert<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges, 0, num_vars, (uint32_t)c->L);
+        k_load_insert<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges, 0, num_vars, (uint32_t)c->L,
+                                                                  c->tmask);
         c->launches++;
     }
     for (int q = 0; q < c->R; q++)
@@ -2265,6 +2472,7 @@ int grg_load_elements(grg_ctx *c, uint32_t num_vars, uint64_t num_elems, const u
     c->elem_loaded = true;
     int st = setup_tables(c, num_vars);
     if (st) return st;
+    c->tmask = 0;                         // element images are rows by source
     cudaStream_t s = c->stream;
     const uint4 *drec = reinterpret_cast<const uint4 *>(elems);
     const uint32_t *dst_ = stamps;
@@ -2346,6 +2554,46 @@ static void launch_join(const grg_ctx *c, int grid, cudaStream_t s, const Dev &d
         k_join<WIN2, WIN2_LO><<<grid, JOIN_WARPS * 32, 0, s>>>(d, recs, n, n_ctr, retry_out);
     else
         k_join<WIN, WIN_LO><<<grid, JOIN_WARPS * 32, 0, s>>>(d, recs, n, n_ctr, retry_out);
+}
+
+// Which pass kernels the rule table needs: k_join unless every record it could
+// see belongs to a destination-stored label (pushed) or only feeds unary rules
+// into one; k_push when a destination-stored label has records, or a unary rule
+// turns a source-stored label into one.
+static void set_passes(grg_ctx *c)
+{
+    const RuleTable &rt = c->rt;
+    c->need_join = rt.nol > 0;
+    c->need_push = false;
+    for (int B = 1; B <= c->L; B++) {
+        if (!rt.track[B]) continue;
+        if (rt.tpose[B]) {
+            c->need_push = true;
+            continue;
+        }
+        if (rt.bin_start[B + 1] > rt.bin_start[B]) c->need_join = true;
+        for (int u = rt.un_start[B]; u < rt.un_start[B + 1]; u++) {
+            if (rt.tpose[rt.un_A[u]]) c->need_push = true;
+            else c->need_join = true;
+        }
+    }
+}
+
+// One join pass over n records (or the device count n_ctr): the kernels the rule
+// table needs, each taking its own records and skipping the others'.
+static void launch_pass(grg_ctx *c, int grid, cudaStream_t s, const Dev &d, const uint4 *recs, uint64_t n, int n_ctr,
+                        uint4 *retry_out, uint64_t &joins)
+{
+    if (c->need_join) {
+        launch_join(c, grid, s, d, recs, n, n_ctr, retry_out);
+        c->launches++;
+        joins++;
+    }
+    if (c->need_push) {
+        k_push<<<c->sms * 8, 256, 0, s>>>(d, recs, n, n_ctr, retry_out);
+        c->launches++;
+        joins++;
+    }
 }
 
 // ---------------------------------------------------------------- join-window tuning
@@ -2556,16 +2804,13 @@ static void first_pass_joins(grg_ctx *c, const Dev &d, uint64_t nd, uint64_t nv,
 {
     cudaStream_t s = c->stream;
     if (split) {
-        launch_join(c, grid_for(c, ((nd + nv) * SPLIT_PARTS + RB - 1) / RB, JOIN_WARPS, 16), s, d, c->sbuf, 0,
-                    C_SPLIT_N, c->rbuf[0]);
-        c->launches++;
-        joins++;
+        launch_pass(c, grid_for(c, ((nd + nv) * SPLIT_PARTS + RB - 1) / RB, JOIN_WARPS, 16), s, d, c->sbuf, 0,
+                    C_SPLIT_N, c->rbuf[0], joins);
         return;
     }
-    launch_join(c, grid_for(c, (nd + RB - 1) / RB, JOIN_WARPS, 16), s, d, c->gbuf, nd, -1, c->rbuf[0]);
-    c->launches++;
-    joins++;
+    launch_pass(c, grid_for(c, (nd + RB - 1) / RB, JOIN_WARPS, 16), s, d, c->gbuf, nd, -1, c->rbuf[0], joins);
     if (nv) {
+        // virtual old-left records: joined by source rows only
         launch_join(c, grid_for(c, (nv + RB - 1) / RB, JOIN_WARPS, 16), s, d, c->vbuf, nv, -1, c->rbuf[0]);
         c->launches++;
         joins++;
@@ -2614,9 +2859,8 @@ static int round_retries(grg_ctx *c, uint64_t nr, uint64_t nf, grg_stats &S, dou
             first_pass_joins(c, d, nd, nv, split, joins);
             rb = 0;
         } else if (nr) {
-            launch_join(c, grid_for(c, (nr + RB - 1) / RB, JOIN_WARPS, 16), s, d, c->rbuf[rb], nr, -1, c->rbuf[rb ^ 1]);
-            c->launches++;
-            joins++;
+            launch_pass(c, grid_for(c, (nr + RB - 1) / RB, JOIN_WARPS, 16), s, d, c->rbuf[rb], nr, -1, c->rbuf[rb ^ 1],
+                        joins);
             rb ^= 1;
         }
         if (c->cand_cap) {
@@ -2660,7 +2904,7 @@ static int round_joins(grg_ctx *c, uint64_t nd, uint64_t nv, grg_stats &S, doubl
         k_split<<<grid_for(c, nd + nv, 256), 256, 0, s>>>(d, c->gbuf, c->vbuf, c->sbuf);
         c->launches++;
     }
-    if (c->tune_pending && !split && nd >= TUNE_MIN_RECORDS) {
+    if (c->tune_pending && c->need_join && !split && nd >= TUNE_MIN_RECORDS) {
         if ((st = tune_first_pass(c, d, nd, nv, joins))) return st;
     } else {
         first_pass_joins(c, d, nd, nv, split, joins);
@@ -2763,7 +3007,8 @@ static std::vector<uint64_t> round_graph_key(const grg_ctx *c, uint32_t rs, uint
                                (uint64_t)c->cand[1], c->cand_cap, (uint64_t)c->chunk, nchunks, (uint64_t)c->drs,
                                (uint64_t)c->drc, (uint64_t)c->dvm, c->pool_cap, c->V, rs, (uint64_t)c->timing,
                                (uint64_t)c->elem_loaded, (uint64_t)c->rt.nol, (uint64_t)c->row_job,
-                               (uint64_t)c->job_cnt, c->max_jobs, (uint64_t)c->join_wide, (uint64_t)c->sbuf};
+                               (uint64_t)c->job_cnt, c->max_jobs, (uint64_t)c->join_wide, (uint64_t)c->sbuf,
+                               (uint64_t)c->need_join, (uint64_t)c->need_push};
     for (int l = 1; l <= c->L; l++) k.push_back(c->rt.dindex[l]);
     // the rule table is a parameter of every recorded launch
     uint64_t w[(sizeof(RuleTable) + 7) / 8] = {0};
@@ -2844,9 +3089,15 @@ static int build_round_graph(grg_ctx *c, uint32_t rs)
     const int jgrid = grid_for(c, ~0u, JOIN_WARPS, 16);
     cudaMemsetAsync(ctr + C_SPLIT_N, 0, 8, s);
     k_split<<<grid_for(c, SPLIT_MAX, 256), 256, 0, s>>>(d, c->gbuf, c->vbuf, c->sbuf);
-    launch_join(c, jgrid, s, d, c->gbuf, 0, C_JN1, c->rbuf[0]);
-    launch_join(c, jgrid, s, d, c->sbuf, 0, C_SPLIT_N, c->rbuf[0]);
-    nk += 3;
+    nk++;
+    {
+        const uint64_t launches0 = c->launches;
+        uint64_t unused = 0;
+        launch_pass(c, jgrid, s, d, c->gbuf, 0, C_JN1, c->rbuf[0], unused);
+        launch_pass(c, jgrid, s, d, c->sbuf, 0, C_SPLIT_N, c->rbuf[0], unused);
+        nk += (int)(c->launches - launches0);
+        c->launches = launches0;
+    }
     if (c->rt.nol) {
         launch_join(c, jgrid, s, d, c->vbuf, 0, C_JN2, c->rbuf[0]);
         nk++;
@@ -2935,7 +3186,7 @@ static int run_rounds(grg_ctx *c, uint64_t max_rounds, grg_stats &S, double &joi
         const unsigned long long halt = c->h_ctr[C_HALT], rounds = c->h_ctr[C_GROUNDS];
         S.rounds += rounds;
         S.delta_elems += c->h_ctr[C_GDSUM];
-        joins += rounds * (c->rt.nol ? 2 : 1);
+        joins += rounds * ((c->need_join ? 1 : 0) + (c->need_push ? 1 : 0) + (c->rt.nol ? 1 : 0));
         c->launches += c->h_ctr[C_ITERS] * c->rg_kernels;
         join_ms += c->h_ctr[C_JNS] * 1e-6;
         done_rounds += rounds;
@@ -3060,6 +3311,7 @@ int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *s
         rt.csr_col[l] = cb.col;
     }
     c->rt = rt;
+    set_passes(c);
     st = read_ctr(c);
     if (st) return st;
     const uint64_t top = c->h_ctr[C_POOL_TOP];
@@ -3089,6 +3341,7 @@ int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *s
     S.window_tuned = (uint64_t)c->tune_source;
     S.window_trial_ms[0] = c->tune_ms[0];
     S.window_trial_ms[1] = c->tune_ms[1];
+    S.column_labels = c->tmask;
     c->tune_pending = false;              // an untimed closure leaves its key for the next one
     S.right_elems = c->h_ctr[C_RIGHT];
     S.out_elems = S.delta_elems;
@@ -3113,7 +3366,8 @@ static int count_pass(grg_ctx *c, uint32_t *deg_e, uint32_t *deg_el, uint32_t fi
     GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_LABEL0, 0, sizeof(unsigned long long) * (MAX_SLOTS + 2), s));
     GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_HASH, 0, 8, s));
     for (int l = 1; l <= c->L; l++)
-        k_count<<<grid_for(c, (uint64_t)c->V * 32, 256), 256, 0, s>>>(d, (uint32_t)l, deg_e, deg_el, first, last, do_hash, 0, c->V, 0, 0);
+        k_count<<<grid_for(c, (uint64_t)c->V * 32, 256), 256, 0, s>>>(d, (uint32_t)l, deg_e, deg_el, first, last, do_hash,
+                                                                       0, c->V, 0, 0, (int)((c->tmask >> (l - 1)) & 1));
     GRG_CUDA(c, cudaGetLastError());
     return read_ctr(c);
 }
@@ -3140,12 +3394,50 @@ int grg_set_hash(grg_ctx *c, uint64_t *hash)
     return GRG_OK;
 }
 
+static int stage_elements(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t *n_out);
+
+// Labels stored by destination are turned back into rows by source; every entry
+// point that reads rows by source (degrees, element images, ranges, streams)
+// calls this first. The graph's element records are staged, the
+// destination-stored ones transposed on the device, 192 x 192 tiles at a time,
+// and everything is reloaded as an element image with no deltas marked. A closed
+// graph stays closed. Not available on a batch context.
+static int rows_by_source(grg_ctx *c)
+{
+    if (!c->tmask || !c->loaded) return GRG_OK;
+    if (c->batch) return fail(c, GRG_E_STATE, "rows by source are not available on a batch context");
+    const bool closed = c->closed;
+    uint64_t n = 0;
+    int st = stage_elements(c, 0, c->V, &n);
+    if (st) return st;
+    uint4 *rows = nullptr;
+    uint32_t *stamps = nullptr;
+    uint64_t m = 0;
+    cudaError_t e = grg_fmt_columns_to_rows(c->xbuf, n, c->tmask, &rows, &m, c->stream);
+    if (e == cudaSuccess) e = cudaMalloc(&stamps, std::max<uint64_t>(m, 1) * 4);
+    if (e == cudaSuccess) e = cudaMemsetAsync(stamps, 0, std::max<uint64_t>(m, 1) * 4, c->stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(rows);
+        cudaFree(stamps);
+        return fail(c, e == cudaErrorMemoryAllocation ? GRG_E_NOMEM : GRG_E_CUDA,
+                    std::string("turning columns into rows: ") + cudaGetErrorString(e));
+    }
+    st = grg_load_elements(c, c->V, m, reinterpret_cast<const uint32_t *>(rows), stamps, ~0u, 1);
+    cudaFree(rows);
+    cudaFree(stamps);
+    if (st) return st;
+    c->closed = closed;
+    return GRG_OK;
+}
+
 int grg_get_degree(grg_ctx *c, uint32_t first_var, uint32_t last_var, uint32_t *degree)
 {
     if (!c || !degree || last_var < first_var) return GRG_E_ARG;
     if (!c->loaded) return fail(c, GRG_E_STATE, "no graph loaded");
     if (last_var >= c->V) return fail(c, GRG_E_RANGE, "vertex range beyond numVars");
     cudaSetDevice(c->device);
+    if (int rs = rows_by_source(c)) return rs;
     const uint64_t n = (uint64_t)last_var - first_var + 1;
     uint32_t *dd = nullptr;
     GRG_CUDA(c, cudaMalloc(&dd, n * 8));
@@ -3175,7 +3467,8 @@ int grg_export_edges(grg_ctx *c, uint64_t cap, uint32_t *src, uint32_t *dst, uin
     GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_EXPORT, 0, 8, s));
     Dev d = make_dev(c);
     for (int l = 1; l <= c->L; l++)
-        k_export<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)l, d32, d32 ? d32 + cap : nullptr, d8, cap);
+        k_export<<<grid_for(c, c->V, 256), 256, 0, s>>>(d, (uint32_t)l, d32, d32 ? d32 + cap : nullptr, d8, cap,
+                                                         (int)((c->tmask >> (l - 1)) & 1));
     int st = read_ctr(c);
     if (st) { cudaFree(d32); cudaFree(d8); return st; }
     *num_out = c->h_ctr[C_EXPORT];
@@ -3191,8 +3484,6 @@ int grg_export_edges(grg_ctx *c, uint64_t cap, uint32_t *src, uint32_t *dst, uin
     return GRG_OK;
 }
 
-static int stage_elements(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t *n_out);
-
 int grg_export_elements(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t cap, uint32_t *elems,
                         uint32_t *stamps, uint64_t *num_out)
 {
@@ -3200,6 +3491,7 @@ int grg_export_elements(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t c
     if (!c->loaded) return fail(c, GRG_E_STATE, "no graph loaded");
     if (v_end > c->V) return fail(c, GRG_E_RANGE, "vertex range beyond the graph");
     cudaSetDevice(c->device);
+    if (int rs = rows_by_source(c)) return rs;
     cudaStream_t s = c->stream;
     Dev d = make_dev(c);
     const uint64_t ntab = (uint64_t)c->L * (v_end - v_begin);
@@ -3322,6 +3614,7 @@ int grg_export_csr5(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t cap, 
     if (!c->loaded) return fail(c, GRG_E_STATE, "no graph loaded");
     if (v_end > c->V) return fail(c, GRG_E_RANGE, "vertex range beyond the graph");
     cudaSetDevice(c->device);
+    if (int rs = rows_by_source(c)) return rs;
     // the stream's length is the range's popcount
     std::vector<uint64_t> counts(c->L + 1, 0);
     uint64_t h = 0, total = 0;
@@ -3464,6 +3757,7 @@ int grg_range_counts(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t *cou
     if (!c->loaded) return fail(c, GRG_E_STATE, "no graph loaded");
     if (v_end > c->V) return fail(c, GRG_E_RANGE, "vertex range beyond the graph");
     cudaSetDevice(c->device);
+    if (int rs = rows_by_source(c)) return rs;
     cudaStream_t s = c->stream;
     Dev d = make_dev(c);
     GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_LABEL0, 0, sizeof(unsigned long long) * (MAX_SLOTS + 2), s));
@@ -3471,7 +3765,7 @@ int grg_range_counts(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t *cou
     if (v_end > v_begin)
         for (int l = 1; l <= c->L; l++)
             k_count<<<grid_for(c, (uint64_t)(v_end - v_begin) * 32, 256), 256, 0, s>>>(
-                d, (uint32_t)l, nullptr, nullptr, 0, 0, hash ? 1 : 0, v_begin, v_end, 0, 0);
+                d, (uint32_t)l, nullptr, nullptr, 0, 0, hash ? 1 : 0, v_begin, v_end, 0, 0, 0);
     GRG_CUDA(c, cudaGetLastError());
     int st = read_ctr(c);
     if (st) return st;
@@ -3489,6 +3783,7 @@ int grg_range_reach(grg_ctx *c, uint32_t v_begin, uint32_t v_end, uint64_t label
     for (uint32_t p = 0; p < num_parts; p++)
         if (bounds[p] > bounds[p + 1]) return fail(c, GRG_E_ARG, "partition bounds must not decrease");
     cudaSetDevice(c->device);
+    if (int rs = rows_by_source(c)) return rs;
     cudaStream_t s = c->stream;
     uint32_t *db = nullptr;                      // bounds, then one flag per partition
     GRG_CUDA(c, cudaMallocAsync((void **)&db, (2 * (size_t)num_parts + 1) * 4, s));
@@ -3535,6 +3830,7 @@ int grg_batch_begin(grg_ctx *c, uint32_t max_vars, uint32_t max_jobs, int num_ru
     if (st) return st;
     cudaSetDevice(c->device);
     c->elem_loaded = false;
+    c->tmask = c->layout_mode ? plan_columns(c->rules, c->R, c->L) : 0;
     RuleTable rt;
     st = build_rules(c, filter, rt);
     if (st) return st;
@@ -3568,6 +3864,7 @@ int grg_batch_begin(grg_ctx *c, uint32_t max_vars, uint32_t max_jobs, int num_ru
     GRG_CUDA(c, cudaMemsetAsync(c->ctr, 0, sizeof(unsigned long long) * NCTR, s));
     GRG_CUDA(c, cudaMemsetAsync(c->dmap, 0, (c->pool_cap / 32 + 2) * 4, s));
     c->rt = rt;   // batch mode keeps every label in hash tables (no CSR copies)
+    set_passes(c);
     c->batch = true;
     c->filter = filter;
     c->loaded = true;
@@ -3640,7 +3937,9 @@ int grg_batch_admit(grg_ctx *c, uint32_t job, uint32_t base, uint32_t num_vars, 
     GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_ERR, 0, 8, s));
     GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_BADIN, 0, 8, s));
     Dev d = make_dev(c);
-    if (num_edges) k_load_hist<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges, base, num_vars, (uint32_t)c->L);
+    if (num_edges)
+        k_load_hist<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges, base, num_vars, (uint32_t)c->L,
+                                                                c->tmask);
     for (int l = 1; l <= c->L; l++)
         if ((eps_mask >> (l - 1)) & 1ull) k_eps_hist<<<grid_for(c, num_vars, 256), 256, 0, s>>>(d, (uint32_t)l, base, num_vars);
     k_load_alloc<<<grid_for(c, (uint64_t)c->L * num_vars, 256), 256, 0, s>>>(d, base, num_vars, (uint32_t)c->L, mc);
@@ -3661,7 +3960,9 @@ int grg_batch_admit(grg_ctx *c, uint32_t job, uint32_t base, uint32_t num_vars, 
     if (c->h_ctr[C_ERR] & ERR_POOL) return fail(c, GRG_E_NOMEM, "element pool too small for the job");
     const uint64_t top1 = c->h_ctr[C_POOL_TOP];
     if (top1 > top0) k_init_region<<<grid_for(c, top1 - top0, 256), 256, 0, s>>>(c->elems, c->dbits, nullptr, top0, top1);
-    if (num_edges) k_load_insert<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges, base, num_vars, (uint32_t)c->L);
+    if (num_edges)
+        k_load_insert<<<grid_for(c, num_edges, 256), 256, 0, s>>>(d, dsrc, ddst, dlab, num_edges, base, num_vars,
+                                                                  (uint32_t)c->L, c->tmask);
     for (int l = 1; l <= c->L; l++)
         if ((eps_mask >> (l - 1)) & 1ull) k_eps_insert<<<grid_for(c, num_vars, 256), 256, 0, s>>>(d, (uint32_t)l, base, num_vars);
     // rows of labels that no active rule derives are packed (as grg_closure does)
@@ -3721,7 +4022,8 @@ int grg_batch_result(grg_ctx *c, uint32_t job, uint32_t label_offset, uint32_t n
     GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_HASH, 0, 8, s));
     for (uint32_t l = label_offset + 1; l <= label_offset + num_labels; l++)
         k_count<<<grid_for(c, (uint64_t)(r1 - r0) * 32, 256), 256, 0, s>>>(d, l, nullptr, nullptr, 0, 0, hash ? 1 : 0,
-                                                                           r0, r1, label_offset, r0);
+                                                                           r0, r1, label_offset, r0,
+                                                                           (int)((c->tmask >> (l - 1)) & 1));
     GRG_CUDA(c, cudaGetLastError());
     int st = read_ctr(c);
     if (st) return st;
@@ -3908,7 +4210,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
 
     // load (grg_load_edges)
     const uint64_t nlab = (uint64_t)num_labels * num_vars;
-    if (num_edges) k_load_hist<<<grid(num_edges, 256, 8), 256, 0, s>>>(d, d_src, d_dst, d_label, num_edges, 0, num_vars, (uint32_t)num_labels);
+    if (num_edges) k_load_hist<<<grid(num_edges, 256, 8), 256, 0, s>>>(d, d_src, d_dst, d_label, num_edges, 0, num_vars, (uint32_t)num_labels, 0ull);
     for (int q = 0; q < num_rules; q++)
         if (rules[3 * q + 1] == 0) k_eps_hist<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)rules[3 * q], 0, num_vars);
     MinCap mc;
@@ -3920,7 +4222,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     if (h[C_ERR] & ERR_POOL) return GRG_E_NOMEM;
     const uint64_t top0 = h[C_POOL_TOP];
     if (top0) k_init_region<<<grid(top0, 256, 8), 256, 0, s>>>(d.elems, d.dbits, nullptr, 0, top0);
-    if (num_edges) k_load_insert<<<grid(num_edges, 256, 8), 256, 0, s>>>(d, d_src, d_dst, d_label, num_edges, 0, num_vars, (uint32_t)num_labels);
+    if (num_edges) k_load_insert<<<grid(num_edges, 256, 8), 256, 0, s>>>(d, d_src, d_dst, d_label, num_edges, 0, num_vars, (uint32_t)num_labels, 0ull);
     for (int q = 0; q < num_rules; q++)
         if (rules[3 * q + 1] == 0) k_eps_insert<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)rules[3 * q], 0, num_vars);
     for (int l = 1; l <= num_labels; l++)
@@ -3997,7 +4299,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
     NA_CUDA(cudaMemsetAsync(d.ctr + C_LABEL0, 0, sizeof(unsigned long long) * (MAX_SLOTS + 2), s));
     NA_CUDA(cudaMemsetAsync(d.ctr + C_HASH, 0, 8, s));
     for (int l = 1; l <= num_labels; l++)
-        k_count<<<grid((uint64_t)num_vars * 32, 256, 8), 256, 0, s>>>(d, (uint32_t)l, nullptr, nullptr, 0, 0, d_set_hash ? 1 : 0, 0, num_vars, 0, 0);
+        k_count<<<grid((uint64_t)num_vars * 32, 256, 8), 256, 0, s>>>(d, (uint32_t)l, nullptr, nullptr, 0, 0, d_set_hash ? 1 : 0, 0, num_vars, 0, 0, 0);
     NA_CUDA(cudaMemcpyAsync(d_label_counts, d.ctr + C_LABEL0 + 1, sizeof(uint64_t) * num_labels,
                             cudaMemcpyDeviceToDevice, s));
     if (d_set_hash) NA_CUDA(cudaMemcpyAsync(d_set_hash, d.ctr + C_HASH, 8, cudaMemcpyDeviceToDevice, s));

@@ -15,6 +15,8 @@
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
+#include <vector>
+
 #include "grg_format.h"
 
 namespace {
@@ -329,5 +331,202 @@ done:
     cudaFree(tmp);
     cudaFree(rcnt);
     cudaFree(roff);
+    return err;
+}
+
+// ------------------------------------------------------------------ columns -> rows
+//
+// Labels stored by destination keep, per (label, destination j), elements over
+// the sources i. Their records are turned into records by source here, 192 x 192
+// tiles at a time: the records of one label whose destinations share a 192-id
+// block jb and whose source elements share a base ib form one tile (at most 192
+// records, one per destination of the block); a warp loads the tile into shared
+// memory and transposes it one 32 x 32 bit block at a time with warp ballots.
+
+namespace {
+
+constexpr int TILE_WARPS = 4;
+constexpr uint64_t NOT_COLUMN = 1ull << 56;   // sort key of records that are copied as they are
+
+__global__ void k_col_keys(const uint4 *__restrict__ rec, uint64_t n, unsigned long long tmask, uint64_t *key,
+                           uint32_t *idx)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint4 b = rec[2 * i + 1];
+        const uint32_t lab = b.z >> 25;
+        const bool col = lab >= 1 && lab <= 63 && ((tmask >> (lab - 1)) & 1ull);
+        key[i] = col ? ((uint64_t)lab << 50) | ((uint64_t)(b.w / EIDS) << 25) | (b.z & BASE_MASK) : NOT_COLUMN;
+        idx[i] = (uint32_t)i;
+    }
+}
+
+// head[i] = 1 where a tile starts among the first nt (column) sorted keys
+__global__ void k_col_heads(const uint64_t *__restrict__ key, uint64_t nt, uint32_t *head)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nt; i += (uint64_t)gridDim.x * blockDim.x)
+        head[i] = (i == 0 || key[i] != key[i - 1]) ? 1u : 0u;
+}
+
+__global__ void k_col_starts(const uint32_t *__restrict__ head, const uint32_t *__restrict__ pos, uint64_t nt,
+                             uint32_t *start)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nt; i += (uint64_t)gridDim.x * blockDim.x)
+        if (head[i]) start[pos[i]] = (uint32_t)i;
+}
+
+// One warp per tile. EMIT = false: cnt[t] = records the tile yields; true: they
+// are written at off[t] (sources ascending within a tile).
+template <bool EMIT>
+__global__ void __launch_bounds__(TILE_WARPS * 32) k_col_tiles(const uint4 *__restrict__ rec, const uint64_t *__restrict__ key,
+                                                            const uint32_t *__restrict__ idx,
+                                                            const uint32_t *__restrict__ start, uint64_t ntiles,
+                                                            uint64_t nt, uint32_t *cnt, const uint64_t *__restrict__ off,
+                                                            uint4 *out)
+{
+    __shared__ uint32_t M[TILE_WARPS][EIDS][7];   // 7 words a row: conflict-free column reads
+    const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t(*m)[7] = M[w];
+    for (uint64_t t = blockIdx.x * (uint64_t)TILE_WARPS + w; t < ntiles; t += (uint64_t)gridDim.x * TILE_WARPS) {
+        const uint64_t a = start[t], z = t + 1 < ntiles ? start[t + 1] : nt;
+        for (uint32_t u = lane; u < EIDS * 7; u += 32) (&m[0][0])[u] = 0;
+        __syncwarp();
+        const uint64_t k = key[a];
+        const uint32_t lab = (uint32_t)(k >> 50), jb = (uint32_t)(k >> 25) & BASE_MASK, ib = (uint32_t)k & BASE_MASK;
+        for (uint64_t r = a + lane; r < z; r += 32) {
+            const uint32_t j = idx[r];
+            const uint4 e0 = rec[2 * j], e1 = rec[2 * j + 1];
+            const uint32_t jo = e1.w - jb * EIDS;      // < 192: the tile's destinations share block jb
+            if (jo < EIDS) {
+                m[jo][0] = e0.x; m[jo][1] = e0.y; m[jo][2] = e0.z; m[jo][3] = e0.w; m[jo][4] = e1.x; m[jo][5] = e1.y;
+            }
+        }
+        __syncwarp();
+        uint64_t made = 0;
+        for (int iw = 0; iw < 6; iw++) {
+            uint32_t o[6];
+#pragma unroll
+            for (int jw = 0; jw < 6; jw++) {
+                const uint32_t v = m[jw * 32 + lane][iw];   // lane = destination jw*32+lane, bits over 32 sources
+                uint32_t res = 0;
+                if (__any_sync(0xffffffffu, v != 0)) {
+#pragma unroll 4
+                    for (int b = 0; b < 32; b++) {
+                        const uint32_t col = __ballot_sync(0xffffffffu, (v >> b) & 1u);
+                        if ((int)lane == b) res = col;   // source iw*32+b: its destinations in word jw
+                    }
+                }
+                o[jw] = res;
+            }
+            const bool any = (o[0] | o[1] | o[2] | o[3] | o[4] | o[5]) != 0;
+            const unsigned msk = __ballot_sync(0xffffffffu, any);
+            if (EMIT && any) {
+                const uint64_t p = off[t] + made + __popc(msk & ((1u << lane) - 1u));
+                out[2 * p] = make_uint4(o[0], o[1], o[2], o[3]);
+                out[2 * p + 1] = make_uint4(o[4], o[5], (lab << 25) | jb, ib * EIDS + iw * 32 + lane);
+            }
+            made += __popc(msk);
+        }
+        if (!EMIT && lane == 0) cnt[t] = (uint32_t)made;
+        __syncwarp();
+    }
+}
+
+// sorted records [from, n) copied as they are to out[dst0 + (i - from)]
+__global__ void k_col_copy(const uint4 *__restrict__ rec, const uint32_t *__restrict__ idx, uint64_t from, uint64_t n,
+                           uint4 *out, uint64_t dst0)
+{
+    for (uint64_t i = from + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t j = idx[i];
+        const uint64_t o = dst0 + (i - from);
+        out[2 * o] = rec[2 * j];
+        out[2 * o + 1] = rec[2 * j + 1];
+    }
+}
+
+__global__ void k_widen32(const uint32_t *in, uint64_t n, uint64_t *out)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = in[i];
+}
+
+}  // namespace
+
+cudaError_t grg_fmt_columns_to_rows(const uint4 *rec, uint64_t n, uint64_t tmask, uint4 **out, uint64_t *n_out,
+                                    cudaStream_t s)
+{
+    cudaError_t err = cudaSuccess;
+    uint64_t *key = nullptr, *toff = nullptr;
+    uint32_t *idx = nullptr, *head = nullptr, *tcnt = nullptr;
+    void *tmp = nullptr;
+    uint4 *res = nullptr;
+    size_t tsort = 0, tscan = 0, tscan2 = 0;
+    uint64_t nt = 0, ntiles = 0, made = 0;
+    *out = nullptr;
+    *n_out = 0;
+    if (!n) return cudaSuccess;
+    FMT_CHECK(cudaMalloc(&key, n * 16));
+    FMT_CHECK(cudaMalloc(&idx, n * 8));
+    FMT_CHECK(cub::DeviceRadixSort::SortPairs(nullptr, tsort, key, key + n, idx, idx + n, n, 0, 57, s));
+    FMT_CHECK(cub::DeviceScan::ExclusiveSum(nullptr, tscan, idx, idx, n + 1, s));
+    FMT_CHECK(cub::DeviceScan::ExclusiveSum(nullptr, tscan2, key, key, n + 1, s));
+    if (tscan2 > tscan) tscan = tscan2;
+    FMT_CHECK(cudaMalloc(&tmp, tsort > tscan ? tsort : tscan));
+    k_col_keys<<<grid_of(n, 256), 256, 0, s>>>(rec, n, tmask, key, idx);
+    FMT_CHECK(cub::DeviceRadixSort::SortPairs(tmp, tsort, key, key + n, idx, idx + n, n, 0, 57, s));
+    {
+        // column records come first; nt = their number (the first key >= NOT_COLUMN)
+        uint64_t lo = 0, hi = n;
+        std::vector<uint64_t> probe(1);
+        while (lo < hi) {          // binary search on the sorted keys, one 8-byte read a step
+            const uint64_t mid = (lo + hi) / 2;
+            FMT_CHECK(cudaMemcpyAsync(probe.data(), key + n + mid, 8, cudaMemcpyDeviceToHost, s));
+            FMT_CHECK(cudaStreamSynchronize(s));
+            if (probe[0] >= NOT_COLUMN) hi = mid; else lo = mid + 1;
+        }
+        nt = lo;
+    }
+    if (nt) {
+        // tile starts: heads -> their positions -> start[]
+        FMT_CHECK(cudaMalloc(&head, (nt + 1) * 12));
+        uint32_t *pos = head + nt + 1, *start = pos + nt + 1;
+        FMT_CHECK(cudaMemsetAsync(head + nt, 0, 4, s));
+        k_col_heads<<<grid_of(nt, 256), 256, 0, s>>>(key + n, nt, head);
+        FMT_CHECK(cub::DeviceScan::ExclusiveSum(tmp, tscan, head, pos, nt + 1, s));
+        uint32_t nt32 = 0;
+        FMT_CHECK(cudaMemcpyAsync(&nt32, pos + nt, 4, cudaMemcpyDeviceToHost, s));
+        FMT_CHECK(cudaStreamSynchronize(s));
+        ntiles = nt32;
+        k_col_starts<<<grid_of(nt, 256), 256, 0, s>>>(head, pos, nt, start);
+        // records per tile, their offsets, then the records
+        FMT_CHECK(cudaMalloc(&tcnt, (ntiles + 1) * 4));
+        FMT_CHECK(cudaMalloc(&toff, (ntiles + 1) * 16));
+        FMT_CHECK(cudaMemsetAsync(tcnt + ntiles, 0, 4, s));
+        const int tg = grid_of((ntiles + TILE_WARPS - 1) / TILE_WARPS, 1);
+        k_col_tiles<false><<<tg, TILE_WARPS * 32, 0, s>>>(rec, key + n, idx + n, start, ntiles, nt, tcnt, nullptr,
+                                                           nullptr);
+        k_widen32<<<grid_of(ntiles + 1, 256), 256, 0, s>>>(tcnt, ntiles + 1, toff + ntiles + 1);
+        FMT_CHECK(cub::DeviceScan::ExclusiveSum(tmp, tscan, toff + ntiles + 1, toff, ntiles + 1, s));
+        FMT_CHECK(cudaMemcpyAsync(&made, toff + ntiles, 8, cudaMemcpyDeviceToHost, s));
+        FMT_CHECK(cudaStreamSynchronize(s));
+        FMT_CHECK(cudaMalloc(&res, (made + (n - nt)) * 32 + 32));
+        k_col_tiles<true><<<tg, TILE_WARPS * 32, 0, s>>>(rec, key + n, idx + n, start, ntiles, nt, nullptr, toff, res);
+    } else {
+        FMT_CHECK(cudaMalloc(&res, n * 32 + 32));
+    }
+    // records stored by source follow, as they are (out index made + (i - nt))
+    if (n > nt) k_col_copy<<<grid_of(n - nt, 256), 256, 0, s>>>(rec, idx + n, nt, n, res, made);
+    FMT_CHECK(cudaGetLastError());
+    FMT_CHECK(cudaStreamSynchronize(s));
+    *out = res;
+    *n_out = made + (n - nt);
+    res = nullptr;
+done:
+    cudaFree(res);
+    cudaFree(toff);
+    cudaFree(tcnt);
+    cudaFree(head);
+    cudaFree(tmp);
+    cudaFree(idx);
+    cudaFree(key);
     return err;
 }

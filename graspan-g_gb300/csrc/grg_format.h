@@ -36,3 +36,12 @@ cudaError_t grg_fmt_csr5_to_records(const uint8_t *bytes, uint64_t num_edges, co
                                     uint32_t v_begin, uint32_t nrows, uint32_t num_vars, uint32_t L, uint4 *into,
                                     uint32_t *into_st, uint64_t into_cap, uint4 **recs, uint32_t **stamps,
                                     uint64_t *n_elems, uint64_t *sum, unsigned *bad, cudaStream_t s);
+
+// Records of a graph whose labels in tmask (bit l-1 = label l) are stored by
+// destination -- record (row j, label << 25 | base of the sources, bits over
+// sources) -- turned into records by source: (row i, label << 25 | base of the
+// destinations, bits over destinations). Records of other labels are copied as
+// they are. *out is a new device array of *n_out records (the caller frees it
+// with cudaFree). Returns after it is complete.
+cudaError_t grg_fmt_columns_to_rows(const uint4 *rec, uint64_t n, uint64_t tmask, uint4 **out, uint64_t *n_out,
+                                    cudaStream_t s);

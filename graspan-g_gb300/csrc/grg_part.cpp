@@ -750,6 +750,8 @@ int grg_part_create(grg_part **out, grg_ctx *ctx, uint32_t num_vars, uint32_t nu
     grg_part *p = new grg_part;
     p->ctx = ctx;
     p->V = num_vars;
+    // partition images are rows by source: the context loads every label that way
+    grg_set_layout(ctx, 0);
     int st = grg_get_rules(ctx, &p->R, p->rules, &p->L);
     if (st) {
         delete p;
@@ -948,6 +950,7 @@ int grg_part_restore(grg_part **out, grg_ctx *ctx, const char *path)
     fseek(f, 0, SEEK_SET);
     grg_part *p = new grg_part;
     p->ctx = ctx;
+    grg_set_layout(ctx, 0);                 // partition images are rows by source
     int st = grg_get_rules(ctx, &p->R, p->rules, &p->L);
     if (!st) {
         for (int q = 0; q < p->R; q++)

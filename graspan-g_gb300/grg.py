@@ -35,6 +35,7 @@ EXPORTS = (
     "grg_part_destroy", "grg_part_load_edges", "grg_part_run", "grg_part_label_counts", "grg_part_bounds",
     "grg_set_device_rounds", "grg_range_reach", "grg_set_join_window", "grg_export_csr5", "grg_load_csr5",
     "grg_part_export_csr5", "grg_part_save", "grg_part_restore", "grg_part_set_checkpoint", "grg_part_set_run_budget",
+    "grg_set_layout",
 )
 
 
@@ -54,6 +55,7 @@ class Stats(ctypes.Structure):
         ("join_phase_cycles", ctypes.c_uint64 * 5), ("window_out_elems", ctypes.c_uint64),
         ("wide_window", ctypes.c_uint64), ("gather_ms", ctypes.c_double),
         ("window_tuned", ctypes.c_uint64), ("window_trial_ms", ctypes.c_double * 2),
+        ("column_labels", ctypes.c_uint64),
     ]
 
     def as_dict(self):
@@ -103,6 +105,7 @@ def load_library(path: str = LIB_PATH):
     L.grg_set_kernel_timing.argtypes = [P, I]
     L.grg_set_device_rounds.argtypes = [P, I]
     L.grg_set_join_window.argtypes = [P, I]
+    L.grg_set_layout.argtypes = [P, I]
     L.grg_transfer_rules.argtypes = [P, I, P, I]
     L.grg_allocate_pool.argtypes = [P, U64]
     L.grg_load_edges.argtypes = [P, U32, U64, P, P, P, I]
@@ -247,6 +250,11 @@ class Context:
         """0 = narrow (8 elements), 1 = wide (10), 2 = tuned per degree key (the
         default), 3 = tuned and measured again even when the key is cached."""
         self._check(self._L.grg_set_join_window(self._h, mode), "set_join_window")
+
+    def set_layout(self, mode: int):
+        """0: every label stored by source; 1 (default): labels the grammar allows
+        stored by destination (pushed joins). Takes effect at the next load."""
+        self._check(self._L.grg_set_layout(self._h, mode), "set_layout")
 
     def set_device_rounds(self, on: bool):
         self._check(self._L.grg_set_device_rounds(self._h, int(bool(on))), "set_device_rounds")

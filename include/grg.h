@@ -76,6 +76,9 @@ typedef struct grg_stats {
     uint64_t window_tuned;         /* how the join window was chosen: 0 fixed by grg_set_join_window,
                                       1 measured in this closure, 2 taken from the tuning cache */
     double window_trial_ms[2];     /* the measured trial passes (narrow, wide) when window_tuned = 1 */
+    uint64_t column_labels;        /* labels stored by destination in this closure (bit l-1 = label l;
+                                      grg_set_layout); their joins are pushes, so right_elems then
+                                      counts the edges of C the pushes walked */
 } grg_stats;
 
 /* Error text of a status code, and the last detailed message of a context. */
@@ -113,6 +116,23 @@ int grg_set_device_rounds(grg_ctx *ctx, int on);
  * cached, and updates the cache. Environment GRG_JOIN_WINDOW=narrow / wide /
  * tuned selects the default. Results are identical in every mode. */
 int grg_set_join_window(grg_ctx *ctx, int mode);
+
+/* Storage layout of the next graph loaded with grg_load_edges (or batch):
+ * mode 1 (the default; environment GRG_LAYOUT=rows selects 0) stores a label
+ * by destination -- the table of (label, j) holds the sources i of edges
+ * (i, j) -- when the grammar allows it: the label is derived, every binary rule
+ * A ::= B C that involves it has a C that is never derived and stores A and B
+ * alike, and no old-left join reads it. A rule A ::= B C is then joined by
+ * pushing each new element of B's column k (up to 192 sources) whole into A's
+ * column j for every edge (k, j) of C, instead of visiting every
+ * source-intermediate pair (the dataflow grammar N ::= N e | e is the case
+ * this is for). Mode 0 stores every label by source, as the reference does.
+ * Results are identical either way; the entry points that read rows by source
+ * (grg_get_degree, grg_export_elements, grg_range_counts, grg_range_reach,
+ * grg_export_csr5) first turn destination-stored labels into rows by source
+ * on the device, once per loaded graph. grg_part_create and grg_part_restore
+ * set mode 0 on their context. */
+int grg_set_layout(grg_ctx *ctx, int mode);
 
 /* Grammar: rules[3*i+{0,1,2}] = LHS, RHS1, RHS2 label ids (1-based, 0 = absent),
  * num_labels = number of distinct labels. Replaces transferRules
