@@ -328,10 +328,17 @@ def serving_measurement(args):
     # vertex space for the whole mix (HBM holds it: tables take ~250 B per vertex of the union grammar)
     max_vars = min(sum(j.num_vars for j in jobs) + args.serve_vmax, 32_000_000)
     max_jobs = min(len(jobs), 512)
+    import torch
+    free, _ = torch.cuda.mem_get_info()
+    budget = free // 4             # admission by projected footprint binds: a quarter of free HBM
     batched = serve.serve(jobs, max_vars=max_vars, max_jobs=max_jobs, realtime=False)  # all jobs available at t=0
-    served = serve.serve(jobs, max_vars=max_vars, max_jobs=max_jobs, realtime=True)    # Poisson arrivals
+    served = serve.serve(jobs, max_vars=max_vars, max_jobs=max_jobs, realtime=True,    # Poisson arrivals
+                         budget_bytes=budget)
     plain = serve.plain(jobs)
     assert served["total_edges"] == plain["total_edges"] == batched["total_edges"]
+    # the admission model against the pool each job used when closed alone
+    ratio = np.array([serve.footprint_bytes(j) / max(r[3], 1) for j, r in zip(jobs, plain["results"])])
+    under = int((ratio < 1.0).sum())
     return {"workload": f"{args.serve_jobs} jobs, V log-uniform 1000..{args.serve_vmax}, edges 3-5 x V, "
                         "half dataflow (block generator, filter 0), half alias (block-confined); Poisson 200 jobs/s",
             "batched_edges_per_s": batched["edges_per_s"], "batched_seconds": batched["makespan_s"],
@@ -339,6 +346,10 @@ def serving_measurement(args):
             "served_edges_per_s": served["edges_per_s"], "served_makespan_s": served["makespan_s"],
             "p50_s": served["p50_s"], "p99_s": served["p99_s"], "p50_admit_s": served["p50_admit_s"],
             "p99_admit_s": served["p99_admit_s"], "plain_edges_per_s": plain["edges_per_s"],
+            "served_budget_bytes": served["budget_bytes"], "served_peak_projected_bytes": served["peak_projected_bytes"],
+            "served_admissions_held_by_budget": served["held_by_budget"],
+            "footprint_model_vs_pool_used": {"min": float(ratio.min()), "p50": float(np.median(ratio)),
+                                             "max": float(ratio.max()), "jobs_under_projected": under},
             "plain_seconds": plain["seconds"], "total_edges": served["total_edges"]}
 
 

@@ -73,10 +73,16 @@ def make_jobs(specs, block=1000):
     return jobs
 
 
+POOL_BYTES_PER_SLOT = 65      # element, delta bitmap, dirty bit (rounded up)
+
+
 def footprint_bytes(j: Job) -> int:
-    """Projected HBM footprint of a job's tables (admission model)."""
+    """Projected HBM footprint of a job's tables (admission model): its input
+    edges twice, 64 slots per vertex and the presized derived rows, at 65 bytes
+    per pool slot. plain() reports the pool each job really used, so the model
+    can be checked against it."""
     slots = 2 * len(j.src) + j.num_vars * 64 + 16 * DERIVED[j.grammar] * j.num_vars
-    return 65 * slots
+    return POOL_BYTES_PER_SLOT * slots
 
 
 class RangeAllocator:
@@ -128,6 +134,8 @@ def serve(jobs, max_vars, max_jobs=256, budget_bytes=None, device=0, realtime=Tr
     pending = collections.deque(sorted(jobs, key=lambda j: j.arrival_s))
     active = {}
     committed = 0
+    peak_committed = 0
+    held_by_budget = 0           # steps at which an arrived job waited for projected memory
     steps = 0
     t0 = time.perf_counter()
     while pending or active:
@@ -137,6 +145,7 @@ def serve(jobs, max_vars, max_jobs=256, budget_bytes=None, device=0, realtime=Tr
             j = pending[0]
             fp = footprint_bytes(j)
             if active and committed + fp > budget_bytes:
+                held_by_budget += 1
                 break
             base = ranges.alloc(j.num_vars)
             if base is None:
@@ -148,6 +157,7 @@ def serve(jobs, max_vars, max_jobs=256, budget_bytes=None, device=0, realtime=Tr
             if not realtime:
                 j.arrival_s = 0.0
             committed += fp
+            peak_committed = max(peak_committed, committed)
             active[j.slot] = j
         if not active:
             if pending:
@@ -170,6 +180,7 @@ def serve(jobs, max_vars, max_jobs=256, budget_bytes=None, device=0, realtime=Tr
     lat_adm = np.array([j.done_s - j.admit_s for j in jobs])
     total = sum(j.edges for j in jobs)
     return {"jobs": len(jobs), "steps": steps, "makespan_s": makespan, "total_edges": total,
+            "budget_bytes": budget_bytes, "peak_projected_bytes": peak_committed, "held_by_budget": held_by_budget,
             "edges_per_s": total / makespan if makespan > 0 else 0.0,
             "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
             "p50_admit_s": float(np.percentile(lat_adm, 50)), "p99_admit_s": float(np.percentile(lat_adm, 99))}
@@ -187,7 +198,8 @@ def plain(jobs, device=0):
         ctx.transfer_rules(rid, len(labels))
         ctx.load_edges(j.num_vars, j.src, j.dst, j.lab)
         st = ctx.closure(0)
-        out.append((st["total_edges"], [int(x) for x in ctx.label_counts()], ctx.set_hash()))
+        out.append((st["total_edges"], [int(x) for x in ctx.label_counts()], ctx.set_hash(),
+                    int(st["pool_elems_used"]) * POOL_BYTES_PER_SLOT))
     dt = time.perf_counter() - t0
     ctx.close()
     total = sum(o[0] for o in out)

@@ -75,17 +75,29 @@ def test_dataflow_small_golden(grg_mod):
     assert ctx.set_hash() == g["hash"]
 
 
-def test_dataflow_blocks_scaled_rounds(grg_mod):
+@pytest.mark.parametrize("layout", [0, 1])
+def test_dataflow_blocks_scaled_rounds(grg_mod, layout):
     """Filter 1 reads only static right-hand rows, so the GPU's rounds equal the
-    oracle's round-synchronous rounds exactly: same count, same new elements."""
+    oracle's round-synchronous rounds exactly, in either storage layout. With
+    every label stored by source the join reads at least the oracle's
+    right-hand elements; stored by destination, N is pushed along e's edges."""
     g = GOLD["dataflow_blocks_b100"]
     w = G.dataflow_blocks(num_blocks=100, num_edges=300_000)
-    ctx, st = gpu_closure(grg_mod, w)
+    ctx = grg_mod.Context(0)
+    ctx.set_layout(layout)
+    ctx.transfer_rules(w.rule_ids(), w.num_labels)
+    ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
+    st = ctx.closure(w.filter_flag)
     assert st["total_edges"] == g["total"]
     assert ctx.set_hash() == g["hash"]
     assert st["rounds"] == g["rounds"] - 1 or st["rounds"] == g["rounds"]
     assert st["delta_elems"] - st["retry_records"] >= 0
-    assert st["right_elems"] >= g["right_elems"]
+    if layout == 0:
+        assert st["column_labels"] == 0
+        assert st["right_elems"] >= g["right_elems"]
+    else:
+        assert st["column_labels"] == 1 << w.labels.index("N")
+    ctx.close()
 
 
 def test_dataflow_blocks_full_size(grg_mod):
@@ -230,6 +242,7 @@ def test_join_windows_equal(grg_mod, oracle_mod, name):
     for mode in (0, 1):
         ctx = grg_mod.Context(0)
         ctx.set_join_window(mode)
+        ctx.set_layout(0)                  # every label by source: the dataflow closure runs k_join too
         ctx.transfer_rules(w.rule_ids(), w.num_labels)
         ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
         st = ctx.closure(w.filter_flag)
@@ -253,6 +266,7 @@ def test_tuned_window_measures_then_reuses(grg_mod, oracle_mod, device_rounds):
     for k in range(2):
         ctx = grg_mod.Context(0)
         ctx.set_join_window(3 if k == 0 else 2)
+        ctx.set_layout(0)                  # the window is a choice of k_join, which source rows run
         ctx.set_device_rounds(device_rounds)
         ctx.transfer_rules(w.rule_ids(), w.num_labels)
         ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
@@ -264,6 +278,7 @@ def test_tuned_window_measures_then_reuses(grg_mod, oracle_mod, device_rounds):
     assert seen[1][0] == 2 and seen[1][1] == seen[0][1] and seen[1][2] == [0.0, 0.0]
     ctx = grg_mod.Context(0)
     ctx.set_join_window(1)
+    ctx.set_layout(0)
     ctx.transfer_rules(w.rule_ids(), w.num_labels)
     ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
     assert ctx.closure(w.filter_flag)["window_tuned"] == 0
@@ -279,9 +294,10 @@ def test_small_rounds_split_and_retry_overflow(grg_mod, oracle_mod, monkeypatch)
              (G.pointsto(seed=45, num_vars=700, num_edges=1800), 0)]
     for w, f in cases:
         r = oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, f, w.src, w.dst, w.lab)
-        for dev in (False, True):
+        for dev, layout in ((False, 1), (True, 1), (True, 0)):
             ctx = grg_mod.Context(0)
             ctx.set_device_rounds(dev)
+            ctx.set_layout(layout)
             ctx.transfer_rules(w.rule_ids(), w.num_labels)
             ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
             st = ctx.closure(f)
