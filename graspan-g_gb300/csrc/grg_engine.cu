@@ -937,6 +937,166 @@ __global__ void __launch_bounds__(256, 4) k_push(Dev d, const uint4 *__restrict_
     }
 }
 
+// k_push with the pushes along CSR rows flattened over the lanes: a warp takes
+// 32 records, and the edges of C that their binary rules walk are dealt out
+// one per lane, so a record whose row of C is long (Zipf-distributed degrees)
+// does not hold its warp while the other lanes idle. Each lane takes its edge's
+// record (output label, base, bits) from the record's lane. Everything else --
+// unary rules, C without a CSR copy, records turned around for a unary rule --
+// stays in the record's own lane, as in k_push. Same results, same retry list.
+constexpr int PUSH_WARPS = 8;
+__global__ void __launch_bounds__(PUSH_WARPS * 32, 4) k_push_flat(Dev d, const uint4 *__restrict__ recs, uint64_t n,
+                                                                  int n_ctr, uint4 *retry_out)
+{
+    if (d.ctr[C_HALT]) return;
+    if (n_ctr >= 0) n = d.ctr[n_ctr];
+    __shared__ uint8_t own_s[PUSH_WARPS][32];
+    __shared__ uint32_t fail_s[PUSH_WARPS];
+    const uint32_t lane = lane_id(), wi = threadIdx.x >> 5;
+    uint8_t *own = own_s[wi];
+    unsigned long long n_left = 0, n_right = 0;
+    const uint64_t nbatch = (n + 31) / 32, nwarps = (uint64_t)gridDim.x * PUSH_WARPS;
+    for (uint64_t bt = blockIdx.x * (uint64_t)PUSH_WARPS + wi; bt < nbatch; bt += nwarps) {
+        const uint64_t i = bt * 32 + lane;
+        const bool have = i < n;
+        uint4 a = make_uint4(0, 0, 0, 0), b = make_uint4(0, 0, EMPTY, 0);
+        if (have) {
+            a = recs[2 * i];
+            b = recs[2 * i + 1];
+        }
+        if (lane == 0) fail_s[wi] = 0;
+        __syncwarp();
+        const uint32_t B = b.z >> KEY_SHIFT, base = b.z & BASE_MASK, row = b.w;
+        const bool valid = have && B >= 1 && B <= (uint32_t)d.rt.L;
+        const bool col = valid && d.rt.tpose[B];
+        Bits bits;
+        bits.w[0] = a.x; bits.w[1] = a.y; bits.w[2] = a.z; bits.w[3] = a.w; bits.w[4] = b.x; bits.w[5] = b.y;
+        bool ok = true;
+        // the record's own lane: everything but pushes along CSR rows
+        if (col) {
+            for (uint32_t u = d.rt.un_start[B]; u < d.rt.un_start[B + 1]; u++) {
+                const uint32_t A = d.rt.un_A[u];
+                ok &= g_insert_t<true>(d, A, row, base, bits, d.rt.track[A]);
+            }
+            for (uint32_t q = d.rt.bin_start[B]; q < d.rt.bin_start[B + 1]; q++) {
+                const uint32_t A = d.rt.bin_A[q], C = d.rt.bin_C[q];
+                if (d.rt.csr_row[C]) continue;
+                n_left++;
+                const size_t ti = (size_t)(C - 1) * d.V + row;
+                const uint64_t de = __ldg(d.desc + ti);
+                const uint32_t off = (uint32_t)de;
+                uint32_t cap = (uint32_t)(de >> 32);
+                if (prefix_table(d, C, cap)) cap = min(cap, __ldcg(d.cnt + ti));
+                for (uint32_t t = 0; t < cap; t++) {
+                    const uint32_t *e = d.elems + (size_t)(off + t) * 8;
+                    const uint32_t ek = __ldcg(e + 6);
+                    if (ek == EMPTY) continue;
+                    const uint32_t eb = (ek & BASE_MASK) * EIDS;
+#pragma unroll 1
+                    for (int x = 0; x < EW; x++) {
+                        uint32_t w = __ldcg(e + x);
+                        while (w) {
+                            const uint32_t j = eb + x * 32 + (__ffs(w) - 1);
+                            w &= w - 1;
+                            n_right++;
+                            ok &= g_insert_t<true>(d, A, j, base, bits, d.rt.track[A]);
+                        }
+                    }
+                }
+            }
+        } else if (valid) {
+            for (uint32_t u = d.rt.un_start[B]; u < d.rt.un_start[B + 1]; u++) {
+                const uint32_t A = d.rt.un_A[u];
+                if (!d.rt.tpose[A]) continue;
+                Bits one;
+                const uint32_t o = row % EIDS;
+#pragma unroll
+                for (int x = 0; x < EW; x++) one.w[x] = (uint32_t)x == (o >> 5) ? 1u << (o & 31) : 0u;
+#pragma unroll 1
+                for (int x = 0; x < EW; x++) {
+                    uint32_t w = bits.w[x];
+                    while (w) {
+                        const uint32_t j = base * EIDS + x * 32 + (__ffs(w) - 1);
+                        w &= w - 1;
+                        ok &= g_insert(d, A, j, row / EIDS, one, d.rt.track[A]);
+                    }
+                }
+            }
+        }
+        // pushes along CSR rows of C, one rule position at a time, edges dealt over the lanes
+        const uint32_t nb = col ? d.rt.bin_start[B + 1] - d.rt.bin_start[B] : 0;
+        const uint32_t maxb = __reduce_max_sync(0xffffffffu, nb);
+        for (uint32_t rho = 0; rho < maxb; rho++) {
+            uint32_t A = 0, C = 0, beg = 0, cnt = 0;
+            if (rho < nb) {
+                const uint32_t q = d.rt.bin_start[B] + rho;
+                A = d.rt.bin_A[q];
+                C = d.rt.bin_C[q];
+                if (d.rt.csr_row[C]) {
+                    const uint2 rw = __ldg(d.rt.csr_row[C] + row);
+                    beg = rw.x;
+                    cnt = rw.y & 0xFFFFFFu;
+                    n_left++;
+                    n_right += cnt;
+                }
+            }
+            uint32_t incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= (uint32_t)o) incl += y;
+            }
+            const uint32_t total = __shfl_sync(0xffffffffu, incl, 31), st = incl - cnt;
+            const uint32_t adj = beg - st;                   // edge f of this lane's record: col[f + adj]
+            uint32_t carry = 0;
+            for (uint32_t f0 = 0; f0 < total; f0 += 32) {
+                // owner of position f: the last lane with edges whose first position is at or below f
+                const bool starts = cnt != 0 && st - f0 < 32u;
+                if (starts) own[st - f0] = (uint8_t)lane;
+                const uint32_t m = __reduce_or_sync(0xffffffffu, starts ? 1u << (st - f0) : 0u);
+                __syncwarp();
+                const uint32_t below = m & (0xFFFFFFFFu >> (31 - lane));
+                const uint32_t o = below ? own[31 - __clz(below)] : carry;
+                const uint32_t last = m ? own[31 - __clz(m)] : carry;
+                __syncwarp();
+                carry = last;
+                const uint32_t f = f0 + lane;
+                const uint32_t oA = __shfl_sync(0xffffffffu, A, o), oC = __shfl_sync(0xffffffffu, C, o);
+                const uint32_t oadj = __shfl_sync(0xffffffffu, adj, o), obase = __shfl_sync(0xffffffffu, base, o);
+                Bits ob;
+#pragma unroll
+                for (int x = 0; x < EW; x++) ob.w[x] = __shfl_sync(0xffffffffu, bits.w[x], o);
+                if (f < total) {
+                    const uint32_t j = __ldg(d.rt.csr_col[oC] + f + oadj);
+                    if (!g_insert_t<true>(d, oA, j, obase, ob, d.rt.track[oA])) atomicOr(&fail_s[wi], 1u << o);
+                }
+            }
+        }
+        __syncwarp();
+        const bool failed = have && (!ok || ((fail_s[wi] >> lane) & 1u));
+        const unsigned fm = __ballot_sync(0xffffffffu, failed);
+        if (fm) {
+            unsigned long long p = 0;
+            if (lane == (uint32_t)(__ffs(fm) - 1)) p = atomicAdd(&d.ctr[C_RETRY_N], (unsigned long long)__popc(fm));
+            p = __shfl_sync(0xffffffffu, p, __ffs(fm) - 1);
+            const uint64_t o = p + __popc(fm & ((1u << lane) - 1u));
+            if (failed && o < d.retry_cap) {
+                retry_out[2 * o] = a;
+                retry_out[2 * o + 1] = b;
+            }
+        }
+        __syncwarp();
+    }
+    for (int o = 16; o; o >>= 1) {
+        n_left += __shfl_xor_sync(0xffffffffu, n_left, o);
+        n_right += __shfl_xor_sync(0xffffffffu, n_right, o);
+    }
+    if (lane == 0) {
+        if (n_left) atomicAdd(&d.ctr[C_LEFT], n_left);
+        if (n_right) atomicAdd(&d.ctr[C_RIGHT], n_right);
+    }
+}
+
 // Small rounds: a warp joins 32 records, so a round of few, dense records (alias
 // rows reach a whole block) leaves most SMs idle. Below SPLIT_MAX records the
 // round's gathered and virtual records are cut into sub-records of at most
@@ -1778,6 +1938,12 @@ struct grg_ctx {
     bool join_wide = true;
     int join_window_mode = 2;              // 0 narrow, 1 wide, 2 tuned per degree key, 3 re-measured
     bool tuned_wide = true;                // the tuned choice for the current closure
+    // right-hand items of CSR-copied labels: destination ids (the CSR copy) or whole
+    // 192-id elements of the label's table
+    int items_mode = 2;                    // 0 ids, 1 elements, 2 tuned per degree key, 3 re-measured
+    bool join_elems = false;               // the form of this closure
+    bool tuned_elems = false;
+    float items_ms[2] = {0, 0};            // measured (ids, elements) when tuned in this closure
     bool tune_pending = false;             // measure both windows in the first large round
     uint64_t tune_key = 0;
     int tune_source = 0;                   // grg_stats.window_tuned
@@ -1798,6 +1964,13 @@ struct grg_ctx {
     // kernels a join pass needs under the current rule table: k_join for records
     // joined by source rows, k_push for records of destination-stored labels
     bool need_join = true, need_push = false;
+    // push kernel: one lane per record (k_push) or edges dealt over the lanes (k_push_flat)
+    int push_mode = 2;                     // 0 per record, 1 flattened, 2 tuned per degree key, 3 re-measured
+    bool push_flat = true;                 // the kernel of this closure
+    bool tuned_flat = true;
+    bool push_pending = false;             // measure both push kernels in the first large round
+    int push_source = 0;                   // grg_stats.push_tuned
+    float push_ms[2] = {0, 0};
     uint64_t launches = 0;
     // CSR copies of static labels, per label; reused by later closures while they fit
     struct CsrBuf {
@@ -2147,6 +2320,10 @@ int grg_create(grg_ctx **out, int device)
     if (jw) c->join_window_mode = !strcmp(jw, "narrow") ? 0 : !strcmp(jw, "wide") ? 1 : 2;
     const char *ly = getenv("GRG_LAYOUT");             // "rows": every label stored by source
     if (ly && !strcmp(ly, "rows")) c->layout_mode = 0;
+    const char *ji = getenv("GRG_JOIN_ITEMS");         // "ids" / "elements"; otherwise chosen per closure
+    if (ji) c->items_mode = !strcmp(ji, "ids") ? 0 : !strcmp(ji, "elements") ? 1 : 2;
+    const char *pm = getenv("GRG_PUSH");               // "lane" / "flat"; otherwise chosen per closure
+    if (pm) c->push_mode = !strcmp(pm, "lane") ? 0 : !strcmp(pm, "flat") ? 1 : 2;
     *out = c;
     return GRG_OK;
 }
@@ -2204,6 +2381,20 @@ int grg_set_device_rounds(grg_ctx *c, int on)
 {
     if (!c) return GRG_E_ARG;
     c->device_rounds = on != 0;
+    return GRG_OK;
+}
+
+int grg_set_join_items(grg_ctx *c, int mode)
+{
+    if (!c || mode < 0 || mode > 3) return GRG_E_ARG;
+    c->items_mode = mode;
+    return GRG_OK;
+}
+
+int grg_set_push(grg_ctx *c, int mode)
+{
+    if (!c || mode < 0 || mode > 3) return GRG_E_ARG;
+    c->push_mode = mode;
     return GRG_OK;
 }
 
@@ -2544,16 +2735,33 @@ __global__ void k_tmark(unsigned long long *ctr, int t0_slot, int acc_slot, int 
 static void choose_window(grg_ctx *c)
 {
     c->join_wide = c->join_window_mode >= 2 ? c->tuned_wide : c->join_window_mode != 0;
+    c->join_elems = c->items_mode >= 2 ? c->tuned_elems : c->items_mode != 0;
+    c->push_flat = c->push_mode >= 2 ? c->tuned_flat : c->push_mode != 0;
 }
 
-// The join kernel in the window chosen for this closure (join_wide).
+// The join kernel in the window chosen for this closure (join_wide), reading the
+// right-hand rows of CSR-copied labels as ids or (join_elems) as table elements.
 static void launch_join(const grg_ctx *c, int grid, cudaStream_t s, const Dev &d, const uint4 *recs, uint64_t n,
                         int n_ctr, uint4 *retry_out)
 {
+    const Dev *dp = &d;
+    Dev de;
+    if (c->join_elems) {
+        de = d;
+        for (int l = 0; l <= MAX_LABELS; l++) de.rt.csr_row[l] = nullptr;
+        dp = &de;
+    }
     if (c->join_wide)
-        k_join<WIN2, WIN2_LO><<<grid, JOIN_WARPS * 32, 0, s>>>(d, recs, n, n_ctr, retry_out);
+        k_join<WIN2, WIN2_LO><<<grid, JOIN_WARPS * 32, 0, s>>>(*dp, recs, n, n_ctr, retry_out);
     else
-        k_join<WIN, WIN_LO><<<grid, JOIN_WARPS * 32, 0, s>>>(d, recs, n, n_ctr, retry_out);
+        k_join<WIN, WIN_LO><<<grid, JOIN_WARPS * 32, 0, s>>>(*dp, recs, n, n_ctr, retry_out);
+}
+
+static bool any_csr(const grg_ctx *c)
+{
+    for (int l = 1; l <= c->L; l++)
+        if (c->rt.csr_row[l]) return true;
+    return false;
 }
 
 // Which pass kernels the rule table needs: k_join unless every record it could
@@ -2590,7 +2798,10 @@ static void launch_pass(grg_ctx *c, int grid, cudaStream_t s, const Dev &d, cons
         joins++;
     }
     if (c->need_push) {
-        k_push<<<c->sms * 8, 256, 0, s>>>(d, recs, n, n_ctr, retry_out);
+        if (c->push_flat)
+            k_push_flat<<<c->sms * 4, PUSH_WARPS * 32, 0, s>>>(d, recs, n, n_ctr, retry_out);
+        else
+            k_push<<<c->sms * 8, 256, 0, s>>>(d, recs, n, n_ctr, retry_out);
         c->launches++;
         joins++;
     }
@@ -2607,7 +2818,9 @@ static void launch_pass(grg_ctx *c, int grid, cudaStream_t s, const Dev &d, cons
 // applying a candidate or re-running a record twice adds nothing.
 
 static std::mutex g_tune_mu;
-static std::map<uint64_t, bool> g_tune_cache;          // degree key -> wide window faster
+struct JoinChoice { bool wide, elems; };
+static std::map<uint64_t, JoinChoice> g_tune_cache;    // degree key -> the faster window and item form
+static std::map<uint64_t, bool> g_push_cache;          // degree key -> flattened push faster
 constexpr uint64_t TUNE_MIN_RECORDS = 1u << 16;        // smaller first rounds are not timed
 
 static int degree_key(grg_ctx *c, uint32_t filter, uint64_t *key)
@@ -2635,20 +2848,40 @@ static int degree_key(grg_ctx *c, uint32_t filter, uint64_t *key)
 // Sets the closure's window from the cache, or marks it for measurement.
 static int tune_begin(grg_ctx *c, uint32_t filter)
 {
-    c->tune_pending = false;
-    c->tune_source = 0;
+    c->tune_pending = c->push_pending = false;
+    c->tune_source = c->push_source = 0;
     c->tune_ms[0] = c->tune_ms[1] = 0;
-    if (c->join_window_mode < 2) return GRG_OK;
+    c->items_ms[0] = c->items_ms[1] = 0;
+    c->push_ms[0] = c->push_ms[1] = 0;
+    // only the choices this closure's pass kernels make are tuned (the window is
+    // k_join's; the push kernel is timed only when the pass is pushes alone)
+    const bool tune_window = (c->join_window_mode >= 2 || c->items_mode >= 2) && c->need_join;
+    const bool tune_push = c->push_mode >= 2 && c->need_push && !c->need_join;
+    if (!tune_window && !tune_push) return GRG_OK;
     int st = degree_key(c, filter, &c->tune_key);
     if (st) return st;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    auto it = g_tune_cache.find(c->tune_key);
-    if (it != g_tune_cache.end() && c->join_window_mode == 2) {
-        c->tuned_wide = it->second;
-        c->tune_source = 2;
-    } else {
-        c->tuned_wide = true;
-        c->tune_pending = true;
+    if (tune_window) {
+        auto it = g_tune_cache.find(c->tune_key);
+        if (it != g_tune_cache.end() && c->join_window_mode != 3 && c->items_mode != 3) {
+            c->tuned_wide = it->second.wide;
+            c->tuned_elems = it->second.elems;
+            c->tune_source = 2;
+        } else {
+            c->tuned_wide = true;
+            c->tuned_elems = false;
+            c->tune_pending = true;
+        }
+    }
+    if (tune_push) {
+        auto it = g_push_cache.find(c->tune_key);
+        if (it != g_push_cache.end() && c->push_mode == 2) {
+            c->tuned_flat = it->second;
+            c->push_source = 2;
+        } else {
+            c->tuned_flat = true;
+            c->push_pending = true;
+        }
     }
     return GRG_OK;
 }
@@ -2673,22 +2906,30 @@ static int tune_first_pass(grg_ctx *c, const Dev &d, uint64_t nd, uint64_t nv, u
     for (int i = 0; i < 4; i++) keep[i] = c->h_ctr[kept[i]];
     const uint64_t nt = std::min(nd, std::max<uint64_t>(TUNE_MIN_RECORDS, nd / 8));
     const int grid = grid_for(c, (nt + RB - 1) / RB, JOIN_WARPS, 16);
-    // an untimed wide pass, then narrow / wide twice, interleaved; each window's best time
-    c->tune_ms[0] = c->tune_ms[1] = 1e30f;
-    for (int it = -1; it < 4; it++) {
-        const int k = it < 0 ? 1 : it & 1;     // 0 narrow, 1 wide
-        c->join_wide = k == 1;
-        if (it >= 0) GRG_CUDA(c, cudaEventRecord(c->ev_t0, s));
-        launch_join(c, grid, s, d, c->gbuf, nt, -1, c->rbuf[0]);
-        c->launches++;
-        joins++;
-        if (it < 0) continue;
-        float ms = 0;
-        GRG_CUDA(c, cudaEventRecord(c->ev_t1, s));
-        GRG_CUDA(c, cudaEventSynchronize(c->ev_t1));
-        GRG_CUDA(c, cudaEventElapsedTime(&ms, c->ev_t0, c->ev_t1));
-        c->tune_ms[k] = std::min(c->tune_ms[k], ms);
-    }
+    // the choices open in this closure: windows unless fixed, item forms unless fixed or no
+    // right-hand label has a CSR copy; an untimed pass, then every combination twice,
+    // interleaved, keeping each one's best time
+    const bool tw = c->join_window_mode >= 2, ti = c->items_mode >= 2 && any_csr(c);
+    const bool fix_wide = c->join_wide, fix_elems = c->join_elems;
+    float best[2][2] = {{1e30f, 1e30f}, {1e30f, 1e30f}};        // [wide][elems]
+    for (int rep = -1; rep < 2; rep++)
+        for (int w = 0; w < 2; w++)
+            for (int e = 0; e < 2; e++) {
+                if ((!tw && w != (int)fix_wide) || (!ti && e != (int)fix_elems)) continue;
+                if (rep < 0 && !(w == 1 || !tw)) continue;         // one untimed (wide) pass per item form
+                c->join_wide = w == 1;
+                c->join_elems = e == 1;
+                if (rep >= 0) GRG_CUDA(c, cudaEventRecord(c->ev_t0, s));
+                launch_join(c, grid, s, d, c->gbuf, nt, -1, c->rbuf[0]);
+                c->launches++;
+                joins++;
+                if (rep < 0) continue;
+                float ms = 0;
+                GRG_CUDA(c, cudaEventRecord(c->ev_t1, s));
+                GRG_CUDA(c, cudaEventSynchronize(c->ev_t1));
+                GRG_CUDA(c, cudaEventElapsedTime(&ms, c->ev_t0, c->ev_t1));
+                best[w][e] = std::min(best[w][e], ms);
+            }
     // the statistics count the round's own pass only
     for (int i = 0; i < 4; i++) {
         c->h_ctr[kept[i]] = keep[i];
@@ -2699,15 +2940,75 @@ static int tune_first_pass(grg_ctx *c, const Dev &d, uint64_t nd, uint64_t nv, u
     // want counters are set, so the real pass would not queue them a second time).
     GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_RETRY_N, 0, 8, s));
     GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_CAND_N, 0, 16, s));    // candidates + failed candidates
-    // the wide window is the measured default (faster on every workload swept): narrow must
-    // win by a margin the trial's noise cannot produce
-    const bool wide = !(c->tune_ms[0] < 0.9f * c->tune_ms[1]);
+    // per item form, the wide window is the measured default (faster on every workload
+    // swept): narrow must win by a margin the trial's noise cannot produce; then the faster
+    // item form with its window
+    bool wide_of[2];
+    float t_of[2];
+    for (int e = 0; e < 2; e++) {
+        wide_of[e] = tw ? !(best[0][e] < 0.9f * best[1][e]) : fix_wide;
+        t_of[e] = best[wide_of[e] ? 1 : 0][e];
+    }
+    const bool elems = ti ? t_of[1] < t_of[0] : fix_elems;
+    const bool wide = wide_of[elems ? 1 : 0];
+    c->tune_ms[0] = best[0][elems ? 1 : 0] < 1e29f ? best[0][elems ? 1 : 0] : 0.f;
+    c->tune_ms[1] = best[1][elems ? 1 : 0] < 1e29f ? best[1][elems ? 1 : 0] : 0.f;
+    c->items_ms[0] = ti ? t_of[0] : 0.f;
+    c->items_ms[1] = ti ? t_of[1] : 0.f;
     c->tuned_wide = c->join_wide = wide;
+    c->tuned_elems = c->join_elems = elems;
     c->tune_pending = false;
     c->tune_source = 1;
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
-        g_tune_cache[c->tune_key] = wide;
+        g_tune_cache[c->tune_key] = JoinChoice{wide, elems};
+    }
+    first_pass_joins(c, d, nd, nv, false, joins);
+    return GRG_OK;
+}
+
+// The first pass of a round whose join pass is pushes only, with the push kernel
+// measured: one lane per record and edges dealt over the lanes, each timed twice,
+// interleaved, on a slice of the round's records after an untimed pass; the
+// faster is kept for this closure and later closures with the degree key.
+// Pushing a record again adds nothing twice.
+static int tune_push_pass(grg_ctx *c, const Dev &d, uint64_t nd, uint64_t nv, uint64_t &joins)
+{
+    cudaStream_t s = c->stream;
+    if (!c->ev_t0) GRG_CUDA(c, cudaEventCreate(&c->ev_t0));
+    if (!c->ev_t1) GRG_CUDA(c, cudaEventCreate(&c->ev_t1));
+    int st = read_ctr(c);
+    if (st) return st;
+    const int kept[2] = {C_LEFT, C_RIGHT};
+    unsigned long long keep[2];
+    for (int i = 0; i < 2; i++) keep[i] = c->h_ctr[kept[i]];
+    const uint64_t nt = std::min(nd, std::max<uint64_t>(TUNE_MIN_RECORDS, nd / 8));
+    c->push_ms[0] = c->push_ms[1] = 1e30f;
+    for (int it = -1; it < 4; it++) {
+        const int k = it < 0 ? 1 : it & 1;     // 0 one lane per record, 1 flattened
+        c->push_flat = k == 1;
+        if (it >= 0) GRG_CUDA(c, cudaEventRecord(c->ev_t0, s));
+        launch_pass(c, 0, s, d, c->gbuf, nt, -1, c->rbuf[0], joins);
+        if (it < 0) continue;
+        float ms = 0;
+        GRG_CUDA(c, cudaEventRecord(c->ev_t1, s));
+        GRG_CUDA(c, cudaEventSynchronize(c->ev_t1));
+        GRG_CUDA(c, cudaEventElapsedTime(&ms, c->ev_t0, c->ev_t1));
+        c->push_ms[k] = std::min(c->push_ms[k], ms);
+    }
+    for (int i = 0; i < 2; i++) {
+        c->h_ctr[kept[i]] = keep[i];
+        GRG_CUDA(c, cudaMemcpyAsync(c->ctr + kept[i], c->h_ctr + kept[i], 8, cudaMemcpyHostToDevice, s));
+    }
+    // the trial passes' retry records are dropped: the round's own pass pushes every record again
+    GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_RETRY_N, 0, 8, s));
+    const bool flat = c->push_ms[1] <= c->push_ms[0];
+    c->tuned_flat = c->push_flat = flat;
+    c->push_pending = false;
+    c->push_source = 1;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_push_cache[c->tune_key] = flat;
     }
     first_pass_joins(c, d, nd, nv, false, joins);
     return GRG_OK;
@@ -2906,6 +3207,8 @@ static int round_joins(grg_ctx *c, uint64_t nd, uint64_t nv, grg_stats &S, doubl
     }
     if (c->tune_pending && c->need_join && !split && nd >= TUNE_MIN_RECORDS) {
         if ((st = tune_first_pass(c, d, nd, nv, joins))) return st;
+    } else if (c->push_pending && c->need_push && !c->need_join && !split && nd >= TUNE_MIN_RECORDS) {
+        if ((st = tune_push_pass(c, d, nd, nv, joins))) return st;
     } else {
         first_pass_joins(c, d, nd, nv, split, joins);
     }
@@ -3008,7 +3311,8 @@ static std::vector<uint64_t> round_graph_key(const grg_ctx *c, uint32_t rs, uint
                                (uint64_t)c->drc, (uint64_t)c->dvm, c->pool_cap, c->V, rs, (uint64_t)c->timing,
                                (uint64_t)c->elem_loaded, (uint64_t)c->rt.nol, (uint64_t)c->row_job,
                                (uint64_t)c->job_cnt, c->max_jobs, (uint64_t)c->join_wide, (uint64_t)c->sbuf,
-                               (uint64_t)c->need_join, (uint64_t)c->need_push};
+                               (uint64_t)c->need_join, (uint64_t)c->need_push, (uint64_t)c->push_flat,
+                               (uint64_t)c->join_elems};
     for (int l = 1; l <= c->L; l++) k.push_back(c->rt.dindex[l]);
     // the rule table is a parameter of every recorded launch
     uint64_t w[(sizeof(RuleTable) + 7) / 8] = {0};
@@ -3246,6 +3550,7 @@ int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *s
     int st = build_rules(c, filter, rt);
     if (st) return st;
     c->rt = rt;
+    set_passes(c);                         // which pass kernels run (the CSR copies do not change it)
     cudaStream_t s = c->stream;
     grg_stats S;
     memset(&S, 0, sizeof S);
@@ -3342,7 +3647,14 @@ int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *s
     S.window_trial_ms[0] = c->tune_ms[0];
     S.window_trial_ms[1] = c->tune_ms[1];
     S.column_labels = c->tmask;
-    c->tune_pending = false;              // an untimed closure leaves its key for the next one
+    S.join_elements = c->need_join && c->join_elems && any_csr(c) ? 1 : 0;
+    S.items_trial_ms[0] = c->items_ms[0];
+    S.items_trial_ms[1] = c->items_ms[1];
+    S.push_flat = c->need_push && c->push_flat ? 1 : 0;
+    S.push_tuned = (uint64_t)c->push_source;
+    S.push_trial_ms[0] = c->push_ms[0];
+    S.push_trial_ms[1] = c->push_ms[1];
+    c->tune_pending = c->push_pending = false;   // an untimed closure leaves its key for the next one
     S.right_elems = c->h_ctr[C_RIGHT];
     S.out_elems = S.delta_elems;
     S.pool_elems_used = c->h_ctr[C_POOL_TOP];

@@ -35,7 +35,7 @@ EXPORTS = (
     "grg_part_destroy", "grg_part_load_edges", "grg_part_run", "grg_part_label_counts", "grg_part_bounds",
     "grg_set_device_rounds", "grg_range_reach", "grg_set_join_window", "grg_export_csr5", "grg_load_csr5",
     "grg_part_export_csr5", "grg_part_save", "grg_part_restore", "grg_part_set_checkpoint", "grg_part_set_run_budget",
-    "grg_set_layout",
+    "grg_set_layout", "grg_set_push", "grg_set_join_items",
 )
 
 
@@ -55,13 +55,17 @@ class Stats(ctypes.Structure):
         ("join_phase_cycles", ctypes.c_uint64 * 5), ("window_out_elems", ctypes.c_uint64),
         ("wide_window", ctypes.c_uint64), ("gather_ms", ctypes.c_double),
         ("window_tuned", ctypes.c_uint64), ("window_trial_ms", ctypes.c_double * 2),
-        ("column_labels", ctypes.c_uint64),
+        ("column_labels", ctypes.c_uint64), ("push_flat", ctypes.c_uint64), ("push_tuned", ctypes.c_uint64),
+        ("push_trial_ms", ctypes.c_double * 2), ("join_elements", ctypes.c_uint64),
+        ("items_trial_ms", ctypes.c_double * 2),
     ]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
         d["join_phase_cycles"] = list(d["join_phase_cycles"])
         d["window_trial_ms"] = list(d["window_trial_ms"])
+        d["push_trial_ms"] = list(d["push_trial_ms"])
+        d["items_trial_ms"] = list(d["items_trial_ms"])
         return d
 
 
@@ -106,6 +110,8 @@ def load_library(path: str = LIB_PATH):
     L.grg_set_device_rounds.argtypes = [P, I]
     L.grg_set_join_window.argtypes = [P, I]
     L.grg_set_layout.argtypes = [P, I]
+    L.grg_set_push.argtypes = [P, I]
+    L.grg_set_join_items.argtypes = [P, I]
     L.grg_transfer_rules.argtypes = [P, I, P, I]
     L.grg_allocate_pool.argtypes = [P, U64]
     L.grg_load_edges.argtypes = [P, U32, U64, P, P, P, I]
@@ -250,6 +256,16 @@ class Context:
         """0 = narrow (8 elements), 1 = wide (10), 2 = tuned per degree key (the
         default), 3 = tuned and measured again even when the key is cached."""
         self._check(self._L.grg_set_join_window(self._h, mode), "set_join_window")
+
+    def set_join_items(self, mode: int):
+        """Right-hand items of CSR-copied labels: 0 ids, 1 table elements, 2 tuned
+        with the window (default), 3 tuned and measured again."""
+        self._check(self._L.grg_set_join_items(self._h, mode), "set_join_items")
+
+    def set_push(self, mode: int):
+        """Push kernel: 0 one lane per record, 1 edges dealt over the lanes, 2 tuned
+        per degree key (default), 3 tuned and measured again."""
+        self._check(self._L.grg_set_push(self._h, mode), "set_push")
 
     def set_layout(self, mode: int):
         """0: every label stored by source; 1 (default): labels the grammar allows

@@ -79,6 +79,14 @@ typedef struct grg_stats {
     uint64_t column_labels;        /* labels stored by destination in this closure (bit l-1 = label l;
                                       grg_set_layout); their joins are pushes, so right_elems then
                                       counts the edges of C the pushes walked */
+    uint64_t push_flat;            /* 1 = pushes dealt the edges of C over the lanes, 0 = one lane per
+                                      record (grg_set_push; 0 when nothing is pushed) */
+    uint64_t push_tuned;           /* how the push kernel was chosen: 0 fixed, 1 measured in this
+                                      closure, 2 taken from the tuning cache */
+    double push_trial_ms[2];       /* the measured trial passes (one lane per record, flattened) */
+    uint64_t join_elements;        /* 1 = k_join read CSR-copied right-hand rows as whole table
+                                      elements, 0 = as destination ids (grg_set_join_items) */
+    double items_trial_ms[2];      /* the measured trial passes (ids, elements) when tuned */
 } grg_stats;
 
 /* Error text of a status code, and the last detailed message of a context. */
@@ -116,6 +124,15 @@ int grg_set_device_rounds(grg_ctx *ctx, int on);
  * cached, and updates the cache. Environment GRG_JOIN_WINDOW=narrow / wide /
  * tuned selects the default. Results are identical in every mode. */
 int grg_set_join_window(grg_ctx *ctx, int mode);
+/* Right-hand items of labels that have a CSR copy (never derived, read as a
+ * binary rule's second symbol): mode 0 reads destination ids (4 bytes each,
+ * one window bit per id), mode 1 reads the label's table elements (32 bytes
+ * each, up to 192 ids ORed at once: fewer items to deal over the lanes when a
+ * row's ids share elements). Mode 2 (the default) tunes the choice together
+ * with the join window (see grg_set_join_window), mode 3 re-measures.
+ * Environment GRG_JOIN_ITEMS=ids / elements selects the default. Results are
+ * identical. */
+int grg_set_join_items(grg_ctx *ctx, int mode);
 
 /* Storage layout of the next graph loaded with grg_load_edges (or batch):
  * mode 1 (the default; environment GRG_LAYOUT=rows selects 0) stores a label
@@ -133,6 +150,15 @@ int grg_set_join_window(grg_ctx *ctx, int mode);
  * on the device, once per loaded graph. grg_part_create and grg_part_restore
  * set mode 0 on their context. */
 int grg_set_layout(grg_ctx *ctx, int mode);
+/* Push kernel for destination-stored labels: mode 0 gives each delta record
+ * one lane, which walks its row of C alone; mode 1 deals the edges of the
+ * rows of C of a warp's 32 records over its lanes (a long row then does not
+ * hold the warp while other lanes idle); mode 2 (the default) tunes the choice
+ * per degree key like the join window (the first closure of a key times both on
+ * a slice of its first large round and keeps the faster, later closures take it
+ * from the process-wide cache); mode 3 measures again. Environment
+ * GRG_PUSH=lane / flat / tuned selects the default. Results are identical. */
+int grg_set_push(grg_ctx *ctx, int mode);
 
 /* Grammar: rules[3*i+{0,1,2}] = LHS, RHS1, RHS2 label ids (1-based, 0 = absent),
  * num_labels = number of distinct labels. Replaces transferRules

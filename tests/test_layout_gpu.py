@@ -87,3 +87,28 @@ def test_column_layout_retries_and_host_rounds(grg_mod, oracle_mod, monkeypatch)
         assert st["column_labels"] != 0
         assert st["total_edges"] == r.total and ctx.set_hash() == r.set_hash, rounds
         ctx.close()
+
+
+@pytest.mark.parametrize("device_rounds", [True, False])
+def test_push_kernels_equal_and_tuned(grg_mod, oracle_mod, device_rounds):
+    """Both push kernels (one lane per record, edges dealt over the lanes) give the
+    oracle's closure; a mode-3 closure times both on its first large round
+    (push_tuned 1), a mode-2 closure of the same input takes the cached choice."""
+    w = G.dataflow_blocks(seed=67 + device_rounds, num_blocks=97, block=1000, num_edges=291_000)
+    r = oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, 1, w.src, w.dst, w.lab)
+    want = (r.label_counts().tolist(), r.set_hash)
+    seen = []
+    for mode in (0, 1, 3, 2):
+        ctx = grg_mod.Context(0)
+        ctx.set_push(mode)
+        ctx.set_device_rounds(device_rounds)
+        ctx.transfer_rules(w.rule_ids(), w.num_labels)
+        ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
+        st = ctx.closure(1)
+        assert (ctx.label_counts().tolist(), ctx.set_hash()) == want, mode
+        assert st["column_labels"] != 0
+        seen.append((st["push_flat"], st["push_tuned"], st["push_trial_ms"]))
+        ctx.close()
+    assert seen[0][:2] == (0, 0) and seen[1][:2] == (1, 0)
+    assert seen[2][1] == 1 and min(seen[2][2]) > 0
+    assert seen[3][1] == 2 and seen[3][0] == seen[2][0]
