@@ -69,7 +69,8 @@ enum : int {
     C_GNS = C_LABEL0 + MAX_SLOTS + 9,   // gather nanoseconds (kernel timing)
     C_BADIN = C_LABEL0 + MAX_SLOTS + 10, // input edges refused: ERR_IN_LABEL / ERR_IN_RANGE bits
     C_DH0 = C_LABEL0 + MAX_SLOTS + 11,   // 8 counters: tables by log2 of their elements (tuning key)
-    NCTR = C_LABEL0 + MAX_SLOTS + 19
+    C_CHECK = C_LABEL0 + MAX_SLOTS + 19, // first failed bounds check of the push kernels: id << 56 | value
+    NCTR = C_LABEL0 + MAX_SLOTS + 20
 };
 // error bits of C_ERR; ERR_IN_* (in C_BADIN) flag input edges that were refused
 // (label outside 1..L, vertex id outside the graph) and never touched a table
@@ -104,7 +105,17 @@ struct RuleTable {
     // 4 bytes per edge instead of a 32-byte element per 192-id block
     const uint2 *csr_row[MAX_LABELS + 1];    // {first edge, degree | min(elements,255) << 24}
     const uint32_t *csr_col[MAX_LABELS + 1];
+    uint32_t csr_n[MAX_LABELS + 1];          // destination ids in each CSR copy
 };
+
+// A failed bounds check (id >= 1): the access is skipped and the first
+// failure's check id and offending value are kept in C_CHECK; the host then
+// returns GRG_E_INTERNAL with them instead of touching memory out of bounds.
+__device__ __forceinline__ bool check_failed(unsigned long long *ctr, unsigned id, unsigned long long value)
+{
+    atomicCAS(&ctr[C_CHECK], 0ull, ((unsigned long long)id << 56) | (value & ((1ull << 56) - 1)));
+    return true;
+}
 
 struct Dev {
     uint32_t *elems;          // pool: 8 words per slot

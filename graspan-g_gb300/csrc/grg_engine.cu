@@ -244,8 +244,11 @@ __global__ void k_eps_hist(Dev d, uint32_t slot, uint32_t first, uint32_t nv)
 struct MinCap { uint32_t cap[MAX_LABELS + 1]; };
 
 // One thread per table of labels 1..L over rows [first, first + nv): size from
-// the edge histogram (held in cnt), bump-allocate.
-__global__ void k_load_alloc(Dev d, uint32_t first, uint32_t nv, uint32_t L, MinCap mc)
+// the edge histogram (held in cnt), bump-allocate. rowmark (nullable, 1 bit per
+// row): the minimum capacities apply only to marked rows -- an element image
+// holds a few partitions' rows, and rows it does not hold never gain edges.
+__global__ void k_load_alloc(Dev d, uint32_t first, uint32_t nv, uint32_t L, MinCap mc,
+                             const uint32_t *__restrict__ rowmark)
 {
     const uint64_t ntables = (uint64_t)L * nv;
     for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < ((ntables + 31) & ~31ull);
@@ -254,6 +257,10 @@ __global__ void k_load_alloc(Dev d, uint32_t first, uint32_t nv, uint32_t L, Min
         const uint64_t t = (uint64_t)(lab - 1) * d.V + first + (u < ntables ? u % nv : 0);
         uint32_t h = u < ntables ? d.cnt[t] : 0;
         uint32_t cap = u < ntables ? mc.cap[lab] : 0;
+        if (rowmark && cap) {
+            const uint32_t row = first + (uint32_t)(u % nv);
+            if (!((rowmark[row >> 5] >> (row & 31)) & 1u)) cap = 0;
+        }
         if (h) {
             const uint32_t need = h + h / 3 + 1;
             if (cap < 4) cap = 4;
@@ -849,7 +856,9 @@ __global__ void __launch_bounds__(256, 4) k_push(Dev d, const uint4 *__restrict_
             b = recs[2 * i + 1];
         }
         const uint32_t B = b.z >> KEY_SHIFT, base = b.z & BASE_MASK, row = b.w;
-        if (i < n && B >= 1 && B <= (uint32_t)d.rt.L) {
+        bool valid = i < n && B >= 1 && B <= (uint32_t)d.rt.L;
+        if (valid && (row >= d.V || (uint64_t)base * EIDS >= d.V)) valid = !check_failed(d.ctr, 1, row);
+        if (valid) {
             Bits bits;
             bits.w[0] = a.x; bits.w[1] = a.y; bits.w[2] = a.z; bits.w[3] = a.w; bits.w[4] = b.x; bits.w[5] = b.y;
             bool ok = true;
@@ -866,15 +875,21 @@ __global__ void __launch_bounds__(256, 4) k_push(Dev d, const uint4 *__restrict_
                     if (cr) {
                         const uint2 rw = __ldg(cr + row);
                         const uint32_t *col = d.rt.csr_col[C] + rw.x;
-                        const uint32_t cnt = rw.y & 0xFFFFFFu;
+                        uint32_t cnt = rw.y & 0xFFFFFFu;
+                        if ((uint64_t)rw.x + cnt > d.rt.csr_n[C]) cnt = check_failed(d.ctr, 5, rw.x) ? 0 : cnt;
                         n_right += cnt;
-                        for (uint32_t t = 0; t < cnt; t++) ok &= g_insert_t<true>(d, A, __ldg(col + t), base, bits, tr);
+                        for (uint32_t t = 0; t < cnt; t++) {
+                            const uint32_t j = __ldg(col + t);
+                            if (j >= d.V || A < 1 || A > (uint32_t)d.rt.L) { check_failed(d.ctr, 7, j); continue; }
+                            ok &= g_insert_t<true>(d, A, j, base, bits, tr);
+                        }
                     } else {
                         const size_t ti = (size_t)(C - 1) * d.V + row;
                         const uint64_t de = __ldg(d.desc + ti);
                         const uint32_t off = (uint32_t)de;
                         uint32_t cap = (uint32_t)(de >> 32);
                         if (prefix_table(d, C, cap)) cap = min(cap, __ldcg(d.cnt + ti));
+                        if ((uint64_t)off + cap > d.pool_cap) cap = check_failed(d.ctr, 2, off) ? 0 : cap;
                         for (uint32_t t = 0; t < cap; t++) {
                             const uint32_t *e = d.elems + (size_t)(off + t) * 8;
                             const uint32_t ek = __ldcg(e + 6);
@@ -887,6 +902,7 @@ __global__ void __launch_bounds__(256, 4) k_push(Dev d, const uint4 *__restrict_
                                     const uint32_t j = eb + x * 32 + (__ffs(w) - 1);
                                     w &= w - 1;
                                     n_right++;
+                                    if (j >= d.V) { check_failed(d.ctr, 3, j); continue; }
                                     ok &= g_insert_t<true>(d, A, j, base, bits, tr);
                                 }
                             }
@@ -907,6 +923,7 @@ __global__ void __launch_bounds__(256, 4) k_push(Dev d, const uint4 *__restrict_
                         while (w) {
                             const uint32_t j = base * EIDS + x * 32 + (__ffs(w) - 1);
                             w &= w - 1;
+                            if (j >= d.V) { check_failed(d.ctr, 4, j); continue; }
                             ok &= g_insert(d, A, j, row / EIDS, one, d.rt.track[A]);
                         }
                     }
@@ -967,7 +984,8 @@ __global__ void __launch_bounds__(PUSH_WARPS * 32, 4) k_push_flat(Dev d, const u
         if (lane == 0) fail_s[wi] = 0;
         __syncwarp();
         const uint32_t B = b.z >> KEY_SHIFT, base = b.z & BASE_MASK, row = b.w;
-        const bool valid = have && B >= 1 && B <= (uint32_t)d.rt.L;
+        bool valid = have && B >= 1 && B <= (uint32_t)d.rt.L;
+        if (valid && (row >= d.V || (uint64_t)base * EIDS >= d.V)) valid = !check_failed(d.ctr, 1, row);
         const bool col = valid && d.rt.tpose[B];
         Bits bits;
         bits.w[0] = a.x; bits.w[1] = a.y; bits.w[2] = a.z; bits.w[3] = a.w; bits.w[4] = b.x; bits.w[5] = b.y;
@@ -987,6 +1005,7 @@ __global__ void __launch_bounds__(PUSH_WARPS * 32, 4) k_push_flat(Dev d, const u
                 const uint32_t off = (uint32_t)de;
                 uint32_t cap = (uint32_t)(de >> 32);
                 if (prefix_table(d, C, cap)) cap = min(cap, __ldcg(d.cnt + ti));
+                if ((uint64_t)off + cap > d.pool_cap) cap = check_failed(d.ctr, 2, off) ? 0 : cap;
                 for (uint32_t t = 0; t < cap; t++) {
                     const uint32_t *e = d.elems + (size_t)(off + t) * 8;
                     const uint32_t ek = __ldcg(e + 6);
@@ -999,6 +1018,7 @@ __global__ void __launch_bounds__(PUSH_WARPS * 32, 4) k_push_flat(Dev d, const u
                             const uint32_t j = eb + x * 32 + (__ffs(w) - 1);
                             w &= w - 1;
                             n_right++;
+                            if (j >= d.V || A < 1 || A > (uint32_t)d.rt.L) { check_failed(d.ctr, 3, j); continue; }
                             ok &= g_insert_t<true>(d, A, j, base, bits, d.rt.track[A]);
                         }
                     }
@@ -1018,6 +1038,7 @@ __global__ void __launch_bounds__(PUSH_WARPS * 32, 4) k_push_flat(Dev d, const u
                     while (w) {
                         const uint32_t j = base * EIDS + x * 32 + (__ffs(w) - 1);
                         w &= w - 1;
+                        if (j >= d.V) { check_failed(d.ctr, 4, j); continue; }
                         ok &= g_insert(d, A, j, row / EIDS, one, d.rt.track[A]);
                     }
                 }
@@ -1036,6 +1057,7 @@ __global__ void __launch_bounds__(PUSH_WARPS * 32, 4) k_push_flat(Dev d, const u
                     const uint2 rw = __ldg(d.rt.csr_row[C] + row);
                     beg = rw.x;
                     cnt = rw.y & 0xFFFFFFu;
+                    if ((uint64_t)beg + cnt > d.rt.csr_n[C]) cnt = check_failed(d.ctr, 5, beg) ? 0 : cnt;
                     n_left++;
                     n_right += cnt;
                 }
@@ -1067,8 +1089,16 @@ __global__ void __launch_bounds__(PUSH_WARPS * 32, 4) k_push_flat(Dev d, const u
 #pragma unroll
                 for (int x = 0; x < EW; x++) ob.w[x] = __shfl_sync(0xffffffffu, bits.w[x], o);
                 if (f < total) {
-                    const uint32_t j = __ldg(d.rt.csr_col[oC] + f + oadj);
-                    if (!g_insert_t<true>(d, oA, j, obase, ob, d.rt.track[oA])) atomicOr(&fail_s[wi], 1u << o);
+                    const uint32_t ci = f + oadj;
+                    if (oC < 1 || oC > (uint32_t)d.rt.L || ci >= d.rt.csr_n[oC]) {
+                        check_failed(d.ctr, 6, ((uint64_t)oC << 32) | ci);
+                    } else {
+                        const uint32_t j = __ldg(d.rt.csr_col[oC] + ci);
+                        if (j >= d.V || oA < 1 || oA > (uint32_t)d.rt.L)
+                            check_failed(d.ctr, 7, ((uint64_t)oA << 32) | j);
+                        else if (!g_insert_t<true>(d, oA, j, obase, ob, d.rt.track[oA]))
+                            atomicOr(&fail_s[wi], 1u << o);
+                    }
                 }
             }
         }
@@ -1731,7 +1761,8 @@ __device__ __forceinline__ bool elem_ok(const Dev &d, uint32_t L, uint32_t key, 
     return lab >= 1 && lab <= L && row < d.V && (uint64_t)base * EIDS < d.V;
 }
 
-__global__ void k_elem_hist(Dev d, const uint4 *recs, uint64_t n, uint32_t L)
+// rowmark (nullable): rows that hold a record get their bit set
+__global__ void k_elem_hist(Dev d, const uint4 *recs, uint64_t n, uint32_t L, uint32_t *rowmark)
 {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint4 e1 = recs[2 * i + 1];
@@ -1740,6 +1771,11 @@ __global__ void k_elem_hist(Dev d, const uint4 *recs, uint64_t n, uint32_t L)
             continue;
         }
         atomicAdd(&d.cnt[(size_t)((e1.z >> KEY_SHIFT) - 1) * d.V + e1.w], 1u);
+        if (rowmark) {
+            const uint32_t bit = 1u << (e1.w & 31);
+            uint32_t *w = rowmark + (e1.w >> 5);
+            if (!(__ldcg(w) & bit)) atomicOr(w, bit);
+        }
     }
 }
 
@@ -1927,6 +1963,8 @@ struct grg_ctx {
     bool stamp_on = false;                 // the pool carries a stamp per slot
     bool elem_loaded = false;              // the current graph came from grg_load_elements
     uint32_t *stamp = nullptr;             // per-slot stamps (pool_cap entries)
+    uint32_t *rowmark = nullptr;           // rows an element image holds (1 bit per vertex)
+    uint64_t rowmark_cap = 0;
     uint32_t run_stamp = 0;                // stamp given to elements that gain bits in this closure
     uint4 *xbuf = nullptr;                 // staged element records (load input / export output)
     uint32_t *xst = nullptr;               // staged stamps
@@ -2342,6 +2380,7 @@ void grg_destroy(grg_ctx *c)
     cudaFree(c->sbuf);
     cudaFree(c->xbuf);
     cudaFree(c->xst);
+    cudaFree(c->rowmark);
     cudaFree(c->cand[0]);
     cudaFree(c->cand[1]);
     cudaFree(c->chunk);
@@ -2532,14 +2571,14 @@ MinCap derived_min_cap(const grg_ctx *c)
 // cnt; the pool grows (and the histogram is rebuilt) until the tables fit.
 // Clears the allocated region. Returns the pool top in *top.
 template <class Hist>
-int alloc_tables(grg_ctx *c, const MinCap &mc, Hist hist, uint64_t *top)
+int alloc_tables(grg_ctx *c, const MinCap &mc, Hist hist, uint64_t *top, const uint32_t *rowmark = nullptr)
 {
     cudaStream_t s = c->stream;
     hist(make_dev(c));
     for (int attempt = 0;; attempt++) {
         GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_POOL_TOP, 0, 8, s));
         GRG_CUDA(c, cudaMemsetAsync(c->ctr + C_ERR, 0, 8, s));
-        k_load_alloc<<<grid_for(c, c->ntables, 256), 256, 0, s>>>(make_dev(c), 0, c->V, (uint32_t)c->L, mc);
+        k_load_alloc<<<grid_for(c, c->ntables, 256), 256, 0, s>>>(make_dev(c), 0, c->V, (uint32_t)c->L, mc, rowmark);
         c->launches++;
         int st = read_ctr(c);
         if (st) return st;
@@ -2683,14 +2722,25 @@ int grg_load_elements(grg_ctx *c, uint32_t num_vars, uint64_t num_elems, const u
         dst_ = c->xst;
     }
     c->launches = 0;
+    // rows the image holds: only those get presized derived rows
+    const uint64_t mwords = ((uint64_t)num_vars + 31) / 32 + 1;
+    if (c->rowmark_cap < mwords) {
+        cudaFree(c->rowmark);
+        c->rowmark = nullptr;
+        c->rowmark_cap = 0;
+        GRG_CUDA(c, cudaMalloc(&c->rowmark, mwords * 4));
+        c->rowmark_cap = mwords;
+    }
     auto hist = [&](Dev d) {
+        GRG_CUDA(c, cudaMemsetAsync(c->rowmark, 0, mwords * 4, s));
         if (num_elems) {
-            k_elem_hist<<<grid_for(c, num_elems, 256), 256, 0, s>>>(d, drec, num_elems, (uint32_t)c->L);
+            k_elem_hist<<<grid_for(c, num_elems, 256), 256, 0, s>>>(d, drec, num_elems, (uint32_t)c->L, c->rowmark);
             c->launches++;
         }
+        return GRG_OK;
     };
     uint64_t top = 0;
-    st = alloc_tables(c, derived_min_cap(c), hist, &top);
+    st = alloc_tables(c, derived_min_cap(c), hist, &top, c->rowmark);
     if (st) return st;
     if (num_elems) {
         k_elem_insert<<<grid_for(c, num_elems, 256), 256, 0, s>>>(make_dev(c), drec, dst_, num_elems, mark_after,
@@ -3614,6 +3664,7 @@ int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *s
         c->launches += 6;
         rt.csr_row[l] = row;
         rt.csr_col[l] = cb.col;
+        rt.csr_n[l] = total;
     }
     c->rt = rt;
     set_passes(c);
@@ -3632,6 +3683,10 @@ int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *s
     bool idle = false;
     st = run_rounds(c, 0, S, join_ms, joins, &idle);
     if (st) return st;
+    if ((st = read_ctr(c))) return st;
+    if (c->h_ctr[C_CHECK])
+        return fail(c, GRG_E_INTERNAL, "bounds check " + std::to_string(c->h_ctr[C_CHECK] >> 56) + " failed (value " +
+                                           std::to_string(c->h_ctr[C_CHECK] & ((1ull << 56) - 1)) + ")");
     GRG_CUDA(c, cudaEventRecord(c->ev_b, s));
     GRG_CUDA(c, cudaEventSynchronize(c->ev_b));
     float ms = 0;
@@ -4254,7 +4309,8 @@ int grg_batch_admit(grg_ctx *c, uint32_t job, uint32_t base, uint32_t num_vars, 
                                                                 c->tmask);
     for (int l = 1; l <= c->L; l++)
         if ((eps_mask >> (l - 1)) & 1ull) k_eps_hist<<<grid_for(c, num_vars, 256), 256, 0, s>>>(d, (uint32_t)l, base, num_vars);
-    k_load_alloc<<<grid_for(c, (uint64_t)c->L * num_vars, 256), 256, 0, s>>>(d, base, num_vars, (uint32_t)c->L, mc);
+    k_load_alloc<<<grid_for(c, (uint64_t)c->L * num_vars, 256), 256, 0, s>>>(d, base, num_vars, (uint32_t)c->L, mc,
+                                                                              nullptr);
     st = read_ctr(c);
     if (st) return st;
     if (c->h_ctr[C_BADIN]) {
@@ -4527,7 +4583,7 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
         if (rules[3 * q + 1] == 0) k_eps_hist<<<grid(num_vars, 256, 8), 256, 0, s>>>(d, (uint32_t)rules[3 * q], 0, num_vars);
     MinCap mc;
     memset(&mc, 0, sizeof mc);
-    k_load_alloc<<<grid(nlab, 256, 8), 256, 0, s>>>(d, 0, num_vars, (uint32_t)num_labels, mc);
+    k_load_alloc<<<grid(nlab, 256, 8), 256, 0, s>>>(d, 0, num_vars, (uint32_t)num_labels, mc, nullptr);
     if ((st = na_read(h, d.ctr, s))) return st;
     if (h[C_BADIN] & ERR_IN_LABEL) return GRG_E_LABEL;
     if (h[C_BADIN] & ERR_IN_RANGE) return GRG_E_RANGE;

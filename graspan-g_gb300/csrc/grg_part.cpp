@@ -38,6 +38,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -169,8 +170,37 @@ struct Pinned {
 
 }  // namespace
 
+// The next device run's input, prepared while the current run computes: a
+// helper thread assembles it in page-locked memory and copies it to the device
+// on a copy stream of its own, and allocates ahead the page-locked buffers that
+// the coming exports fill (pinning host memory costs about as much as copying
+// it). A run whose input was prepared loads it from the device.
+struct Ahead {
+    std::thread th;
+    bool active = false;             // a helper thread was started for `key`
+    int status = GRG_OK;             // the helper's CUDA status
+    std::vector<uint64_t> key;       // the run it prepares: partition ids, kind, marks
+    uint64_t n = 0;                  // records
+    Pinned pin;                      // page-locked staging
+    uint32_t *d_rec = nullptr, *d_st = nullptr;   // device copy
+    uint64_t dcap = 0;
+    cudaStream_t cs = nullptr;
+    cudaEvent_t ev = nullptr;
+    ~Ahead()
+    {
+        if (th.joinable()) th.join();
+        if (ev) cudaEventDestroy(ev);
+        if (cs) cudaStreamDestroy(cs);
+        cudaFree(d_rec);
+        cudaFree(d_st);
+    }
+};
+
 struct grg_part {
     grg_ctx *ctx = nullptr;
+    Ahead ahead;                     // the next run's input (see Ahead)
+    double grow = 0;                 // largest closed/loaded image size ratio seen (export buffer sizing)
+    uint64_t prefetched = 0, prefetch_hits = 0;
     uint32_t V = 0;
     int R = 0, L = 0;
     int rules[3 * GRG_MAX_RULES] = {0};
@@ -522,11 +552,17 @@ int read_state(grg_part *p, FILE *f, uint64_t size)
 }
 
 // Bookkeeping after each completed device run: count it, checkpoint when due.
+int ahead_join(grg_part *p);
+
 int after_run(grg_part *p)
 {
     p->runs_call++;
-    if (p->ckpt_every && !p->ckpt_path.empty() && p->runs_call % p->ckpt_every == 0)
+    if (p->ckpt_every && !p->ckpt_path.empty() && p->runs_call % p->ckpt_every == 0) {
+        // the helper thread may be growing an image's buffers: let it finish first
+        const int st = ahead_join(p);
+        if (st) return st;
         return save_state(p, p->ckpt_path.c_str());
+    }
     return GRG_OK;
 }
 
@@ -542,52 +578,190 @@ int recount(grg_part *p, Image &x)
     return count_image(p, x);
 }
 
-// One device run over the given partitions; the load holds `extra` first (static
-// records of the stream schedule, stamps as given) then the partitions' images.
-// Partitions' records are marked when their stamp is above mark_after.
-int run_once(grg_part *p, uint32_t filter, const std::vector<size_t> &idx, const Image *extra,
-             const bool *keep_label, uint32_t mark_after, uint32_t run_stamp)
+// A device run's input: `extra` first (the stream schedule's static records,
+// stamped 1 in [mark_lo, mark_hi) and 0 elsewhere, so that only the run's own
+// partition's static rows are marked), then the partitions' images (only labels
+// in keep_label when given; with own_one, their stamps count as 1).
+struct RunInput {
+    std::vector<size_t> idx;
+    const Image *extra = nullptr;
+    uint64_t mark_lo = 0, mark_hi = 0;
+    const bool *keep_label = nullptr;
+    bool own_one = false;
+    uint32_t mark_after = 0;
+};
+
+uint64_t input_size(const grg_part *p, const RunInput &in)
 {
-    uint64_t n = extra ? extra->size() : 0;
+    uint64_t n = in.extra ? in.extra->size() : 0;
+    for (size_t i : in.idx) {
+        const Image &x = p->parts[i];
+        if (!in.keep_label) {
+            n += x.size();
+            continue;
+        }
+        for (uint64_t e = 0; e < x.size(); e++)
+            if (in.keep_label[x.rec[8 * e + 6] >> KEY_SHIFT]) n++;
+    }
+    return n;
+}
+
+void stage_input(const grg_part *p, const RunInput &in, uint32_t *rec, uint32_t *st)
+{
+    uint64_t k = 0;
+    if (in.extra && in.extra->size()) {
+        const Image &x = *in.extra;
+        memcpy(rec, x.rec.data(), x.size() * 32);
+        memset(st, 0, x.size() * 4);
+        for (uint64_t e = in.mark_lo; e < in.mark_hi; e++) st[e] = 1;
+        k = x.size();
+    }
+    for (size_t i : in.idx) {
+        const Image &x = p->parts[i];
+        if (!in.keep_label) {                // whole images: one copy each
+            memcpy(rec + 8 * k, x.rec.data(), x.size() * 32);
+            if (in.own_one)
+                for (uint64_t e = 0; e < x.size(); e++) st[k + e] = 1;
+            else
+                memcpy(st + k, x.st.data(), x.size() * 4);
+            k += x.size();
+            continue;
+        }
+        for (uint64_t e = 0; e < x.size(); e++) {
+            if (!in.keep_label[x.rec[8 * e + 6] >> KEY_SHIFT]) continue;
+            memcpy(rec + 8 * k, x.rec.data() + 8 * e, 32);
+            st[k] = in.own_one ? 1u : x.st[e];
+            k++;
+        }
+    }
+}
+
+// Identity of a run's input: what it holds and how it is marked.
+std::vector<uint64_t> input_key(const grg_part *p, const RunInput &in)
+{
+    std::vector<uint64_t> k = {in.extra ? 1ull : 0ull, in.mark_lo, in.mark_hi, in.keep_label ? 1ull : 0ull,
+                               in.own_one ? 1ull : 0ull, in.mark_after};
+    for (size_t i : in.idx) {
+        k.push_back(p->parts[i].id);
+        k.push_back(p->parts[i].size());
+    }
+    return k;
+}
+
+// Waits for the helper thread; the prepared input stays for a run with its key.
+int ahead_join(grg_part *p)
+{
+    Ahead &a = p->ahead;
+    if (a.th.joinable()) a.th.join();
+    return a.status;
+}
+
+void ahead_drop(grg_part *p)
+{
+    ahead_join(p);
+    p->ahead.active = false;
+    p->ahead.key.clear();
+}
+
+// Starts preparing `next` on the helper thread (the partitions it holds must not be
+// changed before the next ahead_join). Image buffers of its partitions are grown
+// ahead to the size their closure is expected to reach.
+int ahead_start(grg_part *p, const RunInput &next)
+{
+    Ahead &a = p->ahead;
+    ahead_drop(p);
+    const uint64_t n = input_size(p, next);
+    if (!n) return GRG_OK;
+    // page-locked and device buffers are sized here, on the calling thread
+    int st = a.pin.ensure(n);
+    if (st) return GRG_OK;                   // no room to prepare: the run stages its input itself
+    if (a.dcap < n) {
+        cudaFree(a.d_rec);
+        cudaFree(a.d_st);
+        a.d_rec = a.d_st = nullptr;
+        a.dcap = 0;
+        const uint64_t c = n + n / 4;
+        if (cudaMalloc(&a.d_rec, c * 32) != cudaSuccess || cudaMalloc(&a.d_st, c * 4) != cudaSuccess) {
+            cudaGetLastError();
+            cudaFree(a.d_rec);
+            cudaFree(a.d_st);
+            a.d_rec = a.d_st = nullptr;
+            return GRG_OK;
+        }
+        a.dcap = c;
+    }
+    if (!a.cs && cudaStreamCreateWithFlags(&a.cs, cudaStreamNonBlocking) != cudaSuccess) return GRG_E_CUDA;
+    if (!a.ev && cudaEventCreateWithFlags(&a.ev, cudaEventDisableTiming) != cudaSuccess) return GRG_E_CUDA;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    a.key = input_key(p, next);
+    a.n = n;
+    a.active = true;
+    a.status = GRG_OK;
+    std::vector<size_t> grow_idx;
+    if (p->grow > 1.0) grow_idx = next.idx;
+    const double grow = p->grow;
+    a.th = std::thread([p, next, n, dev, grow_idx, grow]() {
+        Ahead &h = p->ahead;
+        cudaSetDevice(dev);
+        stage_input(p, next, h.pin.rec, h.pin.st);
+        if (cudaMemcpyAsync(h.d_rec, h.pin.rec, n * 32, cudaMemcpyHostToDevice, h.cs) != cudaSuccess ||
+            cudaMemcpyAsync(h.d_st, h.pin.st, n * 4, cudaMemcpyHostToDevice, h.cs) != cudaSuccess ||
+            cudaEventRecord(h.ev, h.cs) != cudaSuccess) {
+            cudaGetLastError();
+            h.status = GRG_E_CUDA;
+            return;
+        }
+        // the coming export of these partitions finds page-locked room already there
+        for (size_t i : grow_idx) {
+            Image &x = p->parts[i];
+            const uint64_t want = (uint64_t)((double)x.size() * grow * 1.1) + 1024;
+            if (!x.rec.reserve(want * 8) || !x.st.reserve(want)) break;
+        }
+    });
+    p->prefetched++;
+    return GRG_OK;
+}
+
+// One device run over the given partitions; `next` (may be null) is the run the
+// helper thread prepares meanwhile. Partitions' records are marked when their
+// stamp is above mark_after.
+int run_once(grg_part *p, uint32_t filter, const RunInput &in, uint32_t run_stamp, const RunInput *next)
+{
     int st;
+    uint64_t n = 0;
+    const uint32_t *rec = nullptr, *stp = nullptr;
+    int on_device = 0;
     {
         Timer tm(p->S.stage_ms);
-        for (size_t i : idx) {
-            if (!keep_label) {
-                n += p->parts[i].size();
-                continue;
+        Ahead &a = p->ahead;
+        if (a.active) {
+            if ((st = ahead_join(p))) return st;
+            if (a.key == input_key(p, in)) {
+                if (cudaEventSynchronize(a.ev) != cudaSuccess) return GRG_E_CUDA;
+                n = a.n;
+                rec = a.d_rec;
+                stp = a.d_st;
+                on_device = 1;
+                p->prefetch_hits++;
             }
-            for (uint64_t e = 0; e < p->parts[i].size(); e++)
-                if (keep_label[p->parts[i].rec[8 * e + 6] >> KEY_SHIFT]) n++;
+            a.active = false;
         }
-        if ((st = p->in.ensure(n))) return st;
-        uint64_t k = 0;
-        if (extra && extra->size()) {
-            memcpy(p->in.rec, extra->rec.data(), extra->size() * 32);
-            memcpy(p->in.st, extra->st.data(), extra->size() * 4);
-            k = extra->size();
-        }
-        for (size_t i : idx) {
-            const Image &x = p->parts[i];
-            if (!keep_label) {               // whole images: one copy each
-                memcpy(p->in.rec + 8 * k, x.rec.data(), x.size() * 32);
-                memcpy(p->in.st + k, x.st.data(), x.size() * 4);
-                k += x.size();
-                continue;
-            }
-            for (uint64_t e = 0; e < x.size(); e++) {
-                if (!keep_label[x.rec[8 * e + 6] >> KEY_SHIFT]) continue;
-                memcpy(p->in.rec + 8 * k, x.rec.data() + 8 * e, 32);
-                p->in.st[k] = x.st[e];
-                k++;
-            }
+        if (!on_device) {
+            n = input_size(p, in);
+            if ((st = p->in.ensure(n))) return st;
+            stage_input(p, in, p->in.rec, p->in.st);
+            rec = p->in.rec;
+            stp = p->in.st;
         }
     }
     p->S.h2d_bytes += n * 36;
     {
         Timer tm(p->S.load_ms);
-        if ((st = grg_load_elements(p->ctx, p->V, n, p->in.rec, p->in.st, mark_after, 0))) return st;
+        if ((st = grg_load_elements(p->ctx, p->V, n, rec, stp, in.mark_after, on_device))) return st;
     }
+    // the input is on the device: the next run's can be prepared while this one computes
+    if (next && (st = ahead_start(p, *next))) return st;
     grg_stats cs;
     {
         Timer tm(p->S.closure_ms);
@@ -597,12 +771,27 @@ int run_once(grg_part *p, uint32_t filter, const std::vector<size_t> &idx, const
     // run chose holds for the rest (no trial per partition)
     if (cs.window_tuned && !p->window_pinned) {
         grg_set_join_window(p->ctx, cs.wide_window ? 1 : 0);
+        grg_set_join_items(p->ctx, cs.join_elements ? 1 : 0);
         p->window_pinned = true;
     }
     p->S.runs++;
     p->S.rounds += cs.rounds;
     return GRG_OK;
 }
+
+// Largest growth of an image from its run input to its exported closure (sizes the
+// page-locked buffers allocated ahead).
+void note_growth(grg_part *p, uint64_t before, uint64_t after)
+{
+    if (before) p->grow = std::max(p->grow, (double)after / (double)before);
+}
+
+// Every way out of a schedule waits for the helper thread first (it reads the
+// schedule's partitions and static records).
+struct AheadGuard {
+    grg_part *p;
+    ~AheadGuard() { ahead_drop(p); }
+};
 
 int run_stream(grg_part *p, uint32_t filter, const bool *der)
 {
@@ -614,13 +803,29 @@ int run_stream(grg_part *p, uint32_t filter, const bool *der)
     Image stat;
     std::vector<uint64_t> seg;
     bool stale = true;
+    AheadGuard guard{p};                 // declared after stat: joins the helper before stat goes
+    auto input_of = [&](size_t i) {
+        RunInput in;
+        in.idx = {i};
+        in.extra = &stat;
+        in.mark_lo = seg[i];
+        in.mark_hi = seg[i + 1];
+        in.keep_label = derived;
+        in.own_one = true;                   // every derived record of the partition is marked
+        in.mark_after = 0;
+        return in;
+    };
     for (size_t i = 0; i < p->parts.size();) {
         if (p->parts[i].done) {          // closed before a pause
             i++;
             continue;
         }
-        if (p->run_budget && p->runs_call >= p->run_budget) return GRG_PAUSED;
+        if (p->run_budget && p->runs_call >= p->run_budget) {
+            ahead_drop(p);
+            return GRG_PAUSED;
+        }
         if (stale) {
+            ahead_drop(p);               // the prepared input holds the old static records
             uint64_t ns = 0;
             for (const Image &x : p->parts)
                 for (uint64_t e = 0; e < x.size(); e++) ns += !derived[x.rec[8 * e + 6] >> KEY_SHIFT];
@@ -638,24 +843,34 @@ int run_stream(grg_part *p, uint32_t filter, const bool *der)
             }
             stale = false;
         }
-        for (uint64_t e = seg[i]; e < seg[i + 1]; e++) stat.st[e] = 1;
-        Image &x = p->parts[i];
-        for (uint32_t &s : x.st) s = 1;
-        const int st = run_once(p, filter, {i}, &stat, derived, 0, 0);
-        for (uint64_t e = seg[i]; e < seg[i + 1]; e++) stat.st[e] = 0;
+        // the next partition to close, prepared while this one computes
+        size_t i2 = i + 1;
+        while (i2 < p->parts.size() && p->parts[i2].done) i2++;
+        const bool has_next = i2 < p->parts.size() && !(p->run_budget && p->runs_call + 1 >= p->run_budget);
+        const RunInput in = input_of(i);
+        RunInput nx;
+        if (has_next) nx = input_of(i2);
+        const uint64_t before = input_size(p, in) - stat.size();
+        const int st = run_once(p, filter, in, 0, has_next ? &nx : nullptr);
         if (st == GRG_E_NOMEM) {
+            ahead_drop(p);
             if (!split(p, i)) return GRG_E_NOMEM;
             stale = true;
             continue;
         }
-        if (st) return st;
+        if (st) {
+            ahead_drop(p);
+            return st;
+        }
         int s2 = export_image(p, p->parts[i]);
         if (s2) return s2;
+        note_growth(p, before, p->parts[i].size());
         if ((s2 = count_image(p, p->parts[i]))) return s2;
         p->parts[i].done = true;
         if ((s2 = after_run(p))) return s2;
         i++;
     }
+    ahead_drop(p);
     return GRG_OK;
 }
 
@@ -673,6 +888,7 @@ bool reaches(const Image &a, const Image &b)
 
 int run_pairs(grg_part *p, uint32_t filter)
 {
+    AheadGuard guard{p};
     for (;;) {
         bool ran = false, restart = false;
         // pairs whose B-edges cross, then partitions no run has closed since their last change
@@ -681,6 +897,20 @@ int run_pairs(grg_part *p, uint32_t filter)
         for (size_t i = 0; i < m; i++)
             for (size_t j = i + 1; j < m; j++) order.emplace_back(i, j);
         for (size_t i = 0; i < m; i++) order.emplace_back(i, i);
+        auto needed = [&](size_t k) {
+            const size_t i = order[k].first, j = order[k].second;
+            const Image &a = p->parts[i], &b = p->parts[j];
+            const uint32_t t = seen_of(p, a.id, b.id);
+            if (i == j) return a.max_stamp > t;
+            return reaches(a, b) && (a.max_stamp > t || b.max_stamp > t);
+        };
+        auto input_of = [&](size_t k) {
+            RunInput in;
+            in.idx = {order[k].first};
+            if (order[k].second != order[k].first) in.idx.push_back(order[k].second);
+            in.mark_after = seen_of(p, p->parts[order[k].first].id, p->parts[order[k].second].id);
+            return in;
+        };
         // a paused superstep continues where it stopped (later pairs are not starved by a restart)
         size_t k0 = 0;
         if (p->cursor && p->cursor < order.size()) {
@@ -693,34 +923,50 @@ int run_pairs(grg_part *p, uint32_t filter)
             const size_t i = order[k].first, j = order[k].second;
             Image &a = p->parts[i], &b = p->parts[j];
             const uint32_t t = seen_of(p, a.id, b.id);
-            bool need;
-            if (i == j)
-                need = a.max_stamp > t;
-            else
-                need = reaches(a, b) && (a.max_stamp > t || b.max_stamp > t);
-            if (!need) {
+            if (!needed(k)) {
                 p->S.skipped++;
                 continue;
             }
             if (p->run_budget && p->runs_call >= p->run_budget) {
+                ahead_drop(p);
                 p->cursor = k;
                 p->cursor_ran = ran;
                 return GRG_PAUSED;
             }
+            // the next pair this superstep runs, prepared meanwhile when it shares no
+            // partition with this one (this run changes nothing it reads)
+            RunInput nx;
+            bool has_next = false;
+            if (!(p->run_budget && p->runs_call + 1 >= p->run_budget))
+                for (size_t k2 = k + 1; k2 < order.size(); k2++) {
+                    if (!needed(k2)) continue;
+                    const size_t i2 = order[k2].first, j2 = order[k2].second;
+                    if (i2 != i && i2 != j && j2 != i && j2 != j) {
+                        nx = input_of(k2);
+                        has_next = true;
+                    }
+                    break;
+                }
             const uint32_t r = ++p->run_id;
-            std::vector<size_t> idx = {i};
-            if (j != i) idx.push_back(j);
-            const int st = run_once(p, filter, idx, nullptr, nullptr, t, r);
+            const RunInput in = input_of(k);
+            const uint64_t before = input_size(p, in);
+            const int st = run_once(p, filter, in, r, has_next ? &nx : nullptr);
             if (st == GRG_E_NOMEM) {
+                ahead_drop(p);
                 const size_t big = (j != i && b.size() > a.size()) ? j : i;
                 if (!split(p, big)) return GRG_E_NOMEM;
                 restart = true;
                 break;
             }
-            if (st) return st;
-            for (size_t q : idx) {
+            if (st) {
+                ahead_drop(p);
+                return st;
+            }
+            uint64_t after = 0;
+            for (size_t q : in.idx) {
                 int s2 = export_image(p, p->parts[q]);
                 if (s2) return s2;
+                after += p->parts[q].size();
                 if ((s2 = count_image(p, p->parts[q]))) return s2;
                 if ((s2 = reach_image(p, q))) return s2;
                 Image &x = p->parts[q];
@@ -728,14 +974,19 @@ int run_pairs(grg_part *p, uint32_t filter)
                 x.last_run = r;
                 p->seen[pkey(x.id, x.id)] = r;   // a run that holds x closes x's own rows
             }
+            note_growth(p, before, after);
             p->seen[pkey(a.id, b.id)] = r;
+            (void)t;
             ran = true;
             const int s3 = after_run(p);
             if (s3) return s3;
         }
         if (restart) continue;
         p->S.supersteps++;
-        if (!ran) return GRG_OK;
+        if (!ran) {
+            ahead_drop(p);
+            return GRG_OK;
+        }
     }
 }
 
@@ -855,9 +1106,13 @@ int grg_part_run(grg_part *p, uint32_t filter, grg_part_stats *stats)
         if (r[1] && r[2] && der[r[2]]) coupled = true;
     }
     p->S.schedule = coupled ? 1 : 0;
+    p->prefetched = p->prefetch_hits = 0;
     int st = coupled ? run_pairs(p, filter) : run_stream(p, filter, der);
+    p->S.prefetched = p->prefetched;
+    p->S.prefetch_hits = p->prefetch_hits;
     if (p->window_pinned) {                // the context tunes again after this run
         grg_set_join_window(p->ctx, 2);
+        grg_set_join_items(p->ctx, 2);
         p->window_pinned = false;
     }
     if (st == GRG_PAUSED) {

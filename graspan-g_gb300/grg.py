@@ -76,7 +76,7 @@ class PartStats(ctypes.Structure):
         ("splits", ctypes.c_uint64), ("rounds", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64),
         ("d2h_bytes", ctypes.c_uint64), ("ms", ctypes.c_double), ("stage_ms", ctypes.c_double),
         ("load_ms", ctypes.c_double), ("closure_ms", ctypes.c_double), ("export_ms", ctypes.c_double),
-        ("count_ms", ctypes.c_double),
+        ("count_ms", ctypes.c_double), ("prefetched", ctypes.c_uint64), ("prefetch_hits", ctypes.c_uint64),
     ]
 
     def as_dict(self):

@@ -219,10 +219,15 @@ def dataflow_blocks(seed=0x5EED0002, num_blocks=2000, block=1000, num_edges=6_00
 
 
 def alias(seed=0x5EED0003, num_vars=1_000_000, num_base_edges=4_000_000, frac_a=0.6, zipf_s=1.8, cap=256,
-          p_local=0.8, window=256, block=1000):
+          p_local=0.8, window=256, block=1000, partner=0, p_cross=0.02):
     """Alias-analysis graph. block=None draws edges over the whole vertex range
     (every vertex then joins one V class and the closure grows as V^2);
-    block=B confines each vertex's edges to its B-vertex procedure block."""
+    block=B confines each vertex's edges to its B-vertex procedure block.
+    partner=P (with block): a fraction p_cross of the edges go instead to the
+    partner block P blocks away (blocks b and b + P are partners when b // P is
+    even), so procedures call across P-block strides -- with P blocks per
+    partition, across partition boundaries -- while the closure stays bounded
+    (each call graph component is two blocks)."""
     rng = np.random.default_rng(seed)
     labels = grammar_labels(ALIAS_RULES)
     ids = {n: labels.index(n) + 1 for n in labels}
@@ -231,13 +236,22 @@ def alias(seed=0x5EED0003, num_vars=1_000_000, num_base_edges=4_000_000, frac_a=
         bs = (np.arange(num_vars, dtype=np.int64) // block) * block
         be = np.minimum(bs + block, num_vars) - 1
 
+        nblocks = (num_vars + block - 1) // block
+
         def draw(s):
             s = s.astype(np.int64)
             lo, hi = bs[s], be[s]
             local = rng.random(len(s)) < p_local
             d_loc = np.clip(s + rng.integers(-window, window + 1, size=len(s)), lo, hi)
             d_uni = lo + (rng.random(len(s)) * (hi - lo + 1)).astype(np.int64)
-            return np.where(local, d_loc, d_uni).astype(np.uint32)
+            d = np.where(local, d_loc, d_uni)
+            if partner:
+                b = s // block
+                pb = np.where((b // partner) % 2 == 0, b + partner, b - partner)
+                cross = (rng.random(len(s)) < p_cross) & (pb >= 0) & (pb < nblocks)
+                off = d - lo
+                d = np.where(cross, np.minimum(pb * block + off, num_vars - 1), d)
+            return d.astype(np.uint32)
     else:
         def draw(s):
             return _local_dst(rng, s, num_vars, p_local, window)
@@ -254,7 +268,8 @@ def alias(seed=0x5EED0003, num_vars=1_000_000, num_base_edges=4_000_000, frac_a=
     s_all, d_all, l_all = s_all[keep], d_all[keep], l_all[keep]
     order = np.lexsort((l_all, d_all, s_all))
     return Workload("alias", num_vars, ALIAS_RULES, 0, s_all[order], d_all[order], labels, l_all[order],
-                    {"seed": seed, "base_edges": int(len(src)), "block": block})
+                    {"seed": seed, "base_edges": int(len(src)), "block": block, "partner": partner,
+                     "p_cross": p_cross if partner else 0.0})
 
 
 POINTSTO_RULES = [("M", "DV", "d"), ("DV", "-d", "V"), ("V", "MAM", "AMs"), ("MAM", "MAs", "Mq"), ("Mq",),

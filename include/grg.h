@@ -312,6 +312,10 @@ typedef struct {
     double closure_ms;        /*           closures (grg_closure_ex) */
     double export_ms;         /*           reading images back (grg_export_elements) */
     double count_ms;          /*           per-partition counts and reach sets */
+    uint64_t prefetched;      /* runs whose input a helper thread assembled and copied to the device
+                                 (on a copy stream) while the run before computed */
+    uint64_t prefetch_hits;   /* of those, runs that loaded the prepared input (the others were
+                                 superseded by a run the schedule had not foreseen) */
 } grg_part_stats;
 
 /* A partitioned graph over [0, num_vars) on context ctx (which holds the

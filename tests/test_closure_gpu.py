@@ -240,15 +240,19 @@ def test_join_windows_equal(grg_mod, oracle_mod, name):
          "dataflow": lambda: G.dataflow_blocks(seed=43, num_blocks=20, block=500, num_edges=30000)}[name]()
     r = oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, w.filter_flag, w.src, w.dst, w.lab)
     for mode in (0, 1):
-        ctx = grg_mod.Context(0)
-        ctx.set_join_window(mode)
-        ctx.set_layout(0)                  # every label by source: the dataflow closure runs k_join too
-        ctx.transfer_rules(w.rule_ids(), w.num_labels)
-        ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
-        st = ctx.closure(w.filter_flag)
-        assert st["wide_window"] == mode
-        assert ctx.label_counts().tolist() == r.label_counts().tolist() and ctx.set_hash() == r.set_hash
-        ctx.close()
+        for items in (0, 1):
+            ctx = grg_mod.Context(0)
+            ctx.set_join_window(mode)
+            ctx.set_join_items(items)
+            ctx.set_layout(0)              # every label by source: the dataflow closure runs k_join too
+            ctx.transfer_rules(w.rule_ids(), w.num_labels)
+            ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
+            st = ctx.closure(w.filter_flag)
+            assert st["wide_window"] == mode
+            # only the dataflow grammar's e has a CSR copy (a static second symbol)
+            assert st["join_elements"] == (items if name == "dataflow" else 0)
+            assert ctx.label_counts().tolist() == r.label_counts().tolist() and ctx.set_hash() == r.set_hash
+            ctx.close()
 
 
 @pytest.mark.parametrize("device_rounds", [True, False])
@@ -266,16 +270,19 @@ def test_tuned_window_measures_then_reuses(grg_mod, oracle_mod, device_rounds):
     for k in range(2):
         ctx = grg_mod.Context(0)
         ctx.set_join_window(3 if k == 0 else 2)
+        ctx.set_join_items(3 if k == 0 else 2)
         ctx.set_layout(0)                  # the window is a choice of k_join, which source rows run
         ctx.set_device_rounds(device_rounds)
         ctx.transfer_rules(w.rule_ids(), w.num_labels)
         ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
         st = ctx.closure(w.filter_flag)
         assert (ctx.label_counts().tolist(), ctx.set_hash()) == want
-        seen.append((st["window_tuned"], st["wide_window"], st["window_trial_ms"]))
+        seen.append((st["window_tuned"], st["wide_window"], st["window_trial_ms"], st["join_elements"],
+                     st["items_trial_ms"]))
         ctx.close()
-    assert seen[0][0] == 1 and min(seen[0][2]) > 0
+    assert seen[0][0] == 1 and min(seen[0][2]) > 0 and min(seen[0][4]) > 0
     assert seen[1][0] == 2 and seen[1][1] == seen[0][1] and seen[1][2] == [0.0, 0.0]
+    assert seen[1][3] == seen[0][3]                  # the item form comes from the cache too
     ctx = grg_mod.Context(0)
     ctx.set_join_window(1)
     ctx.set_layout(0)

@@ -80,3 +80,50 @@ def test_batch_mix_sample(grg_mod):
         assert j.num_vars == want["num_vars"] and len(j.src) == want["num_edges"]
         assert j.counts == want["labels"], (j.job, j.kind)
         assert j.hash == want["hash"], (j.job, j.kind)
+
+
+def test_alias_8m_cross_partition_pairs(grg_mod, oracle_mod):
+    """The 8M-vertex alias graph with 2% of its edges calling the partner block
+    125 blocks away -- across the boundary of the 64 partitions of 125 blocks --
+    so the pairs schedule must run cross pairs. In-core and out-of-core closures
+    agree; 16 sampled two-block components are closed by the oracle alone and
+    match the GPU's range counts and hashes over their rows."""
+    import numpy as np
+    w = G.alias(seed=0x5EED0006, num_vars=8_000_000, num_base_edges=40_000_000, block=1000, partner=125)
+    ctx = grg_mod.Context(0)
+    ctx.allocate_pool(0)
+    ctx.transfer_rules(w.rule_ids(), w.num_labels)
+    ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
+    st = ctx.closure(0)
+    whole = ([int(x) for x in ctx.label_counts()], ctx.set_hash())
+    # components {b, b + 125} for b // 125 even: sample 16 of them
+    comps = [(b, b + 125) for b in range(0, 8000, 500)][:16]
+    got_counts = np.zeros(w.num_labels, np.uint64)
+    got_hash = 0
+    for b0, b1 in comps:
+        for b in (b0, b1):
+            c, h = ctx.range_counts(b * 1000, (b + 1) * 1000)
+            got_counts += c
+            got_hash = (got_hash + h) & (2**64 - 1)
+    ctx.close()
+    rows = np.zeros(w.num_vars, bool)
+    for b0, b1 in comps:
+        rows[b0 * 1000:(b0 + 1) * 1000] = True
+        rows[b1 * 1000:(b1 + 1) * 1000] = True
+    sel = rows[w.src]
+    assert rows[w.dst[sel]].all()                    # the sampled components are closed
+    r = oracle_mod.closure(w.num_vars, w.rule_ids(), w.num_labels, 0, w.src[sel], w.dst[sel], w.lab[sel])
+    assert got_counts.tolist() == r.label_counts().tolist() and got_hash == r.set_hash
+    # out of core over 64 partitions: cross pairs run, the result equals the in-core one
+    ctx = grg_mod.Context(0)
+    ctx.transfer_rules(w.rule_ids(), w.num_labels)
+    part = grg_mod.Partitioned(ctx, w.num_vars, 64)
+    part.load_edges(w.src, w.dst, w.lab)
+    pst = part.run(0)
+    counts, h = part.label_counts()
+    assert ([int(x) for x in counts], h) == whole
+    assert pst["total_edges"] == st["total_edges"]
+    assert pst["skipped"] < 64 * 63 // 2 + 64          # cross pairs ran
+    assert pst["runs"] > 64
+    part.close()
+    ctx.close()

@@ -61,6 +61,8 @@ def test_dataflow_stream(grg_mod, oracle_mod, f):
     counts, h, st, _ = part_closure(grg_mod, w, f, 4)
     assert (counts, h) == want
     assert st["schedule"] == "stream" and st["runs"] == 4 and st["supersteps"] == 0
+    # each partition's input after the first was assembled and copied while the one before computed
+    assert st["prefetched"] == 3 and st["prefetch_hits"] == 3
 
 
 @pytest.mark.parametrize("seed", range(8))
