@@ -972,8 +972,12 @@ __global__ void __launch_bounds__(PUSH_WARPS * 32, 4) k_push_flat(Dev d, const u
     const uint32_t lane = lane_id(), wi = threadIdx.x >> 5;
     uint8_t *own = own_s[wi];
     unsigned long long n_left = 0, n_right = 0;
-    const uint64_t nbatch = (n + 31) / 32, nwarps = (uint64_t)gridDim.x * PUSH_WARPS;
-    for (uint64_t bt = blockIdx.x * (uint64_t)PUSH_WARPS + wi; bt < nbatch; bt += nwarps) {
+    // warps pull batches of 32 records from the launch's device queue (C_JQ, zeroed before it)
+    const uint64_t nbatch = (n + 31) / 32;
+    uint64_t bt = 0;
+    if (lane == 0) bt = atomicAdd(&d.ctr[C_JQ], 1ull);
+    bt = __shfl_sync(0xffffffffu, bt, 0);
+    for (; bt < nbatch; bt = __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(&d.ctr[C_JQ], 1ull) : 0ull, 0)) {
         const uint64_t i = bt * 32 + lane;
         const bool have = i < n;
         uint4 a = make_uint4(0, 0, 0, 0), b = make_uint4(0, 0, EMPTY, 0);
@@ -1223,9 +1227,14 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
     unsigned long long ph[5] = {0, 0, 0, 0, 0};
     long long ph_t = clock64();
 #endif
-    const uint64_t nwarps = (uint64_t)gridDim.x * JOIN_WARPS;
+    // a persistent grid: each warp pulls its next batch of 32 records from the launch's
+    // device queue (C_JQ, zeroed before the launch), so warps that drew light batches take
+    // more of them instead of idling behind the ones that drew heavy records
     const uint64_t nbatch = (n + RB - 1) / RB;
-    for (uint64_t bt = blockIdx.x * (uint64_t)JOIN_WARPS + (threadIdx.x >> 5); bt < nbatch; bt += nwarps) {
+    uint64_t bt = 0;
+    if (lane == 0) bt = atomicAdd(&d.ctr[C_JQ], 1ull);
+    bt = __shfl_sync(0xffffffffu, bt, 0);
+    for (; bt < nbatch; bt = __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(&d.ctr[C_JQ], 1ull) : 0ull, 0)) {
         const uint64_t ri = bt * RB + lane;
         const bool have = ri < n;
         Bits rb;
@@ -2801,6 +2810,10 @@ static void launch_join(const grg_ctx *c, int grid, cudaStream_t s, const Dev &d
         for (int l = 0; l <= MAX_LABELS; l++) de.rt.csr_row[l] = nullptr;
         dp = &de;
     }
+    // the launch's work queue starts at batch 0; the grid is what the SMs hold at once
+    cudaMemsetAsync(d.ctr + C_JQ, 0, 8, s);
+    const int resident = c->sms * (c->join_wide ? GRG_JOIN_MINB_WIDE : GRG_JOIN_MINB);
+    if (grid > resident) grid = resident;
     if (c->join_wide)
         k_join<WIN2, WIN2_LO><<<grid, JOIN_WARPS * 32, 0, s>>>(*dp, recs, n, n_ctr, retry_out);
     else
@@ -2848,9 +2861,10 @@ static void launch_pass(grg_ctx *c, int grid, cudaStream_t s, const Dev &d, cons
         joins++;
     }
     if (c->need_push) {
-        if (c->push_flat)
+        if (c->push_flat) {
+            cudaMemsetAsync(d.ctr + C_JQ, 0, 8, s);
             k_push_flat<<<c->sms * 4, PUSH_WARPS * 32, 0, s>>>(d, recs, n, n_ctr, retry_out);
-        else
+        } else
             k_push<<<c->sms * 8, 256, 0, s>>>(d, recs, n, n_ctr, retry_out);
         c->launches++;
         joins++;
@@ -4640,12 +4654,17 @@ extern "C" int grg_closure_noalloc(int device, void *stream, int num_rules, cons
         int rb = 0;
         for (int pass = 0;; pass++) {
             const int g = grid((n + RB - 1) / RB, JOIN_WARPS, 16);
+            // each join launch pulls 32-record batches from a queue that starts at 0
             if (pass == 0) {
+                NA_CUDA(cudaMemsetAsync(d.ctr + C_JQ, 0, 8, s));
                 k_join<WIN, WIN_LO><<<g, JOIN_WARPS * 32, 0, s>>>(d, gbuf, nd, -1, rbuf[0]);
-                if (nv)
+                if (nv) {
+                    NA_CUDA(cudaMemsetAsync(d.ctr + C_JQ, 0, 8, s));
                     k_join<WIN, WIN_LO><<<grid((nv + RB - 1) / RB, JOIN_WARPS, 16), JOIN_WARPS * 32, 0, s>>>(d, vbuf, nv,
                                                                                                         -1, rbuf[0]);
+                }
             } else {
+                NA_CUDA(cudaMemsetAsync(d.ctr + C_JQ, 0, 8, s));
                 k_join<WIN, WIN_LO><<<g, JOIN_WARPS * 32, 0, s>>>(d, rbuf[rb], n, -1, rbuf[rb ^ 1]);
             }
             NA_CUDA(cudaGetLastError());

@@ -249,9 +249,9 @@ def test_join_windows_equal(grg_mod, oracle_mod, name):
             ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
             st = ctx.closure(w.filter_flag)
             assert st["wide_window"] == mode
-            # the item form applies to labels with a CSR copy (static second symbols: the
-            # dataflow grammar's e; points-to's d and -a; the alias grammar has none)
-            assert st["join_elements"] == (0 if name == "alias" else items)
+            # the item form applies to labels with a CSR copy, the static second symbols
+            # (dataflow: e; points-to: d and -a; alias: d), so each case exercises both forms
+            assert st["join_elements"] == items
             assert ctx.label_counts().tolist() == r.label_counts().tolist() and ctx.set_hash() == r.set_hash
             ctx.close()
 
