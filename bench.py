@@ -384,6 +384,8 @@ def main():
     ap.add_argument("--workload", default="dataflow", choices=["dataflow", "alias"],
                     help="dataflow: the headline; alias: the 1M-vertex alias closure alone (for profiling; "
                          "implies --quick and --no-cpu-baseline)")
+    ap.add_argument("--alias-vars", type=int, default=1_000_000,
+                    help="vertices of the alias workload (4 base edges per vertex; smaller for profiler captures)")
     args = ap.parse_args()
     world, rank, local = dist_setup(args)
 
@@ -392,9 +394,9 @@ def main():
     if args.workload == "alias" and args.impl == "reference":
         ap.error("--workload alias is a GPU profiling case; the reference arm runs the headline workload")
     if args.workload == "alias":
-        WORKLOAD = ("alias grammar, 1M vertices, 4M base + 4M inverse edges, Zipf(1.8) cap 256, "
-                    "1000-vertex blocks, filter_flag 0")
-        w = G.alias()
+        WORKLOAD = (f"alias grammar, {args.alias_vars} vertices, {4 * args.alias_vars} base + inverse edges, "
+                    "Zipf(1.8) cap 256, 1000-vertex blocks, filter_flag 0")
+        w = G.alias(num_vars=args.alias_vars, num_base_edges=4 * args.alias_vars)
         args.quick = args.no_cpu_baseline = True
     else:
         edges = 6_000_000 * args.blocks // 2000
@@ -512,7 +514,10 @@ def main():
                        "pool_elems_used": s["pool_elems_used"],
                        "join_window": ("wide (10 elements)" if s["wide_window"] else "narrow (8 elements)") +
                        {0: ", fixed", 1: ", measured in this step", 2: ", tuned (degree-key cache)"}[
-                           int(s["window_tuned"])]},
+                           int(s["window_tuned"])],
+                       "join_items": "table elements" if s["join_elements"] else "destination ids",
+                       "push_kernel": (("edges dealt over lanes" if s["push_flat"] else "one lane per record")
+                                       if s["column_labels"] else None)},
             "e2e": {"value": world * total / (e2e_max * 1e-3), "unit": UNIT,
                     "h2d_bytes_per_step": int(w.num_edges * 9), "d2h_bytes_per_step": int(w.num_labels * 8)},
             "roofline": {"bound": "hbm",

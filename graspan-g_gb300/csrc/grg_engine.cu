@@ -2007,7 +2007,7 @@ struct grg_ctx {
     // labels stored by destination in the loaded graph (bit l-1), and whether loads
     // may choose that layout (grg_set_layout)
     uint64_t tmask = 0;
-    int layout_mode = 1;
+    int layout_mode = 0;
     // kernels a join pass needs under the current rule table: k_join for records
     // joined by source rows, k_push for records of destination-stored labels
     bool need_join = true, need_push = false;
@@ -2365,8 +2365,8 @@ int grg_create(grg_ctx **out, int device)
     if (rr && atoll(rr) > 0) c->retry_min = (uint64_t)atoll(rr);
     const char *jw = getenv("GRG_JOIN_WINDOW");        // "narrow" / "wide"; otherwise chosen per closure
     if (jw) c->join_window_mode = !strcmp(jw, "narrow") ? 0 : !strcmp(jw, "wide") ? 1 : 2;
-    const char *ly = getenv("GRG_LAYOUT");             // "rows": every label stored by source
-    if (ly && !strcmp(ly, "rows")) c->layout_mode = 0;
+    const char *ly = getenv("GRG_LAYOUT");             // "columns": labels the grammar allows by destination
+    if (ly) c->layout_mode = !strcmp(ly, "columns") ? 1 : 0;
     const char *ji = getenv("GRG_JOIN_ITEMS");         // "ids" / "elements"; otherwise chosen per closure
     if (ji) c->items_mode = !strcmp(ji, "ids") ? 0 : !strcmp(ji, "elements") ? 1 : 2;
     const char *pm = getenv("GRG_PUSH");               // "lane" / "flat"; otherwise chosen per closure

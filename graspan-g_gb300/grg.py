@@ -268,7 +268,7 @@ class Context:
         self._check(self._L.grg_set_push(self._h, mode), "set_push")
 
     def set_layout(self, mode: int):
-        """0: every label stored by source; 1 (default): labels the grammar allows
+        """0 (default): every label stored by source; 1: labels the grammar allows
         stored by destination (pushed joins). Takes effect at the next load."""
         self._check(self._L.grg_set_layout(self._h, mode), "set_layout")
 

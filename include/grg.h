@@ -135,15 +135,18 @@ int grg_set_join_window(grg_ctx *ctx, int mode);
 int grg_set_join_items(grg_ctx *ctx, int mode);
 
 /* Storage layout of the next graph loaded with grg_load_edges (or batch):
- * mode 1 (the default; environment GRG_LAYOUT=rows selects 0) stores a label
- * by destination -- the table of (label, j) holds the sources i of edges
+ * mode 0 (the default) stores every label by source, as the reference does;
+ * mode 1 (environment GRG_LAYOUT=columns) stores a label by destination -- the table of (label, j) holds the sources i of edges
  * (i, j) -- when the grammar allows it: the label is derived, every binary rule
  * A ::= B C that involves it has a C that is never derived and stores A and B
  * alike, and no old-left join reads it. A rule A ::= B C is then joined by
  * pushing each new element of B's column k (up to 192 sources) whole into A's
  * column j for every edge (k, j) of C, instead of visiting every
  * source-intermediate pair (the dataflow grammar N ::= N e | e is the case
- * this is for). Mode 0 stores every label by source, as the reference does.
+ * this is for). On that grammar's 2M-vertex closure the pushes cost what the
+ * source-row join costs but the delta elements by destination are 2.4x as many
+ * (sources reach a vertex from several blocks), so the gather doubles and
+ * mode 0 is faster; mode 1 stays for inputs where columns are denser.
  * Results are identical either way; the entry points that read rows by source
  * (grg_get_degree, grg_export_elements, grg_range_counts, grg_range_reach,
  * grg_export_csr5) first turn destination-stored labels into rows by source

@@ -286,10 +286,11 @@ def test_tuned_window_measures_then_reuses(grg_mod, oracle_mod, device_rounds):
     assert seen[1][3] == seen[0][3]                  # the item form comes from the cache too
     ctx = grg_mod.Context(0)
     ctx.set_join_window(1)
+    ctx.set_join_items(0)
     ctx.set_layout(0)
     ctx.transfer_rules(w.rule_ids(), w.num_labels)
     ctx.load_edges(w.num_vars, w.src, w.dst, w.lab)
-    assert ctx.closure(w.filter_flag)["window_tuned"] == 0
+    assert ctx.closure(w.filter_flag)["window_tuned"] == 0       # both choices fixed: nothing tuned
     ctx.close()
 
 

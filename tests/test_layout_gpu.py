@@ -79,6 +79,7 @@ def test_column_layout_retries_and_host_rounds(grg_mod, oracle_mod, monkeypatch)
     monkeypatch.setenv("GRG_RETRY_ROOM", "16")
     for rounds in (True, False):
         ctx = grg_mod.Context(0)
+        ctx.set_layout(1)
         ctx.set_device_rounds(rounds)
         ctx.allocate_pool(1 << 20)
         ctx.transfer_rules(w.rule_ids(), w.num_labels)
@@ -100,6 +101,7 @@ def test_push_kernels_equal_and_tuned(grg_mod, oracle_mod, device_rounds):
     seen = []
     for mode in (0, 1, 3, 2):
         ctx = grg_mod.Context(0)
+        ctx.set_layout(1)
         ctx.set_push(mode)
         ctx.set_device_rounds(device_rounds)
         ctx.transfer_rules(w.rule_ids(), w.num_labels)
