@@ -602,6 +602,7 @@ struct __align__(16) WarpSmemT {
     uint32_t rA[RB];              // per record: output label of the current rule pass
     uint32_t rC[RB];              // per record: right operand label
     uint32_t rOff[RB];            // per record: 1 = virtual old-left record
+    uint32_t rlead[RB];           // per record: the first record of its run with the same row and label
     uint32_t kpre[RB + 1];        // exclusive prefix of per-record task counts
     uint8_t own[32];              // per chunk of 32 tasks (items): lane whose record (task) starts there
     uint32_t acc_n;
@@ -1256,6 +1257,15 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
         for (int x = 0; x < EW; x++) w.rbits[lane][x] = rb.w[x];
         w.rrow[lane] = row;
         w.rbase[lane] = base;
+        // a row's records of one label are contiguous (a table's slots are, and the gather
+        // keeps slot order): a run of them shares the window and hash entries of its first
+        // record, so their candidates for one output element merge into one
+        {
+            const uint32_t prow = __shfl_up_sync(0xffffffffu, row, 1), pB = __shfl_up_sync(0xffffffffu, B, 1);
+            const bool start = lane == 0 || !have || B == 0 || prow != row || pB != B;
+            const unsigned sm = __ballot_sync(0xffffffffu, start);
+            w.rlead[lane] = 31 - __clz(sm & (0xFFFFFFFFu >> (31 - lane)));
+        }
         if (lane == 0) w.fail = 0;
         __syncwarp();
         bool ok = true;
@@ -1305,8 +1315,10 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                 const uint32_t rr = chunk_owner(w, my_cnt != 0 && my_st - t0 < 32u, my_st - t0, carry_r);
                 const uint32_t r_st = __shfl_sync(0xffffffffu, my_st, rr);
                 uint32_t r = 0, C = 0, beg = 0, cnt = 0, csr = 0;   // csr: item source 0 table, 1 CSR, 2 delta records
+                uint32_t tr = 0;                                      // the record whose window takes the items
                 if (t < total) {
                     r = rr;
+                    tr = w.rlead[r];
                     C = w.rC[r];
                     const uint32_t k = w.rbase[r] * EIDS + select_bit(w.rbits[r], t - r_st);
                     const uint2 *cr = d.rt.csr_row[C];
@@ -1385,7 +1397,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                     }
                 };
                 // first item of every task in the task's own lane: no search, no broadcast
-                do_item(cnt > 0, r, C, csr, beg);
+                do_item(cnt > 0, tr, C, csr, beg);
                 // the rest, flattened over the lanes
                 const uint32_t cnt1 = cnt ? cnt - 1 : 0;
                 uint32_t incl = cnt1;
@@ -1397,7 +1409,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                 const uint32_t nitems = __shfl_sync(0xffffffffu, incl, 31);
                 // per task: item f sits at beg + 1 + f - (first f of the task); record, label and source packed
                 const uint32_t adj = beg + 1 - (incl - cnt1);
-                const uint32_t pk = r | (C << 8) | (csr << 16);
+                const uint32_t pk = tr | (C << 8) | (csr << 16);
                 const uint32_t s1 = incl - cnt1;             // the task's first flattened item
                 uint32_t carry_o = 0;
                 for (uint32_t f0 = 0; f0 < nitems; f0 += 32) {
@@ -1416,7 +1428,8 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
         }
 
         __syncwarp();
-        const bool failed = have && (!ok || ((w.fail >> lane) & 1u));
+        // a failed insert of a run's merged window re-runs every record of the run
+        const bool failed = have && (!ok || ((w.fail >> w.rlead[lane]) & 1u));
         const unsigned fm = __ballot_sync(0xffffffffu, failed);
         if (fm) {
             unsigned long long p = 0;
