@@ -152,7 +152,7 @@ static void set_columns(RuleTable &rt, uint64_t tmask, int L)
 #define GRG_GATHER_GR 4           // delta records per thread per step of the gather's record pass
 #endif
 #ifndef GRG_JOIN_MINB_WIDE
-#define GRG_JOIN_MINB_WIDE 5
+#define GRG_JOIN_MINB_WIDE 6
 #endif
 #ifdef GRG_PHASE_TIMERS
 #define PH_MARK(i)                                   \
@@ -177,6 +177,13 @@ constexpr int WIN_LO = GRG_WIN_LO;
 constexpr int WIN2 = GRG_WIN2;    // wide window: rows whose destinations spread over many elements
 constexpr int WIN2_LO = GRG_WIN2_LO;
 constexpr int ACC_LG = GRG_ACC_LG;
+#ifndef GRG_WIN_SLOTS
+#define GRG_WIN_SLOTS 16
+#endif
+// dense windows per warp: one per run of a row's records (a batch of 32 records holds ~10
+// runs on the dataflow and alias closures); runs beyond the slots use the hash accumulator
+constexpr int NSLOT = GRG_WIN_SLOTS;
+constexpr uint32_t NO_SLOT = 0xFFu;
 constexpr int ACC = 1 << ACC_LG;  // per-warp hash accumulator entries (candidates outside the window)
 constexpr int ACC_MAX = ACC * 3 / 4;
 
@@ -593,7 +600,8 @@ __global__ void k_oldleft(Dev d, uint32_t q, uint4 *out, uint64_t cap, const uin
 template <int W, int LO>
 struct __align__(16) WarpSmemT {
     static constexpr int kWin = W, kLo = LO;
-    uint32_t win[RB][W][EW];      // dense window accumulator per record
+    uint32_t win[NSLOT][W][EW];   // dense window accumulators, one per run of a row's records
+    uint32_t slot_rec[NSLOT];     // the first record of each window's run
     uint32_t acc_bits[ACC][EW];   // hash accumulator: OR of candidate bitmaps
     uint32_t acc_key[ACC];        // key = record << 25 | base (EMPTY = free)
     uint32_t rbits[RB][EW];       // the batch's delta records
@@ -603,6 +611,7 @@ struct __align__(16) WarpSmemT {
     uint32_t rC[RB];              // per record: right operand label
     uint32_t rOff[RB];            // per record: 1 = virtual old-left record
     uint32_t rlead[RB];           // per record: the first record of its run with the same row and label
+    uint32_t rslot[RB];           // per record: its run's window slot (NO_SLOT: the hash only)
     uint32_t kpre[RB + 1];        // exclusive prefix of per-record task counts
     uint8_t own[32];              // per chunk of 32 tasks (items): lane whose record (task) starts there
     uint32_t acc_n;
@@ -775,26 +784,29 @@ template <class WS>
 __device__ __forceinline__ void win_flush(const Dev &d, WS &w, uint32_t &inserts)
 {
     constexpr int WIN = WS::kWin, WIN_LO = WS::kLo;
+    constexpr int NPOS = (NSLOT * WIN + 31) / 32;
     __syncwarp();
     uint32_t nz = 0;
 #pragma unroll
-    for (int it = 0; it < RB * WIN / 32; it++) {
+    for (int it = 0; it < NPOS; it++) {
         const uint32_t p = it * 32 + lane_id();
-        const uint32_t r = p / WIN, dd = p % WIN;
+        if (p >= (uint32_t)(NSLOT * WIN)) continue;
+        const uint32_t sl = p / WIN, dd = p % WIN;
         uint32_t any = 0;
 #pragma unroll
-        for (int x = 0; x < EW; x++) any |= w.win[r][dd][x];
+        for (int x = 0; x < EW; x++) any |= w.win[sl][dd][x];
         if (any) nz |= 1u << it;
     }
     uint64_t ci = cand_reserve(d, __popc(nz));
 #pragma unroll 1
-    for (int it = 0; it < RB * WIN / 32; it++) {
+    for (int it = 0; it < NPOS; it++) {
         const uint32_t p = it * 32 + lane_id();
-        const uint32_t r = p / WIN, dd = p % WIN;
+        const uint32_t sl = p / WIN, dd = p % WIN;
         if ((nz >> it) & 1u) {
+            const uint32_t r = w.slot_rec[sl];
             Bits b;
 #pragma unroll
-            for (int x = 0; x < EW; x++) { b.w[x] = w.win[r][dd][x]; w.win[r][dd][x] = 0; }
+            for (int x = 0; x < EW; x++) { b.w[x] = w.win[sl][dd][x]; w.win[sl][dd][x] = 0; }
             const uint32_t A = w.rA[r], base = w.rbase[r] + dd - WIN_LO;
             if (ci != ~0ull) {
                 cand_write(d, ci++, b, (A << KEY_SHIFT) | base, w.rrow[r]);
@@ -1219,7 +1231,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
 #pragma unroll
         for (int x = 0; x < EW; x++) w.acc_bits[j][x] = 0;
     }
-    for (int j = lane; j < RB * WIN * EW; j += 32) (&w.win[0][0][0])[j] = 0;
+    for (int j = lane; j < NSLOT * WIN * EW; j += 32) (&w.win[0][0][0])[j] = 0;
     if (lane == 0) w.acc_n = 0;
     __syncwarp();
     unsigned long long n_left = 0, n_right = 0, n_out = 0;
@@ -1264,7 +1276,13 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
             const uint32_t prow = __shfl_up_sync(0xffffffffu, row, 1), pB = __shfl_up_sync(0xffffffffu, B, 1);
             const bool start = lane == 0 || !have || B == 0 || prow != row || pB != B;
             const unsigned sm = __ballot_sync(0xffffffffu, start);
-            w.rlead[lane] = 31 - __clz(sm & (0xFFFFFFFFu >> (31 - lane)));
+            const uint32_t lead = 31 - __clz(sm & (0xFFFFFFFFu >> (31 - lane)));
+            w.rlead[lane] = lead;
+            // the runs take the window slots in order; runs past the last slot use the hash
+            const uint32_t g = __popc(sm & ((1u << lane) - 1u));
+            if (start && g < (uint32_t)NSLOT) w.slot_rec[g] = lane;
+            const uint32_t myslot = __shfl_sync(0xffffffffu, g < (uint32_t)NSLOT ? g : NO_SLOT, lead);
+            w.rslot[lane] = myslot;
         }
         if (lane == 0) w.fail = 0;
         __syncwarp();
@@ -1315,10 +1333,11 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                 const uint32_t rr = chunk_owner(w, my_cnt != 0 && my_st - t0 < 32u, my_st - t0, carry_r);
                 const uint32_t r_st = __shfl_sync(0xffffffffu, my_st, rr);
                 uint32_t r = 0, C = 0, beg = 0, cnt = 0, csr = 0;   // csr: item source 0 table, 1 CSR, 2 delta records
-                uint32_t tr = 0;                                      // the record whose window takes the items
+                uint32_t tr = 0, ts = NO_SLOT;                        // the run's first record and window slot
                 if (t < total) {
                     r = rr;
                     tr = w.rlead[r];
+                    ts = w.rslot[r];
                     C = w.rC[r];
                     const uint32_t k = w.rbase[r] * EIDS + select_bit(w.rbits[r], t - r_st);
                     const uint2 *cr = d.rt.csr_row[C];
@@ -1346,7 +1365,8 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                 // one right-hand item: a CSR destination id (csr 1), a table element (0) or a
                 // delta record of row C[k] (2), ORed into its record's window or, outside it,
                 // the shared hash. Every lane calls this together (the hash needs the warp).
-                auto do_item = [&](bool valid, uint32_t o_r, uint32_t o_C, uint32_t o_csr, uint32_t item) {
+                auto do_item = [&](bool valid, uint32_t o_r, uint32_t o_s, uint32_t o_C, uint32_t o_csr,
+                                   uint32_t item) {
                     bool ok_i = false, pending = false;
                     uint32_t b2 = 0, ob = EMPTY, ckey = 0;
                     Bits ib;
@@ -1373,14 +1393,14 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                         const int dd = (int)b2 - (int)w.rbase[o_r] + WIN_LO;
                         // the statistic the window choice is keyed on: items beyond the narrow window
                         n_out += (unsigned)(dd - WIN_LO + grg::WIN_LO) >= (unsigned)grg::WIN;
-                        if ((unsigned)dd < (unsigned)WIN) {
+                        if ((unsigned)dd < (unsigned)WIN && o_s != NO_SLOT) {
                             if (ob != EMPTY) {
                                 // one destination id: one word of the window
-                                atomicOr(&w.win[o_r][dd][ob >> 5], 1u << (ob & 31));
+                                atomicOr(&w.win[o_s][dd][ob >> 5], 1u << (ob & 31));
                             } else {
 #pragma unroll
                                 for (int x = 0; x < EW; x++)
-                                    if (ib.w[x]) atomicOr(&w.win[o_r][dd][x], ib.w[x]);
+                                    if (ib.w[x]) atomicOr(&w.win[o_s][dd][x], ib.w[x]);
                             }
                         } else {
                             pending = true;
@@ -1397,7 +1417,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                     }
                 };
                 // first item of every task in the task's own lane: no search, no broadcast
-                do_item(cnt > 0, tr, C, csr, beg);
+                do_item(cnt > 0, tr, ts, C, csr, beg);
                 // the rest, flattened over the lanes
                 const uint32_t cnt1 = cnt ? cnt - 1 : 0;
                 uint32_t incl = cnt1;
@@ -1409,7 +1429,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                 const uint32_t nitems = __shfl_sync(0xffffffffu, incl, 31);
                 // per task: item f sits at beg + 1 + f - (first f of the task); record, label and source packed
                 const uint32_t adj = beg + 1 - (incl - cnt1);
-                const uint32_t pk = tr | (C << 8) | (csr << 16);
+                const uint32_t pk = tr | (C << 8) | (csr << 16) | (ts << 24);
                 const uint32_t s1 = incl - cnt1;             // the task's first flattened item
                 uint32_t carry_o = 0;
                 for (uint32_t f0 = 0; f0 < nitems; f0 += 32) {
@@ -1418,7 +1438,8 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                     const uint32_t lo = chunk_owner(w, cnt1 != 0 && s1 - f0 < 32u, s1 - f0, carry_o);
                     const uint32_t o_adj = __shfl_sync(0xffffffffu, adj, lo);
                     const uint32_t o_pk = __shfl_sync(0xffffffffu, pk, lo);
-                    do_item(f < nitems, o_pk & 0xFFu, (o_pk >> 8) & 0xFFu, o_pk >> 16, f + o_adj);
+                    do_item(f < nitems, o_pk & 0xFFu, o_pk >> 24, (o_pk >> 8) & 0xFFu, (o_pk >> 16) & 0xFFu,
+                            f + o_adj);
                 }
             }
             PH_MARK(2);
@@ -2801,9 +2822,9 @@ __global__ void k_tmark(unsigned long long *ctr, int t0_slot, int acc_slot, int 
 // Window of this closure's joins. Measured on dataflow, alias, points-to and
 // small alias jobs, the wide window was fastest or within 1.5% on every one, so
 // it is the default; the narrow window stays selectable. Wide is 10 elements
-// (4 below the record's base) at 5 blocks per SM: 44 KB of shared memory per
-// block; 12 elements fit only 4 blocks and were 1.5% slower on the dataflow
-// and alias closures, 8 elements (6 blocks) 11% slower.
+// (4 below the run's base); with 16 window slots a warp (one per run of a row's
+// records) a block takes 30 KB of shared memory and 80 registers a thread, so 6
+// blocks fit an SM.
 static void choose_window(grg_ctx *c)
 {
     c->join_wide = c->join_window_mode >= 2 ? c->tuned_wide : c->join_window_mode != 0;
