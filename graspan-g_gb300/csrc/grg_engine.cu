@@ -152,7 +152,7 @@ static void set_columns(RuleTable &rt, uint64_t tmask, int L)
 #define GRG_GATHER_GR 4           // delta records per thread per step of the gather's record pass
 #endif
 #ifndef GRG_JOIN_MINB_WIDE
-#define GRG_JOIN_MINB_WIDE 6
+#define GRG_JOIN_MINB_WIDE 7
 #endif
 #ifdef GRG_PHASE_TIMERS
 #define PH_MARK(i)                                   \
@@ -2823,8 +2823,11 @@ __global__ void k_tmark(unsigned long long *ctr, int t0_slot, int acc_slot, int 
 // small alias jobs, the wide window was fastest or within 1.5% on every one, so
 // it is the default; the narrow window stays selectable. Wide is 10 elements
 // (4 below the run's base); with 16 window slots a warp (one per run of a row's
-// records) a block takes 30 KB of shared memory and 80 registers a thread, so 6
-// blocks fit an SM.
+// records) a block takes 30 KB of shared memory, and at 72 registers a thread (a
+// few bytes spilled) 7 blocks fit an SM. Measured on one box: 16 slots at 7
+// blocks 54.4 ms for the 2M-vertex dataflow closure and 317 ms for the 1M alias
+// closure, at 6 blocks 54.6 / 323 ms, 32 slots (one per record) at 5 blocks
+// 66.3 / 334 ms, 12 slots at 7 blocks 53.3 / 328 ms.
 static void choose_window(grg_ctx *c)
 {
     c->join_wide = c->join_window_mode >= 2 ? c->tuned_wide : c->join_window_mode != 0;

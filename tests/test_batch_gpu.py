@@ -115,3 +115,19 @@ def test_refused_admission_leaves_the_batch_usable(grg_mod, oracle_mod):
         counts, h = b.result(k, jj.grammar)
         assert ([int(x) for x in counts], h) == alone(oracle_mod, jj)
     ctx.close()
+
+
+def test_admission_held_by_footprint_budget(grg_mod, oracle_mod):
+    """With a budget of two jobs' projected footprints, arrived jobs wait for memory:
+    the service admits at most what the budget holds (never more than one job beyond
+    it, the one admitted into an empty batch), holds the rest back, and every result
+    still equals the job closed alone."""
+    jobs = small_jobs(n=8, seed=37)
+    fps = sorted(serve.footprint_bytes(j) for j in jobs)
+    budget = fps[-1] + fps[-2]
+    res = serve.serve(jobs, max_vars=sum(j.num_vars for j in jobs), max_jobs=8, realtime=False,
+                      budget_bytes=budget, rounds_per_step=1)
+    assert res["held_by_budget"] > 0
+    assert res["peak_projected_bytes"] <= budget
+    for j in jobs:
+        assert (j.counts, j.hash) == tuple(alone(oracle_mod, j))
