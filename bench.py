@@ -537,6 +537,9 @@ def main():
                        {0: ", fixed", 1: ", measured in this step", 2: ", tuned (degree-key cache)"}[
                            int(s["window_tuned"])],
                        "join_items": "table elements" if s["join_elements"] else "destination ids",
+                       # per-phase join cycles (record load, unary, binary join, flush, retry list): only
+                       # in builds with -DGRG_PHASE_TIMERS
+                       "join_phase_cycles": s["join_phase_cycles"] if any(s["join_phase_cycles"]) else None,
                        "push_kernel": (("edges dealt over lanes" if s["push_flat"] else "one lane per record")
                                        if s["column_labels"] else None)},
             "e2e": {"value": world * total / (e2e_max * 1e-3), "unit": UNIT,
