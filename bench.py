@@ -454,8 +454,7 @@ def main():
         ctx.load_edges_device(w.num_vars, w.num_edges, d_src.data_ptr(), d_dst.data_ptr(), d_lab.data_ptr())
         return ctx.closure(w.filter_flag)
 
-    for _ in range(args.warmup):
-        step(False)
+    warm = [step(False) for _ in range(args.warmup)]
     # timed device-resident steps
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     stats = []
@@ -537,6 +536,9 @@ def main():
                        {0: ", fixed", 1: ", measured in this step", 2: ", tuned (degree-key cache)"}[
                            int(s["window_tuned"])],
                        "join_items": "table elements" if s["join_elements"] else "destination ids",
+                       # the first closure's trial passes (ms): windows [narrow, wide], item forms [ids, elements]
+                       "tuner_trials_ms": warm and {"window": [round(x, 3) for x in warm[0]["window_trial_ms"]],
+                                                    "items": [round(x, 3) for x in warm[0]["items_trial_ms"]]},
                        # per-phase join cycles (record load, unary, binary join, flush, retry list): only
                        # in builds with -DGRG_PHASE_TIMERS
                        "join_phase_cycles": s["join_phase_cycles"] if any(s["join_phase_cycles"]) else None,

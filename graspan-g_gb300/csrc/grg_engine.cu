@@ -618,6 +618,14 @@ struct __align__(16) WarpSmemT {
     uint32_t fail;                // records with a failed insert (retry after growth)
 };
 
+// One right-hand item of a join, loaded: ok (an occupied element or an id), its base,
+// the id within the element (EMPTY for an element) and the element's bits.
+struct Item {
+    bool ok;
+    uint32_t b2, ob;
+    Bits ib;
+};
+
 __device__ __forceinline__ uint32_t popc6(const Bits &b)
 {
     uint32_t c = 0;
@@ -1234,8 +1242,21 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
     for (int j = lane; j < NSLOT * WIN * EW; j += 32) (&w.win[0][0][0])[j] = 0;
     if (lane == 0) w.acc_n = 0;
     __syncwarp();
-    unsigned long long n_left = 0, n_right = 0, n_out = 0;
-    uint32_t inserts = 0;
+    // per-lane work counters, added into the device counters when one nears 2^30 and at the end
+    uint32_t n_left = 0, n_right = 0, n_out = 0, inserts = 0;
+    auto flush_counters = [&]() {
+        unsigned long long s[4] = {inserts, n_left, n_right, n_out};
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+            for (int o = 16; o; o >>= 1) s[i] += __shfl_xor_sync(0xffffffffu, s[i], o);
+        if (lane == 0) {
+            if (s[0]) atomicAdd(&d.ctr[C_INSERTS], s[0]);
+            if (s[1]) atomicAdd(&d.ctr[C_LEFT], s[1]);
+            if (s[2]) atomicAdd(&d.ctr[C_RIGHT], s[2]);
+            if (s[3]) atomicAdd(&d.ctr[C_WOUT], s[3]);
+        }
+        inserts = n_left = n_right = n_out = 0;
+    };
 #ifdef GRG_PHASE_TIMERS
     unsigned long long ph[5] = {0, 0, 0, 0, 0};
     long long ph_t = clock64();
@@ -1355,70 +1376,76 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                         n_right += rw.y >> 24;
                     } else {
                         const size_t ti = (size_t)(C - 1) * d.V + k;
+                        // a prefix-filled table: only slots [0, count) can be occupied. The
+                        // count of a label with such tables loads beside the descriptor.
+                        const bool pl = (d.prefix_mask >> (C - 1)) & 1ull;
                         const uint64_t de = __ldg(d.desc + ti);
+                        const uint32_t used = pl ? __ldcg(d.cnt + ti) : 0u;
                         beg = (uint32_t)de;
                         cnt = (uint32_t)(de >> 32);
-                        // a prefix-filled table: only slots [0, count) can be occupied
-                        if (prefix_table(d, C, cnt)) cnt = min(cnt, __ldcg(d.cnt + ti));
+                        if (pl && cnt <= PREFIX_CAP) cnt = min(cnt, used);
                     }
                 }
                 // one right-hand item: a CSR destination id (csr 1), a table element (0) or a
-                // delta record of row C[k] (2), ORed into its record's window or, outside it,
-                // the shared hash. Every lane calls this together (the hash needs the warp).
-                auto do_item = [&](bool valid, uint32_t o_r, uint32_t o_s, uint32_t o_C, uint32_t o_csr,
-                                   uint32_t item) {
-                    bool ok_i = false, pending = false;
-                    uint32_t b2 = 0, ob = EMPTY, ckey = 0;
-                    Bits ib;
+                // delta record of row C[k] (2). fetch loads it; put ORs it into its run's window
+                // or, outside the window, the shared hash (every lane calls put together: the
+                // hash needs the warp).
+                auto fetch = [&](bool valid, uint32_t o_C, uint32_t o_csr, uint32_t item, Item &it) {
+                    it.ok = false;
+                    it.b2 = 0;
+                    it.ob = EMPTY;
 #pragma unroll
-                    for (int x = 0; x < EW; x++) ib.w[x] = 0;
+                    for (int x = 0; x < EW; x++) it.ib.w[x] = 0;
                     if (valid) {
                         if (o_csr == 1) {
                             const uint32_t dst = __ldg(d.rt.csr_col[o_C] + item);
-                            b2 = dst / EIDS;
-                            ob = dst % EIDS;
-                            ok_i = true;
+                            it.b2 = dst / EIDS;
+                            it.ob = dst % EIDS;
+                            it.ok = true;
                         } else {
                             const uint4 *ep = o_csr == 2 ? d.drec + 2 * (size_t)item
                                                          : reinterpret_cast<const uint4 *>(d.elems + (size_t)item * 8);
                             const uint4 e0 = ep[0], e1 = ep[1];
-                            ok_i = e1.z != EMPTY;
-                            b2 = e1.z & BASE_MASK;
-                            ib.w[0] = e0.x; ib.w[1] = e0.y; ib.w[2] = e0.z; ib.w[3] = e0.w;
-                            ib.w[4] = e1.x; ib.w[5] = e1.y;
-                            n_right += ok_i ? 1 : 0;
+                            it.ok = e1.z != EMPTY;
+                            it.b2 = e1.z & BASE_MASK;
+                            it.ib.w[0] = e0.x; it.ib.w[1] = e0.y; it.ib.w[2] = e0.z; it.ib.w[3] = e0.w;
+                            it.ib.w[4] = e1.x; it.ib.w[5] = e1.y;
+                            n_right += it.ok ? 1 : 0;
                         }
                     }
-                    if (ok_i) {
-                        const int dd = (int)b2 - (int)w.rbase[o_r] + WIN_LO;
+                };
+                auto put = [&](Item &it, uint32_t o_r, uint32_t o_s) {
+                    bool pending = false;
+                    uint32_t ckey = 0;
+                    if (it.ok) {
+                        const int dd = (int)it.b2 - (int)w.rbase[o_r] + WIN_LO;
                         // the statistic the window choice is keyed on: items beyond the narrow window
                         n_out += (unsigned)(dd - WIN_LO + grg::WIN_LO) >= (unsigned)grg::WIN;
                         if ((unsigned)dd < (unsigned)WIN && o_s != NO_SLOT) {
-                            if (ob != EMPTY) {
+                            if (it.ob != EMPTY) {
                                 // one destination id: one word of the window
-                                atomicOr(&w.win[o_s][dd][ob >> 5], 1u << (ob & 31));
+                                atomicOr(&w.win[o_s][dd][it.ob >> 5], 1u << (it.ob & 31));
                             } else {
 #pragma unroll
                                 for (int x = 0; x < EW; x++)
-                                    if (ib.w[x]) atomicOr(&w.win[o_s][dd][x], ib.w[x]);
+                                    if (it.ib.w[x]) atomicOr(&w.win[o_s][dd][x], it.ib.w[x]);
                             }
                         } else {
                             pending = true;
-                            ckey = (o_r << KEY_SHIFT) | b2;
-                            if (ob != EMPTY) {
+                            ckey = (o_r << KEY_SHIFT) | it.b2;
+                            if (it.ob != EMPTY) {
 #pragma unroll
-                                for (int x = 0; x < EW; x++) ib.w[x] = (uint32_t)x == (ob >> 5) ? 1u << (ob & 31) : 0u;
+                                for (int x = 0; x < EW; x++)
+                                    it.ib.w[x] = (uint32_t)x == (it.ob >> 5) ? 1u << (it.ob & 31) : 0u;
                             }
                         }
                     }
                     while (__any_sync(0xffffffffu, pending)) {
-                        if (pending) pending = !acc_insert(w, ckey, ib);
+                        if (pending) pending = !acc_insert(w, ckey, it.ib);
                         if (__any_sync(0xffffffffu, pending)) acc_flush(d, w, inserts);
                     }
                 };
-                // first item of every task in the task's own lane: no search, no broadcast
-                do_item(cnt > 0, tr, ts, C, csr, beg);
-                // the rest, flattened over the lanes
+                // the rest of every task's items, flattened over the lanes
                 const uint32_t cnt1 = cnt ? cnt - 1 : 0;
                 uint32_t incl = cnt1;
 #pragma unroll
@@ -1432,14 +1459,21 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                 const uint32_t pk = tr | (C << 8) | (csr << 16) | (ts << 24);
                 const uint32_t s1 = incl - cnt1;             // the task's first flattened item
                 uint32_t carry_o = 0;
+                // first item of every task in the task's own lane (no search, no broadcast), then
+                // the flattened chunks. (Loading a chunk's items before ORing in the previous
+                // chunk's -- two loads in flight per lane -- measured no faster on the dataflow
+                // and alias closures, at 14 more registers a thread.)
+                Item it;
+                fetch(cnt > 0, C, csr, beg, it);
+                put(it, tr, ts);
                 for (uint32_t f0 = 0; f0 < nitems; f0 += 32) {
                     const uint32_t f = f0 + lane;
                     // owner lane: the last task whose items start at or before f
                     const uint32_t lo = chunk_owner(w, cnt1 != 0 && s1 - f0 < 32u, s1 - f0, carry_o);
                     const uint32_t o_adj = __shfl_sync(0xffffffffu, adj, lo);
                     const uint32_t o_pk = __shfl_sync(0xffffffffu, pk, lo);
-                    do_item(f < nitems, o_pk & 0xFFu, o_pk >> 24, (o_pk >> 8) & 0xFFu, (o_pk >> 16) & 0xFFu,
-                            f + o_adj);
+                    fetch(f < nitems, (o_pk >> 8) & 0xFFu, (o_pk >> 16) & 0xFFu, f + o_adj, it);
+                    put(it, o_pk & 0xFFu, o_pk >> 24);
                 }
             }
             PH_MARK(2);
@@ -1458,10 +1492,12 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
             p = __shfl_sync(0xffffffffu, p, __ffs(fm) - 1);
             const uint64_t o = p + __popc(fm & ((1u << lane) - 1u));
             if (failed && o < d.retry_cap) {
-                retry_out[2 * o] = make_uint4(rb.w[0], rb.w[1], rb.w[2], rb.w[3]);
-                retry_out[2 * o + 1] = make_uint4(rb.w[4], rb.w[5], key, row);
+                const uint32_t *rw = w.rbits[lane];
+                retry_out[2 * o] = make_uint4(rw[0], rw[1], rw[2], rw[3]);
+                retry_out[2 * o + 1] = make_uint4(rw[4], rw[5], key, row);
             }
         }
+        if (__any_sync(0xffffffffu, (n_left | n_right | n_out | inserts) >> 30)) flush_counters();
         __syncwarp();
         PH_MARK(4);
     }
@@ -1470,19 +1506,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
     if (lane == 0)
         for (int i = 0; i < 5; i++) atomicAdd(&d.ctr[C_PH0 + i], ph[i]);
 #endif
-    // per-warp work counters
-    for (int o = 16; o; o >>= 1) {
-        inserts += __shfl_xor_sync(0xffffffffu, inserts, o);
-        n_left += __shfl_xor_sync(0xffffffffu, n_left, o);
-        n_right += __shfl_xor_sync(0xffffffffu, n_right, o);
-        n_out += __shfl_xor_sync(0xffffffffu, n_out, o);
-    }
-    if (lane == 0) {
-        if (n_left) atomicAdd(&d.ctr[C_LEFT], n_left);
-        if (n_right) atomicAdd(&d.ctr[C_RIGHT], n_right);
-        if (n_out) atomicAdd(&d.ctr[C_WOUT], n_out);
-        if (inserts) atomicAdd(&d.ctr[C_INSERTS], (unsigned long long)inserts);
-    }
+    flush_counters();
 }
 
 // Tables of labels 1..L by log2 of their occupied elements (buckets 0..7, the
@@ -2511,7 +2535,9 @@ int grg_transfer_rules(grg_ctx *c, int num_rules, const int *rules, int num_labe
     memcpy(c->rules, rules, sizeof(int) * 3 * (size_t)num_rules);
     // prefix-filled small tables for the labels joins read as table rows: a binary
     // rule's derivable second symbol (delta-left items) and that rule's first
-    // symbol (old-left virtual records scan its rows)
+    // symbol (old-left virtual records scan its rows). A static second symbol's
+    // tables are compacted after the load (k_compact_static), so their rows hold
+    // no empty slots either.
     bool der[GRG_MAX_LABELS + 1] = {false};
     for (int q = 0; q < num_rules; q++) der[rules[3 * q]] = true;
     c->prefix_mask = 0;
@@ -2923,6 +2949,11 @@ struct JoinChoice { bool wide, elems; };
 static std::map<uint64_t, JoinChoice> g_tune_cache;    // degree key -> the faster window and item form
 static std::map<uint64_t, bool> g_push_cache;          // degree key -> flattened push faster
 constexpr uint64_t TUNE_MIN_RECORDS = 1u << 16;        // smaller first rounds are not timed
+// The narrow window replaces the wide default only when the wide trial pass takes at least
+// this long: the 1M-vertex alias closure's trials take ~26 us each, where the two windows
+// swap places by more than the 10% margin from run to run, and the narrow window then
+// costs ~11% over the closure
+constexpr float TUNE_WINDOW_MIN_MS = 0.25f;
 
 static int degree_key(grg_ctx *c, uint32_t filter, uint64_t *key)
 {
@@ -3047,7 +3078,7 @@ static int tune_first_pass(grg_ctx *c, const Dev &d, uint64_t nd, uint64_t nv, u
     bool wide_of[2];
     float t_of[2];
     for (int e = 0; e < 2; e++) {
-        wide_of[e] = tw ? !(best[0][e] < 0.9f * best[1][e]) : fix_wide;
+        wide_of[e] = tw ? !(best[0][e] < 0.9f * best[1][e] && best[1][e] >= TUNE_WINDOW_MIN_MS) : fix_wide;
         t_of[e] = best[wide_of[e] ? 1 : 0][e];
     }
     const bool elems = ti ? t_of[1] < t_of[0] : fix_elems;
