@@ -54,6 +54,11 @@ def _stale(target, deps):
 
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
+    # objects built with other GRG_NVCC_DEFS overrides are stale too
+    defs_file = os.path.join(OUT, "nvcc_defs.txt")
+    defs = " ".join(NVCC_FLAGS)
+    if not os.path.exists(defs_file) or open(defs_file).read() != defs:
+        force = True
     nvcc = _nvcc()
     headers = [os.path.join(INC, "grg.h")] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     jobs = []
@@ -80,6 +85,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
     comp_src = os.path.join(CSRC, "comp.cpp")
     if os.path.exists(comp_src) and (force or _stale(COMP, [comp_src, LIB] + headers)):
         _run(["g++"] + CXX_FLAGS + [comp_src, "-o", COMP, "-L", OUT, "-lgrg", "-Wl,-rpath,$ORIGIN"])
+    with open(defs_file, "w") as f:
+        f.write(defs)
     return LIB
 
 

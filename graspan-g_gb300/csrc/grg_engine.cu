@@ -1460,9 +1460,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                 const uint32_t s1 = incl - cnt1;             // the task's first flattened item
                 uint32_t carry_o = 0;
                 // first item of every task in the task's own lane (no search, no broadcast), then
-                // the flattened chunks. (Loading a chunk's items before ORing in the previous
-                // chunk's -- two loads in flight per lane -- measured no faster on the dataflow
-                // and alias closures, at 14 more registers a thread.)
+                // the flattened chunks
                 Item it;
                 fetch(cnt > 0, C, csr, beg, it);
                 put(it, tr, ts);
