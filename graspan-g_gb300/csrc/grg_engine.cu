@@ -151,6 +151,9 @@ static void set_columns(RuleTable &rt, uint64_t tmask, int L)
 #ifndef GRG_GATHER_GR
 #define GRG_GATHER_GR 4           // delta records per thread per step of the gather's record pass
 #endif
+#ifndef GRG_PREFETCH
+#define GRG_PREFETCH 0            // join prefetches: 1 rows' descriptors one chunk of tasks ahead, 2 items one chunk ahead
+#endif
 #ifndef GRG_JOIN_MINB_WIDE
 #define GRG_JOIN_MINB_WIDE 7
 #endif
@@ -617,6 +620,16 @@ struct __align__(16) WarpSmemT {
     uint32_t acc_n;
     uint32_t fail;                // records with a failed insert (retry after growth)
 };
+
+// Prefetch hints (no register holds the value): a later load of the line finds it in L1 / L2.
+__device__ __forceinline__ void prefetch_l1(const void *p)
+{
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(__cvta_generic_to_global(p)));
+}
+__device__ __forceinline__ void prefetch_l2(const void *p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(p)));
+}
 
 // One right-hand item of a join, loaded: ok (an occupied element or an id), its base,
 // the id within the element (EMPTY for an element) and the element's bits.
@@ -1346,13 +1359,42 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
             const uint32_t total = warp_tasks(w, my_cnt);
             const uint32_t my_st = w.kpre[lane];
             uint32_t carry_r = 0;
+            // task (record r, intermediate k) -> items of row C[k]. The record of task t is the
+            // last record that starts at or before t: records starting in a chunk of 32 tasks
+            // mark their start position, a lane takes the highest mark at or below it
+            auto task_of = [&](uint32_t tq, uint32_t &rq, uint32_t &kq) {
+                rq = chunk_owner(w, my_cnt != 0 && my_st - tq < 32u, my_st - tq, carry_r);
+                const uint32_t r_st = __shfl_sync(0xffffffffu, my_st, rq);
+                kq = tq + lane < total ? w.rbase[rq] * EIDS + select_bit(w.rbits[rq], tq + lane - r_st) : 0u;
+            };
+#if GRG_PREFETCH & 1
+            // each chunk's tasks are found one chunk ahead and the first line their rows'
+            // descriptors (or CSR rows, or delta-index entries) sit in is prefetched
+            auto prefetch_task = [&](uint32_t tq, uint32_t rq, uint32_t kq) {
+                if (tq + lane >= total) return;
+                const uint32_t Cq = w.rC[rq];
+                const size_t ti = (size_t)(Cq - 1) * d.V + kq;
+                if (w.rOff[rq]) {
+                    prefetch_l1(d.drs + ti);
+                } else if (d.rt.csr_row[Cq]) {
+                    prefetch_l1(d.rt.csr_row[Cq] + kq);
+                } else {
+                    prefetch_l1(d.desc + ti);
+                    if ((d.prefix_mask >> (Cq - 1)) & 1ull) prefetch_l2(d.cnt + ti);
+                }
+            };
+            uint32_t next_r, next_k;
+            task_of(0, next_r, next_k);
+#endif
             for (uint32_t t0 = 0; t0 < total; t0 += 32) {
-                // task (record r, intermediate k) -> items of row C[k]. The record of task t
-                // is the last record that starts at or before t: records starting in this
-                // chunk mark their start position, a lane takes the highest mark at or below it
                 const uint32_t t = t0 + lane;
-                const uint32_t rr = chunk_owner(w, my_cnt != 0 && my_st - t0 < 32u, my_st - t0, carry_r);
-                const uint32_t r_st = __shfl_sync(0xffffffffu, my_st, rr);
+                uint32_t rr, k;
+#if GRG_PREFETCH & 1
+                rr = next_r;
+                k = next_k;
+#else
+                task_of(t0, rr, k);
+#endif
                 uint32_t r = 0, C = 0, beg = 0, cnt = 0, csr = 0;   // csr: item source 0 table, 1 CSR, 2 delta records
                 uint32_t tr = 0, ts = NO_SLOT;                        // the run's first record and window slot
                 if (t < total) {
@@ -1360,7 +1402,6 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                     tr = w.rlead[r];
                     ts = w.rslot[r];
                     C = w.rC[r];
-                    const uint32_t k = w.rbase[r] * EIDS + select_bit(w.rbits[r], t - r_st);
                     const uint2 *cr = d.rt.csr_row[C];
                     if (w.rOff[r]) {
                         const size_t ti = (size_t)(C - 1) * d.V + k;
@@ -1386,6 +1427,12 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                         if (pl && cnt <= PREFIX_CAP) cnt = min(cnt, used);
                     }
                 }
+#if GRG_PREFETCH & 1
+                if (t0 + 32 < total) {
+                    task_of(t0 + 32, next_r, next_k);
+                    prefetch_task(t0 + 32, next_r, next_k);
+                }
+#endif
                 // one right-hand item: a CSR destination id (csr 1), a table element (0) or a
                 // delta record of row C[k] (2). fetch loads it; put ORs it into its run's window
                 // or, outside the window, the shared hash (every lane calls put together: the
@@ -1461,15 +1508,43 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                 uint32_t carry_o = 0;
                 // first item of every task in the task's own lane (no search, no broadcast), then
                 // the flattened chunks
+                // owner lane of flattened item f: the last task whose items start at or before f
+                auto item_owner = [&](uint32_t fq, uint32_t &o_adj, uint32_t &o_pk) {
+                    const uint32_t lo = chunk_owner(w, cnt1 != 0 && s1 - fq < 32u, s1 - fq, carry_o);
+                    o_adj = __shfl_sync(0xffffffffu, adj, lo);
+                    o_pk = __shfl_sync(0xffffffffu, pk, lo);
+                };
+#if GRG_PREFETCH & 2
+                // each chunk's items are found one chunk ahead and prefetched into L1
+                auto prefetch_item = [&](uint32_t f, uint32_t o_adj, uint32_t o_pk) {
+                    if (f >= nitems) return;
+                    const uint32_t o_C = (o_pk >> 8) & 0xFFu, o_csr = (o_pk >> 16) & 0xFFu, item = f + o_adj;
+                    if (o_csr == 1) prefetch_l1(d.rt.csr_col[o_C] + item);
+                    else if (o_csr == 2) prefetch_l1(d.drec + 2 * (size_t)item);
+                    else prefetch_l1(d.elems + (size_t)item * 8);
+                };
+                uint32_t n_adj = 0, n_pk = 0;
+                if (nitems) {
+                    item_owner(0, n_adj, n_pk);
+                    prefetch_item(lane, n_adj, n_pk);
+                }
+#endif
                 Item it;
                 fetch(cnt > 0, C, csr, beg, it);
                 put(it, tr, ts);
                 for (uint32_t f0 = 0; f0 < nitems; f0 += 32) {
                     const uint32_t f = f0 + lane;
-                    // owner lane: the last task whose items start at or before f
-                    const uint32_t lo = chunk_owner(w, cnt1 != 0 && s1 - f0 < 32u, s1 - f0, carry_o);
-                    const uint32_t o_adj = __shfl_sync(0xffffffffu, adj, lo);
-                    const uint32_t o_pk = __shfl_sync(0xffffffffu, pk, lo);
+                    uint32_t o_adj, o_pk;
+#if GRG_PREFETCH & 2
+                    o_adj = n_adj;
+                    o_pk = n_pk;
+                    if (f0 + 32 < nitems) {
+                        item_owner(f0 + 32, n_adj, n_pk);
+                        prefetch_item(f + 32, n_adj, n_pk);
+                    }
+#else
+                    item_owner(f0, o_adj, o_pk);
+#endif
                     fetch(f < nitems, (o_pk >> 8) & 0xFFu, (o_pk >> 16) & 0xFFu, f + o_adj, it);
                     put(it, o_pk & 0xFFu, o_pk >> 24);
                 }
