@@ -1510,8 +1510,6 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                     uint32_t ckey = 0;
                     if (it.ok) {
                         const int dd = (int)it.b2 - (int)w.rbase[o_r] + WIN_LO;
-                        // the statistic the window choice is keyed on: items beyond the narrow window
-                        n_out += (unsigned)(dd - WIN_LO + grg::WIN_LO) >= (unsigned)grg::WIN;
                         if ((unsigned)dd < (unsigned)WIN && o_s != NO_SLOT) {
                             if (it.ob != EMPTY) {
                                 // one destination id: one word of the window
@@ -1523,6 +1521,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                             }
                         } else {
                             pending = true;
+                            n_out++;                   // an item the dense windows could not hold
                             ckey = (o_r << KEY_SHIFT) | it.b2;
                             if (it.ob != EMPTY) {
 #pragma unroll

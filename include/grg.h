@@ -69,8 +69,9 @@ typedef struct grg_stats {
     uint64_t join_phase_cycles[5]; /* join-kernel cycles per phase (record load, unary,
                                       binary join, flush, retry list) when built with
                                       -DGRG_PHASE_TIMERS; 0 otherwise */
-    uint64_t window_out_elems;     /* right elements beyond the narrow join window (the
-                                      statistic the window choice is keyed on) */
+    uint64_t window_out_elems;     /* right-hand items the join ORed into its hash
+                                      accumulator: beyond the record's dense window, or of a
+                                      run of records left without a window slot */
     uint64_t wide_window;          /* 1 = the closure ended on the wide join window */
     double gather_ms;              /* time of the rounds' gathers (when kernel timing is on) */
     uint64_t window_tuned;         /* how the join window was chosen: 0 fixed by grg_set_join_window,
