@@ -154,9 +154,6 @@ static void set_columns(RuleTable &rt, uint64_t tmask, int L)
 #ifndef GRG_SELECT
 #define GRG_SELECT 0              // task -> bit: 0 word-by-word search, 1 packed prefix counts, 2 the same with fns
 #endif
-#ifndef GRG_PREFETCH
-#define GRG_PREFETCH 0            // join prefetches: 1 rows' descriptors one chunk of tasks ahead, 2 items one chunk ahead
-#endif
 #ifndef GRG_JOIN_MINB_WIDE
 #define GRG_JOIN_MINB_WIDE 7
 #endif
@@ -617,25 +614,16 @@ struct __align__(16) WarpSmemT {
     uint32_t rrow[RB];
     uint32_t rbase[RB];
     uint32_t rA[RB];              // per record: output label of the current rule pass
-    uint32_t rC[RB];              // per record: right operand label
-    uint32_t rOff[RB];            // per record: 1 = virtual old-left record
-    uint32_t rlead[RB];           // per record: the first record of its run with the same row and label
-    uint32_t rslot[RB];           // per record: its run's window slot (NO_SLOT: the hash only)
+    uint32_t rpk[RB];             // per record, packed: the first record of its run with the same row
+                                  // and label (bits 0-7), the current rule's right operand label
+                                  // (8-15), where that label's rows come from (16-23: 0 tables, 1 CSR
+                                  // copy, 2 delta records of a virtual old-left record) and the
+                                  // run's window slot (24-31, NO_SLOT: the hash only)
     uint32_t kpre[RB + 1];        // exclusive prefix of per-record task counts
     uint8_t own[32];              // per chunk of 32 tasks (items): lane whose record (task) starts there
     uint32_t acc_n;
     uint32_t fail;                // records with a failed insert (retry after growth)
 };
-
-// Prefetch hints (no register holds the value): a later load of the line finds it in L1 / L2.
-__device__ __forceinline__ void prefetch_l1(const void *p)
-{
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(__cvta_generic_to_global(p)));
-}
-__device__ __forceinline__ void prefetch_l2(const void *p)
-{
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(p)));
-}
 
 // One right-hand item of a join, loaded: ok (an occupied element or an id), its base,
 // the id within the element (EMPTY for an element) and the element's bits.
@@ -1351,12 +1339,11 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
             const bool start = lane == 0 || !have || B == 0 || prow != row || pB != B;
             const unsigned sm = __ballot_sync(0xffffffffu, start);
             const uint32_t lead = 31 - __clz(sm & (0xFFFFFFFFu >> (31 - lane)));
-            w.rlead[lane] = lead;
             // the runs take the window slots in order; runs past the last slot use the hash
             const uint32_t g = __popc(sm & ((1u << lane) - 1u));
             if (start && g < (uint32_t)NSLOT) w.slot_rec[g] = lane;
             const uint32_t myslot = __shfl_sync(0xffffffffu, g < (uint32_t)NSLOT ? g : NO_SLOT, lead);
-            w.rslot[lane] = myslot;
+            w.rpk[lane] = lead | (myslot << 24);
         }
         if (lane == 0) w.fail = 0;
         __syncwarp();
@@ -1388,12 +1375,15 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
         const uint32_t qv = virt ? B - OL_SLOT0 : 0;
         const uint32_t nbr = virt ? 1 : real ? d.rt.bin_start[B + 1] - d.rt.bin_start[B] : 0;
         const uint32_t maxb = __reduce_max_sync(0xffffffffu, nbr);
-        w.rOff[lane] = virt;
         for (uint32_t rho = 0; rho < maxb; rho++) {
             const bool hr = rho < nbr;
             const uint32_t q = virt ? qv : d.rt.bin_start[B] + rho;
             w.rA[lane] = !hr ? 0 : virt ? d.rt.ol_A[q] : d.rt.bin_A[q];
-            w.rC[lane] = !hr ? 0 : virt ? d.rt.ol_C[q] : d.rt.bin_C[q];
+            {
+                const uint32_t Cr = !hr ? 0 : virt ? d.rt.ol_C[q] : d.rt.bin_C[q];
+                const uint32_t src = virt ? 2u : (hr && d.rt.csr_row[Cr]) ? 1u : 0u;
+                w.rpk[lane] = (w.rpk[lane] & 0xFF0000FFu) | (Cr << 8) | (src << 16);
+            }
             n_left += hr;
             const uint32_t my_cnt = hr ? nbits : 0;
             const uint32_t total = warp_tasks(w, my_cnt);
@@ -1411,51 +1401,23 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                 kq = tq + lane < total ? w.rbase[rq] * EIDS + select_bit(w.rbits[rq], tq + lane - r_st) : 0u;
 #endif
             };
-#if GRG_PREFETCH & 1
-            // each chunk's tasks are found one chunk ahead and the first line their rows'
-            // descriptors (or CSR rows, or delta-index entries) sit in is prefetched
-            auto prefetch_task = [&](uint32_t tq, uint32_t rq, uint32_t kq) {
-                if (tq + lane >= total) return;
-                const uint32_t Cq = w.rC[rq];
-                const size_t ti = (size_t)(Cq - 1) * d.V + kq;
-                if (w.rOff[rq]) {
-                    prefetch_l1(d.drs + ti);
-                } else if (d.rt.csr_row[Cq]) {
-                    prefetch_l1(d.rt.csr_row[Cq] + kq);
-                } else {
-                    prefetch_l1(d.desc + ti);
-                    if ((d.prefix_mask >> (Cq - 1)) & 1ull) prefetch_l2(d.cnt + ti);
-                }
-            };
-            uint32_t next_r, next_k;
-            task_of(0, next_r, next_k);
-#endif
             for (uint32_t t0 = 0; t0 < total; t0 += 32) {
                 const uint32_t t = t0 + lane;
                 uint32_t rr, k;
-#if GRG_PREFETCH & 1
-                rr = next_r;
-                k = next_k;
-#else
                 task_of(t0, rr, k);
-#endif
-                uint32_t r = 0, C = 0, beg = 0, cnt = 0, csr = 0;   // csr: item source 0 table, 1 CSR, 2 delta records
-                uint32_t tr = 0, ts = NO_SLOT;                        // the run's first record and window slot
+                // the task's record, packed: its run's first record tr, right label C, item
+                // source csr (0 table, 1 CSR, 2 delta records) and run window slot ts
+                const uint32_t pk = t < total ? w.rpk[rr] : 0u;
+                const uint32_t tr = pk & 0xFFu, C = (pk >> 8) & 0xFFu, csr = (pk >> 16) & 0xFFu, ts = pk >> 24;
+                uint32_t beg = 0, cnt = 0;
                 if (t < total) {
-                    r = rr;
-                    tr = w.rlead[r];
-                    ts = w.rslot[r];
-                    C = w.rC[r];
-                    const uint2 *cr = d.rt.csr_row[C];
-                    if (w.rOff[r]) {
+                    if (csr == 2) {
                         const size_t ti = (size_t)(C - 1) * d.V + k;
                         const uint32_t s0 = __ldg(d.drs + ti);
-                        csr = 2;
                         beg = s0;
                         cnt = s0 == EMPTY ? 0 : __ldg(d.drc + ti);
-                    } else if (cr) {
-                        const uint2 rw = __ldg(cr + k);
-                        csr = 1;
+                    } else if (csr == 1) {
+                        const uint2 rw = __ldg(d.rt.csr_row[C] + k);
                         beg = rw.x;
                         cnt = rw.y & 0xFFFFFFu;
                         n_right += rw.y >> 24;
@@ -1471,12 +1433,6 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                         if (pl && cnt <= PREFIX_CAP) cnt = min(cnt, used);
                     }
                 }
-#if GRG_PREFETCH & 1
-                if (t0 + 32 < total) {
-                    task_of(t0 + 32, next_r, next_k);
-                    prefetch_task(t0 + 32, next_r, next_k);
-                }
-#endif
                 // one right-hand item: a CSR destination id (csr 1), a table element (0) or a
                 // delta record of row C[k] (2). fetch loads it; put ORs it into its run's window
                 // or, outside the window, the shared hash (every lane calls put together: the
@@ -1546,7 +1502,6 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                 const uint32_t nitems = __shfl_sync(0xffffffffu, incl, 31);
                 // per task: item f sits at beg + 1 + f - (first f of the task); record, label and source packed
                 const uint32_t adj = beg + 1 - (incl - cnt1);
-                const uint32_t pk = tr | (C << 8) | (csr << 16) | (ts << 24);
                 const uint32_t s1 = incl - cnt1;             // the task's first flattened item
                 uint32_t carry_o = 0;
                 // first item of every task in the task's own lane (no search, no broadcast), then
@@ -1557,37 +1512,13 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                     o_adj = __shfl_sync(0xffffffffu, adj, lo);
                     o_pk = __shfl_sync(0xffffffffu, pk, lo);
                 };
-#if GRG_PREFETCH & 2
-                // each chunk's items are found one chunk ahead and prefetched into L1
-                auto prefetch_item = [&](uint32_t f, uint32_t o_adj, uint32_t o_pk) {
-                    if (f >= nitems) return;
-                    const uint32_t o_C = (o_pk >> 8) & 0xFFu, o_csr = (o_pk >> 16) & 0xFFu, item = f + o_adj;
-                    if (o_csr == 1) prefetch_l1(d.rt.csr_col[o_C] + item);
-                    else if (o_csr == 2) prefetch_l1(d.drec + 2 * (size_t)item);
-                    else prefetch_l1(d.elems + (size_t)item * 8);
-                };
-                uint32_t n_adj = 0, n_pk = 0;
-                if (nitems) {
-                    item_owner(0, n_adj, n_pk);
-                    prefetch_item(lane, n_adj, n_pk);
-                }
-#endif
                 Item it;
                 fetch(cnt > 0, C, csr, beg, it);
                 put(it, tr, ts);
                 for (uint32_t f0 = 0; f0 < nitems; f0 += 32) {
                     const uint32_t f = f0 + lane;
                     uint32_t o_adj, o_pk;
-#if GRG_PREFETCH & 2
-                    o_adj = n_adj;
-                    o_pk = n_pk;
-                    if (f0 + 32 < nitems) {
-                        item_owner(f0 + 32, n_adj, n_pk);
-                        prefetch_item(f + 32, n_adj, n_pk);
-                    }
-#else
                     item_owner(f0, o_adj, o_pk);
-#endif
                     fetch(f < nitems, (o_pk >> 8) & 0xFFu, (o_pk >> 16) & 0xFFu, f + o_adj, it);
                     put(it, o_pk & 0xFFu, o_pk >> 24);
                 }
@@ -1600,7 +1531,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
 
         __syncwarp();
         // a failed insert of a run's merged window re-runs every record of the run
-        const bool failed = have && (!ok || ((w.fail >> w.rlead[lane]) & 1u));
+        const bool failed = have && (!ok || ((w.fail >> (w.rpk[lane] & 0xFFu)) & 1u));
         const unsigned fm = __ballot_sync(0xffffffffu, failed);
         if (fm) {
             unsigned long long p = 0;
