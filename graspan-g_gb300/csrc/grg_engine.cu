@@ -151,9 +151,6 @@ static void set_columns(RuleTable &rt, uint64_t tmask, int L)
 #ifndef GRG_GATHER_GR
 #define GRG_GATHER_GR 4           // delta records per thread per step of the gather's record pass
 #endif
-#ifndef GRG_SELECT
-#define GRG_SELECT 0              // task -> bit: 0 word-by-word search, 1 packed prefix counts, 2 the same with fns
-#endif
 #ifndef GRG_JOIN_MINB_WIDE
 #define GRG_JOIN_MINB_WIDE 7
 #endif
@@ -608,9 +605,6 @@ struct __align__(16) WarpSmemT {
     uint32_t acc_bits[ACC][EW];   // hash accumulator: OR of candidate bitmaps
     uint32_t acc_key[ACC];        // key = record << 25 | base (EMPTY = free)
     uint32_t rbits[RB][EW];       // the batch's delta records
-#if GRG_SELECT
-    uint32_t rpre[RB][2];         // per record: set bits before words 1..4 (bytes) and before word 5
-#endif
     uint32_t rrow[RB];
     uint32_t rbase[RB];
     uint32_t rA[RB];              // per record: output label of the current rule pass
@@ -655,32 +649,6 @@ __device__ __forceinline__ uint32_t select_bit(const uint32_t *bits, uint32_t id
     }
     return pos + select32(wsel, idx);
 }
-
-#if GRG_SELECT
-// Position of the idx-th set bit of record r's bitmap, from its packed per-word prefix counts:
-// a two-level search for the word, then the bit within it.
-template <class WS>
-__device__ __forceinline__ uint32_t select_rec(const WS &w, uint32_t r, uint32_t idx)
-{
-    const uint32_t p = w.rpre[r][0];
-    uint32_t x, before;
-    if (idx >= ((p >> 16) & 0xFFu)) {
-        const uint32_t c3 = p >> 24, c4 = w.rpre[r][1];
-        x = idx >= c3 ? (idx >= c4 ? 5u : 4u) : 3u;
-        before = idx >= c3 ? (idx >= c4 ? c4 : c3) : (p >> 16) & 0xFFu;
-    } else {
-        const uint32_t c0 = p & 0xFFu, c1 = (p >> 8) & 0xFFu;
-        x = idx >= c0 ? (idx >= c1 ? 2u : 1u) : 0u;
-        before = idx >= c0 ? (idx >= c1 ? c1 : c0) : 0u;
-    }
-    const uint32_t wd = w.rbits[r][x];
-#if GRG_SELECT == 2
-    return x * 32 + __fns(wd, 0, (int)(idx - before) + 1);
-#else
-    return x * 32 + select32(wd, idx - before);
-#endif
-}
-#endif
 
 // Exclusive warp prefix of per-lane task counts into kpre[0..RB]; returns the total.
 template <class WS>
@@ -1321,14 +1289,6 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                        base = key & BASE_MASK;
 #pragma unroll
         for (int x = 0; x < EW; x++) w.rbits[lane][x] = rb.w[x];
-#if GRG_SELECT
-        {
-            const uint32_t c0 = __popc(rb.w[0]), c1 = c0 + __popc(rb.w[1]), c2 = c1 + __popc(rb.w[2]),
-                           c3 = c2 + __popc(rb.w[3]);
-            w.rpre[lane][0] = c0 | (c1 << 8) | (c2 << 16) | (c3 << 24);
-            w.rpre[lane][1] = c3 + __popc(rb.w[4]);
-        }
-#endif
         w.rrow[lane] = row;
         w.rbase[lane] = base;
         // a row's records of one label are contiguous (a table's slots are, and the gather
@@ -1395,11 +1355,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
             auto task_of = [&](uint32_t tq, uint32_t &rq, uint32_t &kq) {
                 rq = chunk_owner(w, my_cnt != 0 && my_st - tq < 32u, my_st - tq, carry_r);
                 const uint32_t r_st = __shfl_sync(0xffffffffu, my_st, rq);
-#if GRG_SELECT
-                kq = tq + lane < total ? w.rbase[rq] * EIDS + select_rec(w, rq, tq + lane - r_st) : 0u;
-#else
                 kq = tq + lane < total ? w.rbase[rq] * EIDS + select_bit(w.rbits[rq], tq + lane - r_st) : 0u;
-#endif
             };
             for (uint32_t t0 = 0; t0 < total; t0 += 32) {
                 const uint32_t t = t0 + lane;
