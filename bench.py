@@ -536,6 +536,10 @@ def main():
                        {0: ", fixed", 1: ", measured in this step", 2: ", tuned (degree-key cache)"}[
                            int(s["window_tuned"])],
                        "join_items": "table elements" if s["join_elements"] else "destination ids",
+                       # one closure's join work: (record, rule) pairs, right-hand elements read, the
+                       # items ORed into the hash accumulator instead of a dense window, new elements
+                       "join_work": {"left_records": s["left_elems"], "right_elems": s["right_elems"],
+                                     "hash_items": s["window_out_elems"], "out_elems": s["out_elems"]},
                        # the first closure's trial passes (ms): windows [narrow, wide], item forms [ids, elements]
                        "tuner_trials_ms": warm and {"window": [round(x, 3) for x in warm[0]["window_trial_ms"]],
                                                     "items": [round(x, 3) for x in warm[0]["items_trial_ms"]]},
