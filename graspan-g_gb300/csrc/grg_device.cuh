@@ -71,7 +71,8 @@ enum : int {
     C_DH0 = C_LABEL0 + MAX_SLOTS + 11,   // 8 counters: tables by log2 of their elements (tuning key)
     C_CHECK = C_LABEL0 + MAX_SLOTS + 19, // first failed bounds check of the push kernels: id << 56 | value
     C_JQ = C_LABEL0 + MAX_SLOTS + 20,    // work queue of a join or push launch: next 32-record batch (zeroed before each launch)
-    NCTR = C_LABEL0 + MAX_SLOTS + 21
+    C_NOSLOT = C_LABEL0 + MAX_SLOTS + 21, // of C_WOUT: items of a run of records left without a window slot
+    NCTR = C_LABEL0 + MAX_SLOTS + 22
 };
 // error bits of C_ERR; ERR_IN_* (in C_BADIN) flag input edges that were refused
 // (label outside 1..L, vertex id outside the graph) and never touched a table

@@ -1326,19 +1326,20 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
     if (lane == 0) w.acc_n = 0;
     __syncwarp();
     // per-lane work counters, added into the device counters when one nears 2^30 and at the end
-    uint32_t n_left = 0, n_right = 0, n_out = 0, inserts = 0;
+    uint32_t n_left = 0, n_right = 0, n_out = 0, n_noslot = 0, inserts = 0;
     auto flush_counters = [&]() {
-        unsigned long long s[4] = {inserts, n_left, n_right, n_out};
+        unsigned long long s[5] = {inserts, n_left, n_right, n_out, n_noslot};
 #pragma unroll
-        for (int i = 0; i < 4; i++)
+        for (int i = 0; i < 5; i++)
             for (int o = 16; o; o >>= 1) s[i] += __shfl_xor_sync(0xffffffffu, s[i], o);
         if (lane == 0) {
             if (s[0]) atomicAdd(&d.ctr[C_INSERTS], s[0]);
             if (s[1]) atomicAdd(&d.ctr[C_LEFT], s[1]);
             if (s[2]) atomicAdd(&d.ctr[C_RIGHT], s[2]);
             if (s[3]) atomicAdd(&d.ctr[C_WOUT], s[3]);
+            if (s[4]) atomicAdd(&d.ctr[C_NOSLOT], s[4]);
         }
-        inserts = n_left = n_right = n_out = 0;
+        inserts = n_left = n_right = n_out = n_noslot = 0;
     };
 #ifdef GRG_PHASE_TIMERS
     unsigned long long ph[5] = {0, 0, 0, 0, 0};
@@ -1516,6 +1517,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                         } else {
                             pending = true;
                             n_out++;                   // an item the dense windows could not hold
+                            n_noslot += o_s == NO_SLOT;
                             ckey = (o_r << KEY_SHIFT) | it.b2;
                             if (it.ob != EMPTY) {
 #pragma unroll
@@ -3118,9 +3120,9 @@ static int tune_first_pass(grg_ctx *c, const Dev &d, uint64_t nd, uint64_t nv, u
     if (!c->ev_t1) GRG_CUDA(c, cudaEventCreate(&c->ev_t1));
     int st = read_ctr(c);
     if (st) return st;
-    const int kept[4] = {C_LEFT, C_RIGHT, C_WOUT, C_INSERTS};
-    unsigned long long keep[4];
-    for (int i = 0; i < 4; i++) keep[i] = c->h_ctr[kept[i]];
+    const int kept[5] = {C_LEFT, C_RIGHT, C_WOUT, C_NOSLOT, C_INSERTS};
+    unsigned long long keep[5];
+    for (int i = 0; i < 5; i++) keep[i] = c->h_ctr[kept[i]];
     const uint64_t nt = std::min(nd, std::max<uint64_t>(TUNE_MIN_RECORDS, nd / 8));
     const int grid = grid_for(c, (nt + RB - 1) / RB, JOIN_WARPS, 16);
     // the choices open in this closure: windows unless fixed, item forms unless fixed or no
@@ -3148,7 +3150,7 @@ static int tune_first_pass(grg_ctx *c, const Dev &d, uint64_t nd, uint64_t nv, u
                 best[w][e] = std::min(best[w][e], ms);
             }
     // the statistics count the round's own pass only
-    for (int i = 0; i < 4; i++) {
+    for (int i = 0; i < 5; i++) {
         c->h_ctr[kept[i]] = keep[i];
         GRG_CUDA(c, cudaMemcpyAsync(c->ctr + kept[i], c->h_ctr + kept[i], 8, cudaMemcpyHostToDevice, s));
     }
@@ -3863,6 +3865,7 @@ int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *s
     S.join_launches = joins;
     S.left_elems = c->h_ctr[C_LEFT];
     S.window_out_elems = c->h_ctr[C_WOUT];
+    S.window_noslot_items = c->h_ctr[C_NOSLOT];
     S.gather_ms = c->h_ctr[C_GNS] * 1e-6;
     S.wide_window = c->join_wide ? 1 : 0;
     S.window_tuned = (uint64_t)c->tune_source;

@@ -57,7 +57,7 @@ class Stats(ctypes.Structure):
         ("window_tuned", ctypes.c_uint64), ("window_trial_ms", ctypes.c_double * 2),
         ("column_labels", ctypes.c_uint64), ("push_flat", ctypes.c_uint64), ("push_tuned", ctypes.c_uint64),
         ("push_trial_ms", ctypes.c_double * 2), ("join_elements", ctypes.c_uint64),
-        ("items_trial_ms", ctypes.c_double * 2),
+        ("items_trial_ms", ctypes.c_double * 2), ("window_noslot_items", ctypes.c_uint64),
     ]
 
     def as_dict(self):

@@ -88,6 +88,8 @@ typedef struct grg_stats {
     uint64_t join_elements;        /* 1 = k_join read CSR-copied right-hand rows as whole table
                                       elements, 0 = as destination ids (grg_set_join_items) */
     double items_trial_ms[2];      /* the measured trial passes (ids, elements) when tuned */
+    uint64_t window_noslot_items;  /* of window_out_elems: items of a run of records that drew
+                                      no window slot (a warp has 16 for its 32 records) */
 } grg_stats;
 
 /* Error text of a status code, and the last detailed message of a context. */
