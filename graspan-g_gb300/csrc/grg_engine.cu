@@ -151,11 +151,8 @@ static void set_columns(RuleTable &rt, uint64_t tmask, int L)
 #ifndef GRG_GATHER_GR
 #define GRG_GATHER_GR 4           // delta records per thread per step of the gather's record pass
 #endif
-#ifndef GRG_APPLY_PAIRS
-#define GRG_APPLY_PAIRS 0         // 1: k_apply keeps two candidates' loads in flight per thread
-#endif
 #ifndef GRG_APPLY_MINB
-#define GRG_APPLY_MINB (GRG_APPLY_PAIRS ? 6 : 8)   // k_apply blocks of 256 threads a SM
+#define GRG_APPLY_MINB 8          // k_apply blocks of 256 threads a SM (its grid: this many per SM)
 #endif
 #ifndef GRG_JOIN_MINB_WIDE
 #define GRG_JOIN_MINB_WIDE 7
@@ -837,81 +834,6 @@ __device__ __forceinline__ void win_flush(const Dev &d, WS &w, uint32_t &inserts
 // Insert candidate elements (label, row, base, bits) written by k_join. One
 // thread per candidate: thousands of independent insert chains per SM.
 // Candidates whose table is full go to fail_out (C_AFAIL) for a retry after growth.
-#if GRG_APPLY_PAIRS
-// One candidate of a pair in k_apply: its table, the element its first probe lands on, and
-// that element's words (loaded for both candidates before either is ORed in).
-struct ApplyProbe {
-    uint32_t A, key, s;           // s: the first probe's slot, EMPTY when there is none
-    uint4 c0, c1;
-};
-
-__device__ __forceinline__ void apply_probe_desc(const Dev &d, const uint4 b, ApplyProbe &p, uint64_t &de)
-{
-    p.A = b.z >> KEY_SHIFT;
-    p.key = b.z;
-    p.s = EMPTY;
-    de = p.key == EMPTY ? 0ull : d.desc[(size_t)(p.A - 1) * d.V + b.w];
-}
-
-__device__ __forceinline__ void apply_probe_elem(const Dev &d, uint64_t de, ApplyProbe &p)
-{
-    const uint32_t off = (uint32_t)de, cap = (uint32_t)(de >> 32);
-    if (p.key == EMPTY || cap == 0 || (cap & (cap - 1)) != 0) return;
-    p.s = off + (table_start(d, p.A, p.key & BASE_MASK, cap) & (cap - 1));
-    p.c0 = __ldcg(reinterpret_cast<const uint4 *>(d.elems + (size_t)p.s * 8));
-    p.c1 = __ldcg(reinterpret_cast<const uint4 *>(d.elems + (size_t)p.s * 8 + 4));
-}
-
-// Insert candidates (label, row, base, bits) written by k_join, two per thread: both
-// candidates' descriptors, then both first-probe elements, are loaded before either is ORed
-// in, so each thread keeps two chains of dependent loads in flight. A candidate whose key is
-// not at its first probe takes the general insert. Candidates whose table is full go to
-// fail_out (C_AFAIL) for a retry after growth.
-__global__ void __launch_bounds__(256, GRG_APPLY_MINB) k_apply(Dev d, const uint4 *__restrict__ cand, uint4 *fail_out)
-{
-    if (d.ctr[C_HALT]) return;
-    // the candidate count is read on the device, so the host need not wait for the join
-    const uint64_t n = min((uint64_t)d.ctr[C_CAND_N], d.cand_cap);
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += 2 * stride) {
-        const uint64_t j = i + stride;
-        uint4 a[2], b[2];
-        a[0] = cand[2 * i];
-        b[0] = cand[2 * i + 1];
-        if (j < n) {
-            a[1] = cand[2 * j];
-            b[1] = cand[2 * j + 1];
-        } else {
-            a[1] = make_uint4(0, 0, 0, 0);
-            b[1] = make_uint4(0, 0, EMPTY, 0);
-        }
-        ApplyProbe p[2];
-        uint64_t de[2];
-        apply_probe_desc(d, b[0], p[0], de[0]);
-        apply_probe_desc(d, b[1], p[1], de[1]);
-        apply_probe_elem(d, de[0], p[0]);
-        apply_probe_elem(d, de[1], p[1]);
-#pragma unroll
-        for (int q = 0; q < 2; q++) {
-            if (p[q].key == EMPTY) continue;
-            Bits bits;
-            bits.w[0] = a[q].x; bits.w[1] = a[q].y; bits.w[2] = a[q].z; bits.w[3] = a[q].w;
-            bits.w[4] = b[q].x; bits.w[5] = b[q].y;
-            const bool track = d.rt.track[p[q].A];
-            bool ok;
-            if (p[q].s != EMPTY && p[q].c1.z == p[q].key)
-                ok = g_or_cur(d, p[q].s, bits, track, p[q].c0, p[q].c1);
-            else
-                ok = g_insert_t<true>(d, p[q].A, b[q].w, p[q].key & BASE_MASK, bits, track);
-            if (!ok) {
-                const unsigned long long f = atomicAdd(&d.ctr[C_AFAIL], 1ull);
-                fail_out[2 * f] = a[q];
-                fail_out[2 * f + 1] = b[q];
-            }
-        }
-    }
-}
-#else
 __global__ void __launch_bounds__(256, GRG_APPLY_MINB) k_apply(Dev d, const uint4 *__restrict__ cand, uint4 *fail_out)
 {
     if (d.ctr[C_HALT]) return;
@@ -930,7 +852,6 @@ __global__ void __launch_bounds__(256, GRG_APPLY_MINB) k_apply(Dev d, const uint
         }
     }
 }
-#endif
 
 // Delta records of labels stored by destination (RuleTable::tpose). A record
 // (label B, column k, base, bits = sources i of new edges (i, k)) is pushed
