@@ -151,6 +151,9 @@ static void set_columns(RuleTable &rt, uint64_t tmask, int L)
 #ifndef GRG_GATHER_GR
 #define GRG_GATHER_GR 4           // delta records per thread per step of the gather's record pass
 #endif
+#ifndef GRG_RUN_PASSES
+#define GRG_RUN_PASSES 1          // 1: a batch of more runs than window slots joins in passes, every run with a slot
+#endif
 #ifndef GRG_APPLY_MINB
 #define GRG_APPLY_MINB 8          // k_apply blocks of 256 threads a SM (its grid: this many per SM)
 #endif
@@ -1298,17 +1301,21 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
         // a row's records of one label are contiguous (a table's slots are, and the gather
         // keeps slot order): a run of them shares the window and hash entries of its first
         // record, so their candidates for one output element merge into one
-        {
-            const uint32_t prow = __shfl_up_sync(0xffffffffu, row, 1), pB = __shfl_up_sync(0xffffffffu, B, 1);
-            const bool start = lane == 0 || !have || B == 0 || prow != row || pB != B;
-            const unsigned sm = __ballot_sync(0xffffffffu, start);
-            const uint32_t lead = 31 - __clz(sm & (0xFFFFFFFFu >> (31 - lane)));
-            // the runs take the window slots in order; runs past the last slot use the hash
-            const uint32_t g = __popc(sm & ((1u << lane) - 1u));
-            if (start && g < (uint32_t)NSLOT) w.slot_rec[g] = lane;
-            const uint32_t myslot = __shfl_sync(0xffffffffu, g < (uint32_t)NSLOT ? g : NO_SLOT, lead);
-            w.rpk[lane] = lead | (myslot << 24);
-        }
+        const uint32_t prow = __shfl_up_sync(0xffffffffu, row, 1), pB = __shfl_up_sync(0xffffffffu, B, 1);
+        const bool start = lane == 0 || !have || B == 0 || prow != row || pB != B;
+        const unsigned sm = __ballot_sync(0xffffffffu, start);
+        const uint32_t lead = 31 - __clz(sm & (0xFFFFFFFFu >> (31 - lane)));
+        // runs are numbered in batch order; records past the end of the input come last, so
+        // the batch's runs are those of its valid records. A batch of more runs than a warp has
+        // window slots joins its runs in passes of NSLOT runs, each run with a slot of its own.
+        const uint32_t run = __popc(sm & ((1u << lead) - 1u));
+        const uint32_t nruns = __popc(sm & __ballot_sync(0xffffffffu, have));
+#if GRG_RUN_PASSES
+        const uint32_t npass = nruns > (uint32_t)NSLOT ? (nruns + NSLOT - 1) / NSLOT : 1u;
+#else
+        const uint32_t npass = 1;
+        (void)nruns;
+#endif
         if (lane == 0) w.fail = 0;
         __syncwarp();
         bool ok = true;
@@ -1337,7 +1344,19 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
         // (O_B o D_C, virtual record of rule q): right rows are this round's delta
         // records of C[k], found through the delta index.
         const uint32_t qv = virt ? B - OL_SLOT0 : 0;
-        const uint32_t nbr = virt ? 1 : real ? d.rt.bin_start[B + 1] - d.rt.bin_start[B] : 0;
+        const uint32_t nbr_rec = virt ? 1 : real ? d.rt.bin_start[B + 1] - d.rt.bin_start[B] : 0;
+        for (uint32_t pass = 0; pass < npass; pass++) {
+#if GRG_RUN_PASSES
+        const bool act = run / (uint32_t)NSLOT == pass;
+        if (start && act) w.slot_rec[run % NSLOT] = lane;
+        w.rpk[lane] = lead | ((act ? run % NSLOT : NO_SLOT) << 24);
+#else
+        const bool act = true;
+        if (start && run < (uint32_t)NSLOT) w.slot_rec[run] = lane;
+        w.rpk[lane] = lead | ((run < (uint32_t)NSLOT ? run : NO_SLOT) << 24);
+#endif
+        __syncwarp();
+        const uint32_t nbr = act ? nbr_rec : 0;
         const uint32_t maxb = __reduce_max_sync(0xffffffffu, nbr);
         for (uint32_t rho = 0; rho < maxb; rho++) {
             const bool hr = rho < nbr;
@@ -1488,6 +1507,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
             win_flush(d, w, inserts);
             acc_flush(d, w, inserts);
             PH_MARK(3);
+        }
         }
 
         __syncwarp();
