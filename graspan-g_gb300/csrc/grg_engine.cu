@@ -184,10 +184,12 @@ constexpr int WIN2 = GRG_WIN2;    // wide window: rows whose destinations spread
 constexpr int WIN2_LO = GRG_WIN2_LO;
 constexpr int ACC_LG = GRG_ACC_LG;
 #ifndef GRG_WIN_SLOTS
-#define GRG_WIN_SLOTS 16
+#define GRG_WIN_SLOTS 8
 #endif
-// dense windows per warp: one per run of a row's records (a batch of 32 records holds ~10
-// runs on the dataflow and alias closures); runs beyond the slots use the hash accumulator
+// dense windows per warp: one per run of a row's records; a batch of more runs joins in passes
+// of NSLOT runs (measured, 2M-vertex dataflow / 1M alias closure: 16 slots 54.8 / 272.5 ms,
+// 12 slots 53.4 / 269.7 ms, 8 slots 54.1 / 263.7 ms; 16 slots with runs past the 16th sent to
+// the hash instead of a second pass: 53.9 / 311.5 ms)
 constexpr int NSLOT = GRG_WIN_SLOTS;
 constexpr uint32_t NO_SLOT = 0xFFu;
 constexpr int ACC = 1 << ACC_LG;  // per-warp hash accumulator entries (candidates outside the window)
