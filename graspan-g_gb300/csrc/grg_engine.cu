@@ -1349,167 +1349,168 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
         const uint32_t nbr_rec = virt ? 1 : real ? d.rt.bin_start[B + 1] - d.rt.bin_start[B] : 0;
         for (uint32_t pass = 0; pass < npass; pass++) {
 #if GRG_RUN_PASSES
-        const bool act = run / (uint32_t)NSLOT == pass;
-        if (start && act) w.slot_rec[run % NSLOT] = lane;
-        w.rpk[lane] = lead | ((act ? run % NSLOT : NO_SLOT) << 24);
+            const bool act = run / (uint32_t)NSLOT == pass;
+            if (start && act) w.slot_rec[run % NSLOT] = lane;
+            w.rpk[lane] = lead | ((act ? run % NSLOT : NO_SLOT) << 24);
 #else
-        const bool act = true;
-        if (start && run < (uint32_t)NSLOT) w.slot_rec[run] = lane;
-        w.rpk[lane] = lead | ((run < (uint32_t)NSLOT ? run : NO_SLOT) << 24);
+            const bool act = true;
+            if (start && run < (uint32_t)NSLOT) w.slot_rec[run] = lane;
+            w.rpk[lane] = lead | ((run < (uint32_t)NSLOT ? run : NO_SLOT) << 24);
 #endif
-        __syncwarp();
-        const uint32_t nbr = act ? nbr_rec : 0;
-        const uint32_t maxb = __reduce_max_sync(0xffffffffu, nbr);
-        for (uint32_t rho = 0; rho < maxb; rho++) {
-            const bool hr = rho < nbr;
-            const uint32_t q = virt ? qv : d.rt.bin_start[B] + rho;
-            w.rA[lane] = !hr ? 0 : virt ? d.rt.ol_A[q] : d.rt.bin_A[q];
-            {
-                const uint32_t Cr = !hr ? 0 : virt ? d.rt.ol_C[q] : d.rt.bin_C[q];
-                const uint32_t src = virt ? 2u : (hr && d.rt.csr_row[Cr]) ? 1u : 0u;
-                w.rpk[lane] = (w.rpk[lane] & 0xFF0000FFu) | (Cr << 8) | (src << 16);
-            }
-            n_left += hr;
-            const uint32_t my_cnt = hr ? nbits : 0;
-            const uint32_t total = warp_tasks(w, my_cnt);
-            const uint32_t my_st = w.kpre[lane];
-            uint32_t carry_r = 0;
-            // task (record r, intermediate k) -> items of row C[k]. The record of task t is the
-            // last record that starts at or before t: records starting in a chunk of 32 tasks
-            // mark their start position, a lane takes the highest mark at or below it
-            auto task_of = [&](uint32_t tq, uint32_t &rq, uint32_t &kq) {
-                rq = chunk_owner(w, my_cnt != 0 && my_st - tq < 32u, my_st - tq, carry_r);
-                const uint32_t r_st = __shfl_sync(0xffffffffu, my_st, rq);
-                kq = tq + lane < total ? w.rbase[rq] * EIDS + select_bit(w.rbits[rq], tq + lane - r_st) : 0u;
-            };
-            for (uint32_t t0 = 0; t0 < total; t0 += 32) {
-                const uint32_t t = t0 + lane;
-                uint32_t rr, k;
-                task_of(t0, rr, k);
-                // the task's record, packed: its run's first record tr, right label C, item
-                // source csr (0 table, 1 CSR, 2 delta records) and run window slot ts
-                const uint32_t pk = t < total ? w.rpk[rr] : 0u;
-                const uint32_t tr = pk & 0xFFu, C = (pk >> 8) & 0xFFu, csr = (pk >> 16) & 0xFFu, ts = pk >> 24;
-                uint32_t beg = 0, cnt = 0;
-                if (t < total) {
-                    if (csr == 2) {
-                        const size_t ti = (size_t)(C - 1) * d.V + k;
-                        const uint32_t s0 = __ldg(d.drs + ti);
-                        beg = s0;
-                        cnt = s0 == EMPTY ? 0 : __ldg(d.drc + ti);
-                    } else if (csr == 1) {
-                        const uint2 rw = __ldg(d.rt.csr_row[C] + k);
-                        beg = rw.x;
-                        cnt = rw.y & 0xFFFFFFu;
-                        n_right += rw.y >> 24;
-                    } else {
-                        const size_t ti = (size_t)(C - 1) * d.V + k;
-                        // a prefix-filled table: only slots [0, count) can be occupied. The
-                        // count of a label with such tables loads beside the descriptor.
-                        const bool pl = (d.prefix_mask >> (C - 1)) & 1ull;
-                        const uint64_t de = __ldg(d.desc + ti);
-                        const uint32_t used = pl ? __ldcg(d.cnt + ti) : 0u;
-                        beg = (uint32_t)de;
-                        cnt = (uint32_t)(de >> 32);
-                        if (pl && cnt <= PREFIX_CAP) cnt = min(cnt, used);
-                    }
+            __syncwarp();
+            const uint32_t nbr = act ? nbr_rec : 0;
+            const uint32_t maxb = __reduce_max_sync(0xffffffffu, nbr);
+            for (uint32_t rho = 0; rho < maxb; rho++) {
+                const bool hr = rho < nbr;
+                const uint32_t q = virt ? qv : d.rt.bin_start[B] + rho;
+                w.rA[lane] = !hr ? 0 : virt ? d.rt.ol_A[q] : d.rt.bin_A[q];
+                {
+                    const uint32_t Cr = !hr ? 0 : virt ? d.rt.ol_C[q] : d.rt.bin_C[q];
+                    const uint32_t src = virt ? 2u : (hr && d.rt.csr_row[Cr]) ? 1u : 0u;
+                    w.rpk[lane] = (w.rpk[lane] & 0xFF0000FFu) | (Cr << 8) | (src << 16);
                 }
-                // one right-hand item: a CSR destination id (csr 1), a table element (0) or a
-                // delta record of row C[k] (2). fetch loads it; put ORs it into its run's window
-                // or, outside the window, the shared hash (every lane calls put together: the
-                // hash needs the warp).
-                auto fetch = [&](bool valid, uint32_t o_C, uint32_t o_csr, uint32_t item, Item &it) {
-                    it.ok = false;
-                    it.b2 = 0;
-                    it.ob = EMPTY;
-#pragma unroll
-                    for (int x = 0; x < EW; x++) it.ib.w[x] = 0;
-                    if (valid) {
-                        if (o_csr == 1) {
-                            const uint32_t dst = __ldg(d.rt.csr_col[o_C] + item);
-                            it.b2 = dst / EIDS;
-                            it.ob = dst % EIDS;
-                            it.ok = true;
+                n_left += hr;
+                const uint32_t my_cnt = hr ? nbits : 0;
+                const uint32_t total = warp_tasks(w, my_cnt);
+                const uint32_t my_st = w.kpre[lane];
+                uint32_t carry_r = 0;
+                // task (record r, intermediate k) -> items of row C[k]. The record of task t is the
+                // last record that starts at or before t: records starting in a chunk of 32 tasks
+                // mark their start position, a lane takes the highest mark at or below it
+                auto task_of = [&](uint32_t tq, uint32_t &rq, uint32_t &kq) {
+                    rq = chunk_owner(w, my_cnt != 0 && my_st - tq < 32u, my_st - tq, carry_r);
+                    const uint32_t r_st = __shfl_sync(0xffffffffu, my_st, rq);
+                    kq = tq + lane < total ? w.rbase[rq] * EIDS + select_bit(w.rbits[rq], tq + lane - r_st) : 0u;
+                };
+                for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+                    const uint32_t t = t0 + lane;
+                    uint32_t rr, k;
+                    task_of(t0, rr, k);
+                    // the task's record, packed: its run's first record tr, right label C, item
+                    // source csr (0 table, 1 CSR, 2 delta records) and run window slot ts
+                    const uint32_t pk = t < total ? w.rpk[rr] : 0u;
+                    const uint32_t tr = pk & 0xFFu, C = (pk >> 8) & 0xFFu, csr = (pk >> 16) & 0xFFu, ts = pk >> 24;
+                    uint32_t beg = 0, cnt = 0;
+                    if (t < total) {
+                        if (csr == 2) {
+                            const size_t ti = (size_t)(C - 1) * d.V + k;
+                            const uint32_t s0 = __ldg(d.drs + ti);
+                            beg = s0;
+                            cnt = s0 == EMPTY ? 0 : __ldg(d.drc + ti);
+                        } else if (csr == 1) {
+                            const uint2 rw = __ldg(d.rt.csr_row[C] + k);
+                            beg = rw.x;
+                            cnt = rw.y & 0xFFFFFFu;
+                            n_right += rw.y >> 24;
                         } else {
-                            const uint4 *ep = o_csr == 2 ? d.drec + 2 * (size_t)item
-                                                         : reinterpret_cast<const uint4 *>(d.elems + (size_t)item * 8);
-                            const uint4 e0 = ep[0], e1 = ep[1];
-                            it.ok = e1.z != EMPTY;
-                            it.b2 = e1.z & BASE_MASK;
-                            it.ib.w[0] = e0.x; it.ib.w[1] = e0.y; it.ib.w[2] = e0.z; it.ib.w[3] = e0.w;
-                            it.ib.w[4] = e1.x; it.ib.w[5] = e1.y;
-                            n_right += it.ok ? 1 : 0;
+                            const size_t ti = (size_t)(C - 1) * d.V + k;
+                            // a prefix-filled table: only slots [0, count) can be occupied. The
+                            // count of a label with such tables loads beside the descriptor.
+                            const bool pl = (d.prefix_mask >> (C - 1)) & 1ull;
+                            const uint64_t de = __ldg(d.desc + ti);
+                            const uint32_t used = pl ? __ldcg(d.cnt + ti) : 0u;
+                            beg = (uint32_t)de;
+                            cnt = (uint32_t)(de >> 32);
+                            if (pl && cnt <= PREFIX_CAP) cnt = min(cnt, used);
                         }
                     }
-                };
-                auto put = [&](Item &it, uint32_t o_r, uint32_t o_s) {
-                    bool pending = false;
-                    uint32_t ckey = 0;
-                    if (it.ok) {
-                        const int dd = (int)it.b2 - (int)w.rbase[o_r] + WIN_LO;
-                        if ((unsigned)dd < (unsigned)WIN && o_s != NO_SLOT) {
-                            if (it.ob != EMPTY) {
-                                // one destination id: one word of the window
-                                atomicOr(&w.win[o_s][dd][it.ob >> 5], 1u << (it.ob & 31));
+                    // one right-hand item: a CSR destination id (csr 1), a table element (0) or a
+                    // delta record of row C[k] (2). fetch loads it; put ORs it into its run's window
+                    // or, outside the window, the shared hash (every lane calls put together: the
+                    // hash needs the warp).
+                    auto fetch = [&](bool valid, uint32_t o_C, uint32_t o_csr, uint32_t item, Item &it) {
+                        it.ok = false;
+                        it.b2 = 0;
+                        it.ob = EMPTY;
+#pragma unroll
+                        for (int x = 0; x < EW; x++) it.ib.w[x] = 0;
+                        if (valid) {
+                            if (o_csr == 1) {
+                                const uint32_t dst = __ldg(d.rt.csr_col[o_C] + item);
+                                it.b2 = dst / EIDS;
+                                it.ob = dst % EIDS;
+                                it.ok = true;
                             } else {
-#pragma unroll
-                                for (int x = 0; x < EW; x++)
-                                    if (it.ib.w[x]) atomicOr(&w.win[o_s][dd][x], it.ib.w[x]);
-                            }
-                        } else {
-                            pending = true;
-                            n_out++;                   // an item the dense windows could not hold
-                            n_noslot += o_s == NO_SLOT;
-                            ckey = (o_r << KEY_SHIFT) | it.b2;
-                            if (it.ob != EMPTY) {
-#pragma unroll
-                                for (int x = 0; x < EW; x++)
-                                    it.ib.w[x] = (uint32_t)x == (it.ob >> 5) ? 1u << (it.ob & 31) : 0u;
+                                const uint4 *ep =
+                                    o_csr == 2 ? d.drec + 2 * (size_t)item
+                                               : reinterpret_cast<const uint4 *>(d.elems + (size_t)item * 8);
+                                const uint4 e0 = ep[0], e1 = ep[1];
+                                it.ok = e1.z != EMPTY;
+                                it.b2 = e1.z & BASE_MASK;
+                                it.ib.w[0] = e0.x; it.ib.w[1] = e0.y; it.ib.w[2] = e0.z; it.ib.w[3] = e0.w;
+                                it.ib.w[4] = e1.x; it.ib.w[5] = e1.y;
+                                n_right += it.ok ? 1 : 0;
                             }
                         }
-                    }
-                    while (__any_sync(0xffffffffu, pending)) {
-                        if (pending) pending = !acc_insert(w, ckey, it.ib);
-                        if (__any_sync(0xffffffffu, pending)) acc_flush(d, w, inserts);
-                    }
-                };
-                // the rest of every task's items, flattened over the lanes
-                const uint32_t cnt1 = cnt ? cnt - 1 : 0;
-                uint32_t incl = cnt1;
+                    };
+                    auto put = [&](Item &it, uint32_t o_r, uint32_t o_s) {
+                        bool pending = false;
+                        uint32_t ckey = 0;
+                        if (it.ok) {
+                            const int dd = (int)it.b2 - (int)w.rbase[o_r] + WIN_LO;
+                            if ((unsigned)dd < (unsigned)WIN && o_s != NO_SLOT) {
+                                if (it.ob != EMPTY) {
+                                    // one destination id: one word of the window
+                                    atomicOr(&w.win[o_s][dd][it.ob >> 5], 1u << (it.ob & 31));
+                                } else {
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= (uint32_t)o) incl += y;
+                                    for (int x = 0; x < EW; x++)
+                                        if (it.ib.w[x]) atomicOr(&w.win[o_s][dd][x], it.ib.w[x]);
+                                }
+                            } else {
+                                pending = true;
+                                n_out++;                   // an item the dense windows could not hold
+                                n_noslot += o_s == NO_SLOT;
+                                ckey = (o_r << KEY_SHIFT) | it.b2;
+                                if (it.ob != EMPTY) {
+#pragma unroll
+                                    for (int x = 0; x < EW; x++)
+                                        it.ib.w[x] = (uint32_t)x == (it.ob >> 5) ? 1u << (it.ob & 31) : 0u;
+                                }
+                            }
+                        }
+                        while (__any_sync(0xffffffffu, pending)) {
+                            if (pending) pending = !acc_insert(w, ckey, it.ib);
+                            if (__any_sync(0xffffffffu, pending)) acc_flush(d, w, inserts);
+                        }
+                    };
+                    // the rest of every task's items, flattened over the lanes
+                    const uint32_t cnt1 = cnt ? cnt - 1 : 0;
+                    uint32_t incl = cnt1;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                        if (lane >= (uint32_t)o) incl += y;
+                    }
+                    const uint32_t nitems = __shfl_sync(0xffffffffu, incl, 31);
+                    // per task: item f sits at beg + 1 + f - (first f of the task); record, label and source packed
+                    const uint32_t adj = beg + 1 - (incl - cnt1);
+                    const uint32_t s1 = incl - cnt1;             // the task's first flattened item
+                    uint32_t carry_o = 0;
+                    // first item of every task in the task's own lane (no search, no broadcast), then
+                    // the flattened chunks
+                    // owner lane of flattened item f: the last task whose items start at or before f
+                    auto item_owner = [&](uint32_t fq, uint32_t &o_adj, uint32_t &o_pk) {
+                        const uint32_t lo = chunk_owner(w, cnt1 != 0 && s1 - fq < 32u, s1 - fq, carry_o);
+                        o_adj = __shfl_sync(0xffffffffu, adj, lo);
+                        o_pk = __shfl_sync(0xffffffffu, pk, lo);
+                    };
+                    Item it;
+                    fetch(cnt > 0, C, csr, beg, it);
+                    put(it, tr, ts);
+                    for (uint32_t f0 = 0; f0 < nitems; f0 += 32) {
+                        const uint32_t f = f0 + lane;
+                        uint32_t o_adj, o_pk;
+                        item_owner(f0, o_adj, o_pk);
+                        fetch(f < nitems, (o_pk >> 8) & 0xFFu, (o_pk >> 16) & 0xFFu, f + o_adj, it);
+                        put(it, o_pk & 0xFFu, o_pk >> 24);
+                    }
                 }
-                const uint32_t nitems = __shfl_sync(0xffffffffu, incl, 31);
-                // per task: item f sits at beg + 1 + f - (first f of the task); record, label and source packed
-                const uint32_t adj = beg + 1 - (incl - cnt1);
-                const uint32_t s1 = incl - cnt1;             // the task's first flattened item
-                uint32_t carry_o = 0;
-                // first item of every task in the task's own lane (no search, no broadcast), then
-                // the flattened chunks
-                // owner lane of flattened item f: the last task whose items start at or before f
-                auto item_owner = [&](uint32_t fq, uint32_t &o_adj, uint32_t &o_pk) {
-                    const uint32_t lo = chunk_owner(w, cnt1 != 0 && s1 - fq < 32u, s1 - fq, carry_o);
-                    o_adj = __shfl_sync(0xffffffffu, adj, lo);
-                    o_pk = __shfl_sync(0xffffffffu, pk, lo);
-                };
-                Item it;
-                fetch(cnt > 0, C, csr, beg, it);
-                put(it, tr, ts);
-                for (uint32_t f0 = 0; f0 < nitems; f0 += 32) {
-                    const uint32_t f = f0 + lane;
-                    uint32_t o_adj, o_pk;
-                    item_owner(f0, o_adj, o_pk);
-                    fetch(f < nitems, (o_pk >> 8) & 0xFFu, (o_pk >> 16) & 0xFFu, f + o_adj, it);
-                    put(it, o_pk & 0xFFu, o_pk >> 24);
-                }
+                PH_MARK(2);
+                win_flush(d, w, inserts);
+                acc_flush(d, w, inserts);
+                PH_MARK(3);
             }
-            PH_MARK(2);
-            win_flush(d, w, inserts);
-            acc_flush(d, w, inserts);
-            PH_MARK(3);
-        }
         }
 
         __syncwarp();
