@@ -154,6 +154,9 @@ static void set_columns(RuleTable &rt, uint64_t tmask, int L)
 #ifndef GRG_RUN_PASSES
 #define GRG_RUN_PASSES 1          // 1: a batch of more runs than window slots joins in passes, every run with a slot
 #endif
+#ifndef GRG_OWN_ITEMS
+#define GRG_OWN_ITEMS 1           // items of a task the join takes in the task's own lane before flattening (1 or 2)
+#endif
 #ifndef GRG_APPLY_MINB
 #define GRG_APPLY_MINB 8          // k_apply blocks of 256 threads a SM (its grid: this many per SM)
 #endif
@@ -1474,36 +1477,42 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                             if (__any_sync(0xffffffffu, pending)) acc_flush(d, w, inserts);
                         }
                     };
-                    // the rest of every task's items, flattened over the lanes
-                    const uint32_t cnt1 = cnt ? cnt - 1 : 0;
-                    uint32_t incl = cnt1;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-                        if (lane >= (uint32_t)o) incl += y;
-                    }
-                    const uint32_t nitems = __shfl_sync(0xffffffffu, incl, 31);
-                    // per task: item f sits at beg + 1 + f - (first f of the task); record, label and source packed
-                    const uint32_t adj = beg + 1 - (incl - cnt1);
-                    const uint32_t s1 = incl - cnt1;             // the task's first flattened item
-                    uint32_t carry_o = 0;
-                    // first item of every task in the task's own lane (no search, no broadcast), then
-                    // the flattened chunks
-                    // owner lane of flattened item f: the last task whose items start at or before f
-                    auto item_owner = [&](uint32_t fq, uint32_t &o_adj, uint32_t &o_pk) {
-                        const uint32_t lo = chunk_owner(w, cnt1 != 0 && s1 - fq < 32u, s1 - fq, carry_o);
-                        o_adj = __shfl_sync(0xffffffffu, adj, lo);
-                        o_pk = __shfl_sync(0xffffffffu, pk, lo);
-                    };
+                    // the first GRG_OWN_ITEMS items of every task in the task's own lane (no
+                    // search, no broadcast), then the rest flattened over the lanes
                     Item it;
                     fetch(cnt > 0, C, csr, beg, it);
                     put(it, tr, ts);
-                    for (uint32_t f0 = 0; f0 < nitems; f0 += 32) {
-                        const uint32_t f = f0 + lane;
-                        uint32_t o_adj, o_pk;
-                        item_owner(f0, o_adj, o_pk);
-                        fetch(f < nitems, (o_pk >> 8) & 0xFFu, (o_pk >> 16) & 0xFFu, f + o_adj, it);
-                        put(it, o_pk & 0xFFu, o_pk >> 24);
+#if GRG_OWN_ITEMS >= 2
+                    if (__any_sync(0xffffffffu, cnt > 1)) {
+                        fetch(cnt > 1, C, csr, beg + 1, it);
+                        put(it, tr, ts);
+                    }
+#endif
+                    constexpr uint32_t OWN = GRG_OWN_ITEMS;
+                    const uint32_t cnt1 = cnt > OWN ? cnt - OWN : 0;
+                    if (__any_sync(0xffffffffu, cnt1 != 0)) {
+                        uint32_t incl = cnt1;
+#pragma unroll
+                        for (int o = 1; o < 32; o <<= 1) {
+                            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                            if (lane >= (uint32_t)o) incl += y;
+                        }
+                        const uint32_t nitems = __shfl_sync(0xffffffffu, incl, 31);
+                        // per task: item f sits at beg + OWN + f - (first f of the task); record,
+                        // label and source packed
+                        const uint32_t s1 = incl - cnt1;         // the task's first flattened item
+                        const uint32_t adj = beg + OWN - s1;
+                        uint32_t carry_o = 0;
+                        for (uint32_t f0 = 0; f0 < nitems; f0 += 32) {
+                            const uint32_t f = f0 + lane;
+                            // owner lane of flattened item f: the last task whose items start at
+                            // or before f
+                            const uint32_t lo = chunk_owner(w, cnt1 != 0 && s1 - f0 < 32u, s1 - f0, carry_o);
+                            const uint32_t o_adj = __shfl_sync(0xffffffffu, adj, lo);
+                            const uint32_t o_pk = __shfl_sync(0xffffffffu, pk, lo);
+                            fetch(f < nitems, (o_pk >> 8) & 0xFFu, (o_pk >> 16) & 0xFFu, f + o_adj, it);
+                            put(it, o_pk & 0xFFu, o_pk >> 24);
+                        }
                     }
                 }
                 PH_MARK(2);
