@@ -532,7 +532,7 @@ def main():
                        "join_launches": s["join_launches"], "retry_records": s["retry_records"],
                        "grow_rows": s["grow_rows"], "delta_elems": s["delta_elems"],
                        "pool_elems_used": s["pool_elems_used"],
-                       "join_window": ("wide (10 elements)" if s["wide_window"] else "narrow (8 elements)") +
+                       "join_window": ("wide (12 elements)" if s["wide_window"] else "narrow (8 elements)") +
                        {0: ", fixed", 1: ", measured in this step", 2: ", tuned (degree-key cache)"}[
                            int(s["window_tuned"])],
                        "join_items": "table elements" if s["join_elements"] else "destination ids",

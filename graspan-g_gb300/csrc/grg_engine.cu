@@ -178,10 +178,10 @@ constexpr int RB = 32;            // delta records per warp batch (one per lane)
 constexpr int WIN = GRG_WIN;      // dense accumulator window: elements base-WIN_LO .. base+WIN-1-WIN_LO
 constexpr int WIN_LO = GRG_WIN_LO;
 #ifndef GRG_WIN2
-#define GRG_WIN2 10
-#endif
+#define GRG_WIN2 12               // measured with 8 slots a warp (dataflow / alias, ms): 10 53.6 / 263.5,
+#endif                            // 11 52.6 / 254.3, 12 52.5 / 250.9, 16 52.8 / 264.1
 #ifndef GRG_WIN2_LO
-#define GRG_WIN2_LO 4
+#define GRG_WIN2_LO 5
 #endif
 constexpr int WIN2 = GRG_WIN2;    // wide window: rows whose destinations spread over many elements
 constexpr int WIN2_LO = GRG_WIN2_LO;
@@ -2887,13 +2887,13 @@ __global__ void k_tmark(unsigned long long *ctr, int t0_slot, int acc_slot, int 
 
 // Window of this closure's joins. Measured on dataflow, alias, points-to and
 // small alias jobs, the wide window was fastest or within 1.5% on every one, so
-// it is the default; the narrow window stays selectable. Wide is 10 elements
-// (4 below the run's base); with 16 window slots a warp (one per run of a row's
-// records) a block takes 30 KB of shared memory, and at 72 registers a thread (a
-// few bytes spilled) 7 blocks fit an SM. Measured on one box: 16 slots at 7
-// blocks 54.4 ms for the 2M-vertex dataflow closure and 317 ms for the 1M alias
-// closure, at 6 blocks 54.6 / 323 ms, 32 slots (one per record) at 5 blocks
-// 66.3 / 334 ms, 12 slots at 7 blocks 53.3 / 328 ms.
+// it is the default; the narrow window stays selectable. Wide is 12 elements
+// (5 below the run's base). A warp has 8 window slots, one per run of a row's
+// records, and joins a batch of more runs in passes; a block takes 21 KB of
+// shared memory, and at 72 registers a thread (a few bytes spilled) 7 blocks fit
+// an SM. Earlier layouts, measured on one box (2M-vertex dataflow / 1M alias
+// closure): 16 slots with runs past the 16th in the hash, 10-element windows, 7
+// blocks 54.4 / 317 ms; 32 slots (one per record) at 5 blocks 66.3 / 334 ms.
 static void choose_window(grg_ctx *c)
 {
     c->join_wide = c->join_window_mode >= 2 ? c->tuned_wide : c->join_window_mode != 0;

@@ -253,7 +253,7 @@ class Context:
         self._check(self._L.grg_set_kernel_timing(self._h, int(bool(on))), "set_kernel_timing")
 
     def set_join_window(self, mode: int):
-        """0 = narrow (8 elements), 1 = wide (10), 2 = tuned per degree key (the
+        """0 = narrow (8 elements), 1 = wide (12), 2 = tuned per degree key (the
         default), 3 = tuned and measured again even when the key is cached."""
         self._check(self._L.grg_set_join_window(self._h, mode), "set_join_window")
 

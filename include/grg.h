@@ -115,17 +115,18 @@ int grg_set_kernel_timing(grg_ctx *ctx, int on);
  * host (table growth, buffer room), instead of launching and waiting per
  * round. The results are identical either way. */
 int grg_set_device_rounds(grg_ctx *ctx, int on);
-/* Join window: the join ORs right-hand elements into a dense per-record window
- * of 10 elements (mode 1) or 8 (mode 0); elements outside it go to a small
- * shared-memory hash. Mode 2 (the default) tunes the choice: the closure's input
- * is keyed by its grammar, filter, vertex count and the distribution of its
- * table sizes (elements per label and row, log2 buckets); the first closure of
- * a key whose first round is large times a slice of that round's join in each
- * window and keeps the faster (the wide window unless narrow wins by 10%), and
- * later closures with the key reuse the
- * choice (a process-wide cache). Mode 3 measures again even when the key is
- * cached, and updates the cache. Environment GRG_JOIN_WINDOW=narrow / wide /
- * tuned selects the default. Results are identical in every mode. */
+/* Join window: the join ORs right-hand elements into a dense window per run of
+ * a row's records, of 12 elements (mode 1) or 8 (mode 0); elements outside it
+ * go to a small shared-memory hash. Mode 2 (the default) tunes the choice: the
+ * closure's input is keyed by its grammar, filter, vertex count and the
+ * distribution of its table sizes (elements per label and row, log2 buckets);
+ * the first closure of a key whose first round is large times a slice of that
+ * round's join in each window and keeps the faster (the wide window unless
+ * narrow wins by 10% on a trial of at least 0.25 ms), and later closures with
+ * the key reuse the choice (a process-wide cache). Mode 3 measures again even
+ * when the key is cached, and updates the cache. Environment
+ * GRG_JOIN_WINDOW=narrow / wide / tuned selects the default. Results are
+ * identical in every mode. */
 int grg_set_join_window(grg_ctx *ctx, int mode);
 /* Right-hand items of labels that have a CSR copy (never derived, read as a
  * binary rule's second symbol): mode 0 reads destination ids (4 bytes each,

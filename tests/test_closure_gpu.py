@@ -237,7 +237,7 @@ def test_device_rounds_equal_host_rounds(grg_mod, oracle_mod, name):
 
 @pytest.mark.parametrize("name", ["pointsto", "alias", "dataflow"])
 def test_join_windows_equal(grg_mod, oracle_mod, name):
-    """The narrow (8-element) and wide (10-element) join windows give the oracle's closure."""
+    """The narrow (8-element) and wide (12-element) join windows give the oracle's closure."""
     w = {"pointsto": lambda: G.pointsto(seed=41, num_vars=900, num_edges=2200),
          "alias": lambda: G.alias(seed=42, num_vars=4000, num_base_edges=9000, block=700),
          "dataflow": lambda: G.dataflow_blocks(seed=43, num_blocks=20, block=500, num_edges=30000)}[name]()
