@@ -154,9 +154,6 @@ static void set_columns(RuleTable &rt, uint64_t tmask, int L)
 #ifndef GRG_RUN_PASSES
 #define GRG_RUN_PASSES 1          // 1: a batch of more runs than window slots joins in passes, every run with a slot
 #endif
-#ifndef GRG_OWN_ITEMS
-#define GRG_OWN_ITEMS 1           // items of a task the join takes in the task's own lane before flattening (1 or 2)
-#endif
 #ifndef GRG_APPLY_MINB
 #define GRG_APPLY_MINB 8          // k_apply blocks of 256 threads a SM (its grid: this many per SM)
 #endif
@@ -1477,18 +1474,14 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                             if (__any_sync(0xffffffffu, pending)) acc_flush(d, w, inserts);
                         }
                     };
-                    // the first GRG_OWN_ITEMS items of every task in the task's own lane (no
-                    // search, no broadcast), then the rest flattened over the lanes
+                    // the first item of every task in the task's own lane (no search, no
+                    // broadcast), then the rest flattened over the lanes. (A second item in the
+                    // own lane before flattening measured slower: 53.2 -> 58.7 ms on the 2M-vertex
+                    // dataflow closure, 252.4 -> 268.3 ms on the 1M alias closure.)
                     Item it;
                     fetch(cnt > 0, C, csr, beg, it);
                     put(it, tr, ts);
-#if GRG_OWN_ITEMS >= 2
-                    if (__any_sync(0xffffffffu, cnt > 1)) {
-                        fetch(cnt > 1, C, csr, beg + 1, it);
-                        put(it, tr, ts);
-                    }
-#endif
-                    constexpr uint32_t OWN = GRG_OWN_ITEMS;
+                    constexpr uint32_t OWN = 1;
                     const uint32_t cnt1 = cnt > OWN ? cnt - OWN : 0;
                     if (__any_sync(0xffffffffu, cnt1 != 0)) {
                         uint32_t incl = cnt1;
