@@ -2330,6 +2330,12 @@ int grow_pool(grg_ctx *c, uint64_t min_elems)
 // Candidate buffers of a round (4 per delta record; a full buffer falls back to direct inserts).
 int ensure_cand(grg_ctx *c, uint64_t nd)
 {
+    // environment GRG_DIRECT_INSERTS=1: no candidate buffers, every join inserts directly
+    static const bool direct = [] {
+        const char *e = getenv("GRG_DIRECT_INSERTS");
+        return e && e[0] == '1';
+    }();
+    if (direct) return GRG_OK;
     // capped at 2^26 candidates (2 GiB a buffer): past it, joins insert directly
     const uint64_t want = std::min<uint64_t>(std::max<uint64_t>(4 * nd, 1 << 20), 1ull << 26);
     if (want <= c->cand_cap) return GRG_OK;
