@@ -72,7 +72,8 @@ enum : int {
     C_CHECK = C_LABEL0 + MAX_SLOTS + 19, // first failed bounds check of the push kernels: id << 56 | value
     C_JQ = C_LABEL0 + MAX_SLOTS + 20,    // work queue of a join or push launch: next 32-record batch (zeroed before each launch)
     C_NOSLOT = C_LABEL0 + MAX_SLOTS + 21, // of C_WOUT: items of a run of records left without a window slot
-    NCTR = C_LABEL0 + MAX_SLOTS + 22
+    C_CANDS = C_LABEL0 + MAX_SLOTS + 22,  // candidates k_apply inserted over the closure
+    NCTR = C_LABEL0 + MAX_SLOTS + 23
 };
 // error bits of C_ERR; ERR_IN_* (in C_BADIN) flag input edges that were refused
 // (label outside 1..L, vertex id outside the graph) and never touched a table

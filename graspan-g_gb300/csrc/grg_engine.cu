@@ -844,6 +844,7 @@ __global__ void __launch_bounds__(256, GRG_APPLY_MINB) k_apply(Dev d, const uint
     if (d.ctr[C_HALT]) return;
     // the candidate count is read on the device, so the host need not wait for the join
     const uint64_t n = min((uint64_t)d.ctr[C_CAND_N], d.cand_cap);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && n) atomicAdd(&d.ctr[C_CANDS], (unsigned long long)n);
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint4 a = cand[2 * i], b = cand[2 * i + 1];
         if (b.z == EMPTY) continue;
@@ -3818,6 +3819,8 @@ int grg_closure_ex(grg_ctx *c, uint32_t filter, uint32_t run_stamp, grg_stats *s
     S.left_elems = c->h_ctr[C_LEFT];
     S.window_out_elems = c->h_ctr[C_WOUT];
     S.window_noslot_items = c->h_ctr[C_NOSLOT];
+    S.candidates = c->h_ctr[C_CANDS];
+    S.join_inserts = c->h_ctr[C_INSERTS];
     S.gather_ms = c->h_ctr[C_GNS] * 1e-6;
     S.wide_window = c->join_wide ? 1 : 0;
     S.window_tuned = (uint64_t)c->tune_source;

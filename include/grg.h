@@ -89,7 +89,11 @@ typedef struct grg_stats {
                                       elements, 0 = as destination ids (grg_set_join_items) */
     double items_trial_ms[2];      /* the measured trial passes (ids, elements) when tuned */
     uint64_t window_noslot_items;  /* of window_out_elems: items of a run of records that drew
-                                      no window slot (a warp has 16 for its 32 records) */
+                                      no window slot (0 unless built with -DGRG_RUN_PASSES=0) */
+    uint64_t candidates;           /* elements the joins wrote as candidates for k_apply
+                                      (joins insert directly when there is no buffer) */
+    uint64_t join_inserts;         /* element inserts the joins made themselves (unary rules,
+                                      and flushes without a candidate buffer) */
 } grg_stats;
 
 /* Error text of a status code, and the last detailed message of a context. */
