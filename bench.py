@@ -541,7 +541,8 @@ def main():
                        "join_work": {"left_records": s["left_elems"], "right_elems": s["right_elems"],
                                      "hash_items": s["window_out_elems"],
                                      "hash_items_no_slot": s["window_noslot_items"], "out_elems": s["out_elems"],
-                                     "candidates": s["candidates"], "join_inserts": s["join_inserts"]},
+                                     "candidates": s["candidates"], "join_inserts": s["join_inserts"],
+                                     "direct_inserts": bool(s["direct_inserts"])},
                        # the first closure's trial passes (ms): windows [narrow, wide], item forms [ids, elements]
                        "tuner_trials_ms": warm and {"window": [round(x, 3) for x in warm[0]["window_trial_ms"]],
                                                     "items": [round(x, 3) for x in warm[0]["items_trial_ms"]]},

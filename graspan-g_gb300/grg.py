@@ -58,7 +58,7 @@ class Stats(ctypes.Structure):
         ("column_labels", ctypes.c_uint64), ("push_flat", ctypes.c_uint64), ("push_tuned", ctypes.c_uint64),
         ("push_trial_ms", ctypes.c_double * 2), ("join_elements", ctypes.c_uint64),
         ("items_trial_ms", ctypes.c_double * 2), ("window_noslot_items", ctypes.c_uint64),
-        ("candidates", ctypes.c_uint64), ("join_inserts", ctypes.c_uint64),
+        ("candidates", ctypes.c_uint64), ("join_inserts", ctypes.c_uint64), ("direct_inserts", ctypes.c_uint64),
     ]
 
     def as_dict(self):

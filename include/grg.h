@@ -94,6 +94,10 @@ typedef struct grg_stats {
                                       (joins insert directly when there is no buffer) */
     uint64_t join_inserts;         /* element inserts the joins made themselves (unary rules,
                                       and flushes without a candidate buffer) */
+    uint64_t direct_inserts;       /* 1 = the joins inserted their elements themselves (the
+                                      default for grammars with a derivable right-hand label;
+                                      environment GRG_DIRECT_INSERTS=0 / 1 overrides), 0 = they
+                                      wrote candidates that k_apply inserted */
 } grg_stats;
 
 /* Error text of a status code, and the last detailed message of a context. */

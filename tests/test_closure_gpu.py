@@ -317,3 +317,24 @@ def test_small_rounds_split_and_retry_overflow(grg_mod, oracle_mod, monkeypatch)
                 assert st["retry_records"] > 16 and st["grow_rows"] > 0
             assert ctx.label_counts().tolist() == r.label_counts().tolist() and ctx.set_hash() == r.set_hash
             ctx.close()
+
+
+@pytest.mark.parametrize("mode", ["0", "1", None])
+@pytest.mark.parametrize("name", ["alias", "pointsto", "dataflow"])
+def test_insert_modes_equal_oracle(grg_mod, oracle_mod, monkeypatch, name, mode):
+    """Joins that write candidates for k_apply (GRG_DIRECT_INSERTS=0) and joins that insert
+    directly (1) give the oracle's closure, also with a pool small enough that tables grow and
+    inserts fail and re-run; by default a grammar with a derivable right-hand label (alias,
+    points-to) inserts directly and the dataflow grammar writes candidates."""
+    w = {"alias": lambda: G.alias(seed=71, num_vars=20_000, num_base_edges=80_000, block=500),
+         "pointsto": lambda: G.pointsto(seed=72, num_vars=1500, num_edges=5000),
+         "dataflow": lambda: G.dataflow_blocks(seed=73, num_blocks=30, num_edges=90_000)}[name]()
+    if mode is None:
+        monkeypatch.delenv("GRG_DIRECT_INSERTS", raising=False)
+    else:
+        monkeypatch.setenv("GRG_DIRECT_INSERTS", mode)
+    for pool in (0, 1 << 18):
+        r, st = assert_same_as_oracle(grg_mod, oracle_mod, w, pool_bytes=pool, edges=False)
+        want = (name != "dataflow") if mode is None else mode == "1"
+        assert st["direct_inserts"] == want
+        assert (st["candidates"] == 0) == want
