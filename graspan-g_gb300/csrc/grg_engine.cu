@@ -155,8 +155,9 @@ static void set_columns(RuleTable &rt, uint64_t tmask, int L)
 #define GRG_RUN_PASSES 1          // 1: a batch of more runs than window slots joins in passes, every run with a slot
 #endif
 #ifndef GRG_APPLY_MINB
-#define GRG_APPLY_MINB 8          // k_apply blocks of 256 threads a SM (its grid: this many per SM)
-#endif
+#define GRG_APPLY_MINB 6          // k_apply blocks of 256 threads a SM (its grid: this many per SM); at 6
+#endif                            // its 36 registers need no spills (8: 32 and spills; 2M dataflow closure
+                                  // 53.0 / 53.2 ms at 8 against 52.3 / 52.3 at 6 on two boxes)
 #ifndef GRG_JOIN_MINB_WIDE
 #define GRG_JOIN_MINB_WIDE 7
 #endif
