@@ -154,9 +154,6 @@ static void set_columns(RuleTable &rt, uint64_t tmask, int L)
 #ifndef GRG_RUN_PASSES
 #define GRG_RUN_PASSES 1          // 1: a batch of more runs than window slots joins in passes, every run with a slot
 #endif
-#ifndef GRG_FLUSH_WHOLE
-#define GRG_FLUSH_WHOLE false     // direct inserts of a join's flush: true reads the whole element at a probe
-#endif
 #ifndef GRG_APPLY_MINB
 #define GRG_APPLY_MINB 6          // k_apply blocks of 256 threads a SM (its grid: this many per SM); at 6
 #endif                            // its 36 registers need no spills (8: 32 and spills; 2M dataflow closure
@@ -790,7 +787,7 @@ __device__ __forceinline__ void acc_flush(const Dev &d, WS &w, uint32_t &inserts
             if (ci != ~0ull) {
                 cand_write(d, ci++, b, (A << KEY_SHIFT) | (k & BASE_MASK), w.rrow[r]);
             } else {
-                if (!g_insert_t<GRG_FLUSH_WHOLE>(d, A, w.rrow[r], k & BASE_MASK, b, d.rt.track[A])) atomicOr(&w.fail, 1u << r);
+                if (!g_insert(d, A, w.rrow[r], k & BASE_MASK, b, d.rt.track[A])) atomicOr(&w.fail, 1u << r);
                 inserts++;
             }
         }
@@ -832,7 +829,7 @@ __device__ __forceinline__ void win_flush(const Dev &d, WS &w, uint32_t &inserts
             if (ci != ~0ull) {
                 cand_write(d, ci++, b, (A << KEY_SHIFT) | base, w.rrow[r]);
             } else {
-                if (!g_insert_t<GRG_FLUSH_WHOLE>(d, A, w.rrow[r], base, b, d.rt.track[A])) atomicOr(&w.fail, 1u << r);
+                if (!g_insert(d, A, w.rrow[r], base, b, d.rt.track[A])) atomicOr(&w.fail, 1u << r);
                 inserts++;
             }
         }
