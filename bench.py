@@ -48,6 +48,9 @@ sys.path[:0] = [ROOT, os.path.join(ROOT, "graspan-g_gb300")]
 
 import numpy as np  # noqa: E402
 
+# DRAM bytes (read + write) per join pass measured by ncu on the named workload, with the file
+# that records the capture
+TRAFFIC = {("dataflow", 2000): (584.0e6, "profiles/traffic_dataflow_blocks_2000.md")}
 METRIC = "closure_edges_per_sec"
 UNIT = "edges/s"
 WORKLOAD = ("dataflow_blocks: 2000 blocks x 1000 vertices, 6M 'e' edges + 6M 'N' seeds, "
@@ -511,10 +514,10 @@ def main():
         join_ms = statistics.mean(x["join_ms"] for x in stats)
         launches = s["rounds"]
         achieved = alg_bytes / (join_ms * 1e-3) / 1e9 if (join_ms > 0 and alg_bytes) else None
-        # DRAM bytes of a full-size launch are not captured: counters beyond the launch time
-        # are taken on a small case only (profiles/), whose per-launch figures do not map to
-        # a full-size round
-        traffic = None
+        # DRAM bytes per join pass (k_join + k_apply) of the headline closure, from a one-pass
+        # ncu capture of every launch of one closure (profiles/traffic_dataflow_blocks_2000.md);
+        # other workloads have no capture
+        traffic = TRAFFIC.get((args.workload, args.blocks)) if not s["column_labels"] else None
         cb = None if args.no_cpu_baseline else cpu_baseline(w)
         # the other configurations run once, on a single GPU (replica runs hold every GPU meanwhile)
         single = world == 1 and not args.quick
@@ -557,7 +560,9 @@ def main():
                          "kernel": "join pass (" + ("k_push" if s["column_labels"] else "k_join + k_apply") + ")",
                          "achieved": achieved, "peak": hbm,
                          "peak_kind": peak_kind, "unit": "GB/s",
-                         "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
+                         "frac": (achieved / hbm) if achieved else None,
+                         "traffic": traffic and traffic[0],
+                         "traffic_source": traffic and traffic[1],
                          "alg_bytes_per_launch": alg_bytes / launches if alg_bytes else None,
                          "alg_bytes_source": "oracle counts of the workload" if _oracle_alg_elems(args, w) else
                          "engine counters", "launches_per_step": launches, "join_ms_per_step": join_ms,
