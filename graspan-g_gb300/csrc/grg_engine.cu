@@ -154,6 +154,9 @@ static void set_columns(RuleTable &rt, uint64_t tmask, int L)
 #ifndef GRG_RUN_PASSES
 #define GRG_RUN_PASSES 1          // 1: a batch of more runs than window slots joins in passes, every run with a slot
 #endif
+#ifndef GRG_LD256
+#define GRG_LD256 0               // 1: a join loads a right-hand element with one 256-bit load
+#endif
 #ifndef GRG_APPLY_MINB
 #define GRG_APPLY_MINB 6          // k_apply blocks of 256 threads a SM (its grid: this many per SM); at 6
 #endif                            // its 36 registers need no spills (8: 32 and spills; 2M dataflow closure
@@ -1436,7 +1439,17 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                                 const uint4 *ep =
                                     o_csr == 2 ? d.drec + 2 * (size_t)item
                                                : reinterpret_cast<const uint4 *>(d.elems + (size_t)item * 8);
+#if GRG_LD256
+                                // one 32-byte load (elements and records sit at 32-byte offsets of
+                                // allocations aligned to at least 256 bytes)
+                                uint4 e0, e1;
+                                asm volatile("ld.global.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                                             : "=r"(e0.x), "=r"(e0.y), "=r"(e0.z), "=r"(e0.w), "=r"(e1.x),
+                                               "=r"(e1.y), "=r"(e1.z), "=r"(e1.w)
+                                             : "l"(ep));
+#else
                                 const uint4 e0 = ep[0], e1 = ep[1];
+#endif
                                 it.ok = e1.z != EMPTY;
                                 it.b2 = e1.z & BASE_MASK;
                                 it.ib.w[0] = e0.x; it.ib.w[1] = e0.y; it.ib.w[2] = e0.z; it.ib.w[3] = e0.w;
