@@ -184,6 +184,46 @@ __device__ __forceinline__ uint32_t table_limit(const Dev &d, uint32_t slot, uin
 
 struct Bits { uint32_t w[EW]; };
 
+#ifndef GRG_LD256
+#define GRG_LD256 1   // 32-byte elements and records move with one 256-bit access (0: two 128-bit ones)
+#endif
+// One 32-byte element or record: every such address is a 32-byte offset into an allocation
+// aligned to at least 256 bytes. ld32 is a plain load, ld32_cg one that skips L1 (for
+// elements other threads update), st32 a plain store.
+__device__ __forceinline__ void ld32(const void *p, uint4 &a, uint4 &b)
+{
+#if GRG_LD256
+    asm volatile("ld.global.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(a.x), "=r"(a.y), "=r"(a.z), "=r"(a.w), "=r"(b.x), "=r"(b.y), "=r"(b.z), "=r"(b.w)
+                 : "l"(p));
+#else
+    a = reinterpret_cast<const uint4 *>(p)[0];
+    b = reinterpret_cast<const uint4 *>(p)[1];
+#endif
+}
+__device__ __forceinline__ void ld32_cg(const void *p, uint4 &a, uint4 &b)
+{
+#if GRG_LD256
+    asm volatile("ld.global.cg.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(a.x), "=r"(a.y), "=r"(a.z), "=r"(a.w), "=r"(b.x), "=r"(b.y), "=r"(b.z), "=r"(b.w)
+                 : "l"(p));
+#else
+    a = __ldcg(reinterpret_cast<const uint4 *>(p));
+    b = __ldcg(reinterpret_cast<const uint4 *>(p) + 1);
+#endif
+}
+__device__ __forceinline__ void st32(void *p, const uint4 a, const uint4 b)
+{
+#if GRG_LD256
+    asm volatile("st.global.v8.u32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "r"(a.x), "r"(a.y),
+                 "r"(a.z), "r"(a.w), "r"(b.x), "r"(b.y), "r"(b.z), "r"(b.w)
+                 : "memory");
+#else
+    reinterpret_cast<uint4 *>(p)[0] = a;
+    reinterpret_cast<uint4 *>(p)[1] = b;
+#endif
+}
+
 __device__ __forceinline__ uint64_t splitmix64(uint64_t x)
 {
     x += 0x9E3779B97F4A7C15ull;
@@ -231,8 +271,9 @@ __device__ __forceinline__ bool g_or_cur(const Dev &d, uint32_t s, const Bits b,
 __device__ __forceinline__ bool g_or_into(const Dev &d, uint32_t s, const Bits b, bool track)
 {
     const uint32_t *e = d.elems + (size_t)s * 8;
-    return g_or_cur(d, s, b, track, __ldcg(reinterpret_cast<const uint4 *>(e)),
-                    __ldcg(reinterpret_cast<const uint4 *>(e + 4)));
+    uint4 c0, c1;
+    ld32_cg(e, c0, c1);
+    return g_or_cur(d, s, b, track, c0, c1);
 }
 
 // OR `b` into element (slot, row, base). Returns false when the table is full
@@ -261,8 +302,7 @@ __device__ __forceinline__ bool g_insert_t(const Dev &d, uint32_t slot, uint32_t
             uint32_t *kp = d.elems + (size_t)q * 8 + 6;
             uint32_t k;
             if (whole) {
-                c0 = __ldcg(reinterpret_cast<const uint4 *>(d.elems + (size_t)q * 8));
-                c1 = __ldcg(reinterpret_cast<const uint4 *>(d.elems + (size_t)q * 8 + 4));
+                ld32_cg(d.elems + (size_t)q * 8, c0, c1);
                 k = c1.z;
             } else {
                 k = __ldcg(kp);

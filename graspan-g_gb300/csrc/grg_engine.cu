@@ -154,9 +154,6 @@ static void set_columns(RuleTable &rt, uint64_t tmask, int L)
 #ifndef GRG_RUN_PASSES
 #define GRG_RUN_PASSES 1          // 1: a batch of more runs than window slots joins in passes, every run with a slot
 #endif
-#ifndef GRG_LD256
-#define GRG_LD256 0               // 1: a join loads a right-hand element with one 256-bit load
-#endif
 #ifndef GRG_APPLY_MINB
 #define GRG_APPLY_MINB 6          // k_apply blocks of 256 threads a SM (its grid: this many per SM); at 6
 #endif                            // its 36 registers need no spills (8: 32 and spills; 2M dataflow closure
@@ -495,24 +492,17 @@ __global__ void k_gather_recs(Dev d, const uint32_t *__restrict__ slots, uint4 *
         }
 #pragma unroll
         for (int u = 0; u < GR; u++) {
-            if (i0 + u * stride < n) {
-                const uint4 *b = reinterpret_cast<const uint4 *>(d.dbits + sl[u] * 8);
-                b0[u] = b[0];
-                b1[u] = b[1];
-            }
+            if (i0 + u * stride < n) ld32(d.dbits + sl[u] * 8, b0[u], b1[u]);
         }
 #pragma unroll
         for (int u = 0; u < GR; u++) {
             const uint64_t i = i0 + u * stride;
             if (i >= n) continue;
             const uint64_t s = sl[u];
-            uint4 *b = reinterpret_cast<uint4 *>(d.dbits + s * 8);
             // words 0-5 cleared; 6-7 keep the slot's key and row
-            b[0] = make_uint4(0, 0, 0, 0);
-            b[1] = make_uint4(0, 0, b1[u].z, b1[u].w);
+            st32(d.dbits + s * 8, make_uint4(0, 0, 0, 0), make_uint4(0, 0, b1[u].z, b1[u].w));
             if (run_stamp) d.stamp[s] = run_stamp;     // gained bits during this run
-            out[2 * i] = b0[u];
-            out[2 * i + 1] = b1[u];
+            st32(out + 2 * i, b0[u], b1[u]);
             const uint32_t lab = b1[u].z >> KEY_SHIFT, row = b1[u].w;
             if (lab <= (uint32_t)MAX_LABELS && d.rt.dindex[lab]) {
                 const size_t ti = (size_t)(lab - 1) * d.V + row;
@@ -761,8 +751,7 @@ __device__ __forceinline__ uint64_t cand_reserve(const Dev &d, uint32_t cnt)
 
 __device__ __forceinline__ void cand_write(const Dev &d, uint64_t i, const Bits &b, uint32_t key, uint32_t row)
 {
-    d.cand[2 * i] = make_uint4(b.w[0], b.w[1], b.w[2], b.w[3]);
-    d.cand[2 * i + 1] = make_uint4(b.w[4], b.w[5], key, row);
+    st32(d.cand + 2 * i, make_uint4(b.w[0], b.w[1], b.w[2], b.w[3]), make_uint4(b.w[4], b.w[5], key, row));
 }
 
 // Flush the hash accumulator: entry (r, base) goes to row (rA[r], rrow[r]),
@@ -850,7 +839,8 @@ __global__ void __launch_bounds__(256, GRG_APPLY_MINB) k_apply(Dev d, const uint
     const uint64_t n = min((uint64_t)d.ctr[C_CAND_N], d.cand_cap);
     if (blockIdx.x == 0 && threadIdx.x == 0 && n) atomicAdd(&d.ctr[C_CANDS], (unsigned long long)n);
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint4 a = cand[2 * i], b = cand[2 * i + 1];
+        uint4 a, b;
+        ld32(cand + 2 * i, a, b);
         if (b.z == EMPTY) continue;
         Bits bits;
         bits.w[0] = a.x; bits.w[1] = a.y; bits.w[2] = a.z; bits.w[3] = a.w; bits.w[4] = b.x; bits.w[5] = b.y;
@@ -1289,7 +1279,8 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
         Bits rb;
         uint32_t key = EMPTY, row = 0;
         if (have) {
-            const uint4 a = recs[2 * ri], b = recs[2 * ri + 1];
+            uint4 a, b;
+            ld32(recs + 2 * ri, a, b);
             rb.w[0] = a.x; rb.w[1] = a.y; rb.w[2] = a.z; rb.w[3] = a.w; rb.w[4] = b.x; rb.w[5] = b.y;
             key = b.z;
             row = b.w;
@@ -1439,17 +1430,8 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                                 const uint4 *ep =
                                     o_csr == 2 ? d.drec + 2 * (size_t)item
                                                : reinterpret_cast<const uint4 *>(d.elems + (size_t)item * 8);
-#if GRG_LD256
-                                // one 32-byte load (elements and records sit at 32-byte offsets of
-                                // allocations aligned to at least 256 bytes)
                                 uint4 e0, e1;
-                                asm volatile("ld.global.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-                                             : "=r"(e0.x), "=r"(e0.y), "=r"(e0.z), "=r"(e0.w), "=r"(e1.x),
-                                               "=r"(e1.y), "=r"(e1.z), "=r"(e1.w)
-                                             : "l"(ep));
-#else
-                                const uint4 e0 = ep[0], e1 = ep[1];
-#endif
+                                ld32(ep, e0, e1);
                                 it.ok = e1.z != EMPTY;
                                 it.b2 = e1.z & BASE_MASK;
                                 it.ib.w[0] = e0.x; it.ib.w[1] = e0.y; it.ib.w[2] = e0.z; it.ib.w[3] = e0.w;
