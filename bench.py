@@ -50,7 +50,7 @@ import numpy as np  # noqa: E402
 
 # DRAM bytes (read + write) per join pass measured by ncu on the named workload, with the file
 # that records the capture
-TRAFFIC = {("dataflow", 2000): (584.0e6, "profiles/traffic_dataflow_blocks_2000.md")}
+TRAFFIC = {("dataflow", 2000): (559.0e6, "profiles/traffic_dataflow_blocks_2000.md")}
 METRIC = "closure_edges_per_sec"
 UNIT = "edges/s"
 WORKLOAD = ("dataflow_blocks: 2000 blocks x 1000 vertices, 6M 'e' edges + 6M 'N' seeds, "
