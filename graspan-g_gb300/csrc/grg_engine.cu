@@ -154,6 +154,9 @@ static void set_columns(RuleTable &rt, uint64_t tmask, int L)
 #ifndef GRG_RUN_PASSES
 #define GRG_RUN_PASSES 1          // 1: a batch of more runs than window slots joins in passes, every run with a slot
 #endif
+#ifndef GRG_WIN_PRECHECK
+#define GRG_WIN_PRECHECK 0        // 1: items of derivable right-hand labels OR only the window words they add to
+#endif
 #ifndef GRG_APPLY_MINB
 #define GRG_APPLY_MINB 6          // k_apply blocks of 256 threads a SM (its grid: this many per SM); at 6
 #endif                            // its 36 registers need no spills (8: 32 and spills; 2M dataflow closure
@@ -1362,7 +1365,10 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                 w.rA[lane] = !hr ? 0 : virt ? d.rt.ol_A[q] : d.rt.bin_A[q];
                 {
                     const uint32_t Cr = !hr ? 0 : virt ? d.rt.ol_C[q] : d.rt.bin_C[q];
-                    const uint32_t src = virt ? 2u : (hr && d.rt.csr_row[Cr]) ? 1u : 0u;
+                    // item source 0 table, 1 CSR, 2 delta records; +4: a derivable right-hand
+                    // label, whose dense rows mostly OR bits the window already holds
+                    const uint32_t src = (virt ? 2u : (hr && d.rt.csr_row[Cr]) ? 1u : 0u) |
+                                         (GRG_WIN_PRECHECK && hr && d.rt.track[Cr] ? 4u : 0u);
                     w.rpk[lane] = (w.rpk[lane] & 0xFF0000FFu) | (Cr << 8) | (src << 16);
                 }
                 n_left += hr;
@@ -1388,12 +1394,12 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                     const uint32_t tr = pk & 0xFFu, C = (pk >> 8) & 0xFFu, csr = (pk >> 16) & 0xFFu, ts = pk >> 24;
                     uint32_t beg = 0, cnt = 0;
                     if (t < total) {
-                        if (csr == 2) {
+                        if ((csr & 3u) == 2) {
                             const size_t ti = (size_t)(C - 1) * d.V + k;
                             const uint32_t s0 = __ldg(d.drs + ti);
                             beg = s0;
                             cnt = s0 == EMPTY ? 0 : __ldg(d.drc + ti);
-                        } else if (csr == 1) {
+                        } else if ((csr & 3u) == 1) {
                             const uint2 rw = __ldg(d.rt.csr_row[C] + k);
                             beg = rw.x;
                             cnt = rw.y & 0xFFFFFFu;
@@ -1421,14 +1427,14 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
 #pragma unroll
                         for (int x = 0; x < EW; x++) it.ib.w[x] = 0;
                         if (valid) {
-                            if (o_csr == 1) {
+                            if ((o_csr & 3u) == 1) {
                                 const uint32_t dst = __ldg(d.rt.csr_col[o_C] + item);
                                 it.b2 = dst / EIDS;
                                 it.ob = dst % EIDS;
                                 it.ok = true;
                             } else {
                                 const uint4 *ep =
-                                    o_csr == 2 ? d.drec + 2 * (size_t)item
+                                    (o_csr & 3u) == 2 ? d.drec + 2 * (size_t)item
                                                : reinterpret_cast<const uint4 *>(d.elems + (size_t)item * 8);
                                 uint4 e0, e1;
                                 ld32(ep, e0, e1);
@@ -1440,7 +1446,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                             }
                         }
                     };
-                    auto put = [&](Item &it, uint32_t o_r, uint32_t o_s) {
+                    auto put = [&](Item &it, uint32_t o_r, uint32_t o_s, bool pre) {
                         bool pending = false;
                         uint32_t ckey = 0;
                         if (it.ok) {
@@ -1449,6 +1455,15 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                                 if (it.ob != EMPTY) {
                                     // one destination id: one word of the window
                                     atomicOr(&w.win[o_s][dd][it.ob >> 5], 1u << (it.ob & 31));
+                                } else if (pre) {
+                                    // only the words with bits the window lacks (a stale read
+                                    // costs an atomic, never a bit: bits stay until the flush)
+                                    const uint2 *wp = reinterpret_cast<const uint2 *>(&w.win[o_s][dd][0]);
+                                    const uint2 q0 = wp[0], q1 = wp[1], q2 = wp[2];
+                                    const uint32_t cur[EW] = {q0.x, q0.y, q1.x, q1.y, q2.x, q2.y};
+#pragma unroll
+                                    for (int x = 0; x < EW; x++)
+                                        if (it.ib.w[x] & ~cur[x]) atomicOr(&w.win[o_s][dd][x], it.ib.w[x]);
                                 } else {
 #pragma unroll
                                     for (int x = 0; x < EW; x++)
@@ -1477,7 +1492,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                     // dataflow closure, 252.4 -> 268.3 ms on the 1M alias closure.)
                     Item it;
                     fetch(cnt > 0, C, csr, beg, it);
-                    put(it, tr, ts);
+                    put(it, tr, ts, (csr & 4u) != 0);
                     constexpr uint32_t OWN = 1;
                     const uint32_t cnt1 = cnt > OWN ? cnt - OWN : 0;
                     if (__any_sync(0xffffffffu, cnt1 != 0)) {
@@ -1501,7 +1516,7 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                             const uint32_t o_adj = __shfl_sync(0xffffffffu, adj, lo);
                             const uint32_t o_pk = __shfl_sync(0xffffffffu, pk, lo);
                             fetch(f < nitems, (o_pk >> 8) & 0xFFu, (o_pk >> 16) & 0xFFu, f + o_adj, it);
-                            put(it, o_pk & 0xFFu, o_pk >> 24);
+                            put(it, o_pk & 0xFFu, o_pk >> 24, ((o_pk >> 16) & 4u) != 0);
                         }
                     }
                 }
