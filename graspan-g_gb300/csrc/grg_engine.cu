@@ -155,7 +155,7 @@ static void set_columns(RuleTable &rt, uint64_t tmask, int L)
 #define GRG_RUN_PASSES 1          // 1: a batch of more runs than window slots joins in passes, every run with a slot
 #endif
 #ifndef GRG_WIN_PRECHECK
-#define GRG_WIN_PRECHECK 1        // items of derivable right-hand labels OR only the window words they add to
+#define GRG_WIN_PRECHECK 1        // items of derivable right-hand labels (2: of every label) OR only the window words they add to
 #endif                            // (1M alias closure 230.6 -> 209.4 ms; 2M dataflow closure unchanged, 52.5)
 #ifndef GRG_APPLY_MINB
 #define GRG_APPLY_MINB 6          // k_apply blocks of 256 threads a SM (its grid: this many per SM); at 6
@@ -1367,8 +1367,8 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                     const uint32_t Cr = !hr ? 0 : virt ? d.rt.ol_C[q] : d.rt.bin_C[q];
                     // item source 0 table, 1 CSR, 2 delta records; +4: a derivable right-hand
                     // label, whose dense rows mostly OR bits the window already holds
-                    const uint32_t src = (virt ? 2u : (hr && d.rt.csr_row[Cr]) ? 1u : 0u) |
-                                         (GRG_WIN_PRECHECK && hr && d.rt.track[Cr] ? 4u : 0u);
+                    const bool pre = GRG_WIN_PRECHECK == 2 || (GRG_WIN_PRECHECK == 1 && d.rt.track[Cr]);
+                    const uint32_t src = (virt ? 2u : (hr && d.rt.csr_row[Cr]) ? 1u : 0u) | (hr && pre ? 4u : 0u);
                     w.rpk[lane] = (w.rpk[lane] & 0xFF0000FFu) | (Cr << 8) | (src << 16);
                 }
                 n_left += hr;
