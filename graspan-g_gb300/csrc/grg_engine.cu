@@ -155,8 +155,9 @@ static void set_columns(RuleTable &rt, uint64_t tmask, int L)
 #define GRG_RUN_PASSES 1          // 1: a batch of more runs than window slots joins in passes, every run with a slot
 #endif
 #ifndef GRG_WIN_PRECHECK
-#define GRG_WIN_PRECHECK 1        // items of derivable right-hand labels (2: of every label) OR only the window words they add to
-#endif                            // (1M alias closure 230.6 -> 209.4 ms; 2M dataflow closure unchanged, 52.5)
+#define GRG_WIN_PRECHECK 1        // items of derivable right-hand labels (2: of every label) OR only the
+#endif                            // window words they add to (1M alias closure 230.6 -> 209.4 ms; 2M
+                                  // dataflow closure 52.5 ms either way, 53.2 with every label)
 #ifndef GRG_APPLY_MINB
 #define GRG_APPLY_MINB 6          // k_apply blocks of 256 threads a SM (its grid: this many per SM); at 6
 #endif                            // its 36 registers need no spills (8: 32 and spills; 2M dataflow closure
