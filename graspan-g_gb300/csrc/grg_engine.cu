@@ -158,9 +158,6 @@ static void set_columns(RuleTable &rt, uint64_t tmask, int L)
 #define GRG_WIN_PRECHECK 1        // items of derivable right-hand labels (2: of every label) OR only the
 #endif                            // window words they add to (1M alias closure 230.6 -> 209.4 ms; 2M
                                   // dataflow closure 52.5 ms either way, 53.2 with every label)
-#ifndef GRG_APPLY_WHOLE
-#define GRG_APPLY_WHOLE true      // k_apply's probes read the whole element (false: the key only)
-#endif
 #ifndef GRG_APPLY_MINB
 #define GRG_APPLY_MINB 6          // k_apply blocks of 256 threads a SM (its grid: this many per SM); at 6
 #endif                            // its 36 registers need no spills (8: 32 and spills; 2M dataflow closure
@@ -852,7 +849,7 @@ __global__ void __launch_bounds__(256, GRG_APPLY_MINB) k_apply(Dev d, const uint
         Bits bits;
         bits.w[0] = a.x; bits.w[1] = a.y; bits.w[2] = a.z; bits.w[3] = a.w; bits.w[4] = b.x; bits.w[5] = b.y;
         const uint32_t A = b.z >> KEY_SHIFT;
-        if (!g_insert_t<GRG_APPLY_WHOLE>(d, A, b.w, b.z & BASE_MASK, bits, d.rt.track[A])) {
+        if (!g_insert_t<true>(d, A, b.w, b.z & BASE_MASK, bits, d.rt.track[A])) {
             const unsigned long long f = atomicAdd(&d.ctr[C_AFAIL], 1ull);
             fail_out[2 * f] = a;
             fail_out[2 * f + 1] = b;
