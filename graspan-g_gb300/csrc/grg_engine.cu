@@ -617,8 +617,9 @@ struct __align__(16) WarpSmemT {
     uint32_t rpk[RB];             // per record, packed: the first record of its run with the same row
                                   // and label (bits 0-7), the current rule's right operand label
                                   // (8-15), where that label's rows come from (16-23: 0 tables, 1 CSR
-                                  // copy, 2 delta records of a virtual old-left record) and the
-                                  // run's window slot (24-31, NO_SLOT: the hash only)
+                                  // copy, 2 delta records of a virtual old-left record; +4 when its
+                                  // items pre-check the window) and the run's window slot (24-31,
+                                  // NO_SLOT: the hash only)
     uint32_t kpre[RB + 1];        // exclusive prefix of per-record task counts
     uint8_t own[32];              // per chunk of 32 tasks (items): lane whose record (task) starts there
     uint32_t acc_n;
@@ -1390,7 +1391,8 @@ __global__ void __launch_bounds__(JOIN_WARPS * 32, (W <= 8 ? GRG_JOIN_MINB : GRG
                     uint32_t rr, k;
                     task_of(t0, rr, k);
                     // the task's record, packed: its run's first record tr, right label C, item
-                    // source csr (0 table, 1 CSR, 2 delta records) and run window slot ts
+                    // source csr (low bits 0 table, 1 CSR, 2 delta records; +4 window pre-check)
+                    // and run window slot ts
                     const uint32_t pk = t < total ? w.rpk[rr] : 0u;
                     const uint32_t tr = pk & 0xFFu, C = (pk >> 8) & 0xFFu, csr = (pk >> 16) & 0xFFu, ts = pk >> 24;
                     uint32_t beg = 0, cnt = 0;
