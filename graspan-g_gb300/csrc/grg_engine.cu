@@ -163,8 +163,8 @@ static void set_columns(RuleTable &rt, uint64_t tmask, int L)
 #endif                            // its 36 registers need no spills (8: 32 and spills; 2M dataflow closure
                                   // 53.0 / 53.2 ms at 8 against 52.3 / 52.3 at 6 on two boxes)
 #ifndef GRG_JOIN_MINB_WIDE
-#define GRG_JOIN_MINB_WIDE 7
-#endif
+#define GRG_JOIN_MINB_WIDE 8      // wide join blocks a SM: 8 at 64 registers (with spills) measured 51.3 /
+#endif                            // 195.3 ms on the 2M dataflow / 1M alias closures against 52.5 / 207.7 at 7
 #ifdef GRG_PHASE_TIMERS
 #define PH_MARK(i)                                   \
     do {                                             \
@@ -2921,8 +2921,8 @@ __global__ void k_tmark(unsigned long long *ctr, int t0_slot, int acc_slot, int 
 // small alias jobs, the wide window was fastest or within 1.5% on every one, so
 // it is the default; the narrow window stays selectable. Wide is 12 elements
 // (5 below the run's base). A warp has 8 window slots, one per run of a row's
-// records, and joins a batch of more runs in passes; a block takes 21 KB of
-// shared memory, and at 72 registers a thread (a few bytes spilled) 7 blocks fit
+// records, and joins a batch of more runs in passes; a block takes 22 KB of
+// shared memory, and at 64 registers a thread (some bytes spilled) 8 blocks fit
 // an SM. Earlier layouts, measured on one box (2M-vertex dataflow / 1M alias
 // closure): 16 slots with runs past the 16th in the hash, 10-element windows, 7
 // blocks 54.4 / 317 ms; 32 slots (one per record) at 5 blocks 66.3 / 334 ms.
